@@ -1,0 +1,1002 @@
+// Host side of the C ABI declared in include/hssgpu.h: plan construction
+// (validation, level lists, workspace and factor-storage layout), buffer
+// management, launch sequencing and the FP64 iterative refinement loop.
+#include "hssgpu.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hss_internal.h"
+#include "hss_launch.h"
+
+using namespace hss;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? HSS_ERR_OOM : HSS_ERR_CUDA;
+}
+
+#define CUDA_TRY(x)                                   \
+  do {                                                \
+    cudaError_t e_ = (x);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #x);  \
+  } while (0)
+
+// Grow-only device buffer.
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    release();
+    size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    else p = nullptr;
+    return e;
+  }
+};
+
+// Pinned host buffer.
+template <typename T>
+struct HBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  HBuf() = default;
+  HBuf(const HBuf&) = delete;
+  HBuf& operator=(const HBuf&) = delete;
+  ~HBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMallocHost((void**)&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) cap = std::max<size_t>(n, 1);
+    return e;
+  }
+};
+
+// Slot table on the device, re-uploaded only when its contents change.
+struct SlotTable {
+  DBuf<Slot> dev;
+  std::vector<Slot> last;
+  cudaError_t upload(const std::vector<Slot>& s, cudaStream_t st) {
+    if (s.size() == last.size() && dev.p &&
+        std::memcmp(s.data(), last.data(), s.size() * sizeof(Slot)) == 0)
+      return cudaSuccess;
+    cudaError_t e = dev.ensure(s.size());
+    if (e != cudaSuccess) return e;
+    // pageable source: the copy is staged before the call returns
+    e = cudaMemcpyAsync(dev.p, s.data(), s.size() * sizeof(Slot), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) last = s;
+    return e;
+  }
+};
+
+struct Seg {
+  int64_t off = 0, cnt = 0;
+};
+
+inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
+
+// Launch accounting and optional CUDA-event bracketing of one kernel kind.
+int64_t g_launches = 0;
+struct TraceState {
+  int kind = -1;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+} g_trace;
+
+cudaEvent_t trace_event() {
+  if (g_trace.used == g_trace.pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    g_trace.pool.push_back(e);
+  }
+  return g_trace.pool[g_trace.used++];
+}
+
+// Runs `launch` (which issues one kernel when cnt > 0) and brackets it with
+// events when its kind is being traced.
+template <typename F>
+void traced(int kind, int64_t cnt, cudaStream_t st, F&& launch) {
+  if (cnt <= 0) return;
+  const bool on = g_trace.kind == kind;
+  if (on) {
+    cudaEvent_t a = trace_event();
+    if (a) cudaEventRecord(a, st);
+  }
+  launch();
+  ++g_launches;
+  if (on) {
+    cudaEvent_t b = trace_event();
+    if (b) cudaEventRecord(b, st);
+  }
+}
+
+}  // namespace
+
+struct hss_plan_s {
+  int device = 0;
+  int32_t ntrees = 0;
+  std::vector<Node> nodes;              // host copy, device pointers inside
+  std::vector<int32_t> tree_root;
+  std::vector<int64_t> tree_m, tree_n;
+  double* d_gen = nullptr;
+  Node* d_nodes = nullptr;
+  Task* d_tasks = nullptr;
+  std::vector<Seg> by_h, by_d, mv_up, mv_dn;
+  Seg leaves;
+  int64_t ws_mv = 0, ws_sv = 0;         // workspace rows
+  int64_t fac_elems = 0;                // factor storage elements
+  int max_m = 0, max_n = 0;
+  int32_t* d_err = nullptr;
+  DBuf<double> mv_ws;
+  SlotTable mv_slots;
+  DBuf<double> hB, hC;                  // staging for the _host product
+  hss_factor_s* fused[2] = {nullptr, nullptr};   // storage reused by hss_ulvfactsolve_host
+  ~hss_plan_s();
+};
+
+struct hss_factor_s {
+  hss_plan_s* plan = nullptr;
+  int prec = HSS_PREC_FP64;
+  void* d_fac = nullptr;
+  size_t fac_bytes = 0;
+  DBuf<char> sv_ws;
+  SlotTable fac_slots, sv_slots, sv_slots_ref, mv_slots;
+  DBuf<double> R, bn2, rn2, scale;
+  HBuf<double> h_bn2, h_rn2;
+  DBuf<double> hB, hX;                  // staging for the _host solve
+  ~hss_factor_s() {
+    if (d_fac) cudaFree(d_fac);
+  }
+};
+
+hss_plan_s::~hss_plan_s() {
+  delete fused[0];
+  delete fused[1];
+  if (d_gen) cudaFree(d_gen);
+  if (d_nodes) cudaFree(d_nodes);
+  if (d_tasks) cudaFree(d_tasks);
+  if (d_err) cudaFree(d_err);
+}
+
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// plan construction
+// ---------------------------------------------------------------------------
+
+struct TreeIn {
+  int64_t nnodes;
+  const int64_t* table;
+  const double* packed;
+  int64_t npacked;
+};
+
+// Generator pointers are recorded as offsets into the forest's packed buffer
+// during validation and turned into device pointers after the upload.
+struct GenOffsets {
+  int64_t D = -1, U = -1, V = -1, B12 = -1, B21 = -1, R1 = -1, R2 = -1, W1 = -1, W2 = -1;
+};
+
+// Host-only phase: validates every tree (the dimension checks of `checkdims`,
+// src/hssmatrix.jl:308-322, plus the ULV size rules of src/ulvfactor.jl:27-28),
+// numbers nodes, computes depths, heights, leaf offsets, ULV reduce sizes,
+// workspace and factor-storage layout, and the level task lists.
+int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<GenOffsets>& go,
+                std::vector<Task>& tasks, std::vector<int64_t>& gbases) {
+  P->ntrees = (int32_t)trees.size();
+  int64_t total_nodes = 0, total_gen = 0;
+  for (auto& t : trees) {
+    if (t.nnodes <= 0 || t.table == nullptr) return fail(HSS_ERR_INVALID, "empty node table");
+    if (t.npacked < 0) return fail(HSS_ERR_INVALID, "negative packed length");
+    total_nodes += t.nnodes;
+    gbases.push_back(total_gen);
+    total_gen += align16(t.npacked);
+  }
+  gbases.push_back(total_gen);
+  if (total_nodes > (int64_t)INT32_MAX) return fail(HSS_ERR_BAD_DIMS, "too many nodes");
+  P->nodes.assign(total_nodes, Node{});
+  go.assign(total_nodes, GenOffsets{});
+  int64_t nbase = 0;
+  int max_h = 0, max_d = 0;
+  int64_t ws_mv = 0, ws_sv = 0, fac = 0;
+  for (size_t ti = 0; ti < trees.size(); ++ti) {
+    const TreeIn& t = trees[ti];
+    const int64_t nn = t.nnodes;
+    const int64_t gbase = gbases[ti];
+    auto F = [&](int64_t i, int f) { return t.table[i * HSS_NODE_FIELDS + f]; };
+    auto gchk = [&](int64_t off, int64_t len, const char* what, int64_t* out) -> int {
+      if (len == 0) { *out = -1; return HSS_OK; }
+      if (off < 0 || off + len > t.npacked)
+        return fail(HSS_ERR_BAD_DIMS, std::string("generator block out of range: ") + what);
+      *out = gbase + off;
+      return HSS_OK;
+    };
+    // topology
+    std::vector<int32_t> parent(nn, -1);
+    for (int64_t i = 0; i < nn; ++i) {
+      const int64_t l = F(i, 0), r = F(i, 1);
+      if ((l < 0) != (r < 0)) return fail(HSS_ERR_BAD_DIMS, "node with only one child");
+      for (int64_t c : {l, r}) {
+        if (c < 0) continue;
+        if (c >= nn || c == 0) return fail(HSS_ERR_BAD_DIMS, "child index out of range");
+        if (parent[c] != -1) return fail(HSS_ERR_BAD_DIMS, "node with two parents");
+        parent[c] = (int32_t)i;
+      }
+    }
+    for (int64_t i = 1; i < nn; ++i)
+      if (parent[i] < 0) return fail(HSS_ERR_BAD_DIMS, "unreachable node");
+    // pre-order traversal (left first) from the root
+    std::vector<int32_t> pre;
+    pre.reserve(nn);
+    {
+      std::vector<int32_t> stack{0};
+      while (!stack.empty() && (int64_t)pre.size() <= nn) {
+        int32_t x = stack.back();
+        stack.pop_back();
+        pre.push_back(x);
+        if (F(x, 0) >= 0) {
+          stack.push_back((int32_t)F(x, 1));
+          stack.push_back((int32_t)F(x, 0));
+        }
+      }
+    }
+    if ((int64_t)pre.size() != nn) return fail(HSS_ERR_BAD_DIMS, "node table is not a tree");
+    Node* N = P->nodes.data() + nbase;
+    GenOffsets* O = go.data() + nbase;
+    for (int64_t i = 0; i < nn; ++i) {
+      Node& x = N[i];
+      x.left = F(i, 0) >= 0 ? (int32_t)(nbase + F(i, 0)) : -1;
+      x.right = F(i, 1) >= 0 ? (int32_t)(nbase + F(i, 1)) : -1;
+      x.parent = parent[i] >= 0 ? (int32_t)(nbase + parent[i]) : -1;
+      x.leaf = F(i, 0) < 0;
+      x.root = i == 0;
+      x.tree = (int32_t)ti;
+    }
+    for (int32_t i : pre) {
+      N[i].depth = i == 0 ? 0 : N[parent[i]].depth + 1;
+      max_d = std::max(max_d, N[i].depth);
+    }
+    int64_t row = 0, col = 0;
+    for (int32_t i : pre) {   // leaf offsets in pre-order
+      if (N[i].leaf) {
+        N[i].row0 = row;
+        N[i].col0 = col;
+        row += F(i, 2);
+        col += F(i, 3);
+      }
+    }
+    // post-order: sizes, generator blocks, ULV reduce sizes
+    for (auto it = pre.rbegin(); it != pre.rend(); ++it) {
+      const int32_t i = *it;
+      Node& x = N[i];
+      GenOffsets& o = O[i];
+      const bool root = i == 0;
+      x.ku = root ? 0 : (int32_t)F(i, 4);
+      x.kv = root ? 0 : (int32_t)F(i, 5);
+      if (F(i, 4) < 0 || F(i, 5) < 0 || F(i, 4) > (1 << 20) || F(i, 5) > (1 << 20))
+        return fail(HSS_ERR_BAD_DIMS, "generator rank out of range");
+      int rc;
+      if (x.leaf) {
+        const int64_t m = F(i, 2), n = F(i, 3);
+        if (m <= 0 || n <= 0 || m > (1 << 20) || n > (1 << 20))
+          return fail(HSS_ERR_BAD_DIMS, "leaf block size out of range");
+        x.gm = (int32_t)m;
+        x.gn = (int32_t)n;
+        x.height = 0;
+        x.m = x.gm;
+        x.n = x.gn;
+        if ((rc = gchk(F(i, 6), m * n, "D", &o.D))) return rc;
+        if ((rc = gchk(F(i, 7), m * x.ku, "U", &o.U))) return rc;
+        if ((rc = gchk(F(i, 8), n * x.kv, "V", &o.V))) return rc;
+      } else {
+        const Node& c1 = N[F(i, 0)];
+        const Node& c2 = N[F(i, 1)];
+        if ((int64_t)c1.gm + c2.gm > (1LL << 31) - 1 || (int64_t)c1.gn + c2.gn > (1LL << 31) - 1)
+          return fail(HSS_ERR_BAD_DIMS, "matrix too large");
+        x.gm = c1.gm + c2.gm;
+        x.gn = c1.gn + c2.gn;
+        x.row0 = c1.row0;
+        x.col0 = c1.col0;
+        x.height = std::max(c1.height, c2.height) + 1;
+        if ((rc = gchk(F(i, 9), (int64_t)c1.ku * c2.kv, "B12", &o.B12))) return rc;
+        if ((rc = gchk(F(i, 10), (int64_t)c2.ku * c1.kv, "B21", &o.B21))) return rc;
+        if ((rc = gchk(F(i, 11), (int64_t)c1.ku * x.ku, "R1", &o.R1))) return rc;
+        if ((rc = gchk(F(i, 12), (int64_t)c2.ku * x.ku, "R2", &o.R2))) return rc;
+        if ((rc = gchk(F(i, 13), (int64_t)c1.kv * x.kv, "W1", &o.W1))) return rc;
+        if ((rc = gchk(F(i, 14), (int64_t)c2.kv * x.kv, "W2", &o.W2))) return rc;
+        x.m = c1.mr + c2.mr;   // merged block (src/ulvfactor.jl:75)
+        x.n = c1.nr + c2.nr;
+      }
+      max_h = std::max(max_h, x.height);
+      if (root) {
+        if (x.m != x.n)
+          return fail(HSS_ERR_BAD_DIMS, "root block of the ULV reduction is not square");
+        x.k = x.m; x.mk = 0; x.nk = 0; x.mr = x.m; x.nr = x.n; x.lower_u = 0;
+      } else {
+        x.k = std::min(x.ku, x.m);               // src/ulvfactor.jl:27
+        x.mk = x.m - x.k;
+        x.nk = std::min(x.mk, x.n);              // :28
+        if (x.mk > x.n)
+          return fail(HSS_ERR_BAD_DIMS, "m - k > n in the ULV reduction (trsm needs a square L1)");
+        x.mr = x.m - x.mk;
+        x.nr = x.n - x.nk;
+        x.lower_u = x.mk > 0;
+      }
+      P->max_m = std::max(P->max_m, x.m);
+      P->max_n = std::max(P->max_n, x.n);
+    }
+    {
+      // Block shapes follow from the ranks, so a rank that disagrees with the
+      // stored blocks shows up as overlapping blocks: require them disjoint.
+      std::vector<std::pair<int64_t, int64_t>> blocks;
+      for (int64_t i = 0; i < nn; ++i) {
+        const Node& x = N[i];
+        const GenOffsets& o = O[i];
+        auto add = [&](int64_t off, int64_t len) {
+          if (off >= 0 && len > 0) blocks.emplace_back(off, len);
+        };
+        if (x.leaf) {
+          add(o.D, (int64_t)x.gm * x.gn);
+          add(o.U, (int64_t)x.gm * x.ku);
+          add(o.V, (int64_t)x.gn * x.kv);
+        } else {
+          const Node& c1 = N[x.left - nbase];
+          const Node& c2 = N[x.right - nbase];
+          add(o.B12, (int64_t)c1.ku * c2.kv);
+          add(o.B21, (int64_t)c2.ku * c1.kv);
+          add(o.R1, (int64_t)c1.ku * x.ku);
+          add(o.R2, (int64_t)c2.ku * x.ku);
+          add(o.W1, (int64_t)c1.kv * x.kv);
+          add(o.W2, (int64_t)c2.kv * x.kv);
+        }
+      }
+      std::sort(blocks.begin(), blocks.end());
+      for (size_t b = 1; b < blocks.size(); ++b)
+        if (blocks[b - 1].first + blocks[b - 1].second > blocks[b].first)
+          return fail(HSS_ERR_BAD_DIMS, "generator blocks overlap: ranks disagree with the stored blocks");
+    }
+    P->tree_root.push_back((int32_t)nbase);
+    P->tree_m.push_back(N[0].gm);
+    P->tree_n.push_back(N[0].gn);
+    // workspace rows and factor storage (elements)
+    for (int32_t i : pre) {
+      Node& x = N[i];
+      x.wz = ws_mv; ws_mv += x.kv;
+      x.wf = ws_mv; ws_mv += x.ku;
+      x.wb = ws_sv; ws_sv += x.m;
+      x.wu = ws_sv; ws_sv += x.kv;
+      x.wx = ws_sv; ws_sv += x.n;
+      x.fD = fac; fac += align16((int64_t)x.m * x.n);
+      x.fU = fac; fac += align16((int64_t)x.m * x.ku);
+      x.fV = fac; fac += align16((int64_t)x.n * x.kv);
+      x.ftq = fac; fac += align16(x.root ? 0 : x.k);
+      x.ftl = fac; fac += align16(x.mk);
+      if (!x.leaf) {
+        const Node& c1 = N[F(i, 0)];
+        const Node& c2 = N[F(i, 1)];
+        x.fT12 = fac; fac += align16((int64_t)c1.mr * c2.kv);
+        x.fT21 = fac; fac += align16((int64_t)c2.mr * c1.kv);
+      }
+      if (x.root) { x.fpiv = fac; fac += align16(x.m); }
+    }
+    nbase += nn;
+  }
+  P->ws_mv = std::max<int64_t>(ws_mv, 1);
+  P->ws_sv = std::max<int64_t>(ws_sv, 1);
+  P->fac_elems = std::max<int64_t>(fac, 1);
+  // task lists
+  auto add_seg = [&](std::vector<Seg>& v, auto pred, int nlev, bool by_height) {
+    v.assign(nlev + 1, Seg{});
+    for (int lv = 0; lv <= nlev; ++lv) {
+      v[lv].off = (int64_t)tasks.size();
+      for (int64_t i = 0; i < total_nodes; ++i) {
+        const Node& x = P->nodes[i];
+        if ((by_height ? x.height : x.depth) == lv && pred(x))
+          tasks.push_back(Task{nullptr, (int32_t)i, x.tree});
+      }
+      v[lv].cnt = (int64_t)tasks.size() - v[lv].off;
+    }
+  };
+  add_seg(P->by_h, [](const Node&) { return true; }, max_h, true);
+  add_seg(P->by_d, [](const Node&) { return true; }, max_d, false);
+  add_seg(P->mv_up, [](const Node& x) { return !x.leaf && !x.root; }, max_h, true);
+  add_seg(P->mv_dn, [](const Node& x) { return !x.leaf; }, max_d, false);
+  P->leaves.off = (int64_t)tasks.size();
+  for (int64_t i = 0; i < total_nodes; ++i)
+    if (P->nodes[i].leaf) tasks.push_back(Task{nullptr, (int32_t)i, P->nodes[i].tree});
+  P->leaves.cnt = (int64_t)tasks.size() - P->leaves.off;
+  return HSS_OK;
+}
+
+int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
+  for (auto& t : trees)
+    if (t.npacked > 0 && t.packed == nullptr) return fail(HSS_ERR_INVALID, "null packed buffer");
+  std::vector<GenOffsets> go;
+  std::vector<Task> tasks;
+  std::vector<int64_t> gbases;
+  int rc = layout_plan(P, trees, go, tasks, gbases);
+  if (rc) return rc;
+  // device phase
+  CUDA_TRY(cudaGetDevice(&P->device));
+  const int64_t total_gen = gbases.back();
+  CUDA_TRY(cudaMalloc((void**)&P->d_gen, std::max<int64_t>(total_gen, 1) * sizeof(double)));
+  CUDA_TRY(cudaMalloc((void**)&P->d_err, sizeof(int32_t)));
+  CUDA_TRY(cudaMemset(P->d_err, 0, sizeof(int32_t)));
+  for (size_t ti = 0; ti < trees.size(); ++ti)
+    if (trees[ti].npacked > 0)
+      CUDA_TRY(cudaMemcpy(P->d_gen + gbases[ti], trees[ti].packed, trees[ti].npacked * sizeof(double),
+                          cudaMemcpyHostToDevice));
+  auto gp = [&](int64_t off) -> const double* { return off < 0 ? nullptr : P->d_gen + off; };
+  for (size_t i = 0; i < P->nodes.size(); ++i) {
+    Node& x = P->nodes[i];
+    const GenOffsets& o = go[i];
+    x.D = gp(o.D); x.U = gp(o.U); x.V = gp(o.V);
+    x.B12 = gp(o.B12); x.B21 = gp(o.B21);
+    x.R1 = gp(o.R1); x.R2 = gp(o.R2); x.W1 = gp(o.W1); x.W2 = gp(o.W2);
+  }
+  const int64_t total_nodes = (int64_t)P->nodes.size();
+  CUDA_TRY(cudaMalloc((void**)&P->d_nodes, total_nodes * sizeof(Node)));
+  CUDA_TRY(cudaMemcpy(P->d_nodes, P->nodes.data(), total_nodes * sizeof(Node), cudaMemcpyHostToDevice));
+  for (auto& t : tasks) t.nodes = P->d_nodes;
+  CUDA_TRY(cudaMalloc((void**)&P->d_tasks, std::max<size_t>(tasks.size(), 1) * sizeof(Task)));
+  CUDA_TRY(cudaMemcpy(P->d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice));
+  return HSS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// launch sequences
+// ---------------------------------------------------------------------------
+
+void run_matvec(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
+  const Task* T = P->d_tasks;
+  traced(HSS_TRACE_MV_LEAF, P->leaves.cnt, st,
+         [&] { launch_mv_leaf(T + P->leaves.off, P->leaves.cnt, slots, st); });
+  for (size_t h = 1; h < P->mv_up.size(); ++h)
+    traced(HSS_TRACE_MV_UP, P->mv_up[h].cnt, st,
+           [&] { launch_mv_up(T + P->mv_up[h].off, P->mv_up[h].cnt, slots, st); });
+  for (size_t d = 0; d < P->mv_dn.size(); ++d)
+    traced(HSS_TRACE_MV_DOWN, P->mv_dn[d].cnt, st,
+           [&] { launch_mv_down(T + P->mv_dn[d].off, P->mv_dn[d].cnt, slots, st); });
+  traced(HSS_TRACE_MV_FINAL, P->leaves.cnt, st,
+         [&] { launch_mv_leaf_final(T + P->leaves.off, P->leaves.cnt, slots, st); });
+}
+
+template <typename T>
+void run_factor(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
+  for (size_t h = 0; h < P->by_h.size(); ++h)
+    traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, P->by_h[h].cnt, st, [&] {
+      launch_ulv_factor<T>(P->d_tasks + P->by_h[h].off, P->by_h[h].cnt, slots, P->max_m, P->max_n, st);
+    });
+}
+
+template <typename T>
+void run_solve(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
+  for (size_t h = 0; h < P->by_h.size(); ++h)
+    traced(HSS_TRACE_SOLVE_UP, P->by_h[h].cnt, st,
+           [&] { launch_ulv_solve_up<T>(P->d_tasks + P->by_h[h].off, P->by_h[h].cnt, slots, st); });
+  for (size_t d = 0; d < P->by_d.size(); ++d)
+    traced(HSS_TRACE_SOLVE_DOWN, P->by_d[d].cnt, st,
+           [&] { launch_ulv_solve_down<T>(P->d_tasks + P->by_d[d].off, P->by_d[d].cnt, slots, st); });
+}
+
+struct Cols {   // per-tree product / solve operands
+  const double* B;
+  int64_t ldb;
+  int64_t r;
+  double* C;
+  int64_t ldc;
+};
+
+int check_cols(hss_plan_s* P, const std::vector<Cols>& io, bool solve) {
+  for (int32_t t = 0; t < P->ntrees; ++t) {
+    const Cols& c = io[t];
+    if (c.r < 0) return fail(HSS_ERR_BAD_DIMS, "negative number of right-hand sides");
+    if (c.r == 0) continue;
+    if (c.B == nullptr || c.C == nullptr) return fail(HSS_ERR_INVALID, "null operand");
+    const int64_t rows_in = solve ? P->tree_m[t] : P->tree_n[t];
+    const int64_t rows_out = solve ? P->tree_n[t] : P->tree_m[t];
+    if (c.ldb < rows_in)
+      return fail(HSS_ERR_BAD_DIMS, "First dimension of B does not match second dimension of A");
+    if (c.ldc < rows_out) return fail(HSS_ERR_BAD_DIMS, "Dimensions of C don't match up with A and B.");
+    if (c.r > (1 << 24)) return fail(HSS_ERR_BAD_DIMS, "too many right-hand sides");
+  }
+  return HSS_OK;
+}
+
+int matmul_impl(hss_plan_s* P, const std::vector<Cols>& io, double alpha, double beta,
+                cudaStream_t st, const double* const* Y, double* colnorm2, const int64_t* cn_off,
+                SlotTable& table) {
+  int64_t rmax = 0;
+  for (auto& c : io) rmax = std::max(rmax, c.r);
+  if (rmax == 0) return HSS_OK;
+  CUDA_TRY(P->mv_ws.ensure((size_t)P->ws_mv * rmax));
+  std::vector<Slot> s(P->ntrees);
+  for (int32_t t = 0; t < P->ntrees; ++t) {
+    Slot& x = s[t];
+    std::memset(&x, 0, sizeof(Slot));
+    x.B = io[t].B; x.ldb = io[t].ldb;
+    x.C = io[t].C; x.ldc = io[t].ldc;
+    x.Y = Y ? Y[t] : io[t].C;
+    x.ldy = Y ? io[t].ldb : io[t].ldc;
+    x.alpha = alpha; x.beta = beta;
+    x.ws = P->mv_ws.p; x.ldws = P->ws_mv;
+    x.r = (int32_t)io[t].r;
+    x.colnorm2 = colnorm2 ? colnorm2 + cn_off[t] : nullptr;
+    x.err = P->d_err;
+  }
+  CUDA_TRY(table.upload(s, st));
+  run_matvec(P, table.dev.p, st);
+  CUDA_TRY(cudaGetLastError());
+  return HSS_OK;
+}
+
+template <typename T>
+int factor_impl(hss_factor_s* f, cudaStream_t st) {
+  hss_plan_s* P = f->plan;
+  std::vector<Slot> s(P->ntrees);
+  for (auto& x : s) {
+    std::memset(&x, 0, sizeof(Slot));
+    x.fbase = f->d_fac;
+    x.err = P->d_err;
+  }
+  CUDA_TRY(f->fac_slots.upload(s, st));
+  run_factor<T>(P, f->fac_slots.dev.p, st);
+  CUDA_TRY(cudaGetLastError());
+  return HSS_OK;
+}
+
+template <typename T>
+int solve_pass(hss_factor_s* f, const std::vector<Cols>& io, const double* scale,
+               const int64_t* off, int mode, cudaStream_t st) {
+  SlotTable& table = mode ? f->sv_slots_ref : f->sv_slots;
+  hss_plan_s* P = f->plan;
+  int64_t rmax = 0;
+  for (auto& c : io) rmax = std::max(rmax, c.r);
+  if (rmax == 0) return HSS_OK;
+  CUDA_TRY(f->sv_ws.ensure((size_t)P->ws_sv * rmax * sizeof(T)));
+  std::vector<Slot> s(P->ntrees);
+  for (int32_t t = 0; t < P->ntrees; ++t) {
+    Slot& x = s[t];
+    std::memset(&x, 0, sizeof(Slot));
+    x.B = io[t].B; x.ldb = io[t].ldb;
+    x.C = io[t].C; x.ldc = io[t].ldc;
+    x.ws = f->sv_ws.p; x.ldws = P->ws_sv;
+    x.fbase = f->d_fac;
+    x.colscale = scale ? scale + off[t] : nullptr;
+    x.r = (int32_t)io[t].r;
+    x.mode = mode;
+    x.err = P->d_err;
+  }
+  CUDA_TRY(table.upload(s, st));
+  run_solve<T>(P, table.dev.p, st);
+  CUDA_TRY(cudaGetLastError());
+  return HSS_OK;
+}
+
+int read_dev_err(hss_plan_s* P, cudaStream_t st) {
+  int32_t e = 0;
+  CUDA_TRY(cudaMemcpyAsync(&e, P->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (e == DEV_SINGULAR) {
+    cudaMemsetAsync(P->d_err, 0, sizeof(int32_t), st);
+    return fail(HSS_ERR_SINGULAR, "root block of the ULV factorization is singular");
+  }
+  return HSS_OK;
+}
+
+int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t maxit,
+               hss_solve_stats* stats, cudaStream_t st) {
+  hss_plan_s* P = f->plan;
+  int rc = check_cols(P, io, true);
+  if (rc) return rc;
+  const bool fp32 = f->prec == HSS_PREC_FP32;
+  const bool refine = fp32 || tol > 0.0;
+  if (stats) { stats->iterations = 0; stats->converged = refine ? 0 : 1; stats->residual = -1.0; }
+  std::vector<int64_t> off(P->ntrees + 1, 0), roff(P->ntrees + 1, 0);
+  for (int32_t t = 0; t < P->ntrees; ++t) {
+    off[t + 1] = off[t] + io[t].r;
+    roff[t + 1] = roff[t] + io[t].r * P->tree_m[t];
+  }
+  const int64_t rtot = off[P->ntrees];
+  if (rtot == 0) { if (stats) stats->converged = 1; return HSS_OK; }
+  const double* scale = nullptr;
+  if (refine) {
+    CUDA_TRY(f->bn2.ensure(rtot));
+    CUDA_TRY(f->rn2.ensure(rtot));
+    CUDA_TRY(f->scale.ensure(rtot));
+    CUDA_TRY(f->R.ensure(std::max<int64_t>(roff[P->ntrees], 1)));
+    CUDA_TRY(f->h_bn2.ensure(rtot));
+    CUDA_TRY(f->h_rn2.ensure(rtot));
+    CUDA_TRY(cudaMemsetAsync(f->bn2.p, 0, rtot * sizeof(double), st));
+    for (int32_t t = 0; t < P->ntrees; ++t) {
+      launch_colnorm2(io[t].B, io[t].ldb, P->tree_m[t], io[t].r, f->bn2.p + off[t], st);
+      ++g_launches;
+    }
+    if (fp32) {
+      launch_sqrt_scale(f->bn2.p, f->scale.p, rtot, st);
+      ++g_launches;
+      scale = f->scale.p;
+    }
+    CUDA_TRY(cudaMemcpyAsync(f->h_bn2.p, f->bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  rc = fp32 ? solve_pass<float>(f, io, scale, off.data(), 0, st)
+            : solve_pass<double>(f, io, scale, off.data(), 0, st);
+  if (rc) return rc;
+  if (!refine) return HSS_OK;
+  // iterative refinement: r = b - A x (FP64 HSS product), x += A_f^{-1} r
+  std::vector<Cols> rio(P->ntrees), xin(P->ntrees);
+  std::vector<const double*> Y(P->ntrees);
+  for (int32_t t = 0; t < P->ntrees; ++t) {
+    xin[t] = Cols{io[t].C, io[t].ldc, io[t].r, f->R.p + roff[t], P->tree_m[t]};
+    rio[t] = Cols{f->R.p + roff[t], P->tree_m[t], io[t].r, io[t].C, io[t].ldc};
+    Y[t] = io[t].B;
+  }
+  // the product's beta term reads B with B's leading dimension
+  std::vector<Cols> mvio(P->ntrees);
+  for (int32_t t = 0; t < P->ntrees; ++t) mvio[t] = xin[t];
+  double res = 0.0;
+  for (int32_t it = 0;; ++it) {
+    CUDA_TRY(cudaMemsetAsync(f->rn2.p, 0, rtot * sizeof(double), st));
+    {
+      // R = -A x + B
+      int64_t rmax = 0;
+      for (auto& c : mvio) rmax = std::max(rmax, c.r);
+      CUDA_TRY(P->mv_ws.ensure((size_t)P->ws_mv * rmax));
+      std::vector<Slot> s(P->ntrees);
+      for (int32_t t = 0; t < P->ntrees; ++t) {
+        Slot& x = s[t];
+        std::memset(&x, 0, sizeof(Slot));
+        x.B = mvio[t].B; x.ldb = mvio[t].ldb;
+        x.C = mvio[t].C; x.ldc = mvio[t].ldc;
+        x.Y = io[t].B; x.ldy = io[t].ldb;
+        x.alpha = -1.0; x.beta = 1.0;
+        x.ws = P->mv_ws.p; x.ldws = P->ws_mv;
+        x.r = (int32_t)mvio[t].r;
+        x.colnorm2 = f->rn2.p + off[t];
+        x.err = P->d_err;
+      }
+      CUDA_TRY(f->mv_slots.upload(s, st));
+      run_matvec(P, f->mv_slots.dev.p, st);
+      CUDA_TRY(cudaGetLastError());
+    }
+    CUDA_TRY(cudaMemcpyAsync(f->h_rn2.p, f->rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    res = 0.0;
+    for (int64_t j = 0; j < rtot; ++j) {
+      const double bn = std::sqrt(f->h_bn2.p[j]);
+      const double rn = std::sqrt(f->h_rn2.p[j]);
+      const double rel = bn > 0.0 ? rn / bn : rn;
+      if (!(rel <= res)) res = rel;   // NaN propagates
+    }
+    if (stats) { stats->iterations = it; stats->residual = res; }
+    if (res <= tol) {
+      if (stats) stats->converged = 1;
+      return read_dev_err(P, st);
+    }
+    if (it >= maxit || std::isnan(res)) break;
+    launch_sqrt_scale(f->rn2.p, f->scale.p, rtot, st);
+    ++g_launches;
+    rc = fp32 ? solve_pass<float>(f, rio, f->scale.p, off.data(), 1, st)
+              : solve_pass<double>(f, rio, f->scale.p, off.data(), 1, st);
+    if (rc) return rc;
+  }
+  rc = read_dev_err(P, st);
+  if (rc) return rc;
+  return fail(HSS_ERR_NO_CONVERGENCE, "iterative refinement did not reach the tolerance (residual " +
+                                          std::to_string(res) + ")");
+}
+
+int copy_in(DBuf<double>& d, const double* h, int64_t rows, int64_t ld, int64_t r, cudaStream_t st) {
+  CUDA_TRY(d.ensure((size_t)std::max<int64_t>(rows * r, 1)));
+  if (rows * r > 0)
+    CUDA_TRY(cudaMemcpy2DAsync(d.p, rows * sizeof(double), h, ld * sizeof(double), rows * sizeof(double),
+                               r, cudaMemcpyHostToDevice, st));
+  return HSS_OK;
+}
+
+int copy_out(double* h, int64_t ld, const double* d, int64_t rows, int64_t r, cudaStream_t st) {
+  if (rows * r > 0)
+    CUDA_TRY(cudaMemcpy2DAsync(h, ld * sizeof(double), d, rows * sizeof(double), rows * sizeof(double), r,
+                               cudaMemcpyDeviceToHost, st));
+  return HSS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+const char* hss_last_error(void) { return g_err.c_str(); }
+int32_t hss_version(void) { return 1; }
+
+int hss_create(int64_t nnodes, const int64_t* nodes, const double* packed, int64_t npacked,
+               hss_handle* out) {
+  if (!out) return fail(HSS_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  auto* P = new hss_plan_s();
+  int rc = build_plan(P, {TreeIn{nnodes, nodes, packed, npacked}});
+  if (rc) { delete P; return rc; }
+  *out = P;
+  return HSS_OK;
+}
+
+int hss_create_batch(int32_t count, const int64_t* nnodes, const int64_t* const* nodes,
+                     const double* const* packed, const int64_t* npacked, hss_handle* out) {
+  if (!out || count <= 0 || !nnodes || !nodes || !packed || !npacked)
+    return fail(HSS_ERR_INVALID, "bad batch arguments");
+  *out = nullptr;
+  std::vector<TreeIn> trees;
+  for (int32_t i = 0; i < count; ++i) trees.push_back(TreeIn{nnodes[i], nodes[i], packed[i], npacked[i]});
+  auto* P = new hss_plan_s();
+  int rc = build_plan(P, trees);
+  if (rc) { delete P; return rc; }
+  *out = P;
+  return HSS_OK;
+}
+
+int hss_inspect(int64_t nnodes, const int64_t* nodes, int64_t npacked, int64_t* info) {
+  hss_plan_s P;
+  std::vector<GenOffsets> go;
+  std::vector<Task> tasks;
+  std::vector<int64_t> gbases;
+  int rc = layout_plan(&P, {TreeIn{nnodes, nodes, nullptr, npacked}}, go, tasks, gbases);
+  if (rc) return rc;
+  if (info)
+    for (int64_t i = 0; i < nnodes; ++i) {
+      const Node& x = P.nodes[i];
+      const int64_t v[HSS_INFO_FIELDS] = {x.depth, x.height, x.row0, x.col0, x.m, x.n, x.ku,
+                                          x.kv, x.k, x.mk, x.nk, x.leaf, x.tree};
+      std::memcpy(info + i * HSS_INFO_FIELDS, v, sizeof(v));
+    }
+  return HSS_OK;
+}
+
+int hss_destroy(hss_handle h) {
+  delete h;
+  return HSS_OK;
+}
+
+int hss_size(hss_handle h, int32_t tree, int64_t* m, int64_t* n) {
+  if (!h || tree < 0 || tree >= h->ntrees) return fail(HSS_ERR_INVALID, "bad handle or tree");
+  if (m) *m = h->tree_m[tree];
+  if (n) *n = h->tree_n[tree];
+  return HSS_OK;
+}
+
+int hss_ntrees(hss_handle h, int32_t* count) {
+  if (!h || !count) return fail(HSS_ERR_INVALID, "bad handle");
+  *count = h->ntrees;
+  return HSS_OK;
+}
+
+int hss_node_info(hss_handle h, int64_t node, int64_t* f) {
+  if (!h || !f || node < 0 || node >= (int64_t)h->nodes.size()) return fail(HSS_ERR_INVALID, "bad node");
+  const Node& x = h->nodes[node];
+  const int64_t v[HSS_INFO_FIELDS] = {x.depth, x.height, x.row0, x.col0, x.m, x.n, x.ku,
+                                      x.kv, x.k, x.mk, x.nk, x.leaf, x.tree};
+  std::memcpy(f, v, sizeof(v));
+  return HSS_OK;
+}
+
+int hss_ulv_cols(hss_handle h, int64_t node, int64_t* cols, int64_t cap, int64_t* len) {
+  if (!h || !len || node < 0 || node >= (int64_t)h->nodes.size()) return fail(HSS_ERR_INVALID, "bad node");
+  // cols of a leaf: its column range; of a branch: the un-eliminated tails of
+  // its children (src/ulvfactor.jl:62,76)
+  std::vector<int64_t> out;
+  std::vector<int64_t> tmp;
+  struct Rec {
+    const std::vector<Node>& N;
+    void run(int32_t i, std::vector<int64_t>& o) const {
+      const Node& x = N[i];
+      if (x.leaf) {
+        for (int64_t c = 0; c < x.n; ++c) o.push_back(x.col0 + c);
+        return;
+      }
+      std::vector<int64_t> a, b;
+      run(x.left, a);
+      run(x.right, b);
+      const Node& c1 = N[x.left];
+      const Node& c2 = N[x.right];
+      o.insert(o.end(), a.begin() + c1.nk, a.end());
+      o.insert(o.end(), b.begin() + c2.nk, b.end());
+    }
+  } rec{h->nodes};
+  rec.run((int32_t)node, out);
+  *len = (int64_t)out.size();
+  if (cols) std::memcpy(cols, out.data(), std::min<int64_t>(cap, *len) * sizeof(int64_t));
+  return HSS_OK;
+}
+
+int hss_matmul(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC, int64_t ldc,
+               double alpha, double beta, void* stream) {
+  if (!h) return fail(HSS_ERR_INVALID, "null handle");
+  if (h->ntrees != 1) return fail(HSS_ERR_INVALID, "use hss_matmul_batch for a forest");
+  std::vector<Cols> io{Cols{dB, ldb, r, dC, ldc}};
+  int rc = check_cols(h, io, false);
+  if (rc) return rc;
+  return matmul_impl(h, io, alpha, beta, (cudaStream_t)stream, nullptr, nullptr, nullptr, h->mv_slots);
+}
+
+int hss_matmul_batch(hss_handle h, const double* const* dB, const int64_t* ldb, const int64_t* r,
+                     double* const* dC, const int64_t* ldc, double alpha, double beta, void* stream) {
+  if (!h || !dB || !ldb || !r || !dC || !ldc) return fail(HSS_ERR_INVALID, "bad batch arguments");
+  std::vector<Cols> io(h->ntrees);
+  for (int32_t t = 0; t < h->ntrees; ++t) io[t] = Cols{dB[t], ldb[t], r[t], dC[t], ldc[t]};
+  int rc = check_cols(h, io, false);
+  if (rc) return rc;
+  return matmul_impl(h, io, alpha, beta, (cudaStream_t)stream, nullptr, nullptr, nullptr, h->mv_slots);
+}
+
+int hss_matmul_host(hss_handle h, const double* B, int64_t ldb, int64_t r, double* C, int64_t ldc,
+                    double alpha, double beta) {
+  if (!h) return fail(HSS_ERR_INVALID, "null handle");
+  if (h->ntrees != 1) return fail(HSS_ERR_INVALID, "host product takes a single matrix");
+  if (r == 0) return HSS_OK;
+  const int64_t m = h->tree_m[0], n = h->tree_n[0];
+  std::vector<Cols> io{Cols{B, ldb, r, C, ldc}};
+  int rc = check_cols(h, io, false);
+  if (rc) return rc;
+  cudaStream_t st = 0;
+  if ((rc = copy_in(h->hB, B, n, ldb, r, st))) return rc;
+  CUDA_TRY(h->hC.ensure((size_t)m * r));
+  if (beta != 0.0 && (rc = copy_in(h->hC, C, m, ldc, r, st))) return rc;
+  std::vector<Cols> dio{Cols{h->hB.p, n, r, h->hC.p, m}};
+  if ((rc = matmul_impl(h, dio, alpha, beta, st, nullptr, nullptr, nullptr, h->mv_slots))) return rc;
+  if ((rc = copy_out(C, ldc, h->hC.p, m, r, st))) return rc;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return HSS_OK;
+}
+
+int hss_ulvfactor(hss_handle h, int32_t precision, hss_factor* out, void* stream) {
+  if (!h || !out) return fail(HSS_ERR_INVALID, "null handle");
+  if (precision != HSS_PREC_FP64 && precision != HSS_PREC_FP32)
+    return fail(HSS_ERR_INVALID, "precision must be HSS_PREC_FP64 or HSS_PREC_FP32");
+  *out = nullptr;
+  auto* f = new hss_factor_s();
+  f->plan = h;
+  f->prec = precision;
+  const size_t es = precision == HSS_PREC_FP32 ? sizeof(float) : sizeof(double);
+  f->fac_bytes = (size_t)h->fac_elems * es;
+  cudaError_t e = cudaMalloc(&f->d_fac, f->fac_bytes);
+  if (e != cudaSuccess) {
+    delete f;
+    return cuda_fail(e, "cudaMalloc(factor)");
+  }
+  int rc = precision == HSS_PREC_FP32 ? factor_impl<float>(f, (cudaStream_t)stream)
+                                      : factor_impl<double>(f, (cudaStream_t)stream);
+  if (rc) { delete f; return rc; }
+  *out = f;
+  return HSS_OK;
+}
+
+int hss_factor_destroy(hss_factor f) {
+  delete f;
+  return HSS_OK;
+}
+
+int hss_ulvrefactor(hss_factor f, void* stream) {
+  if (!f) return fail(HSS_ERR_INVALID, "null factor");
+  return f->prec == HSS_PREC_FP32 ? factor_impl<float>(f, (cudaStream_t)stream)
+                                  : factor_impl<double>(f, (cudaStream_t)stream);
+}
+
+int hss_trace_begin(int32_t kind) {
+  if (kind < -1 || kind >= HSS_TRACE_KINDS) return fail(HSS_ERR_INVALID, "unknown trace kind");
+  g_trace.kind = kind;
+  g_trace.used = 0;
+  return HSS_OK;
+}
+
+int hss_trace_end(double* total_ms, int64_t* launches) {
+  double tot = 0.0;
+  int64_t n = 0;
+  for (size_t i = 0; i + 1 < g_trace.used; i += 2) {
+    float ms = 0.f;
+    CUDA_TRY(cudaEventSynchronize(g_trace.pool[i + 1]));
+    CUDA_TRY(cudaEventElapsedTime(&ms, g_trace.pool[i], g_trace.pool[i + 1]));
+    tot += ms;
+    ++n;
+  }
+  g_trace.kind = -1;
+  g_trace.used = 0;
+  if (total_ms) *total_ms = tot;
+  if (launches) *launches = n;
+  return HSS_OK;
+}
+
+int64_t hss_launch_counter(void) { return g_launches; }
+
+int hss_factor_bytes(hss_factor f, int64_t* bytes) {
+  if (!f || !bytes) return fail(HSS_ERR_INVALID, "null factor");
+  *bytes = (int64_t)f->fac_bytes;
+  return HSS_OK;
+}
+
+int hss_ulvsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double* dX, int64_t ldx,
+                 double tol, int32_t maxit, hss_solve_stats* stats, void* stream) {
+  if (!f) return fail(HSS_ERR_INVALID, "null factor");
+  if (f->plan->ntrees != 1) return fail(HSS_ERR_INVALID, "use hss_ulvsolve_batch for a forest");
+  return solve_impl(f, {Cols{dB, ldb, r, dX, ldx}}, tol, maxit, stats, (cudaStream_t)stream);
+}
+
+int hss_ulvsolve_batch(hss_factor f, const double* const* dB, const int64_t* ldb, const int64_t* r,
+                       double* const* dX, const int64_t* ldx, double tol, int32_t maxit,
+                       hss_solve_stats* stats, void* stream) {
+  if (!f || !dB || !ldb || !r || !dX || !ldx) return fail(HSS_ERR_INVALID, "bad batch arguments");
+  std::vector<Cols> io(f->plan->ntrees);
+  for (int32_t t = 0; t < f->plan->ntrees; ++t) io[t] = Cols{dB[t], ldb[t], r[t], dX[t], ldx[t]};
+  return solve_impl(f, io, tol, maxit, stats, (cudaStream_t)stream);
+}
+
+int hss_ulvsolve_host(hss_factor f, const double* B, int64_t ldb, int64_t r, double* X, int64_t ldx,
+                      double tol, int32_t maxit, hss_solve_stats* stats) {
+  if (!f) return fail(HSS_ERR_INVALID, "null factor");
+  hss_plan_s* P = f->plan;
+  if (P->ntrees != 1) return fail(HSS_ERR_INVALID, "host solve takes a single matrix");
+  const int64_t m = P->tree_m[0], n = P->tree_n[0];
+  std::vector<Cols> io{Cols{B, ldb, r, X, ldx}};
+  int rc = check_cols(P, io, true);
+  if (rc) return rc;
+  if (r == 0) return HSS_OK;
+  cudaStream_t st = 0;
+  if ((rc = copy_in(f->hB, B, m, ldb, r, st))) return rc;
+  CUDA_TRY(f->hX.ensure((size_t)n * r));
+  rc = solve_impl(f, {Cols{f->hB.p, m, r, f->hX.p, n}}, tol, maxit, stats, st);
+  if (rc && rc != HSS_ERR_NO_CONVERGENCE) return rc;
+  int rc2 = copy_out(X, ldx, f->hX.p, n, r, st);
+  if (rc2) return rc2;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (!rc) rc = read_dev_err(P, st);
+  return rc;
+}
+
+int hss_ulvfactsolve_host(hss_handle h, int32_t precision, const double* B, int64_t ldb, int64_t r,
+                          double* X, int64_t ldx, double tol, int32_t maxit, hss_solve_stats* stats) {
+  if (!h) return fail(HSS_ERR_INVALID, "null handle");
+  if (precision != HSS_PREC_FP64 && precision != HSS_PREC_FP32)
+    return fail(HSS_ERR_INVALID, "precision must be HSS_PREC_FP64 or HSS_PREC_FP32");
+  // the factorization is recomputed on every call; only its storage is reused
+  int rc;
+  hss_factor& f = h->fused[precision];
+  if (f == nullptr) rc = hss_ulvfactor(h, precision, &f, nullptr);
+  else rc = hss_ulvrefactor(f, nullptr);
+  if (rc) return rc;
+  return hss_ulvsolve_host(f, B, ldb, r, X, ldx, tol, maxit, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,62 @@
+// Internal data layout shared by the host plan code and the sm_103a kernels.
+//
+// A plan is a forest of HSS generator trees held on one GPU:
+//   * all generators of all trees live in one FP64 buffer (the packed layout
+//     the caller uploads, column-major blocks);
+//   * a device array of `Node` descriptors (one per tree node) carries sizes,
+//     generator pointers and workspace / factor-storage offsets;
+//   * task lists group nodes by height (post-order sweeps: product upsweep,
+//     ULV factor, ULV solve upward) and by depth (pre-order sweeps: product
+//     downsweep, ULV solve downward).  One kernel launch processes one list,
+//     one thread block per node, across every tree of the forest.
+// Per-call data (right-hand sides, outputs, workspace, factor storage) is in
+// a small `Slot` table indexed by Task::slot, so tasks of different plans can
+// be mixed in one launch.
+#pragma once
+#include <cstdint>
+
+namespace hss {
+
+struct Node {
+  int32_t left, right, parent, leaf;   // indices into the same node array; -1 if none
+  int32_t root, depth, height, tree;
+  // ULV reduce-problem sizes (src/ulvfactor.jl:22-57): leaf m x n = D; a branch
+  // holds the merged block of its children's reduced parts (src/ulvfactor.jl:74-79).
+  int32_t m, n, ku, kv;                // ku/kv = gensize (src/hssmatrix.jl:254-262)
+  int32_t k, mk, nk, mr;               // k=min(ku,m), mk=m-k, nk=min(mk,n), mr=m-mk
+  int32_t nr, gm, gn, lower_u;         // nr=n-nk; gm x gn = rows x cols of the subtree
+                                       // lower_u: 1 if the reduced U is tril (QL done)
+  int64_t row0, col0;                  // first row / column of the subtree
+  const double *D, *U, *V;             // leaf generators (ld = m, m, n)
+  const double *B12, *B21, *R1, *R2, *W1, *W2;   // branch generators
+  // workspace row offsets: product Z (kv rows), F (ku rows);
+  // solve b (m rows), u (kv rows), x (n rows)
+  int64_t wz, wf, wb, wu, wx;
+  // factor storage element offsets: D (m x n; root: LU), U (m x ku),
+  // V (n x kv), tau_ql (k), tau_lq (mk), T12 (mr1 x kv2), T21 (mr2 x kv1), pivots (root)
+  int64_t fD, fU, fV, ftq, ftl, fT12, fT21, fpiv;
+};
+
+struct Task {
+  const Node* nodes;   // node array the index refers to
+  int32_t node;
+  int32_t slot;
+};
+
+struct Slot {
+  const double* B;  int64_t ldb;      // product input / solve right-hand side
+  double* C;        int64_t ldc;      // product output / solve output
+  const double* Y;  int64_t ldy;      // product beta-term input (may alias C)
+  double alpha, beta;
+  void* ws;         int64_t ldws;     // workspace (double for products, T for solves)
+  void* fbase;                        // factor storage (T)
+  const double* colscale;             // solve: rhs column j is divided by colscale[j]
+  double* colnorm2;                   // product: += sum_i C(i,j)^2 per column (nullable)
+  int32_t r, mode;                    // solve: mode 0 x = s*d, 1 x += s*d
+  int32_t* err;                       // device status word (nullable)
+};
+
+// device status codes written into Slot::err
+enum { DEV_OK = 0, DEV_SINGULAR = 1, DEV_BAD = 2 };
+
+}  // namespace hss

@@ -1,0 +1,29 @@
+// Kernel launch wrappers (implemented in hss_kernels.cu, used by hss_capi.cpp).
+#pragma once
+#include <cuda_runtime.h>
+#include "hss_internal.h"
+
+namespace hss {
+
+// HSS x dense product (reference src/matmul.jl:18-62), one launch per list.
+void launch_mv_leaf(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+void launch_mv_up(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+void launch_mv_down(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+void launch_mv_leaf_final(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+
+// ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
+template <typename T>
+void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,
+                       cudaStream_t st);
+template <typename T>
+void launch_ulv_solve_up(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+template <typename T>
+void launch_ulv_solve_down(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+
+// out[j] += sum_i B(i,j)^2 for i < n, j < r (out must be zeroed by the caller).
+void launch_colnorm2(const double* B, int64_t ldb, int64_t n, int64_t r, double* out,
+                     cudaStream_t st);
+// s[j] = sqrt(n2[j]) (1 where n2[j] == 0).
+void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st);
+
+}  // namespace hss

@@ -1,0 +1,275 @@
+"""GPU arithmetic behind the reference's operators, through the C ABI.
+
+* ``matmul(hssA, B)``         -- ``*(hssA, B)`` (src/matmul.jl:13-15)
+* ``mul(C, hssA, B, a, b)``   -- ``mul!(C, hssA, B, a, b)`` (src/matmul.jl:18-28)
+* ``ulvfactsolve(hssA, b)``   -- ``ulvfactsolve`` (src/ulvfactor.jl:10-19), plain FP64
+* ``ldiv(hssA, b)``           -- ``hssA \\ b`` (src/hssmatrix.jl:234)
+* ``ulvfactor(hssA, prec)``   -- resident factorization (new; the reference's
+                                 factor-only reduction is src/ulvdivide.jl:58-85)
+
+Host arrays are column-major float64; 1-D inputs are treated as n x 1 like the
+reference's vector methods.  Every call runs the CUDA library; if it cannot be
+loaded the call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr, iptr
+from .packing import pack
+
+PREC = {"fp64": _lib.HSS_PREC_FP64, "fp32": _lib.HSS_PREC_FP32,
+        _lib.HSS_PREC_FP64: _lib.HSS_PREC_FP64, _lib.HSS_PREC_FP32: _lib.HSS_PREC_FP32}
+
+
+def _ptr(x):
+    """Device pointer of a torch tensor / int / None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream
+
+
+def _as_cols(B, rows):
+    B = np.asarray(B, dtype=np.float64)
+    vec = B.ndim == 1
+    if vec:
+        B = B.reshape(-1, 1)
+    if B.ndim != 2:
+        raise ValueError("expected a vector or a matrix")
+    if B.shape[0] != rows:
+        raise ValueError(f"DimensionMismatch: expected {rows} rows, got {B.shape[0]}")
+    return np.asfortranarray(B), vec
+
+
+class DeviceHss:
+    """One generator tree (or a forest, via ``from_trees``) resident on the GPU."""
+
+    def __init__(self, h=None, *, _handle=None, _ntrees=1):
+        self.lib = _lib.load()
+        self.handle = C.c_void_p()
+        if _handle is not None:
+            self.handle = _handle
+        else:
+            table, packed = pack(h)
+            check(self.lib.hss_create(table.shape[0], iptr(table), dptr(packed), packed.size,
+                                      C.byref(self.handle)))
+        n = C.c_int32()
+        check(self.lib.hss_ntrees(self.handle, C.byref(n)))
+        self.ntrees = n.value
+        self.sizes = []
+        for t in range(self.ntrees):
+            m, nn = C.c_int64(), C.c_int64()
+            check(self.lib.hss_size(self.handle, t, C.byref(m), C.byref(nn)))
+            self.sizes.append((m.value, nn.value))
+        self.m, self.n = self.sizes[0]
+
+    @classmethod
+    def from_trees(cls, trees):
+        """A forest of independent matrices in one plan (the batched form)."""
+        lib = _lib.load()
+        packs = [pack(h) for h in trees]
+        cnt = len(packs)
+        nn = np.array([t.shape[0] for t, _p in packs], dtype=np.int64)
+        npk = np.array([p.size for _t, p in packs], dtype=np.int64)
+        tabs = (_lib.PI64 * cnt)(*[iptr(t) for t, _p in packs])
+        pks = (_lib.PD * cnt)(*[dptr(p) for _t, p in packs])
+        handle = C.c_void_p()
+        check(lib.hss_create_batch(cnt, iptr(nn), tabs, pks, iptr(npk), C.byref(handle)))
+        obj = cls(_handle=handle)
+        obj._keep = packs
+        return obj
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.lib.hss_destroy(self.handle)
+                self.handle = C.c_void_p()
+        except Exception:
+            pass
+
+    # -- bookkeeping ------------------------------------------------------
+    def node_info(self, node):
+        f = np.zeros(_lib.INFO_FIELDS, dtype=np.int64)
+        check(self.lib.hss_node_info(self.handle, node, iptr(f)))
+        keys = ["depth", "height", "row0", "col0", "m", "n", "ku", "kv", "k", "mk", "nk", "leaf", "tree"]
+        return dict(zip(keys, (int(v) for v in f)))
+
+    def ulv_cols(self, node):
+        ln = C.c_int64()
+        check(self.lib.hss_ulv_cols(self.handle, node, None, 0, C.byref(ln)))
+        out = np.zeros(max(ln.value, 1), dtype=np.int64)
+        check(self.lib.hss_ulv_cols(self.handle, node, iptr(out), out.size, C.byref(ln)))
+        return out[:ln.value]
+
+    # -- products -----------------------------------------------------------
+    def matmul_host(self, B, alpha=1.0, beta=0.0, C_=None):
+        B, vec = _as_cols(B, self.n)
+        r = B.shape[1]
+        if C_ is None:
+            out = np.zeros((self.m, r), order="F")
+            beta = 0.0
+        else:
+            out = C_
+        check(self.lib.hss_matmul_host(self.handle, dptr(B), B.shape[0], r, dptr(out),
+                                       out.shape[0], float(alpha), float(beta)))
+        return out.reshape(-1) if vec else out
+
+    def matmul_device(self, dB, ldb, r, dC, ldc, alpha=1.0, beta=0.0, stream=None):
+        check(self.lib.hss_matmul(self.handle, _ptr(dB), ldb, r, _ptr(dC), ldc, float(alpha),
+                                  float(beta), _stream(stream)))
+
+    def matmul_batch_device(self, dBs, ldbs, rs, dCs, ldcs, alpha=1.0, beta=0.0, stream=None):
+        k = self.ntrees
+        B = (C.c_void_p * k)(*[_ptr(x) for x in dBs])
+        Cc = (C.c_void_p * k)(*[_ptr(x) for x in dCs])
+        ldb = np.asarray(ldbs, np.int64)
+        ldc = np.asarray(ldcs, np.int64)
+        r = np.asarray(rs, np.int64)
+        check(self.lib.hss_matmul_batch(self.handle, B, iptr(ldb), iptr(r), Cc, iptr(ldc),
+                                        float(alpha), float(beta), _stream(stream)))
+
+    # -- ULV ------------------------------------------------------------------
+    def ulvfactor(self, precision="fp64", stream=None):
+        return UlvFactor(self, PREC[precision], stream)
+
+
+class UlvFactor:
+    """A resident ULV factorization (FP64, or FP32 refined in FP64)."""
+
+    def __init__(self, dev: DeviceHss, prec: int, stream=None):
+        self.dev = dev
+        self.lib = dev.lib
+        self.prec = prec
+        self.handle = C.c_void_p()
+        check(self.lib.hss_ulvfactor(dev.handle, prec, C.byref(self.handle), _stream(stream)))
+        self.stats = _lib.SolveStats()
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.lib.hss_factor_destroy(self.handle)
+                self.handle = C.c_void_p()
+        except Exception:
+            pass
+
+    def refactor(self, stream=None):
+        """Recompute the factorization in place (no allocation)."""
+        check(self.lib.hss_ulvrefactor(self.handle, _stream(stream)))
+
+    def nbytes(self):
+        b = C.c_int64()
+        check(self.lib.hss_factor_bytes(self.handle, C.byref(b)))
+        return b.value
+
+    def default_tol(self):
+        return 1e-10 if self.prec == _lib.HSS_PREC_FP32 else 0.0
+
+    def solve(self, b, tol=None, maxit=10):
+        """x = A \\ b with host arrays."""
+        tol = self.default_tol() if tol is None else tol
+        b, vec = _as_cols(b, self.dev.m)
+        r = b.shape[1]
+        x = np.zeros((self.dev.n, r), order="F")
+        check(self.lib.hss_ulvsolve_host(self.handle, dptr(b), b.shape[0], r, dptr(x), x.shape[0],
+                                         float(tol), int(maxit), C.byref(self.stats)))
+        return x.reshape(-1) if vec else x
+
+    def solve_device(self, dB, ldb, r, dX, ldx, tol=None, maxit=10, stream=None):
+        tol = self.default_tol() if tol is None else tol
+        check(self.lib.hss_ulvsolve(self.handle, _ptr(dB), ldb, r, _ptr(dX), ldx, float(tol),
+                                    int(maxit), C.byref(self.stats), _stream(stream)))
+        return self.stats
+
+    def solve_batch_device(self, dBs, ldbs, rs, dXs, ldxs, tol=None, maxit=10, stream=None):
+        tol = self.default_tol() if tol is None else tol
+        k = self.dev.ntrees
+        B = (C.c_void_p * k)(*[_ptr(x) for x in dBs])
+        X = (C.c_void_p * k)(*[_ptr(x) for x in dXs])
+        ldb = np.asarray(ldbs, np.int64)
+        ldx = np.asarray(ldxs, np.int64)
+        r = np.asarray(rs, np.int64)
+        check(self.lib.hss_ulvsolve_batch(self.handle, B, iptr(ldb), iptr(r), X, iptr(ldx),
+                                          float(tol), int(maxit), C.byref(self.stats),
+                                          _stream(stream)))
+        return self.stats
+
+
+def trace_begin(kind):
+    """Bracket every launch of one kernel kind (``_lib.TRACE`` key) with CUDA events."""
+    lib = _lib.load()
+    check(lib.hss_trace_begin(_lib.TRACE[kind] if isinstance(kind, str) else int(kind)))
+
+
+def trace_end():
+    """(summed device milliseconds, number of launches) since ``trace_begin``."""
+    lib = _lib.load()
+    ms, n = C.c_double(), C.c_int64()
+    check(lib.hss_trace_end(C.byref(ms), C.byref(n)))
+    return ms.value, n.value
+
+
+def launch_counter():
+    return _lib.load().hss_launch_counter()
+
+
+# ---------------------------------------------------------------------------
+# reference-shaped entry points
+# ---------------------------------------------------------------------------
+
+
+def matmul(hssA, B):
+    """``hssA * B`` (src/matmul.jl:13-15)."""
+    return hssA.device().matmul_host(B)
+
+
+def mul(C_, hssA, B, alpha=1.0, beta=0.0):
+    """``mul!(C, hssA, B, alpha, beta)`` (src/matmul.jl:18-28): overwrites C."""
+    dev = hssA.device()
+    B, _vec = _as_cols(B, dev.n)
+    if not (isinstance(C_, np.ndarray) and C_.dtype == np.float64 and C_.flags.f_contiguous):
+        raise ValueError("C must be a column-major float64 array")
+    Cv = C_.reshape(C_.shape[0], -1, order="F")
+    if Cv.shape != (dev.m, B.shape[1]):
+        raise ValueError("Dimensions of C don't match up with A and B.")
+    dev.matmul_host(B, alpha, beta, Cv)
+    return C_
+
+
+def ulvfactor(hssA, precision="fp64"):
+    """Resident ULV factorization of ``hssA``."""
+    return hssA.device().ulvfactor(precision)
+
+
+def ulvfactsolve(hssA, b):
+    """``ulvfactsolve(hssA, b)`` (src/ulvfactor.jl:10): FP64 factor + solve."""
+    return ldiv(hssA, b, precision="fp64")
+
+
+def ldiv(hssA, b, precision="fp64", tol=None, maxit=10, stats=None):
+    """``hssA \\ b`` (src/hssmatrix.jl:234).  ``precision='fp32'`` factors in FP32 and
+    refines with FP64 HSS products to ``tol`` (default 1e-10 relative residual)."""
+    dev = hssA.device()
+    prec = PREC[precision]
+    tol = (1e-10 if prec == _lib.HSS_PREC_FP32 else 0.0) if tol is None else tol
+    b, vec = _as_cols(b, dev.m)
+    r = b.shape[1]
+    x = np.zeros((dev.n, r), order="F")
+    st = _lib.SolveStats()
+    check(dev.lib.hss_ulvfactsolve_host(dev.handle, prec, dptr(b), b.shape[0], r, dptr(x), x.shape[0],
+                                        float(tol), int(maxit), C.byref(st)))
+    if stats is not None:
+        stats.update(iterations=st.iterations, converged=bool(st.converged), residual=st.residual)
+    return x.reshape(-1) if vec else x

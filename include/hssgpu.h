@@ -1,0 +1,179 @@
+/*
+ * hssgpu.h -- C ABI of the GB300 (sm_103a) HSS hot path.
+ *
+ * The library holds an HSS matrix's generator tree (D, U, V, R, W, B) on one
+ * GPU as packed FP64 arrays with level-ordered task lists, and runs:
+ *   - the HSS x dense product      (reference: src/matmul.jl:13-62,
+ *                                   `*(hssA, B)` :13, `mul!(C, hssA, B, a, b)` :18),
+ *   - the implicit ULV factorization and solve, split into a resident
+ *     factorization and a solve      (reference: src/ulvfactor.jl:10-107,
+ *                                   `ulvfactsolve` :10, reached by `hssA \ B`,
+ *                                   src/hssmatrix.jl:234; factor-only
+ *                                   reduction src/ulvdivide.jl:58-85),
+ *   - FP32 factorization + FP64 iterative refinement (new; same API),
+ *   - batched forests of independent matrices, and the sampling products of
+ *     randomized compression (reference: src/compression.jl:278-430).
+ *
+ * Conventions (mirroring the Julia reference): matrices are column-major
+ * with an explicit leading dimension; indices are 0-based here.  Every entry
+ * point returns an hss_status; hss_last_error() gives a message.  Device
+ * pointers ("d" prefix) must live on the handle's device; "_host" variants
+ * take host memory and synchronise.  A handle must not be used from two host
+ * threads or two streams at the same time.
+ */
+#ifndef HSSGPU_H
+#define HSSGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  HSS_OK = 0,
+  HSS_ERR_BAD_DIMS = 1,       /* DimensionMismatch / ArgumentError in the reference */
+  HSS_ERR_OOM = 2,
+  HSS_ERR_SINGULAR = 3,       /* root LU hit an exact zero pivot (reference: SingularException) */
+  HSS_ERR_NO_CONVERGENCE = 4, /* refinement did not reach the tolerance in maxit steps */
+  HSS_ERR_TIMEOUT = 5,
+  HSS_ERR_CUDA = 6,
+  HSS_ERR_INVALID = 7         /* null handle, bad argument */
+} hss_status;
+
+typedef enum { HSS_PREC_FP64 = 0, HSS_PREC_FP32 = 1 } hss_precision;
+
+typedef struct hss_plan_s* hss_handle;
+typedef struct hss_factor_s* hss_factor;
+
+/* Node table: one row of HSS_NODE_FIELDS int64 per node, node 0 = root,
+ * children after their parent (any order otherwise).  Field meaning:
+ *   [0] left child (-1 for a leaf)   [1] right child (-1 for a leaf)
+ *   [2] leaf rows m  (branch: 0)     [3] leaf cols n (branch: 0)
+ *   [4] ku: columns of U (leaf) or of R1/R2 (branch); 0 at the root
+ *   [5] kv: columns of V (leaf) or of W1/W2 (branch); 0 at the root
+ *   [6] D  [7] U  [8] V       element offsets into `packed` (leaf)
+ *   [9] B12 [10] B21 [11] R1 [12] R2 [13] W1 [14] W2   (branch; -1 if empty)
+ *   [15] reserved (0)
+ * Block shapes follow the reference's HssMatrix fields (src/hssmatrix.jl:11-67):
+ *   D m x n, U m x ku, V n x kv; B12 ku(left) x kv(right), B21 ku(right) x kv(left),
+ *   R1 ku(left) x ku, R2 ku(right) x ku, W1 kv(left) x kv, W2 kv(right) x kv.  */
+#define HSS_NODE_FIELDS 16
+
+/* Replaces the construction of `HssMatrix` (src/hssmatrix.jl:36-67): uploads a
+ * packed generator tree.  Checks the same dimensions as `checkdims`
+ * (src/hssmatrix.jl:308-322) and returns HSS_ERR_BAD_DIMS otherwise. */
+int hss_create(int64_t nnodes, const int64_t* nodes, const double* packed,
+               int64_t npacked, hss_handle* out);
+
+/* A forest of `count` independent matrices sharing one plan (batched form).
+ * nnodes[i], nodes[i], packed[i], npacked[i] describe matrix i as above. */
+int hss_create_batch(int32_t count, const int64_t* nnodes, const int64_t* const* nodes,
+                     const double* const* packed, const int64_t* npacked, hss_handle* out);
+
+/* Host-only validation of one node table (no GPU needed): the same checks as
+ * hss_create, and on success the per-node bookkeeping of hss_node_info for
+ * every node into info[nnodes * HSS_INFO_FIELDS] (nullable).  Lets a caller
+ * validate a tree before uploading it (reference: `checkdims`,
+ * src/hssmatrix.jl:308-322). */
+int hss_inspect(int64_t nnodes, const int64_t* nodes, int64_t npacked, int64_t* info);
+
+int hss_destroy(hss_handle h);
+
+/* size(hssA) (src/hssmatrix.jl:94) of matrix `tree` of the forest. */
+int hss_size(hss_handle h, int32_t tree, int64_t* m, int64_t* n);
+int hss_ntrees(hss_handle h, int32_t* count);
+
+/* Per-node bookkeeping for bit-exact checks: fields
+ * [0] depth [1] height [2] row0 [3] col0 [4] m [5] n [6] ku [7] kv
+ * [8] k [9] mk [10] nk [11] leaf [12] tree  (ULV reduce-problem sizes). */
+#define HSS_INFO_FIELDS 13
+int hss_node_info(hss_handle h, int64_t node, int64_t* fields);
+
+/* `cols` of node `node` in `_ulvfactsolve!` (src/ulvfactor.jl:62,76), 0-based.
+ * Writes at most cap entries, returns the length in *len. */
+int hss_ulv_cols(hss_handle h, int64_t node, int64_t* cols, int64_t cap, int64_t* len);
+
+/* mul!(C, hssA, B, alpha, beta) (src/matmul.jl:18-28) on the device.
+ * B is n x r (ldb), C is m x r (ldc); stream is a cudaStream_t (NULL = default). */
+int hss_matmul(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC,
+               int64_t ldc, double alpha, double beta, void* stream);
+
+/* Same, with host B and C; copies in, computes, copies out, synchronises. */
+int hss_matmul_host(hss_handle h, const double* B, int64_t ldb, int64_t r, double* C,
+                    int64_t ldc, double alpha, double beta);
+
+/* Batched product over a forest: matrix i uses dB[i], dC[i], r[i] (device). */
+int hss_matmul_batch(hss_handle h, const double* const* dB, const int64_t* ldb,
+                     const int64_t* r, double* const* dC, const int64_t* ldc,
+                     double alpha, double beta, void* stream);
+
+/* ULV factorization (new entry point: the reference only has the fused
+ * `ulvfactsolve`, src/ulvfactor.jl:10; its factor-only reduction is
+ * src/ulvdivide.jl:58-85).  precision = HSS_PREC_FP64 or HSS_PREC_FP32.
+ * Asynchronous on `stream`; errors surface at the next synchronising call. */
+int hss_ulvfactor(hss_handle h, int32_t precision, hss_factor* out, void* stream);
+int hss_factor_destroy(hss_factor f);
+
+/* Recompute an existing factorization in place (same plan and precision),
+ * e.g. after the generators changed or to re-run without allocating. */
+int hss_ulvrefactor(hss_factor f, void* stream);
+
+typedef struct {
+  int32_t iterations;      /* refinement steps taken (0 for a plain solve) */
+  int32_t converged;       /* 1 if every column reached tol */
+  double residual;         /* max over columns of ||b - A x|| / ||b|| (when computed) */
+} hss_solve_stats;
+
+/* x = A \ b with the resident factorization (reference semantics of
+ * `ulvfactsolve`, src/ulvfactor.jl:10-107).  For an FP32 factor the solve is
+ * refined with FP64 HSS products until max_j ||b_j - A x_j|| / ||b_j|| <= tol
+ * or maxit steps (HSS_ERR_NO_CONVERGENCE).  For an FP64 factor tol <= 0 skips
+ * the residual; tol > 0 refines in FP64 the same way.  Device pointers. */
+int hss_ulvsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double* dX,
+                 int64_t ldx, double tol, int32_t maxit, hss_solve_stats* stats,
+                 void* stream);
+int hss_ulvsolve_host(hss_factor f, const double* B, int64_t ldb, int64_t r, double* X,
+                      int64_t ldx, double tol, int32_t maxit, hss_solve_stats* stats);
+
+/* Batched solve over a forest factor: matrix i uses dB[i], dX[i], r[i]. */
+int hss_ulvsolve_batch(hss_factor f, const double* const* dB, const int64_t* ldb,
+                       const int64_t* r, double* const* dX, const int64_t* ldx,
+                       double tol, int32_t maxit, hss_solve_stats* stats, void* stream);
+
+/* `hssA \ B` (src/hssmatrix.jl:234 -> src/ulvfactor.jl:10): factor + solve in
+ * one call with host buffers. */
+int hss_ulvfactsolve_host(hss_handle h, int32_t precision, const double* B, int64_t ldb,
+                          int64_t r, double* X, int64_t ldx, double tol, int32_t maxit,
+                          hss_solve_stats* stats);
+
+/* Device memory held by a factorization (bytes). */
+int hss_factor_bytes(hss_factor f, int64_t* bytes);
+
+/* Profiling aid: bracket every launch of one kernel kind with CUDA events on
+ * its stream (-1 disables), then read the summed device time and the number
+ * of launches (hss_trace_end synchronises on the recorded events). */
+enum {
+  HSS_TRACE_MV_LEAF = 0,      /* leaf D*B and V^T*B          (src/matmul.jl:34,46) */
+  HSS_TRACE_MV_UP = 1,        /* W1^T Z1 + W2^T Z2           (src/matmul.jl:39) */
+  HSS_TRACE_MV_DOWN = 2,      /* B12 Z2 + R1 F, B21 Z1 + R2 F (src/matmul.jl:50-56) */
+  HSS_TRACE_MV_FINAL = 3,     /* leaf C += U F               (src/matmul.jl:47) */
+  HSS_TRACE_FACTOR_LEAF = 4,  /* ULV reduction of the leaves (src/ulvfactor.jl:22-57) */
+  HSS_TRACE_FACTOR_MERGE = 5, /* merge + reduction per level (src/ulvfactor.jl:74-89) */
+  HSS_TRACE_SOLVE_UP = 6,     /* upward solve per level */
+  HSS_TRACE_SOLVE_DOWN = 7,   /* Q^T back-application per level (src/ulvfactor.jl:98-107) */
+  HSS_TRACE_KINDS = 8
+};
+int hss_trace_begin(int32_t kind);
+int hss_trace_end(double* total_ms, int64_t* launches);
+
+/* Number of kernels this library has launched in the process so far. */
+int64_t hss_launch_counter(void);
+
+const char* hss_last_error(void);
+int32_t hss_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HSSGPU_H */

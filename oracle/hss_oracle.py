@@ -1,0 +1,932 @@
+"""CPU restatement of the HssMatrices.jl hot path -- TEST INFRASTRUCTURE ONLY.
+
+This module is the correctness oracle.  Only ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py`` may import it; the product (the CUDA
+library and its host package) never does.
+
+It restates, in NumPy + LAPACK (``scipy.linalg.lapack.dgeqrf/dormqr``), the
+algorithms of the reference (file:line within bonevbs/HssMatrices.jl v0.1.6):
+
+* cluster trees            -- src/clustertree.jl:14-35 (``bisection_cluster``)
+* the HSS generator tree    -- src/hssmatrix.jl:11-67 (leaf D,U,V / branch
+                              A11,A22,B12,B21,R1,W1,R2,W2), ``size`` :94,
+                              ``gensize`` :254-262, ``hssrank`` :251,
+                              ``rooted`` :266, ``full`` :270-305
+* HSS x dense product       -- src/matmul.jl:13-62 (``mul!``, ``_matmatup``,
+                              ``_matmatdown!``)
+* implicit ULV factor+solve -- src/ulvfactor.jl:10-107 (``ulvfactsolve``,
+                              ``_ulvreduce!``, ``_ulvfactsolve!``,
+                              ``_ulvfactsolve_topdown!``)
+* deterministic compression -- src/compression.jl:22-133 (``compress``)
+* randomized compression    -- src/compression.jl:278-475 (``randcompress``,
+                              ``randcompress_adaptive``, ``_randcompress!``,
+                              ``_interpolate``, ``hss_blkdiag``)
+
+LAPACK conventions.  The reference calls ``geqlf!/ormql!`` (QL of U) and
+``gelqf!/ormlq!`` (LQ of the top block of D).  SciPy does not wrap those, so:
+QL of U is the QR (``dgeqrf``) of U with rows and columns reversed, and the LQ
+of X is the QR of X^T.  Both generate the same Householder reflectors as the
+LAPACK routines (``dlarfg`` on the same vectors), so results agree to rounding.
+
+Parity status.  Julia is not available, and the reference's test-suite holds no
+golden vectors (tolerance-only checks, unseeded ``randn``), so bit-level parity
+with the reference is UNPINNED.  What is pinned: the reference's own tolerance
+tests (test/runtests.jl:36-67) pass on this restatement, on the same fixtures,
+and the integer cluster-tree bookkeeping is restated exactly.  The rank rule of
+``LowRankApprox.pqrfact`` (a dependency absent from the reference tree) is
+restated from its documented behaviour (stop when either atol or rtol is met,
+README.md:43), so compressed ranks are unpinned too.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+import scipy.linalg as sla
+from scipy.linalg import lapack
+
+# ---------------------------------------------------------------------------
+# options (src/HssMatrices.jl:52-108)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class HssOptions:
+    """Restates ``HssOptions`` and its defaults (src/HssMatrices.jl:52-67)."""
+
+    atol: float = 1e-9
+    rtol: float = 1e-9
+    leafsize: int = 64
+    noversampling: int = 10
+    stepsize: int = 20
+    verbose: bool = False
+
+    def check(self):
+        """``chkopts!`` (src/HssMatrices.jl:90-96)."""
+        if not self.atol >= 0.0:
+            raise ValueError("atol")
+        if not self.rtol >= 0.0:
+            raise ValueError("rtol")
+        if not self.leafsize >= 1:
+            raise ValueError("leafsize")
+        if not self.stepsize >= 1:
+            raise ValueError("stepsize")
+        if not self.noversampling >= 1:
+            raise ValueError("noversampling")
+        return self
+
+
+# ---------------------------------------------------------------------------
+# cluster trees (src/binarytree.jl:7-54, src/clustertree.jl:14-35)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class ClusterTree:
+    """A ``BinaryNode{UnitRange{Int}}``; ``lo``/``hi`` are 1-based inclusive, as in Julia."""
+
+    lo: int
+    hi: int
+    left: Optional["ClusterTree"] = None
+    right: Optional["ClusterTree"] = None
+
+    def __len__(self):
+        return self.hi - self.lo + 1
+
+    def isleaf(self):
+        return self.left is None and self.right is None
+
+
+def bisection_cluster(n, leafsize: int = 64) -> ClusterTree:
+    """``bisection_cluster(1:n; leafsize)`` (src/clustertree.jl:14-20, 27-35).
+
+    ``n`` is an int (range 1:n) or a (lo, hi) 1-based inclusive pair.
+    Split point ``ceil(len/2)`` (:30), leaf when ``len <= leafsize`` (:29).
+    """
+    if leafsize < 1:
+        raise ValueError("leafsize")
+    lo, hi = (1, n) if isinstance(n, (int, np.integer)) else n
+    if hi - lo + 1 <= 0:
+        raise ValueError("Index range must be larger or equal to 0")
+    return _bisection_cluster(lo, hi, leafsize)
+
+
+def _bisection_cluster(lo, hi, leafsize):
+    node = ClusterTree(lo, hi)
+    length = hi - lo + 1
+    if length > leafsize:
+        h = (length + 1) // 2  # convert(Int, ceil(size(range,1)/2))
+        node.left = _bisection_cluster(lo, lo + h - 1, leafsize)
+        node.right = _bisection_cluster(lo + h, hi, leafsize)
+    return node
+
+
+def cluster_leaves(t: ClusterTree):
+    """Leaf ranges in pre-order (list of (lo, hi) 1-based)."""
+    if t.isleaf():
+        return [(t.lo, t.hi)]
+    return cluster_leaves(t.left) + cluster_leaves(t.right)
+
+
+def cluster_depth(t: ClusterTree):
+    """``depth`` (src/binarytree.jl:27-40)."""
+    if t.isleaf():
+        return 1
+    return 1 + max(cluster_depth(t.left), cluster_depth(t.right))
+
+
+def compatible(a: ClusterTree, b: ClusterTree):
+    """``compatible`` (src/binarytree.jl:68-74): same branching structure."""
+    if a.isleaf() and b.isleaf():
+        return True
+    if a.isleaf() or b.isleaf():
+        return False
+    return compatible(a.left, b.left) and compatible(a.right, b.right)
+
+
+# ---------------------------------------------------------------------------
+# HSS generator tree (src/hssmatrix.jl:11-67)
+# ---------------------------------------------------------------------------
+
+
+class HssMatrix:
+    """Restates ``mutable struct HssMatrix`` (src/hssmatrix.jl:11-67).
+
+    Leaf: ``D`` (m x n), ``U`` (m x ku), ``V`` (n x kv).
+    Branch: ``A11``, ``A22``, ``B12`` (ku1 x kv2), ``B21`` (ku2 x kv1),
+    ``R1`` (ku1 x kR), ``R2`` (ku2 x kR), ``W1`` (kv1 x kW), ``W2`` (kv2 x kW);
+    at the root R/W have zero columns (:52-53).
+    """
+
+    def __init__(self):
+        self.leafnode = True
+        self.rootnode = True
+        self.D = self.U = self.V = None
+        self.A11 = self.A22 = None
+        self.B12 = self.B21 = None
+        self.R1 = self.W1 = self.R2 = self.W2 = None
+        self.sz1 = self.sz2 = None
+
+    @classmethod
+    def leaf(cls, D, U=None, V=None, rootnode=None):
+        """Leaf constructors (src/hssmatrix.jl:36-44)."""
+        h = cls()
+        D = np.asarray(D, dtype=float)
+        m, n = D.shape
+        h.leafnode = True
+        if U is None:
+            h.rootnode = True if rootnode is None else rootnode
+            U = np.zeros((m, 0))
+            V = np.zeros((n, 0))
+        else:
+            h.rootnode = False if rootnode is None else rootnode
+            if U.shape[0] != m:
+                raise ValueError("D and U must have same number of rows")
+            if V.shape[0] != n:
+                raise ValueError("D and V must have same number of columns")
+        h.D, h.U, h.V = D, np.asarray(U, float), np.asarray(V, float)
+        return h
+
+    @classmethod
+    def branch(cls, A11, A22, B12, B21, R1=None, W1=None, R2=None, W2=None, rootnode=None):
+        """Branch constructors (src/hssmatrix.jl:46-67)."""
+        h = cls()
+        h.leafnode = False
+        h.A11, h.A22 = A11, A22
+        h.B12, h.B21 = np.asarray(B12, float), np.asarray(B21, float)
+        h.sz1, h.sz2 = A11.size(), A22.size()
+        if R1 is None:
+            h.rootnode = True if rootnode is None else rootnode
+            kr1, kw1 = gensize(A11)
+            kr2, kw2 = gensize(A22)
+            h.R1, h.W1 = np.zeros((kr1, 0)), np.zeros((kw1, 0))
+            h.R2, h.W2 = np.zeros((kr2, 0)), np.zeros((kw2, 0))
+        else:
+            h.rootnode = False if rootnode is None else rootnode
+            if R1.shape[1] != R2.shape[1]:
+                raise ValueError("R1 and R2 must have same number of columns")
+            if W1.shape[1] != W2.shape[1]:
+                raise ValueError("W1 and W2 must have same number of rows")
+            h.R1, h.W1, h.R2, h.W2 = (np.asarray(x, float) for x in (R1, W1, R2, W2))
+        return h
+
+    def isleaf(self):
+        return self.leafnode
+
+    def size(self):
+        """``size`` (src/hssmatrix.jl:94)."""
+        if self.leafnode:
+            return self.D.shape
+        return (self.sz1[0] + self.sz2[0], self.sz1[1] + self.sz2[1])
+
+    @property
+    def shape(self):
+        return self.size()
+
+
+def gensize(h: HssMatrix):
+    """``gensize`` (src/hssmatrix.jl:254-262): (#cols of U or R, #cols of V or W)."""
+    if h.leafnode:
+        return h.U.shape[1], h.V.shape[1]
+    kr = h.R1.shape[1]
+    if kr != h.R2.shape[1]:
+        raise ValueError("dimensions of column-translators do not match")
+    kw = h.W1.shape[1]
+    if kw != h.W2.shape[1]:
+        raise ValueError("dimensions of row-translators do not match")
+    return kr, kw
+
+
+def hssrank(h: HssMatrix):
+    """``hssrank`` (src/hssmatrix.jl:251)."""
+    if h.leafnode:
+        return 0
+    return max(hssrank(h.A11), hssrank(h.A22), *h.B12.shape, *h.B21.shape)
+
+
+def rooted(h: HssMatrix):
+    """``rooted`` (src/hssmatrix.jl:266): same node with zero-column top translators."""
+    if h.leafnode:
+        return HssMatrix.leaf(h.D, rootnode=True)
+    return HssMatrix.branch(h.A11, h.A22, h.B12, h.B21, rootnode=True)
+
+
+def full(h: HssMatrix):
+    """``full`` / ``_full!`` (src/hssmatrix.jl:270-305)."""
+    if h.leafnode:
+        return h.D.copy()
+    m, n = h.size()
+    A = np.zeros((m, n))
+    k = max(hssrank(h), 1)
+    U = np.zeros((m, k + 1))
+    V = np.zeros((n, k + 1))
+    _full(h, A, U, V, 0, 0, True)
+    return A
+
+
+def _full(h, A, U, V, ro, co, rootnode):
+    if h.leafnode:
+        m, n = h.D.shape
+        A[ro:ro + m, co:co + n] = h.D
+        U[ro:ro + m, :h.U.shape[1]] = h.U
+        V[co:co + n, :h.V.shape[1]] = h.V
+        return
+    m1, n1 = h.sz1
+    m2, n2 = h.sz2
+    ru1, rv1 = gensize(h.A11)
+    ru2, rv2 = gensize(h.A22)
+    _full(h.A11, A, U, V, ro, co, False)
+    _full(h.A22, A, U, V, ro + m1, co + n1, False)
+    A[ro:ro + m1, co + n1:co + n1 + n2] = U[ro:ro + m1, :ru1] @ h.B12 @ V[co + n1:co + n1 + n2, :rv2].T
+    A[ro + m1:ro + m1 + m2, co:co + n1] = U[ro + m1:ro + m1 + m2, :ru2] @ h.B21 @ V[co:co + n1, :rv1].T
+    if not rootnode:
+        u1 = U[ro:ro + m1, :ru1] @ h.R1
+        u2 = U[ro + m1:ro + m1 + m2, :ru2] @ h.R2
+        v1 = V[co:co + n1, :rv1] @ h.W1
+        v2 = V[co + n1:co + n1 + n2, :rv2] @ h.W2
+        U[ro:ro + m1, :u1.shape[1]] = u1
+        U[ro + m1:ro + m1 + m2, :u2.shape[1]] = u2
+        V[co:co + n1, :v1.shape[1]] = v1
+        V[co + n1:co + n1 + n2, :v2.shape[1]] = v2
+
+
+def adjoint(h: HssMatrix):
+    """``adjoint`` (src/hssmatrix.jl:165-171) for real matrices."""
+    if h.leafnode:
+        return HssMatrix.leaf(h.D.T.copy(), h.V.copy(), h.U.copy(), rootnode=h.rootnode) if not (
+            h.rootnode and h.U.shape[1] == 0 and h.V.shape[1] == 0) else HssMatrix.leaf(h.D.T.copy(), rootnode=True)
+    out = HssMatrix.branch(adjoint(h.A11), adjoint(h.A22), h.B21.T.copy(), h.B12.T.copy(),
+                           h.W1.copy(), h.R1.copy(), h.W2.copy(), h.R2.copy(), rootnode=h.rootnode)
+    return out
+
+
+def iter_nodes(h: HssMatrix):
+    """Pre-order traversal."""
+    yield h
+    if not h.leafnode:
+        yield from iter_nodes(h.A11)
+        yield from iter_nodes(h.A22)
+
+
+def generator_entries(h: HssMatrix):
+    """Number of stored generator entries (D, U, V, R, W, B) in the tree."""
+    tot = 0
+    for x in iter_nodes(h):
+        if x.leafnode:
+            tot += x.D.size + x.U.size + x.V.size
+        else:
+            tot += x.B12.size + x.B21.size + x.R1.size + x.R2.size + x.W1.size + x.W2.size
+    return tot
+
+
+# ---------------------------------------------------------------------------
+# HSS x dense (src/matmul.jl:13-62)
+# ---------------------------------------------------------------------------
+
+
+def matmul(h: HssMatrix, B, alpha=1.0, beta=0.0, C=None):
+    """``mul!(C, hssA, B, alpha, beta)`` (src/matmul.jl:18-28); ``*`` (:13-15) when C is None."""
+    B = np.asarray(B, dtype=float)
+    vec = B.ndim == 1
+    if vec:
+        B = B.reshape(-1, 1)
+    m, n = h.size()
+    if B.shape[0] != n:
+        raise ValueError("First dimension of B does not match second dimension of A")
+    if C is None:
+        C = np.zeros((m, B.shape[1]))
+        beta = 0.0
+    else:
+        C = np.array(C, dtype=float, copy=True).reshape(m, B.shape[1])
+    if C.shape != (m, B.shape[1]):
+        raise ValueError("Dimensions of C don't match up with A and B.")
+    if h.leafnode:
+        C[:] = alpha * (h.D @ B) + beta * C
+    else:
+        h = rooted(h)
+        Z = _matmatup(h, B)
+        _matmatdown(C, h, B, Z, None, alpha, beta)
+    return C.reshape(-1) if vec else C
+
+
+class _ZNode:
+    __slots__ = ("data", "left", "right")
+
+    def __init__(self, data, left=None, right=None):
+        self.data, self.left, self.right = data, left, right
+
+
+def _matmatup(h, B):
+    """Post-order sweep (src/matmul.jl:32-42): leaf V'B, branch W1'Z1 + W2'Z2."""
+    if h.leafnode:
+        return _ZNode(h.V.T @ B)
+    n1 = h.sz1[1]
+    Z1 = _matmatup(h.A11, B[:n1])
+    Z2 = _matmatup(h.A22, B[n1:])
+    return _ZNode(h.W1.T @ Z1.data + h.W2.T @ Z2.data, Z1, Z2)
+
+
+def _matmatdown(C, h, B, Z, F, alpha, beta):
+    """Pre-order sweep (src/matmul.jl:44-62)."""
+    if h.leafnode:
+        C[:] = alpha * (h.D @ B) + beta * C
+        if F is not None:
+            C += alpha * (h.U @ F)
+        return
+    m1, n1 = h.sz1
+    if F is not None:
+        F1 = h.B12 @ Z.right.data + h.R1 @ F
+        F2 = h.B21 @ Z.left.data + h.R2 @ F
+    else:
+        F1 = h.B12 @ Z.right.data
+        F2 = h.B21 @ Z.left.data
+    _matmatdown(C[:m1], h.A11, B[:n1], Z.left, F1, alpha, beta)
+    _matmatdown(C[m1:], h.A22, B[n1:], Z.right, F2, alpha, beta)
+
+
+# ---------------------------------------------------------------------------
+# LAPACK helpers: QL via reversed QR, LQ via QR of the transpose
+# ---------------------------------------------------------------------------
+
+
+def _geqrf(A):
+    qr, tau, _work, info = lapack.dgeqrf(np.asfortranarray(A, dtype=float))
+    if info != 0:
+        raise RuntimeError("dgeqrf failed")
+    return qr, tau
+
+
+def _ormqr(side, trans, qr, tau, C):
+    C = np.asfortranarray(C, dtype=float)
+    if C.size == 0 or tau.size == 0:
+        return np.array(C, copy=True)
+    lwork = max(1, 64 * max(C.shape))
+    out, _work, info = lapack.dormqr(side, trans, qr, tau, C, lwork)
+    if info != 0:
+        raise RuntimeError("dormqr failed")
+    return out
+
+
+class QLFact:
+    """``geqlf!(U)`` of an m x k block (k < m): U = Q [0; L]."""
+
+    def __init__(self, U):
+        self.m, self.k = U.shape
+        self.qr, self.tau = _geqrf(U[::-1, ::-1])
+
+    def L(self):
+        R = np.triu(self.qr[:self.k, :self.k])
+        return R[::-1, ::-1].copy()
+
+    def apply_qt(self, C):
+        """``ormql!('L', 'T', ...)``: C <- Q^T C."""
+        return _ormqr("L", "T", self.qr, self.tau, C[::-1])[::-1].copy()
+
+
+class LQFact:
+    """``gelqf!(X)`` of an mk x n block: X = L Q (L = R^T, Q = Qqr^T of QR(X^T))."""
+
+    def __init__(self, X):
+        self.mk, self.n = X.shape
+        self.qr, self.tau = _geqrf(X.T)
+
+    def L(self):
+        r = min(self.mk, self.n)
+        return np.triu(self.qr[:r, :self.mk]).T.copy()  # mk x r lower trapezoidal
+
+    def apply_right_qt(self, C):
+        """``ormlq!('R', 'T', ...)``: C <- C Q^T."""
+        return _ormqr("L", "T", self.qr, self.tau, C.T).T.copy()
+
+    def apply_left_q(self, C):
+        """``ormlq!('L', 'N', ...)``: C <- Q C."""
+        return _ormqr("L", "T", self.qr, self.tau, C)
+
+    def apply_left_qt(self, C):
+        """``ormlq!('L', 'T', ...)``: C <- Q^T C."""
+        return _ormqr("L", "N", self.qr, self.tau, C)
+
+
+# ---------------------------------------------------------------------------
+# implicit ULV factor + solve (src/ulvfactor.jl:10-107)
+# ---------------------------------------------------------------------------
+
+
+def ulvfactsolve(h: HssMatrix, b):
+    """``ulvfactsolve(hssA, b)`` (src/ulvfactor.jl:10-19); ``hssA \\ b`` (src/hssmatrix.jl:234)."""
+    b = np.asarray(b, dtype=float)
+    vec = b.ndim == 1
+    if vec:
+        b = b.reshape(-1, 1)
+    if h.leafnode:
+        x = np.linalg.solve(h.D, b)
+    else:
+        z = np.zeros((h.size()[1], b.shape[1]))
+        *_, QV = _ulvfactsolve(h, b.copy(), z, 0, rootnode=True)
+        _ulvfactsolve_topdown(QV, z)
+        x = z
+    return x.reshape(-1) if vec else x
+
+
+def _ulvreduce(D, U, V, b):
+    """``_ulvreduce!(D, U, V, b)`` (src/ulvfactor.jl:22-57)."""
+    m, n = D.shape
+    if m != U.shape[0]:
+        raise ValueError("D and U have different first dimensions")
+    if n != V.shape[0]:
+        raise ValueError("D and V have different second dimensions")
+    r = b.shape[1]
+    k = min(U.shape[1], m)
+    nk = min(m - k, n)
+    if k >= m:  # nothing can be eliminated (:32-36)
+        u = np.zeros((V.shape[1], r))
+        zloc = np.zeros((0, r))
+        return D, U, V, b, zloc, u, m - k, nk, None
+    qlf = QLFact(U)                                   # geqlf!(U)          :39
+    U = np.tril(qlf.L())                              # tril(U[end-k+1:end,:]) :40
+    D = qlf.apply_qt(D)                               # ormql!('L',T,..,D)  :41
+    b = qlf.apply_qt(b)                               # ormql!('L',T,..,b)  :42
+    lqf = LQFact(D[:m - k, :])                        # gelqf!(D[1:m-k,:])  :44
+    L1 = lqf.L()[:, :nk]                              # tril(lqf[1])[:,1:nk] :45-46
+    L2 = lqf.apply_right_qt(D[m - k:, :])             # ormlq!('R',T,..)    :47
+    zloc = sla.solve_triangular(L1, b[:m - k], lower=True)  # trsm           :48
+    b = b[m - k:] - L2[:, :nk] @ zloc                 # :49
+    V = lqf.apply_left_q(V)                           # ormlq!('L','N',..,V) :50
+    u = V[:m - k, :].T @ zloc                         # :51
+    D = L2[:, nk:]                                    # :53
+    V = V[nk:, :]                                     # :54
+    return D, U, V, b, zloc, u, m - k, nk, lqf
+
+
+class _QVNode:
+    __slots__ = ("cols", "lqf", "left", "right")
+
+    def __init__(self, cols=None, lqf=None):
+        self.cols, self.lqf, self.left, self.right = cols, lqf, None, None
+
+
+def _ulvfactsolve(h, b, z, co, rootnode=False):
+    """``_ulvfactsolve!`` (src/ulvfactor.jl:60-96); ``cols`` are 0-based here."""
+    if h.leafnode:
+        cols = co + np.arange(h.size()[1], dtype=np.int64)           # :62
+        D, U, V = h.D.copy(), h.U.copy(), h.V.copy()                   # :63
+        D, U, V, b, zloc, u, mk, nk, lqf = _ulvreduce(D, U, V, b)     # :64
+        z[cols[:mk]] = zloc                                            # :65
+        QV = _QVNode(cols, lqf)                                        # :66
+        return b, u, D, U, V, cols, nk, QV
+    m1, n1 = h.sz1
+    b1, b2 = b[:m1].copy(), b[m1:].copy()                              # :69
+    b1, u1, D1, U1, V1, cols1, nk1, QV1 = _ulvfactsolve(h.A11, b1, z, co)
+    b2, u2, D2, U2, V2, cols2, nk2, QV2 = _ulvfactsolve(h.A22, b2, z, co + n1)
+    b = np.vstack([b1, b2]) - np.vstack([U1 @ h.B12 @ u2, U2 @ h.B21 @ u1])   # :74
+    D = np.block([[D1, U1 @ h.B12 @ V2.T], [U2 @ h.B21 @ V1.T, D2]])          # :75
+    cols = np.concatenate([cols1[nk1:], cols2[nk2:]])                          # :76
+    U = np.vstack([U1 @ h.R1, U2 @ h.R2])                                      # :78
+    V = np.vstack([V1 @ h.W1, V2 @ h.W2])                                      # :79
+    if rootnode:                                                               # :82-86
+        z[cols] = np.linalg.solve(D, b)
+        u = np.zeros((0, b.shape[1]))
+        QV = _QVNode()
+        nk = D.shape[1]
+    else:                                                                      # :87-91
+        D, U, V, b, zloc, u, mk, nk, lqf = _ulvreduce(D, U, V, b)
+        u = u + h.W1.T @ u1 + h.W2.T @ u2
+        z[cols[:mk]] = zloc
+        QV = _QVNode(cols, lqf)
+    QV.left, QV.right = QV1, QV2
+    return b, u, D, U, V, cols, nk, QV
+
+
+def _ulvfactsolve_topdown(QV, z):
+    """``_ulvfactsolve_topdown!`` (src/ulvfactor.jl:98-107): z[cols] = Q^T z[cols], pre-order."""
+    if QV.cols is not None and QV.lqf is not None:
+        z[QV.cols] = QV.lqf.apply_left_qt(z[QV.cols])
+    if QV.left is not None:
+        _ulvfactsolve_topdown(QV.left, z)
+    if QV.right is not None:
+        _ulvfactsolve_topdown(QV.right, z)
+
+
+def ulv_cols(h: HssMatrix):
+    """The per-node ``cols`` bookkeeping of ``_ulvfactsolve!`` (src/ulvfactor.jl:62,76),
+    pre-order list of (cols, mk, nk) with 0-based column indices, root last entry
+    being its full ``cols``.  Depends only on sizes and ranks, never on values."""
+    out = []
+
+    def rec(x, co, root):
+        if x.leafnode:
+            m, n = x.D.shape
+            cols = co + np.arange(n, dtype=np.int64)
+            k = min(x.U.shape[1], m)
+            mk = m - k
+            nk = min(mk, n)
+            out.append((cols, mk, nk))
+            return cols, nk, (k if k < m else m), x.V.shape[1], x.U.shape[1]
+        m1, n1 = x.sz1
+        idx = len(out)
+        out.append(None)
+        c1, nk1, mr1, kv1, ku1 = rec(x.A11, co, False)
+        c2, nk2, mr2, kv2, ku2 = rec(x.A22, co + n1, False)
+        cols = np.concatenate([c1[nk1:], c2[nk2:]])
+        m = mr1 + mr2
+        n = len(cols)
+        if root:
+            out[idx] = (cols, 0, 0)
+            return cols, 0, m, 0, 0
+        ku = x.R1.shape[1]
+        k = min(ku, m)
+        mk = m - k
+        nk = min(mk, n)
+        out[idx] = (cols, mk, nk)
+        return cols, nk, (k if k < m else m), x.W1.shape[1], ku
+
+    rec(h, 0, True)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# deterministic compression (src/compression.jl:22-133)
+# ---------------------------------------------------------------------------
+
+
+def _compress_block(A, atol, rtol):
+    """``_compress_block!`` (src/compression.jl:22-30): truncated column-pivoted QR,
+    returns (Q, R[:, invperm(p)]).  The rank rule restates ``LowRankApprox.pqrfact``'s
+    documented tolerance (stop once atol or rtol is met): keep |R_ii| > max(atol, rtol*|R_11|)."""
+    m, n = A.shape
+    if m == 0 or n == 0:
+        return np.zeros((m, 0)), np.zeros((0, n))
+    Q, R, p = sla.qr(A, mode="economic", pivoting=True)
+    d = np.abs(np.diag(R))
+    thr = max(atol, rtol * d[0])
+    rk = int(np.sum(d > thr)) if d[0] > 0 else 0
+    inv = np.empty_like(p)
+    inv[p] = np.arange(len(p))
+    return Q[:, :rk].copy(), R[:rk, :][:, inv].copy()
+
+
+def compress(A, rcl: ClusterTree, ccl: ClusterTree, atol=1e-9, rtol=1e-9):
+    """``compress(A, rcl, ccl; atol, rtol)`` (src/compression.jl:47-63)."""
+    A = np.asarray(A, dtype=float)
+    if not compatible(rcl, ccl):
+        raise ValueError("row and column clusters are not compatible")
+    m, n = len(rcl), len(ccl)
+    if A.shape != (m, n):
+        raise ValueError("size of row- and column-cluster-trees must match")
+    Brow = np.zeros((m, 0))
+    Bcol = np.zeros((0, n))
+    if rcl.isleaf():
+        return HssMatrix.leaf(A[rcl.lo - 1:rcl.hi, ccl.lo - 1:ccl.hi].copy(), rootnode=True)
+    h, _, _ = _compress(A, Brow, Bcol, rcl, ccl, atol, rtol, rootnode=True)
+    return h
+
+
+def _compress_leaf(A, Brow, Bcol, rows, cols, atol, rtol):
+    """Leaf case of ``_compress!`` (src/compression.jl:66-74)."""
+    U, Brow = _compress_block(Brow, atol, rtol)
+    V, Bc = _compress_block(Bcol.T.copy(), atol, rtol)
+    D = A[rows[0] - 1:rows[1], cols[0] - 1:cols[1]].copy()
+    return HssMatrix.leaf(D, U, V), Brow, Bc.T.copy()
+
+
+def _compress(A, Brow, Bcol, rcl, ccl, atol, rtol, rootnode=False):
+    """Branch case of ``_compress!`` (src/compression.jl:77-133)."""
+    m1, m2 = len(rcl.left), len(rcl.right)
+    n1, n2 = len(ccl.left), len(ccl.right)
+    r1 = (rcl.left.lo - 1, rcl.left.hi)
+    r2 = (rcl.right.lo - 1, rcl.right.hi)
+    c1 = (ccl.left.lo - 1, ccl.left.hi)
+    c2 = (ccl.right.lo - 1, ccl.right.hi)
+    Brow1 = np.hstack([A[r1[0]:r1[1], c2[0]:c2[1]], Brow[:m1, :]])
+    Bcol1 = np.vstack([A[r2[0]:r2[1], c1[0]:c1[1]], Bcol[:, :n1]])
+    if rcl.left.isleaf() and ccl.left.isleaf():
+        A11, Brow1, Bcol1 = _compress_leaf(A, Brow1, Bcol1, (rcl.left.lo, rcl.left.hi),
+                                           (ccl.left.lo, ccl.left.hi), atol, rtol)
+    elif not rcl.left.isleaf() and not ccl.left.isleaf():
+        A11, Brow1, Bcol1 = _compress(A, Brow1, Bcol1, rcl.left, ccl.left, atol, rtol)
+    else:
+        raise ValueError("row and column clusters are not compatible")
+    Brow2 = np.hstack([Bcol1[:m2, :], Brow[m1:, :]])
+    Bcol2 = np.vstack([Brow1[:, :n2], Bcol[:, n1:]])
+    if rcl.right.isleaf() and ccl.right.isleaf():
+        A22, Brow2, Bcol2 = _compress_leaf(A, Brow2, Bcol2, (rcl.right.lo, rcl.right.hi),
+                                           (ccl.right.lo, ccl.right.hi), atol, rtol)
+    elif not rcl.right.isleaf() and not ccl.right.isleaf():
+        A22, Brow2, Bcol2 = _compress(A, Brow2, Bcol2, rcl.right, ccl.right, atol, rtol)
+    else:
+        raise ValueError("row and column clusters are not compatible")
+    rm1, rn1 = Brow1.shape[0], Bcol1.shape[1]
+    B12 = Bcol2[:rm1, :].copy()
+    B21 = Brow2[:, :rn1].copy()
+    Brow = np.vstack([Brow1[:, n2:], Brow2[:, rn1:]])
+    Bcol = np.hstack([Bcol1[m2:, :], Bcol2[rm1:, :]])
+    if not rootnode:
+        R, Brow = _compress_block(Brow, atol, rtol)
+        R1, R2 = R[:rm1, :].copy(), R[rm1:, :].copy()
+        W, Bc = _compress_block(Bcol.T.copy(), atol, rtol)
+        Bcol = Bc.T.copy()
+        W1, W2 = W[:rn1, :].copy(), W[rn1:, :].copy()
+        h = HssMatrix.branch(A11, A22, B12, B21, R1, W1, R2, W2, rootnode=False)
+    else:
+        h = HssMatrix.branch(A11, A22, B12, B21, rootnode=True)
+    return h, Brow, Bcol
+
+
+def hss(A, leafsize=64, atol=1e-9, rtol=1e-9):
+    """``hss(A; leafsize, atol, rtol)`` for dense A (src/hssmatrix.jl:71-76)."""
+    A = np.asarray(A, dtype=float)
+    rcl = bisection_cluster(A.shape[0], leafsize)
+    ccl = bisection_cluster(A.shape[1], leafsize)
+    return compress(A, rcl, ccl, atol, rtol)
+
+
+# ---------------------------------------------------------------------------
+# randomized compression (src/compression.jl:278-475)
+# ---------------------------------------------------------------------------
+
+
+def _interpolate(A, atol, rtol):
+    """``_interpolate`` (src/compression.jl:433-444): ID via ``qr(A, ColumnNorm())``.
+    Threshold ``min(atol, rtol*|R11|)`` (:439)."""
+    if A.shape[1] == 0:
+        return np.zeros((0, 0)), np.zeros(0, dtype=np.int64)
+    if A.shape[0] == 0:
+        return np.zeros((0, A.shape[1])), np.zeros(0, dtype=np.int64)
+    _Q, R, p = sla.qr(A, mode="economic", pivoting=True)
+    tol = min(atol, rtol * abs(R[0, 0]))
+    rk = int(np.sum(np.abs(np.diag(R)) > tol))
+    J = p[:rk].astype(np.int64)
+    inv = np.empty_like(p)
+    inv[p] = np.arange(len(p))
+    X = sla.solve_triangular(R[:rk, :rk], R[:rk, :][:, inv], lower=False) if rk else np.zeros((0, A.shape[1]))
+    return X, J
+
+
+def hss_blkdiag(A, rcl: ClusterTree, ccl: ClusterTree, rootnode=True):
+    """``hss_blkdiag`` (src/compression.jl:447-475): rank-0 HSS of the diagonal blocks."""
+    if rcl.isleaf():
+        D = np.asarray(A[rcl.lo - 1:rcl.hi, ccl.lo - 1:ccl.hi], dtype=float).copy()
+        if rootnode:
+            return HssMatrix.leaf(D, rootnode=True)
+        return HssMatrix.leaf(D, np.zeros((D.shape[0], 0)), np.zeros((D.shape[1], 0)))
+    A11 = hss_blkdiag(A, rcl.left, ccl.left, rootnode=False)
+    A22 = hss_blkdiag(A, rcl.right, ccl.right, rootnode=False)
+    z = np.zeros((0, 0))
+    if rootnode:
+        return HssMatrix.branch(A11, A22, z, z, rootnode=True)
+    return HssMatrix.branch(A11, A22, z, z, z, z, z, z, rootnode=False)
+
+
+def randcompress(A, rcl, ccl, kest, atol=1e-9, rtol=1e-9, noversampling=10, rng=None):
+    """``randcompress(A, rcl, ccl, kest)`` (src/compression.jl:278-294)."""
+    rng = np.random.default_rng(0) if rng is None else rng
+    A = np.asarray(A, dtype=float)
+    m, n = A.shape
+    if not compatible(rcl, ccl):
+        raise ValueError("row and column clusters are not compatible")
+    h = hss_blkdiag(A, rcl, ccl)
+    s = kest + noversampling
+    Ocol = rng.standard_normal((n, s))
+    Orow = rng.standard_normal((m, s))
+    Scol = A @ Ocol
+    Srow = A.T @ Orow
+    h = _randcompress(h, A, Scol, Srow, Ocol, Orow, 0, 0, atol, rtol, rootnode=True)[0]
+    return h
+
+
+def randcompress_adaptive(A, rcl, ccl, kest=10, atol=1e-9, rtol=1e-9, noversampling=10,
+                          stepsize=20, rng=None, stats=None):
+    """``randcompress_adaptive`` (src/compression.jl:312-355)."""
+    rng = np.random.default_rng(0) if rng is None else rng
+    A = np.asarray(A, dtype=float)
+    m, n = A.shape
+    maxrank = n
+    if not compatible(rcl, ccl):
+        raise ValueError("row and column clusters are not compatible")
+    h = hss_blkdiag(A, rcl, ccl)
+    k, r, bs = kest, noversampling, stepsize
+    Ocol = rng.standard_normal((n, k + r))
+    Orow = rng.standard_normal((m, k + r))
+    Scol = A @ Ocol
+    Srow = A.T @ Orow
+    failed = True
+    rounds = 0
+    while failed and k < maxrank:
+        h = _randcompress(h, A, Scol, Srow, Ocol, Orow, 0, 0, atol, rtol, rootnode=True)[0]
+        Ocol_t = rng.standard_normal((n, bs))
+        Orow_t = rng.standard_normal((m, bs))
+        Scol_t = A @ Ocol_t
+        Srow_t = A.T @ Orow_t
+        nrm = math.sqrt(1.0 / bs) * np.linalg.norm(Scol_t)
+        nrm_est = math.sqrt(1.0 / bs) * np.linalg.norm(Scol_t - matmul(h, Ocol_t))
+        failed = nrm_est > atol and nrm_est > rtol * nrm
+        rounds += 1
+        if failed:
+            Ocol = np.hstack([Ocol, Ocol_t])
+            Orow = np.hstack([Orow, Orow_t])
+            Scol = np.hstack([Scol, Scol_t])
+            Srow = np.hstack([Srow, Srow_t])
+            k += bs
+    if stats is not None:
+        stats.update(rounds=rounds, k=k, samples=k + r)
+    return h
+
+
+def _randcompress(h, A, Scol, Srow, Ocol, Orow, ro, co, atol, rtol, rootnode=False):
+    """``_randcompress!`` (src/compression.jl:358-430).  Slices are copied, as Julia does."""
+    if h.leafnode:
+        Scol = Scol - h.D @ Ocol                                  # :360
+        Srow = Srow - h.D.T @ Orow                                # :361
+        Xcol, Jcol = _interpolate(Scol.T, atol, rtol)             # :366
+        h.U = Xcol.T.copy()
+        Scol = Scol[Jcol, :]
+        U = h.U
+        Jcol = ro + Jcol
+        Xrow, Jrow = _interpolate(Srow.T, atol, rtol)             # :373
+        h.V = Xrow.T.copy()
+        Srow = Srow[Jrow, :]
+        V = h.V
+        Jrow = co + Jrow
+        h.rootnode = rootnode
+        return h, Scol, Srow, Ocol, Orow, Jcol, Jrow, U, V
+    m1, n1 = h.sz1
+    (h.A11, Scol1, Srow1, Ocol1, Orow1, Jcol1, Jrow1, U1, V1) = _randcompress(
+        h.A11, A, Scol[:m1].copy(), Srow[:n1].copy(), Ocol[:n1].copy(), Orow[:m1].copy(), ro, co, atol, rtol)
+    (h.A22, Scol2, Srow2, Ocol2, Orow2, Jcol2, Jrow2, U2, V2) = _randcompress(
+        h.A22, A, Scol[m1:].copy(), Srow[n1:].copy(), Ocol[n1:].copy(), Orow[m1:].copy(),
+        ro + m1, co + n1, atol, rtol)
+    Ocol2 = V2.T @ Ocol2                                          # :384-387
+    Ocol1 = V1.T @ Ocol1
+    Orow2 = U2.T @ Orow2
+    Orow1 = U1.T @ Orow1
+    Jcol = np.concatenate([Jcol1, Jcol2])
+    Jrow = np.concatenate([Jrow1, Jrow2])
+    Ocol = np.vstack([Ocol1, Ocol2])
+    Orow = np.vstack([Orow1, Orow2])
+    h.B12 = A[np.ix_(Jcol1, Jrow2)].copy()                      # :394-395
+    h.B21 = A[np.ix_(Jcol2, Jrow1)].copy()
+    Scol = np.vstack([Scol1 - h.B12 @ Ocol2, Scol2 - h.B21 @ Ocol1])    # :397
+    Srow = np.vstack([Srow1 - h.B21.T @ Orow2, Srow2 - h.B12.T @ Orow1])  # :398
+    h.sz1, h.sz2 = h.A11.size(), h.A22.size()
+    if rootnode:
+        rk1, wk1 = gensize(h.A11)
+        rk2, wk2 = gensize(h.A22)
+        h.R1, h.R2 = np.zeros((rk1, 0)), np.zeros((rk2, 0))
+        h.W1, h.W2 = np.zeros((wk1, 0)), np.zeros((wk2, 0))
+        h.rootnode = True
+        U = np.zeros((rk1 + rk2, 0))
+        V = np.zeros((wk1 + wk2, 0))
+    else:
+        Xcol, Jcolloc = _interpolate(Scol.T, atol, rtol)          # :413
+        h.R1 = Xcol[:, :Scol1.shape[0]].T.copy()
+        h.R2 = Xcol[:, Scol1.shape[0]:].T.copy()
+        if Xcol.shape[0] == 0:
+            h.R1 = np.zeros((Scol1.shape[0], 0))
+            h.R2 = np.zeros((Scol2.shape[0], 0))
+        Scol = Scol[Jcolloc, :]
+        Jcol = Jcol[Jcolloc]
+        U = np.vstack([h.R1, h.R2])
+        Xrow, Jrowloc = _interpolate(Srow.T, atol, rtol)          # :421
+        h.W1 = Xrow[:, :Srow1.shape[0]].T.copy()
+        h.W2 = Xrow[:, Srow1.shape[0]:].T.copy()
+        if Xrow.shape[0] == 0:
+            h.W1 = np.zeros((Srow1.shape[0], 0))
+            h.W2 = np.zeros((Srow2.shape[0], 0))
+        Srow = Srow[Jrowloc, :]
+        Jrow = Jrow[Jrowloc]
+        V = np.vstack([h.W1, h.W2])
+        h.rootnode = False
+    return h, Scol, Srow, Ocol, Orow, Jcol, Jrow, U, V
+
+
+# ---------------------------------------------------------------------------
+# fixtures: kernel matrices and synthetic generator trees
+# ---------------------------------------------------------------------------
+
+
+def cauchy_matrix(n=2001, lo=-1.0, hi=1.0):
+    """A_ij = 1/(x_i - y_j), 1 on the diagonal, x = y = n uniform points in [lo, hi]
+    (README.md:15-18 kernel; ``-1:0.001:1`` is n=2001)."""
+    x = np.linspace(lo, hi, n)
+    d = x[:, None] - x[None, :]
+    with np.errstate(divide="ignore"):
+        A = np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 1.0)
+    return A
+
+
+def runtests_matrix(n=2001):
+    """The reference suite's fixture K(x,y) = (x-y) > 0 ? 0.001/(x-y) : 2 on -1:0.001:1
+    (test/runtests.jl:19-20)."""
+    x = np.linspace(-1.0, 1.0, n)
+    d = x[:, None] - x[None, :]
+    return np.where(d > 0, 0.001 / np.where(d > 0, d, 1.0), 2.0)
+
+
+def _orth(rng, m, k):
+    """Orthonormal m x k (Q of QR of randn)."""
+    if k == 0:
+        return np.zeros((m, 0))
+    Q, _ = np.linalg.qr(rng.standard_normal((m, k)))
+    return Q[:, :k]
+
+
+def synthetic_hss(n, leafsize, k, rng, diag_shift=4.0, bscale=0.5):
+    """Synthetic HSS from seeded generators, on ``bisection_cluster(n, leafsize)``:
+    leaf D = randn(m,m)/sqrt(m) + shift*I; leaf U, V orthonormal m x min(k, m);
+    branch [R1;R2], [W1;W2] orthonormal (k1+k2) x min(k, k1+k2);
+    B12, B21 = bscale*randn/sqrt(k)."""
+    cl = bisection_cluster(n, leafsize)
+
+    def build(t, root):
+        if t.isleaf():
+            m = len(t)
+            D = rng.standard_normal((m, m)) / math.sqrt(m) + diag_shift * np.eye(m)
+            if root:
+                return HssMatrix.leaf(D, rootnode=True), 0
+            kk = min(k, m)
+            return HssMatrix.leaf(D, _orth(rng, m, kk), _orth(rng, m, kk)), kk
+        A11, k1 = build(t.left, False)
+        A22, k2 = build(t.right, False)
+        B12 = bscale * rng.standard_normal((k1, k2)) / math.sqrt(max(k, 1))
+        B21 = bscale * rng.standard_normal((k2, k1)) / math.sqrt(max(k, 1))
+        if root:
+            return HssMatrix.branch(A11, A22, B12, B21, rootnode=True), 0
+        kk = min(k, k1 + k2)
+        R = _orth(rng, k1 + k2, kk)
+        W = _orth(rng, k1 + k2, kk)
+        return HssMatrix.branch(A11, A22, B12, B21, R[:k1], W[:k1], R[k1:], W[k1:], rootnode=False), kk
+
+    h, _ = build(cl, True)
+    return h
+
+
+def matvec_bytes(h: HssMatrix, r: int, itemsize=8):
+    """Algorithmic bytes of one HSS product with r right-hand sides: every generator
+    entry once, plus B read and C written."""
+    m, n = h.size()
+    return itemsize * (generator_entries(h) + r * (m + n))
+
+
+def cond_estimate(h: HssMatrix, iters=30, rng=None):
+    """2-norm condition estimate from power iteration on A^T A (HSS products) and
+    inverse power iteration (two ULV solves per step)."""
+    rng = np.random.default_rng(12345) if rng is None else rng
+    ht = adjoint(h)
+    n = h.size()[1]
+    x = rng.standard_normal(n)
+    x /= np.linalg.norm(x)
+    smax = 0.0
+    for _ in range(iters):
+        y = matmul(ht, matmul(h, x))
+        smax = math.sqrt(np.linalg.norm(y))
+        x = y / np.linalg.norm(y)
+    x = rng.standard_normal(n)
+    x /= np.linalg.norm(x)
+    inv = 0.0
+    for _ in range(iters):
+        y = ulvfactsolve(h, ulvfactsolve(ht, x))
+        inv = math.sqrt(np.linalg.norm(y))
+        x = y / np.linalg.norm(y)
+    return smax * inv

@@ -1,0 +1,122 @@
+"""Host-side logic without a GPU: ABI exports, packing, validation, bookkeeping."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, ROOT, load_golden, unpack_tree
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "hssgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(hss_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(lib, pkg):
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(pkg._lib.EXPORTS) == syms
+    assert lib.hss_version() >= 1
+
+
+def _inspect(lib, table, npacked):
+    info = np.zeros((table.shape[0], 13), dtype=np.int64)
+    rc = lib.hss_inspect(table.shape[0], table.ctypes.data_as(C.POINTER(C.c_int64)), npacked,
+                         info.ctypes.data_as(C.POINTER(C.c_int64)))
+    return rc, info
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_packer_matches_golden_layout(pkg, orc, name):
+    """The package's packer produces the same table and buffer as the fixture script."""
+    g = load_golden(name)
+    h = unpack_tree(g["table"], g["packed"], orc)
+    table, packed = pkg.pack(pkg.HssMatrix.from_tree(h))
+    assert np.array_equal(table, g["table"])
+    assert np.array_equal(packed, g["packed"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_inspect_bookkeeping_bit_exact(lib, orc, name):
+    """Depth/height/offsets and ULV sizes from the C library equal the oracle's bookkeeping
+    (src/ulvfactor.jl:27-28,62,76; src/clustertree.jl:27-35)."""
+    g = load_golden(name)
+    rc, info = _inspect(lib, g["table"], g["packed"].size)
+    assert rc == 0, lib.hss_last_error()
+    h = unpack_tree(g["table"], g["packed"], orc)
+    cols = orc.ulv_cols(h)   # pre-order, same numbering as the table
+    assert len(cols) == info.shape[0]
+    for i, (c, mk, nk) in enumerate(cols):
+        assert info[i, 5] == len(c), i          # n of the reduce problem = len(cols)
+        if i:
+            assert info[i, 9] == mk and info[i, 10] == nk, i
+    # cols rebuilt from the library's sizes equal the oracle's, element by element
+    def rebuild(i):
+        t = g["table"][i]
+        if t[0] < 0:
+            return list(range(info[i, 3], info[i, 3] + info[i, 5]))
+        a, b = rebuild(t[0]), rebuild(t[1])
+        return a[info[t[0], 10]:] + b[info[t[1], 10]:]
+    flat = np.concatenate([np.array(rebuild(i), dtype=np.int64) for i in range(info.shape[0])])
+    assert np.array_equal(flat, g["cols"])
+    # leaf offsets follow bisection order
+    m, _n = g["size"]
+    leaves = [i for i in range(info.shape[0]) if info[i, 11]]
+    assert sum(g["table"][i, 2] for i in leaves) == m
+
+
+def test_inspect_rejects_bad_trees(lib, pkg, orc):
+    g = load_golden("synthetic_perfect")
+    t = g["table"].copy()
+    t[1, 4] += 1          # left child's U rank no longer matches its parent's B12/R1
+    rc, _ = _inspect(lib, t, g["packed"].size)
+    assert rc == pkg._lib.HSS_ERR_BAD_DIMS
+    t = g["table"].copy()
+    t[1, 1] = -1          # a node with one child
+    rc, _ = _inspect(lib, t, g["packed"].size)
+    assert rc == pkg._lib.HSS_ERR_BAD_DIMS
+    t = g["table"].copy()
+    rc, _ = _inspect(lib, t, g["packed"].size - 1)   # last block out of range
+    assert rc == pkg._lib.HSS_ERR_BAD_DIMS
+    t = g["table"].copy()
+    t[2, 0] = 1           # cycle back to an ancestor
+    t[2, 1] = 2
+    rc, _ = _inspect(lib, t, g["packed"].size)
+    assert rc == pkg._lib.HSS_ERR_BAD_DIMS
+    # non-square leaf root
+    one = np.full((1, 16), -1, dtype=np.int64)
+    one[0, 2:6] = [3, 4, 0, 0]
+    one[0, 6] = 0
+    one[0, 15] = 0
+    rc, _ = _inspect(lib, one, 12)
+    assert rc == pkg._lib.HSS_ERR_BAD_DIMS
+
+
+def test_host_mirror_api(pkg, orc):
+    rng = np.random.default_rng(0)
+    h = pkg.HssMatrix.from_tree(orc.synthetic_hss(300, 64, 8, rng))
+    assert h.size() == (300, 300) and h.size(1) == 300
+    assert pkg.hssrank(h) == 8
+    assert pkg.gensize(h.A11) == (8, 8)
+    assert repr(h) == "300x300 HssMatrix{Float64}"
+    with pytest.raises(ValueError):
+        pkg.HssMatrix.leaf(np.zeros((3, 3)), np.zeros((2, 1)), np.zeros((3, 1)))
+    o = pkg.HssOptions.current(leafsize=32)
+    assert o.leafsize == 32 and pkg.HssOptions.current().leafsize == 64
+    with pytest.raises(ValueError):
+        pkg.HssOptions.current(atol=-1.0).check()
+
+
+def test_synthetic_generator_matches_oracle(pkg, orc):
+    """The package's benchmark inputs are the same trees the oracle builds from the same seed."""
+    a = pkg.synthetic_hss(1152, 64, 48, np.random.default_rng(5))
+    b = orc.synthetic_hss(1152, 64, 48, np.random.default_rng(5))
+    ta, pa = pkg.pack(a)
+    tb, pb = pkg.pack(pkg.HssMatrix.from_tree(b))
+    assert np.array_equal(ta, tb) and np.array_equal(pa, pb)
+    assert pkg.generator_entries(a) == orc.generator_entries(b) == pa.size
