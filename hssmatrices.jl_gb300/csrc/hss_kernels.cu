@@ -795,7 +795,10 @@ void launch_colnorm2(const double* B, int64_t ldb, int64_t n, int64_t r, double*
   if (n <= 0 || r <= 0) return;
   int64_t bx = (n + NT - 1) / NT;
   if (bx > 64) bx = 64;
-  colnorm2_kernel<<<dim3((unsigned)bx, (unsigned)r), NT, 0, st>>>(B, ldb, n, r, out);
+  for (int64_t j0 = 0; j0 < r; j0 += 65535) {
+    const int64_t rc = r - j0 < 65535 ? r - j0 : 65535;
+    colnorm2_kernel<<<dim3((unsigned)bx, (unsigned)rc), NT, 0, st>>>(B + j0 * ldb, ldb, n, rc, out + j0);
+  }
 }
 void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st) {
   if (r <= 0) return;
