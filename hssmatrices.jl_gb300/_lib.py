@@ -38,7 +38,7 @@ EXPORTS = [
     "hss_ulv_cols", "hss_matmul", "hss_matmul_host", "hss_matmul_batch", "hss_ulvfactor",
     "hss_factor_destroy", "hss_ulvsolve", "hss_ulvsolve_host", "hss_ulvsolve_batch",
     "hss_ulvfactsolve_host", "hss_factor_bytes", "hss_last_error", "hss_version", "hss_ulvrefactor",
-    "hss_trace_begin", "hss_trace_end", "hss_launch_counter",
+    "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option",
 ]
 
 
@@ -93,6 +93,7 @@ def _declare(lib):
         "hss_trace_begin": (C.c_int, [I32]),
         "hss_trace_end": (C.c_int, [C.POINTER(D), PI64]),
         "hss_launch_counter": (C.c_int64, []),
+        "hss_set_option": (C.c_int, [I32, I64]),
         "hss_last_error": (C.c_char_p, []),
         "hss_version": (C.c_int32, []),
     }

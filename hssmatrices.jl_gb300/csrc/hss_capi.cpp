@@ -102,12 +102,15 @@ struct SlotTable {
 
 struct Seg {
   int64_t off = 0, cnt = 0;
+  int mmax = 0, nmax = 0, kumax = 0, kvmax = 0;   // largest node of the list
 };
 
 inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
 
 // Launch accounting and optional CUDA-event bracketing of one kernel kind.
 int64_t g_launches = 0;
+// Forces the global-memory factor kernel for every level (parity tests of the two kernels).
+bool g_generic_factor = false;
 struct TraceState {
   int kind = -1;
   std::vector<cudaEvent_t> pool;
@@ -423,8 +426,13 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
       v[lv].off = (int64_t)tasks.size();
       for (int64_t i = 0; i < total_nodes; ++i) {
         const Node& x = P->nodes[i];
-        if ((by_height ? x.height : x.depth) == lv && pred(x))
+        if ((by_height ? x.height : x.depth) == lv && pred(x)) {
           tasks.push_back(Task{nullptr, (int32_t)i, x.tree});
+          v[lv].mmax = std::max(v[lv].mmax, x.m);
+          v[lv].nmax = std::max(v[lv].nmax, x.n);
+          v[lv].kumax = std::max(v[lv].kumax, x.ku);
+          v[lv].kvmax = std::max(v[lv].kvmax, x.kv);
+        }
       }
       v[lv].cnt = (int64_t)tasks.size() - v[lv].off;
     }
@@ -495,10 +503,15 @@ void run_matvec(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
 
 template <typename T>
 void run_factor(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
-  for (size_t h = 0; h < P->by_h.size(); ++h)
-    traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, P->by_h[h].cnt, st, [&] {
-      launch_ulv_factor<T>(P->d_tasks + P->by_h[h].off, P->by_h[h].cnt, slots, P->max_m, P->max_n, st);
+  for (size_t h = 0; h < P->by_h.size(); ++h) {
+    const Seg& g = P->by_h[h];
+    traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, g.cnt, st, [&] {
+      if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax))
+        launch_ulv_factor_fast<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, st);
+      else
+        launch_ulv_factor<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
     });
+  }
 }
 
 template <typename T>
@@ -622,7 +635,8 @@ int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t
   int rc = check_cols(P, io, true);
   if (rc) return rc;
   const bool fp32 = f->prec == HSS_PREC_FP32;
-  const bool refine = fp32 || tol > 0.0;
+  // tol < 0: a single solve in the factor's precision, no residual
+  const bool refine = tol >= 0.0 && (fp32 || tol > 0.0);
   if (stats) { stats->iterations = 0; stats->converged = refine ? 0 : 1; stats->residual = -1.0; }
   std::vector<int64_t> off(P->ntrees + 1, 0), roff(P->ntrees + 1, 0);
   for (int32_t t = 0; t < P->ntrees; ++t) {
@@ -940,6 +954,14 @@ int hss_trace_end(double* total_ms, int64_t* launches) {
 }
 
 int64_t hss_launch_counter(void) { return g_launches; }
+
+int hss_set_option(int32_t option, int64_t value) {
+  if (option == HSS_OPT_GENERIC_FACTOR) {
+    g_generic_factor = value != 0;
+    return HSS_OK;
+  }
+  return fail(HSS_ERR_INVALID, "unknown option");
+}
 
 int hss_factor_bytes(hss_factor f, int64_t* bytes) {
   if (!f || !bytes) return fail(HSS_ERR_INVALID, "null factor");

@@ -1,0 +1,430 @@
+// ULV reduction of one node per thread block, for nodes up to 128 x 128 with
+// ranks up to 64 (every node of the leafsize-128 and leafsize-64 workloads).
+//
+// Same arithmetic and reflector order as ulv_factor_kernel (hss_kernels.cu),
+// restated from src/ulvfactor.jl:22-57 and :74-79, but with the working block
+// on chip:
+//   P0  load the leaf generators (FP64 -> T) or assemble the merged block of
+//       the children into shared memory (D: m x n, U: m x ku, ld odd);
+//   P1  QL of U with Q^T applied to D (geqlf!/ormql!, :39-41) in shared
+//       memory: one thread per column and row quarter, partial dot products
+//       combined through shared memory;
+//   P2  LQ of D[0:mk, :] with the reflectors applied to the rows below and to
+//       V (gelqf!/ormlq!, :44-50) with D held in registers: thread (row j,
+//       quarter q) owns D[j, 32q:32q+32]; the reflector row is broadcast
+//       through a bank-padded shared vector; V lives in registers as 16-row
+//       strips per column.
+// The root block gets an LU with partial pivoting in shared memory instead.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "hss_internal.h"
+#include "hss_launch.h"
+
+namespace hss {
+
+namespace {
+
+constexpr int FT = 512;           // threads per block
+constexpr int FW = FT / 32;
+constexpr int FMAX = 128;         // max m, n
+constexpr int FKMAX = 64;         // max ku, kv
+constexpr int PART_COLS = FMAX + FKMAX;
+constexpr size_t kFastSmemCap = 226 * 1024;   // dynamic part; the static part is < 1 KB
+
+template <typename T>
+__device__ __forceinline__ T wsum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T bsum(T v, T* red) {
+  v = wsum(v);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  T s = T(0);
+#pragma unroll
+  for (int i = 0; i < FW; ++i) s += red[i];
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ void larfg(T alpha, T ss, T& beta, T& tau, T& scal) {
+  if (ss == T(0)) {
+    tau = T(0);
+    beta = alpha;
+    scal = T(1);
+  } else {
+    const T xnorm = sqrt(ss);
+    beta = -copysign(hypot(alpha, xnorm), alpha);
+    tau = (beta - alpha) / beta;
+    scal = T(1) / (alpha - beta);
+  }
+}
+
+// padded index of the broadcast vector: 33 slots per 32 entries (no bank conflicts)
+__device__ __forceinline__ int vp(int i) { return i + (i >> 5); }
+
+// LU with partial pivoting of an m x m block in shared memory (ld = ld).
+template <typename T>
+__device__ void lu_smem(T* A, int m, int ld, int32_t* piv, int32_t* err, T* bv, int* bi, int* prow) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int c = 0; c < m; ++c) {
+    T best = T(-1);
+    int idx = m;
+    for (int i = c + tid; i < m; i += FT) {
+      const T a = fabs(A[i + c * ld]);
+      if (a > best) { best = a; idx = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+      if (ob > best || (ob == best && oi < idx)) { best = ob; idx = oi; }
+    }
+    if (lane == 0) { bv[warp] = best; bi[warp] = idx; }
+    __syncthreads();
+    if (tid == 0) {
+      T b = bv[0];
+      int ix = bi[0];
+      for (int w = 1; w < FW; ++w)
+        if (bv[w] > b || (bv[w] == b && bi[w] < ix)) { b = bv[w]; ix = bi[w]; }
+      if (ix >= m) ix = c;
+      *prow = ix;
+      piv[c] = ix;
+      if (A[ix + c * ld] == T(0) && err != nullptr) atomicExch(err, DEV_SINGULAR);
+    }
+    __syncthreads();
+    const int p = *prow;
+    if (p != c)
+      for (int j = tid; j < m; j += FT) {
+        const T t = A[c + j * ld];
+        A[c + j * ld] = A[p + j * ld];
+        A[p + j * ld] = t;
+      }
+    __syncthreads();
+    const T d = A[c + c * ld];
+    if (d != T(0))
+      for (int i = c + 1 + tid; i < m; i += FT) A[i + c * ld] /= d;
+    __syncthreads();
+    const int rem = m - c - 1;
+    for (int o = tid; o < rem * rem; o += FT) {
+      const int i = c + 1 + o % rem, j = c + 1 + o / rem;
+      A[i + j * ld] -= A[i + c * ld] * A[c + j * ld];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __restrict__ tasks,
+                                                                const Slot* __restrict__ slots,
+                                                                int LDD, int nmax, int kumax) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ T red[FW];
+  __shared__ T scal3[3];
+  __shared__ int bi[FW];
+  __shared__ int prow;
+  const Task tk = tasks[blockIdx.x];
+  const Node* nodes = tk.nodes;
+  const Node& nd = nodes[tk.node];
+  const Slot& sl = slots[tk.slot];
+  T* fb = (T*)sl.fbase;
+  const int m = nd.m, n = nd.n, ku = nd.ku, kv = nd.kv;
+  T* sD = (T*)smraw;                                // m x n, ld LDD
+  T* sU = sD + (size_t)LDD * nmax;                  // m x ku, ld LDD
+  T* part = sU + (size_t)LDD * (kumax > 0 ? kumax : 1);
+  T* sv = part + 4 * PART_COLS;                     // padded broadcast vector
+  T* gD = fb + nd.fD;
+  T* gU = fb + nd.fU;
+  T* gV = fb + nd.fV;
+  const int tid = threadIdx.x;
+
+  // ---- P0: load or assemble the node's block --------------------------------
+  if (nd.leaf) {
+    for (int e = tid; e < m * n; e += FT) sD[(e % m) + (e / m) * LDD] = (T)nd.D[e];
+    if (!nd.root)
+      for (int e = tid; e < m * ku; e += FT) sU[(e % m) + (e / m) * LDD] = (T)nd.U[e];
+  } else {
+    const Node& c1 = nodes[nd.left];
+    const Node& c2 = nodes[nd.right];
+    const T* D1 = fb + c1.fD + c1.mk + (int64_t)c1.nk * c1.m;
+    const T* D2 = fb + c2.fD + c2.mk + (int64_t)c2.nk * c2.m;
+    const T* U1 = fb + c1.fU + c1.mk;
+    const T* U2 = fb + c2.fU + c2.mk;
+    const T* V1 = fb + c1.fV + c1.nk;
+    const T* V2 = fb + c2.fV + c2.nk;
+    T* T12 = fb + nd.fT12;
+    T* T21 = fb + nd.fT21;
+    for (int o = tid; o < c1.mr * c2.kv; o += FT) {
+      const int i = o % c1.mr, j = o / c1.mr;
+      const int lmax = c1.lower_u ? min(i + 1, c1.ku) : c1.ku;
+      T s = T(0);
+      for (int l = 0; l < lmax; ++l) s += U1[i + (int64_t)l * c1.m] * (T)nd.B12[l + (int64_t)j * c1.ku];
+      T12[i + (int64_t)j * c1.mr] = s;
+    }
+    for (int o = tid; o < c2.mr * c1.kv; o += FT) {
+      const int i = o % c2.mr, j = o / c2.mr;
+      const int lmax = c2.lower_u ? min(i + 1, c2.ku) : c2.ku;
+      T s = T(0);
+      for (int l = 0; l < lmax; ++l) s += U2[i + (int64_t)l * c2.m] * (T)nd.B21[l + (int64_t)j * c2.ku];
+      T21[i + (int64_t)j * c2.mr] = s;
+    }
+    if (!nd.root) {
+      for (int o = tid; o < m * ku; o += FT) {
+        const int i = o % m, j = o / m;
+        T s = T(0);
+        if (i < c1.mr) {
+          const int lmax = c1.lower_u ? min(i + 1, c1.ku) : c1.ku;
+          for (int l = 0; l < lmax; ++l) s += U1[i + (int64_t)l * c1.m] * (T)nd.R1[l + (int64_t)j * c1.ku];
+        } else {
+          const int i2 = i - c1.mr;
+          const int lmax = c2.lower_u ? min(i2 + 1, c2.ku) : c2.ku;
+          for (int l = 0; l < lmax; ++l) s += U2[i2 + (int64_t)l * c2.m] * (T)nd.R2[l + (int64_t)j * c2.ku];
+        }
+        sU[i + j * LDD] = s;
+      }
+      for (int o = tid; o < n * kv; o += FT) {
+        const int i = o % n, j = o / n;
+        T s = T(0);
+        if (i < c1.nr) {
+          for (int l = 0; l < c1.kv; ++l) s += V1[i + (int64_t)l * c1.n] * (T)nd.W1[l + (int64_t)j * c1.kv];
+        } else {
+          const int i2 = i - c1.nr;
+          for (int l = 0; l < c2.kv; ++l) s += V2[i2 + (int64_t)l * c2.n] * (T)nd.W2[l + (int64_t)j * c2.kv];
+        }
+        gV[i + (int64_t)j * n] = s;
+      }
+    }
+    __syncthreads();   // T12 / T21 (global) visible to the block
+    for (int o = tid; o < m * n; o += FT) {
+      const int i = o % m, j = o / m;
+      T val;
+      if (i < c1.mr) {
+        if (j < c1.nr) {
+          val = D1[i + (int64_t)j * c1.m];
+        } else {
+          const int j2 = j - c1.nr;
+          T s = T(0);
+          for (int l = 0; l < c2.kv; ++l) s += T12[i + (int64_t)l * c1.mr] * V2[j2 + (int64_t)l * c2.n];
+          val = s;
+        }
+      } else {
+        const int i2 = i - c1.mr;
+        if (j < c1.nr) {
+          T s = T(0);
+          for (int l = 0; l < c1.kv; ++l) s += T21[i2 + (int64_t)l * c2.mr] * V1[j + (int64_t)l * c1.n];
+          val = s;
+        } else {
+          val = D2[i2 + (int64_t)(j - c1.nr) * c2.m];
+        }
+      }
+      sD[i + j * LDD] = val;
+    }
+  }
+  __syncthreads();
+
+  if (nd.root) {
+    lu_smem(sD, m, LDD, (int32_t*)(fb + nd.fpiv), sl.err, red, bi, &prow);
+    for (int e = tid; e < m * n; e += FT) gD[e] = sD[(e % m) + (e / m) * LDD];
+    return;
+  }
+  if (nd.mk == 0) {
+    // nothing to eliminate: the block passes up as it is (src/ulvfactor.jl:32-36)
+    for (int e = tid; e < m * n; e += FT) gD[e] = sD[(e % m) + (e / m) * LDD];
+    for (int e = tid; e < m * ku; e += FT) gU[e] = sU[(e % m) + (e / m) * LDD];
+    if (nd.leaf)
+      for (int e = tid; e < n * kv; e += FT) gV[e] = (T)nd.V[e];
+    return;
+  }
+
+  const int k = nd.k, mk = nd.mk;
+  T* tq = fb + nd.ftq;
+  T* tl = fb + nd.ftl;
+
+  // ---- P1: QL of U, Q^T applied to D (shared memory) -------------------------
+  {
+    const int cs = tid & 127, rq = tid >> 7, r0 = rq * 32;
+    for (int c = k - 1; c >= 0; --c) {
+      const int p = mk + c;
+      T* u = sU + c * LDD;
+      T ss = (tid < p) ? u[tid] * u[tid] : T(0);
+      ss = bsum(ss, red);
+      if (tid == 0) {
+        T beta, tau, sc;
+        larfg(u[p], ss, beta, tau, sc);
+        scal3[0] = beta; scal3[1] = tau; scal3[2] = sc;
+      }
+      __syncthreads();
+      const T tau = scal3[1];
+      if (tau != T(0) && tid < p) u[tid] *= scal3[2];
+      __syncthreads();
+      if (tid == 0) { u[p] = scal3[0]; tq[c] = tau; }
+      if (tau == T(0)) { __syncthreads(); continue; }
+      const int lim = min(32, p + 1 - r0);   // rows r0 .. r0+lim-1 are <= p
+      T vr[32];
+#pragma unroll
+      for (int l = 0; l < 32; ++l) {
+        const int i = r0 + l;
+        vr[l] = (l < lim) ? (i < p ? u[i] : T(1)) : T(0);
+      }
+      const int ncols = c + n;
+      for (int col = cs; col < ncols; col += 128) {
+        const T* cp = col < n ? sD + col * LDD : sU + (col - n) * LDD;
+        T s = T(0);
+#pragma unroll
+        for (int l = 0; l < 32; ++l)
+          if (l < lim) s += vr[l] * cp[r0 + l];
+        part[rq * PART_COLS + col] = s;
+      }
+      __syncthreads();
+      for (int col = cs; col < ncols; col += 128) {
+        T* cp = col < n ? sD + col * LDD : sU + (col - n) * LDD;
+        const T w = tau * (part[col] + part[PART_COLS + col] + part[2 * PART_COLS + col] +
+                           part[3 * PART_COLS + col]);
+#pragma unroll
+        for (int l = 0; l < 32; ++l)
+          if (l < lim) cp[r0 + l] -= w * vr[l];
+      }
+      __syncthreads();
+    }
+  }
+  for (int e = tid; e < m * ku; e += FT) gU[e] = sU[(e % m) + (e / m) * LDD];
+
+  // ---- P2: LQ of D[0:mk, :], applied to D[i+1:m, :] and to V (registers) ----
+  const int j = tid >> 2, q = tid & 3, c0 = q * 32;
+  const unsigned gmask = 0xFu << ((tid & 31) & ~3);     // the 4 lanes of row j
+  T d[32];
+#pragma unroll
+  for (int l = 0; l < 32; ++l) {
+    const int col = c0 + l;
+    d[l] = (j < m && col < n) ? sD[j + col * LDD] : T(0);
+  }
+  const int vcol = tid >> 4, vseg = tid & 15;
+  T vv[2][8];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int c = vcol + 32 * h;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int row = 8 * vseg + r;
+      T x = T(0);
+      if (c < kv && row < n) x = nd.leaf ? (T)nd.V[row + (int64_t)c * n] : gV[row + (int64_t)c * n];
+      vv[h][r] = x;
+    }
+  }
+  const int nl = min(mk, n);
+  for (int i = 0; i < nl; ++i) {
+    if (j == i) {
+      T ss = T(0), mine = T(0);
+#pragma unroll
+      for (int l = 0; l < 32; ++l) {
+        const int col = c0 + l;
+        if (col > i) ss += d[l] * d[l];
+        if (col == i) mine = d[l];
+      }
+      ss += __shfl_xor_sync(gmask, ss, 1);
+      ss += __shfl_xor_sync(gmask, ss, 2);
+      const T alpha = __shfl_sync(gmask, mine, i >> 5, 4);
+      T beta, tau, sc;
+      larfg(alpha, ss, beta, tau, sc);
+#pragma unroll
+      for (int l = 0; l < 32; ++l) {
+        const int col = c0 + l;
+        if (col > i && tau != T(0)) d[l] *= sc;
+        if (col == i) d[l] = beta;
+        sv[vp(col)] = col < i ? T(0) : (col == i ? T(1) : d[l]);
+      }
+      if (q == 0) { scal3[1] = tau; tl[i] = tau; }
+    }
+    __syncthreads();
+    const T tau = scal3[1];
+    if (tau != T(0)) {
+      if (j > i && j < m) {
+        T w = T(0);
+#pragma unroll
+        for (int l = 0; l < 32; ++l) w += d[l] * sv[vp(c0 + l)];
+        w += __shfl_xor_sync(gmask, w, 1);
+        w += __shfl_xor_sync(gmask, w, 2);
+        w *= tau;
+#pragma unroll
+        for (int l = 0; l < 32; ++l) d[l] -= w * sv[vp(c0 + l)];
+      }
+      {
+        // every lane takes part (columns >= kv hold zeros): full-warp shuffles
+        T w0 = T(0), w1 = T(0);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          const T s = sv[vp(8 * vseg + r)];
+          w0 += s * vv[0][r];
+          w1 += s * vv[1][r];
+        }
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+          w0 += __shfl_xor_sync(0xffffffffu, w0, o);
+          w1 += __shfl_xor_sync(0xffffffffu, w1, o);
+        }
+        w0 *= tau;
+        w1 *= tau;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          const T s = sv[vp(8 * vseg + r)];
+          vv[0][r] -= w0 * s;
+          vv[1][r] -= w1 * s;
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int l = 0; l < 32; ++l) {
+    const int col = c0 + l;
+    if (j < m && col < n) gD[j + (int64_t)col * m] = d[l];
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int c = vcol + 32 * h;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int row = 8 * vseg + r;
+      if (c < kv && row < n) gV[row + (int64_t)c * n] = vv[h][r];
+    }
+  }
+}
+
+}  // namespace
+
+template <typename T>
+size_t factor_fast_smem(int mmax, int nmax, int kumax) {
+  const int LDD = mmax | 1;
+  return ((size_t)LDD * nmax + (size_t)LDD * (kumax > 0 ? kumax : 1) + 4 * PART_COLS + (FMAX + FMAX / 32 + 8)) *
+         sizeof(T);
+}
+
+template <typename T>
+bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax) {
+  return mmax <= FMAX && nmax <= FMAX && kumax <= FKMAX && kvmax <= FKMAX &&
+         factor_fast_smem<T>(mmax, nmax, kumax) <= kFastSmemCap;
+}
+
+template <typename T>
+void launch_ulv_factor_fast(const Task* t, int64_t nt, const Slot* s, int mmax, int nmax, int kumax,
+                            cudaStream_t st) {
+  if (nt <= 0) return;
+  const size_t smem = factor_fast_smem<T>(mmax, nmax, kumax);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(ulv_factor_fast_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmemCap);
+    attr_set = true;
+  }
+  ulv_factor_fast_kernel<T><<<(unsigned)nt, FT, smem, st>>>(t, s, mmax | 1, nmax, kumax);
+}
+
+template bool factor_fast_fits<double>(int, int, int, int);
+template bool factor_fast_fits<float>(int, int, int, int);
+template void launch_ulv_factor_fast<double>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
+template void launch_ulv_factor_fast<float>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
+
+}  // namespace hss

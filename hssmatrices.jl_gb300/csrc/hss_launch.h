@@ -16,6 +16,11 @@ template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,
                        cudaStream_t st);
 template <typename T>
+bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax);
+template <typename T>
+void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax,
+                            cudaStream_t st);
+template <typename T>
 void launch_ulv_solve_up(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
 template <typename T>
 void launch_ulv_solve_down(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);

@@ -128,8 +128,9 @@ typedef struct {
 /* x = A \ b with the resident factorization (reference semantics of
  * `ulvfactsolve`, src/ulvfactor.jl:10-107).  For an FP32 factor the solve is
  * refined with FP64 HSS products until max_j ||b_j - A x_j|| / ||b_j|| <= tol
- * or maxit steps (HSS_ERR_NO_CONVERGENCE).  For an FP64 factor tol <= 0 skips
- * the residual; tol > 0 refines in FP64 the same way.  Device pointers. */
+ * or maxit steps (HSS_ERR_NO_CONVERGENCE).  For an FP64 factor tol = 0 skips
+ * the residual; tol > 0 refines in FP64 the same way.  tol < 0 is a single
+ * solve in the factor's precision without any residual.  Device pointers. */
 int hss_ulvsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double* dX,
                  int64_t ldx, double tol, int32_t maxit, hss_solve_stats* stats,
                  void* stream);
@@ -169,6 +170,12 @@ int hss_trace_end(double* total_ms, int64_t* launches);
 
 /* Number of kernels this library has launched in the process so far. */
 int64_t hss_launch_counter(void);
+
+/* Process-wide switches.  HSS_OPT_GENERIC_FACTOR = 1 routes every ULV
+ * factorization level to the global-memory kernel (used to test the on-chip
+ * kernel against it); 0 (default) picks the on-chip kernel where it fits. */
+enum { HSS_OPT_GENERIC_FACTOR = 1 };
+int hss_set_option(int32_t option, int64_t value);
 
 const char* hss_last_error(void);
 int32_t hss_version(void);

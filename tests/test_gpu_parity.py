@@ -165,3 +165,24 @@ def test_singular_root_raises(pkg):
     B = pkg.HssMatrix.branch(l1, l2, z[:2, :2], z[:2, :2])
     with pytest.raises(np.linalg.LinAlgError):
         pkg.ldiv(B, np.ones(8))
+
+
+@pytest.mark.parametrize("name", ["synthetic_perfect", "synthetic_uneven", "synthetic_earlyexit",
+                                  "cauchy2001_compress"])
+def test_factor_kernels_agree(pkg, lib, orc, name):
+    """The on-chip factor kernel and the global-memory one give the same solves."""
+    g, h, A = _golden(pkg, orc, name)
+    out = {}
+    for generic in (0, 1):
+        assert lib.hss_set_option(1, generic) == 0
+        try:
+            for prec in ("fp64", "fp32"):
+                F = pkg.ulvfactor(A, prec)
+                out[generic, prec] = F.solve(g["b"], tol=-1.0)
+        finally:
+            lib.hss_set_option(1, 0)
+    assert rel(out[0, "fp64"], out[1, "fp64"]) <= SOLVE_TOL.get(name, 1e-12)
+    assert rel(out[0, "fp64"], g["z"]) <= SOLVE_TOL.get(name, 1e-12)
+    # unrefined FP32 solves: both within FP32 accuracy of the FP64 answer
+    for generic in (0, 1):
+        assert rel(out[generic, "fp32"], g["z"]) <= (1e-2 if name == "cauchy2001_compress" else 1e-4)
