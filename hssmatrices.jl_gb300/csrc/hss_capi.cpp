@@ -103,6 +103,7 @@ struct SlotTable {
 struct Seg {
   int64_t off = 0, cnt = 0;
   int mmax = 0, nmax = 0, kumax = 0, kvmax = 0;   // largest node of the list
+  int c1u = 0, c2u = 0, c1v = 0, c2v = 0;          // largest children's ranks (branches)
 };
 
 inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
@@ -406,6 +407,7 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
       x.fV = fac; fac += align16((int64_t)x.n * x.kv);
       x.ftq = fac; fac += align16(x.root ? 0 : x.k);
       x.ftl = fac; fac += align16(x.mk);
+      x.fQt = fac; fac += align16((int64_t)x.n * x.mk);
       if (!x.leaf) {
         const Node& c1 = N[F(i, 0)];
         const Node& c2 = N[F(i, 1)];
@@ -432,6 +434,14 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
           v[lv].nmax = std::max(v[lv].nmax, x.n);
           v[lv].kumax = std::max(v[lv].kumax, x.ku);
           v[lv].kvmax = std::max(v[lv].kvmax, x.kv);
+          if (!x.leaf) {
+            const Node& c1 = P->nodes[x.left];
+            const Node& c2 = P->nodes[x.right];
+            v[lv].c1u = std::max(v[lv].c1u, c1.ku);
+            v[lv].c2u = std::max(v[lv].c2u, c2.ku);
+            v[lv].c1v = std::max(v[lv].c1v, c1.kv);
+            v[lv].c2v = std::max(v[lv].c2v, c2.kv);
+          }
         }
       }
       v[lv].cnt = (int64_t)tasks.size() - v[lv].off;
@@ -489,14 +499,25 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
 
 void run_matvec(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
   const Task* T = P->d_tasks;
+  constexpr size_t kStagedCap = 200 * 1024;
   traced(HSS_TRACE_MV_LEAF, P->leaves.cnt, st,
          [&] { launch_mv_leaf(T + P->leaves.off, P->leaves.cnt, slots, st); });
-  for (size_t h = 1; h < P->mv_up.size(); ++h)
-    traced(HSS_TRACE_MV_UP, P->mv_up[h].cnt, st,
-           [&] { launch_mv_up(T + P->mv_up[h].off, P->mv_up[h].cnt, slots, st); });
-  for (size_t d = 0; d < P->mv_dn.size(); ++d)
-    traced(HSS_TRACE_MV_DOWN, P->mv_dn[d].cnt, st,
-           [&] { launch_mv_down(T + P->mv_dn[d].off, P->mv_dn[d].cnt, slots, st); });
+  for (size_t h = 1; h < P->mv_up.size(); ++h) {
+    const Seg& g = P->mv_up[h];
+    traced(HSS_TRACE_MV_UP, g.cnt, st, [&] {
+      const size_t sm = mv_up_staged_smem(g.kvmax, g.c1v, g.c2v);
+      if (sm <= kStagedCap) launch_mv_up_staged(T + g.off, g.cnt, slots, sm, st);
+      else launch_mv_up(T + g.off, g.cnt, slots, st);
+    });
+  }
+  for (size_t d = 0; d < P->mv_dn.size(); ++d) {
+    const Seg& g = P->mv_dn[d];
+    traced(HSS_TRACE_MV_DOWN, g.cnt, st, [&] {
+      const size_t sm = mv_down_staged_smem(g.kumax, g.c1u, g.c2u, g.c1v, g.c2v);
+      if (sm <= kStagedCap) launch_mv_down_staged(T + g.off, g.cnt, slots, sm, st);
+      else launch_mv_down(T + g.off, g.cnt, slots, st);
+    });
+  }
   traced(HSS_TRACE_MV_FINAL, P->leaves.cnt, st,
          [&] { launch_mv_leaf_final(T + P->leaves.off, P->leaves.cnt, slots, st); });
 }
@@ -515,13 +536,25 @@ void run_factor(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
 }
 
 template <typename T>
-void run_solve(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
-  for (size_t h = 0; h < P->by_h.size(); ++h)
-    traced(HSS_TRACE_SOLVE_UP, P->by_h[h].cnt, st,
-           [&] { launch_ulv_solve_up<T>(P->d_tasks + P->by_h[h].off, P->by_h[h].cnt, slots, st); });
-  for (size_t d = 0; d < P->by_d.size(); ++d)
-    traced(HSS_TRACE_SOLVE_DOWN, P->by_d[d].cnt, st,
-           [&] { launch_ulv_solve_down<T>(P->d_tasks + P->by_d[d].off, P->by_d[d].cnt, slots, st); });
+void run_solve(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
+  for (size_t h = 0; h < P->by_h.size(); ++h) {
+    const Seg& g = P->by_h[h];
+    traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
+      if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
+        launch_ulv_solve_up_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, rmax, st);
+      else
+        launch_ulv_solve_up<T>(P->d_tasks + g.off, g.cnt, slots, st);
+    });
+  }
+  for (size_t d = 0; d < P->by_d.size(); ++d) {
+    const Seg& g = P->by_d[d];
+    traced(HSS_TRACE_SOLVE_DOWN, g.cnt, st, [&] {
+      if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
+        launch_ulv_solve_down_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.nmax, rmax, st);
+      else
+        launch_ulv_solve_down<T>(P->d_tasks + g.off, g.cnt, slots, st);
+    });
+  }
 }
 
 struct Cols {   // per-tree product / solve operands
@@ -613,7 +646,7 @@ int solve_pass(hss_factor_s* f, const std::vector<Cols>& io, const double* scale
     x.err = P->d_err;
   }
   CUDA_TRY(table.upload(s, st));
-  run_solve<T>(P, table.dev.p, st);
+  run_solve<T>(P, table.dev.p, (int)rmax, st);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }

@@ -378,10 +378,12 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
     }
     __syncthreads();
   }
+  T* gQt = fb + nd.fQt;
 #pragma unroll
   for (int l = 0; l < 32; ++l) {
     const int col = c0 + l;
     if (j < m && col < n) gD[j + (int64_t)col * m] = d[l];
+    if (j < mk && col < n) gQt[col + (int64_t)j * n] = col < j ? T(0) : (col == j ? T(1) : d[l]);
   }
 #pragma unroll
   for (int h = 0; h < 2; ++h) {

@@ -33,8 +33,9 @@ struct Node {
   // solve b (m rows), u (kv rows), x (n rows)
   int64_t wz, wf, wb, wu, wx;
   // factor storage element offsets: D (m x n; root: LU), U (m x ku),
-  // V (n x kv), tau_ql (k), tau_lq (mk), T12 (mr1 x kv2), T21 (mr2 x kv1), pivots (root)
-  int64_t fD, fU, fV, ftq, ftl, fT12, fT21, fpiv;
+  // V (n x kv), tau_ql (k), tau_lq (mk), T12 (mr1 x kv2), T21 (mr2 x kv1), pivots (root),
+  // Qt (n x mk): the LQ reflectors as columns (explicit 1 on the diagonal, 0 above)
+  int64_t fD, fU, fV, ftq, ftl, fT12, fT21, fpiv, fQt;
 };
 
 struct Task {

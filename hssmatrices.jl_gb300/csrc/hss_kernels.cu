@@ -244,6 +244,115 @@ __global__ void __launch_bounds__(NT) mv_down_kernel(const Task* __restrict__ ta
   }
 }
 
+// Staged variants of the two translator sweeps: every operand of the node is
+// first copied into shared memory with all threads (independent, coalesced
+// loads), then the small products run out of shared memory.  Right-hand sides
+// are processed in chunks of MV_RC columns.
+constexpr int MV_RC = 32;
+
+__device__ __forceinline__ void stage(double* dst, const double* __restrict__ src, int64_t cnt) {
+  for (int64_t e = threadIdx.x; e < cnt; e += NT) dst[e] = src[e];
+}
+// dst(c + l*cols) = src(l + c*rows): a transposed copy (rows x cols source)
+__device__ __forceinline__ void stage_t(double* dst, const double* __restrict__ src, int rows, int cols) {
+  for (int e = threadIdx.x; e < rows * cols; e += NT) {
+    const int l = e % rows, c = e / rows;
+    dst[c + l * cols] = src[e];
+  }
+}
+__device__ __forceinline__ void stage_cols(double* dst, const double* __restrict__ src, int rows, int64_t ld,
+                                           int ncols) {
+  for (int e = threadIdx.x; e < rows * ncols; e += NT) {
+    const int i = e % rows, j = e / rows;
+    dst[e] = src[i + (int64_t)j * ld];
+  }
+}
+
+// Upsweep, non-root branch: Z = W1^T Z1 + W2^T Z2 (src/matmul.jl:39).
+__global__ void __launch_bounds__(NT) mv_up_staged_kernel(const Task* __restrict__ tasks,
+                                                          const Slot* __restrict__ slots) {
+  extern __shared__ __align__(16) double sm[];
+  const Task tk = tasks[blockIdx.x];
+  const Node& nd = tk.nodes[tk.node];
+  const Node& c1 = tk.nodes[nd.left];
+  const Node& c2 = tk.nodes[nd.right];
+  const Slot& sl = slots[tk.slot];
+  const double* ws = (const double*)sl.ws;
+  const int64_t ld = sl.ldws;
+  const int kv = nd.kv, k1 = c1.kv, k2 = c2.kv, r = sl.r;
+  double* W1t = sm;                  // kv x k1 (transposed)
+  double* W2t = W1t + kv * k1;       // kv x k2
+  double* Z1 = W2t + kv * k2;        // k1 x MV_RC
+  double* Z2 = Z1 + k1 * MV_RC;      // k2 x MV_RC
+  stage_t(W1t, nd.W1, k1, kv);
+  stage_t(W2t, nd.W2, k2, kv);
+  for (int j0 = 0; j0 < r; j0 += MV_RC) {
+    const int nc = min(MV_RC, r - j0);
+    stage_cols(Z1, ws + c1.wz + (int64_t)j0 * ld, k1, ld, nc);
+    stage_cols(Z2, ws + c2.wz + (int64_t)j0 * ld, k2, ld, nc);
+    __syncthreads();
+    double* Z = (double*)sl.ws + nd.wz + (int64_t)j0 * ld;
+    for (int o = threadIdx.x; o < kv * nc; o += NT) {
+      const int c = o % kv, j = o / kv;
+      double s = 0.0;
+      for (int l = 0; l < k1; ++l) s = fma(W1t[c + l * kv], Z1[l + j * k1], s);
+      for (int l = 0; l < k2; ++l) s = fma(W2t[c + l * kv], Z2[l + j * k2], s);
+      Z[c + (int64_t)j * ld] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// Downsweep, branch: F1 = B12 Z2 + R1 F, F2 = B21 Z1 + R2 F (src/matmul.jl:50-56).
+__global__ void __launch_bounds__(NT) mv_down_staged_kernel(const Task* __restrict__ tasks,
+                                                            const Slot* __restrict__ slots) {
+  extern __shared__ __align__(16) double sm[];
+  const Task tk = tasks[blockIdx.x];
+  const Node& nd = tk.nodes[tk.node];
+  const Node& c1 = tk.nodes[nd.left];
+  const Node& c2 = tk.nodes[nd.right];
+  const Slot& sl = slots[tk.slot];
+  double* ws = (double*)sl.ws;
+  const int64_t ld = sl.ldws;
+  const int ku = nd.root ? 0 : nd.ku, u1 = c1.ku, u2 = c2.ku, v1 = c1.kv, v2 = c2.kv, r = sl.r;
+  double* B12 = sm;                  // u1 x v2
+  double* B21 = B12 + u1 * v2;       // u2 x v1
+  double* R1 = B21 + u2 * v1;        // u1 x ku
+  double* R2 = R1 + u1 * ku;         // u2 x ku
+  double* Z1 = R2 + u2 * ku;         // v1 x MV_RC
+  double* Z2 = Z1 + v1 * MV_RC;      // v2 x MV_RC
+  double* Fs = Z2 + v2 * MV_RC;      // ku x MV_RC
+  stage(B12, nd.B12, (int64_t)u1 * v2);
+  stage(B21, nd.B21, (int64_t)u2 * v1);
+  if (ku > 0) {
+    stage(R1, nd.R1, (int64_t)u1 * ku);
+    stage(R2, nd.R2, (int64_t)u2 * ku);
+  }
+  for (int j0 = 0; j0 < r; j0 += MV_RC) {
+    const int nc = min(MV_RC, r - j0);
+    stage_cols(Z1, ws + c1.wz + (int64_t)j0 * ld, v1, ld, nc);
+    stage_cols(Z2, ws + c2.wz + (int64_t)j0 * ld, v2, ld, nc);
+    if (ku > 0) stage_cols(Fs, ws + nd.wf + (int64_t)j0 * ld, ku, ld, nc);
+    __syncthreads();
+    for (int o = threadIdx.x; o < (u1 + u2) * nc; o += NT) {
+      double s = 0.0;
+      if (o < u1 * nc) {
+        const int i = o % u1, j = o / u1;
+        for (int l = 0; l < v2; ++l) s = fma(B12[i + l * u1], Z2[l + j * v2], s);
+        for (int l = 0; l < ku; ++l) s = fma(R1[i + l * u1], Fs[l + j * ku], s);
+        ws[c1.wf + i + (int64_t)(j0 + j) * ld] = s;
+      } else {
+        const int o2 = o - u1 * nc;
+        const int i = o2 % u2, j = o2 / u2;
+        for (int l = 0; l < v1; ++l) s = fma(B21[i + l * u2], Z1[l + j * v1], s);
+        for (int l = 0; l < ku; ++l) s = fma(R2[i + l * u2], Fs[l + j * ku], s);
+        ws[c2.wf + i + (int64_t)(j0 + j) * ld] = s;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Leaves: C += alpha U F (src/matmul.jl:47), and per-column sums of squares.
 __global__ void __launch_bounds__(NT) mv_leaf_final_kernel(const Task* __restrict__ tasks,
                                                            const Slot* __restrict__ slots) {
@@ -525,6 +634,12 @@ __global__ void __launch_bounds__(NT) ulv_factor_kernel(const Task* __restrict__
   if (nd.mk == 0) return;   // k >= m: nothing to eliminate (src/ulvfactor.jl:32-36)
   ql_sweep(U, D, fb + nd.ftq, m, n, nd.k, red);
   lq_sweep(D, V, fb + nd.ftl, m, n, nd.mk, kv, red);
+  __syncthreads();
+  T* Qt = fb + nd.fQt;
+  for (int e = tid; e < nd.mk * n; e += NT) {
+    const int col = e % n, i = e / n;
+    Qt[col + (int64_t)i * n] = col < i ? T(0) : (col == i ? T(1) : D[i + (int64_t)col * m]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -766,6 +881,30 @@ void launch_mv_up(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
 }
 void launch_mv_down(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
   if (nt > 0) mv_down_kernel<<<(unsigned)nt, NT, 0, st>>>(t, s);
+}
+
+size_t mv_up_staged_smem(int kv, int k1max, int k2max) {
+  return sizeof(double) * ((size_t)kv * (k1max + k2max) + (size_t)(k1max + k2max) * MV_RC);
+}
+size_t mv_down_staged_smem(int ku, int u1, int u2, int v1, int v2) {
+  return sizeof(double) * ((size_t)u1 * v2 + (size_t)u2 * v1 + (size_t)(u1 + u2) * ku +
+                           (size_t)(v1 + v2 + ku) * MV_RC);
+}
+void launch_mv_up_staged(const Task* t, int64_t nt, const Slot* s, size_t smem, cudaStream_t st) {
+  static bool set = false;
+  if (!set) {
+    cudaFuncSetAttribute(mv_up_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    set = true;
+  }
+  if (nt > 0) mv_up_staged_kernel<<<(unsigned)nt, NT, smem, st>>>(t, s);
+}
+void launch_mv_down_staged(const Task* t, int64_t nt, const Slot* s, size_t smem, cudaStream_t st) {
+  static bool set = false;
+  if (!set) {
+    cudaFuncSetAttribute(mv_down_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    set = true;
+  }
+  if (nt > 0) mv_down_staged_kernel<<<(unsigned)nt, NT, smem, st>>>(t, s);
 }
 void launch_mv_leaf_final(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
   if (nt > 0) mv_leaf_final_kernel<<<(unsigned)nt, NT, 0, st>>>(t, s);

@@ -10,6 +10,12 @@ void launch_mv_leaf(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t s
 void launch_mv_up(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
 void launch_mv_down(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
 void launch_mv_leaf_final(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+// Shared-memory staged translator sweeps; smem from the *_smem helpers with the
+// level's largest ranks (children's and the node's own).
+size_t mv_up_staged_smem(int kv, int k1max, int k2max);
+size_t mv_down_staged_smem(int ku, int u1, int u2, int v1, int v2);
+void launch_mv_up_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, cudaStream_t st);
+void launch_mv_down_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, cudaStream_t st);
 
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>
@@ -20,6 +26,12 @@ bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax);
 template <typename T>
 void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax,
                             cudaStream_t st);
+// Register-resident solve sweeps for nodes with m, n <= 256 (hss_solve.cu).
+bool solve_reg_fits(int mmax, int nmax);
+template <typename T>
+void launch_ulv_solve_up_reg(const Task* t, int64_t ntasks, const Slot* s, int mmax, int r, cudaStream_t st);
+template <typename T>
+void launch_ulv_solve_down_reg(const Task* t, int64_t ntasks, const Slot* s, int nmax, int r, cudaStream_t st);
 template <typename T>
 void launch_ulv_solve_up(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
 template <typename T>
