@@ -104,6 +104,7 @@ struct Seg {
   int64_t off = 0, cnt = 0;
   int mmax = 0, nmax = 0, kumax = 0, kvmax = 0;   // largest node of the list
   int c1u = 0, c2u = 0, c1v = 0, c2v = 0;          // largest children's ranks (branches)
+  int kmax = 0, mkmax = 0;                         // largest ULV k and m - k
 };
 
 inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
@@ -434,6 +435,8 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
           v[lv].nmax = std::max(v[lv].nmax, x.n);
           v[lv].kumax = std::max(v[lv].kumax, x.ku);
           v[lv].kvmax = std::max(v[lv].kvmax, x.kv);
+          v[lv].kmax = std::max(v[lv].kmax, x.root ? 0 : x.k);
+          v[lv].mkmax = std::max(v[lv].mkmax, x.mk);
           if (!x.leaf) {
             const Node& c1 = P->nodes[x.left];
             const Node& c2 = P->nodes[x.right];
@@ -541,7 +544,7 @@ void run_solve(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
     const Seg& g = P->by_h[h];
     traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
       if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
-        launch_ulv_solve_up_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, rmax, st);
+        launch_ulv_solve_up_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.kmax, g.mkmax, rmax, st);
       else
         launch_ulv_solve_up<T>(P->d_tasks + g.off, g.cnt, slots, st);
     });
@@ -550,7 +553,7 @@ void run_solve(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
     const Seg& g = P->by_d[d];
     traced(HSS_TRACE_SOLVE_DOWN, g.cnt, st, [&] {
       if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
-        launch_ulv_solve_down_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.nmax, rmax, st);
+        launch_ulv_solve_down_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.nmax, g.mkmax, rmax, st);
       else
         launch_ulv_solve_down<T>(P->d_tasks + g.off, g.cnt, slots, st);
     });

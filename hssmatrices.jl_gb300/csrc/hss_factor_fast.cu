@@ -30,6 +30,7 @@ constexpr int FMAX = 128;         // max m, n
 constexpr int FKMAX = 64;         // max ku, kv
 constexpr int PART_COLS = FMAX + FKMAX;
 constexpr size_t kFastSmemCap = 226 * 1024;   // dynamic part; the static part is < 1 KB
+constexpr int SVLEN = FMAX + FMAX / 32 + 8;     // padded broadcast vector
 
 template <typename T>
 __device__ __forceinline__ T wsum(T v) {
@@ -127,6 +128,7 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
   __shared__ T scal3[3];
   __shared__ int bi[FW];
   __shared__ int prow;
+  __shared__ T stau[2];
   const Task tk = tasks[blockIdx.x];
   const Node* nodes = tk.nodes;
   const Node& nd = nodes[tk.node];
@@ -244,8 +246,88 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
   T* tq = fb + nd.ftq;
   T* tl = fb + nd.ftl;
 
-  // ---- P1: QL of U, Q^T applied to D (shared memory) -------------------------
-  {
+  // ---- P1: QL of U, Q^T applied to D -------------------------------------------
+  // Broadcast vectors are double-buffered: while every thread applies reflector
+  // c, the owner of the next column (already updated) builds reflector c-1, so
+  // each step needs one barrier.
+  T* sv0 = sv;
+  T* sv1 = sv + SVLEN;
+  if constexpr (sizeof(T) == 4) {
+    // FP32: column-owner registers.  Thread (column cl, quarter q) holds rows
+    // 32q..32q+31 of D[:, cl] and, for cl < ku, of U[:, cl].
+    const int cl = tid >> 2, q = tid & 3, r0 = q * 32;
+    const unsigned gm = 0xFu << ((tid & 31) & ~3);
+    T dc[32], uc[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+      const int row = r0 + l;
+      dc[l] = (row < m && cl < n) ? sD[row + cl * LDD] : T(0);
+      uc[l] = (row < m && cl < ku) ? sU[row + cl * LDD] : T(0);
+    }
+    auto ql_reflector = [&](int c, T* buf, int slot) {   // called by the 4 owners of U[:, c]
+      const int p = mk + c;
+      T ss = T(0), mine = T(0);
+#pragma unroll
+      for (int l = 0; l < 32; ++l) {
+        const int row = r0 + l;
+        if (row < p) ss += uc[l] * uc[l];
+        if (row == p) mine = uc[l];
+      }
+      ss += __shfl_xor_sync(gm, ss, 1);
+      ss += __shfl_xor_sync(gm, ss, 2);
+      const T alpha = __shfl_sync(gm, mine, p >> 5, 4);
+      T beta, tau, sc;
+      larfg(alpha, ss, beta, tau, sc);
+#pragma unroll
+      for (int l = 0; l < 32; ++l) {
+        const int row = r0 + l;
+        if (row < p && tau != T(0)) uc[l] *= sc;
+        if (row == p) uc[l] = beta;
+        buf[vp(row)] = row < p ? uc[l] : (row == p ? T(1) : T(0));
+      }
+      if (q == 0) { stau[slot] = tau; tq[c] = tau; }
+    };
+    if (cl == k - 1) ql_reflector(k - 1, sv0, 0);
+    __syncthreads();
+    for (int c = k - 1; c >= 0; --c) {
+      const int cur = (k - 1 - c) & 1;
+      const T* svc = cur ? sv1 : sv0;
+      const T tau = stau[cur];
+      if (tau != T(0)) {
+        if (cl < n) {
+          T w = T(0);
+#pragma unroll
+          for (int l = 0; l < 32; ++l) w += svc[vp(r0 + l)] * dc[l];
+          w += __shfl_xor_sync(gm, w, 1);
+          w += __shfl_xor_sync(gm, w, 2);
+          w *= tau;
+#pragma unroll
+          for (int l = 0; l < 32; ++l) dc[l] -= w * svc[vp(r0 + l)];
+        }
+        if (cl < c) {
+          T w = T(0);
+#pragma unroll
+          for (int l = 0; l < 32; ++l) w += svc[vp(r0 + l)] * uc[l];
+          w += __shfl_xor_sync(gm, w, 1);
+          w += __shfl_xor_sync(gm, w, 2);
+          w *= tau;
+#pragma unroll
+          for (int l = 0; l < 32; ++l) uc[l] -= w * svc[vp(r0 + l)];
+        }
+      }
+      if (c >= 1 && cl == c - 1) ql_reflector(c - 1, cur ? sv0 : sv1, cur ^ 1);
+      __syncthreads();
+    }
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+      const int row = r0 + l;
+      if (row < m && cl < ku) gU[row + (int64_t)cl * m] = uc[l];
+      if (row < m && cl < n) sD[row + cl * LDD] = dc[l];
+    }
+    __syncthreads();
+  } else {
+    // FP64: the working block stays in shared memory; one thread per column
+    // and row quarter, partial dot products combined through shared memory.
     const int cs = tid & 127, rq = tid >> 7, r0 = rq * 32;
     for (int c = k - 1; c >= 0; --c) {
       const int p = mk + c;
@@ -263,7 +345,7 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
       __syncthreads();
       if (tid == 0) { u[p] = scal3[0]; tq[c] = tau; }
       if (tau == T(0)) { __syncthreads(); continue; }
-      const int lim = min(32, p + 1 - r0);   // rows r0 .. r0+lim-1 are <= p
+      const int lim = min(32, p + 1 - r0);
       T vr[32];
 #pragma unroll
       for (int l = 0; l < 32; ++l) {
@@ -273,11 +355,11 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
       const int ncols = c + n;
       for (int col = cs; col < ncols; col += 128) {
         const T* cp = col < n ? sD + col * LDD : sU + (col - n) * LDD;
-        T s = T(0);
+        T sacc = T(0);
 #pragma unroll
         for (int l = 0; l < 32; ++l)
-          if (l < lim) s += vr[l] * cp[r0 + l];
-        part[rq * PART_COLS + col] = s;
+          if (l < lim) sacc += vr[l] * cp[r0 + l];
+        part[rq * PART_COLS + col] = sacc;
       }
       __syncthreads();
       for (int col = cs; col < ncols; col += 128) {
@@ -290,8 +372,8 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
       }
       __syncthreads();
     }
+    for (int e = tid; e < m * ku; e += FT) gU[e] = sU[(e % m) + (e / m) * LDD];
   }
-  for (int e = tid; e < m * ku; e += FT) gU[e] = sU[(e % m) + (e / m) * LDD];
 
   // ---- P2: LQ of D[0:mk, :], applied to D[i+1:m, :] and to V (registers) ----
   const int j = tid >> 2, q = tid & 3, c0 = q * 32;
@@ -316,50 +398,53 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
     }
   }
   const int nl = min(mk, n);
-  for (int i = 0; i < nl; ++i) {
-    if (j == i) {
-      T ss = T(0), mine = T(0);
+  auto lq_reflector = [&](int i, T* buf, int slot) {   // called by the 4 owners of row i
+    T ss = T(0), mine = T(0);
 #pragma unroll
-      for (int l = 0; l < 32; ++l) {
-        const int col = c0 + l;
-        if (col > i) ss += d[l] * d[l];
-        if (col == i) mine = d[l];
-      }
-      ss += __shfl_xor_sync(gmask, ss, 1);
-      ss += __shfl_xor_sync(gmask, ss, 2);
-      const T alpha = __shfl_sync(gmask, mine, i >> 5, 4);
-      T beta, tau, sc;
-      larfg(alpha, ss, beta, tau, sc);
-#pragma unroll
-      for (int l = 0; l < 32; ++l) {
-        const int col = c0 + l;
-        if (col > i && tau != T(0)) d[l] *= sc;
-        if (col == i) d[l] = beta;
-        sv[vp(col)] = col < i ? T(0) : (col == i ? T(1) : d[l]);
-      }
-      if (q == 0) { scal3[1] = tau; tl[i] = tau; }
+    for (int l = 0; l < 32; ++l) {
+      const int col = c0 + l;
+      if (col > i) ss += d[l] * d[l];
+      if (col == i) mine = d[l];
     }
-    __syncthreads();
-    const T tau = scal3[1];
+    ss += __shfl_xor_sync(gmask, ss, 1);
+    ss += __shfl_xor_sync(gmask, ss, 2);
+    const T alpha = __shfl_sync(gmask, mine, i >> 5, 4);
+    T beta, tau, sc;
+    larfg(alpha, ss, beta, tau, sc);
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+      const int col = c0 + l;
+      if (col > i && tau != T(0)) d[l] *= sc;
+      if (col == i) d[l] = beta;
+      buf[vp(col)] = col < i ? T(0) : (col == i ? T(1) : d[l]);
+    }
+    if (q == 0) { stau[slot] = tau; tl[i] = tau; }
+  };
+  if (nl > 0 && j == 0) lq_reflector(0, sv0, 0);
+  __syncthreads();
+  for (int i = 0; i < nl; ++i) {
+    const int cur = i & 1;
+    const T* svc = cur ? sv1 : sv0;
+    const T tau = stau[cur];
     if (tau != T(0)) {
       if (j > i && j < m) {
         T w = T(0);
 #pragma unroll
-        for (int l = 0; l < 32; ++l) w += d[l] * sv[vp(c0 + l)];
+        for (int l = 0; l < 32; ++l) w += d[l] * svc[vp(c0 + l)];
         w += __shfl_xor_sync(gmask, w, 1);
         w += __shfl_xor_sync(gmask, w, 2);
         w *= tau;
 #pragma unroll
-        for (int l = 0; l < 32; ++l) d[l] -= w * sv[vp(c0 + l)];
+        for (int l = 0; l < 32; ++l) d[l] -= w * svc[vp(c0 + l)];
       }
       {
         // every lane takes part (columns >= kv hold zeros): full-warp shuffles
         T w0 = T(0), w1 = T(0);
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          const T s = sv[vp(8 * vseg + r)];
-          w0 += s * vv[0][r];
-          w1 += s * vv[1][r];
+          const T sv_r = svc[vp(8 * vseg + r)];
+          w0 += sv_r * vv[0][r];
+          w1 += sv_r * vv[1][r];
         }
 #pragma unroll
         for (int o = 1; o < 16; o <<= 1) {
@@ -370,12 +455,13 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
         w1 *= tau;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          const T s = sv[vp(8 * vseg + r)];
-          vv[0][r] -= w0 * s;
-          vv[1][r] -= w1 * s;
+          const T sv_r = svc[vp(8 * vseg + r)];
+          vv[0][r] -= w0 * sv_r;
+          vv[1][r] -= w1 * sv_r;
         }
       }
     }
+    if (i + 1 < nl && j == i + 1) lq_reflector(i + 1, cur ? sv0 : sv1, cur ^ 1);
     __syncthreads();
   }
   T* gQt = fb + nd.fQt;
@@ -401,8 +487,7 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
 template <typename T>
 size_t factor_fast_smem(int mmax, int nmax, int kumax) {
   const int LDD = mmax | 1;
-  return ((size_t)LDD * nmax + (size_t)LDD * (kumax > 0 ? kumax : 1) + 4 * PART_COLS + (FMAX + FMAX / 32 + 8)) *
-         sizeof(T);
+  return ((size_t)LDD * nmax + (size_t)LDD * (kumax > 0 ? kumax : 1) + 4 * PART_COLS + 2 * SVLEN) * sizeof(T);
 }
 
 template <typename T>

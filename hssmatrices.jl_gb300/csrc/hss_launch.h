@@ -29,9 +29,11 @@ void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mm
 // Register-resident solve sweeps for nodes with m, n <= 256 (hss_solve.cu).
 bool solve_reg_fits(int mmax, int nmax);
 template <typename T>
-void launch_ulv_solve_up_reg(const Task* t, int64_t ntasks, const Slot* s, int mmax, int r, cudaStream_t st);
+void launch_ulv_solve_up_reg(const Task* t, int64_t ntasks, const Slot* s, int mmax, int kmax, int mkmax, int r,
+                             cudaStream_t st);
 template <typename T>
-void launch_ulv_solve_down_reg(const Task* t, int64_t ntasks, const Slot* s, int nmax, int r, cudaStream_t st);
+void launch_ulv_solve_down_reg(const Task* t, int64_t ntasks, const Slot* s, int nmax, int mkmax, int r,
+                               cudaStream_t st);
 template <typename T>
 void launch_ulv_solve_up(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
 template <typename T>

@@ -15,6 +15,7 @@
 // Downward pass per node (src/ulvfactor.jl:98-107): x <- Q_lq^T x, then the
 // un-eliminated tail goes to the children (or the output at a leaf).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 #include "hss_internal.h"
 #include "hss_launch.h"
@@ -77,11 +78,12 @@ __device__ __forceinline__ void upper_solve(T (&b)[RPT], const T* __restrict__ A
 
 template <typename T, int TPC, int MR>
 __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ tasks,
-                                                       const Slot* __restrict__ slots) {
+                                                       const Slot* __restrict__ slots, int stage_cap) {
   constexpr int RPT = MR / TPC;
   constexpr int CPB = ST / TPC;
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sb = (T*)smraw;   // LDS x CPB
+  T* sfac = sb + LDS * CPB;   // staged factor blocks (stage_cap elements)
   const Task tk = tasks[blockIdx.x];
   const Node* nodes = tk.nodes;
   const Node& nd = nodes[tk.node];
@@ -93,6 +95,25 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
   const int tid = threadIdx.x, g = tid / TPC, gl = tid % TPC;
   const int k = nd.k, mk = nd.mk, nk = nd.nk;
   T* u = ws + nd.wu;
+  // Factor blocks read inside the sequential sweeps are copied on chip once:
+  // the QL reflectors (m x k) and L1 (mk x mk), or the root LU (m x m).
+  const T* Up = fb + nd.fU;     // ld m
+  const T* Lp = fb + nd.fD;     // ld m
+  int ldL = m;
+  if (nd.root) {
+    if (m * m <= stage_cap) {
+      for (int e = tid; e < m * m; e += ST) sfac[e] = Lp[e];
+      Lp = sfac;
+    }
+  } else if (mk > 0 && m * k + mk * mk <= stage_cap) {
+    T* sU = sfac;
+    T* sL = sfac + m * k;
+    for (int e = tid; e < m * k; e += ST) sU[e] = Up[e];
+    for (int e = tid; e < mk * mk; e += ST) sL[e] = Lp[(e % mk) + (int64_t)(e / mk) * m];
+    Up = sU;
+    Lp = sL;
+    ldL = mk;
+  }
   for (int j0 = 0; j0 < r; j0 += CPB) {
     // ---- gather b for this chunk of columns into shared memory
     if (nd.leaf) {
@@ -143,7 +164,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
     __syncthreads();
     const int j = j0 + g;
     if (nd.root) {
-      const T* A = fb + nd.fD;
+      const T* A = Lp;
       const int32_t* piv = (const int32_t*)(fb + nd.fpiv);
       if (gl == 0) {
         T* col = sb + g * LDS;
@@ -173,9 +194,8 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
       continue;
     }
     if (mk > 0) {
-      const T* Uf = fb + nd.fU;
+      const T* Uf = Up;
       const T* tq = fb + nd.ftq;
-      const T* Df = fb + nd.fD;
       T b[RPT];
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
@@ -204,7 +224,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
         }
       }
       // zloc = L1 \ b[0:mk] (trsm, src/ulvfactor.jl:48)
-      lower_solve<T, TPC, RPT, false>(b, Df, m, mk, gl);
+      lower_solve<T, TPC, RPT, false>(b, Lp, ldL, mk, gl);
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
         const int row = gl + s * TPC;
@@ -241,9 +261,11 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
 
 template <typename T, int TPC, int MR>
 __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict__ tasks,
-                                                         const Slot* __restrict__ slots) {
+                                                         const Slot* __restrict__ slots, int stage_cap) {
   constexpr int RPT = MR / TPC;
   constexpr int CPB = ST / TPC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sQ = (T*)smraw;
   const Task tk = tasks[blockIdx.x];
   const Node* nodes = tk.nodes;
   const Node& nd = nodes[tk.node];
@@ -254,6 +276,12 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
   const int n = nd.n, r = sl.r;
   const int tid = threadIdx.x, g = tid / TPC, gl = tid % TPC;
   const T* x = ws + nd.wx;
+  const T* Qt = fb + nd.fQt;
+  if (!nd.root && nd.mk > 0 && n * nd.mk <= stage_cap) {
+    for (int e = tid; e < n * nd.mk; e += ST) sQ[e] = Qt[e];
+    Qt = sQ;
+    __syncthreads();
+  }
   for (int j0 = 0; j0 < r; j0 += CPB) {
     const int j = j0 + g;
     const bool act = j < r;
@@ -265,7 +293,6 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
     }
     if (!nd.root && nd.mk > 0) {
       // z[cols] = Q_lq^T z[cols]: reflectors i = mk-1 .. 0 (src/ulvfactor.jl:102)
-      const T* Qt = fb + nd.fQt;
       const T* tl = fb + nd.ftl;
       const int nl = min(nd.mk, n);
       for (int i = nl - 1; i >= 0; --i) {
@@ -315,20 +342,33 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
   }
 }
 
+constexpr size_t kSolveSmemCap = 200 * 1024;
+
 template <typename T, int TPC, int MR>
-void up_launch(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
-  const size_t smem = (size_t)LDS * (ST / TPC) * sizeof(T);
+void up_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStream_t st) {
+  const size_t base = (size_t)LDS * (ST / TPC) * sizeof(T);
+  size_t smem = base + want * sizeof(T);
+  if (smem > kSolveSmemCap) smem = base;   // factor blocks stay in global memory
   static bool set = false;
   if (!set) {
-    cudaFuncSetAttribute(ulv_solve_up_reg<T, TPC, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(ulv_solve_up_reg<T, TPC, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSolveSmemCap);
     set = true;
   }
-  ulv_solve_up_reg<T, TPC, MR><<<(unsigned)nt, ST, smem, st>>>(t, s);
+  ulv_solve_up_reg<T, TPC, MR><<<(unsigned)nt, ST, smem, st>>>(t, s, (int)((smem - base) / sizeof(T)));
 }
 
 template <typename T, int TPC, int MR>
-void down_launch(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
-  ulv_solve_down_reg<T, TPC, MR><<<(unsigned)nt, ST, 0, st>>>(t, s);
+void down_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStream_t st) {
+  size_t smem = want * sizeof(T);
+  if (smem > kSolveSmemCap) smem = 0;
+  static bool set = false;
+  if (!set) {
+    cudaFuncSetAttribute(ulv_solve_down_reg<T, TPC, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSolveSmemCap);
+    set = true;
+  }
+  ulv_solve_down_reg<T, TPC, MR><<<(unsigned)nt, ST, smem, st>>>(t, s, (int)(smem / sizeof(T)));
 }
 
 }  // namespace
@@ -336,26 +376,31 @@ void down_launch(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
 bool solve_reg_fits(int mmax, int nmax) { return mmax <= 256 && nmax <= 256; }
 
 template <typename T>
-void launch_ulv_solve_up_reg(const Task* t, int64_t nt, const Slot* s, int mmax, int r, cudaStream_t st) {
+void launch_ulv_solve_up_reg(const Task* t, int64_t nt, const Slot* s, int mmax, int kmax, int mkmax, int r,
+                             cudaStream_t st) {
   if (nt <= 0) return;
   const bool wide = r > 8;
-  if (mmax <= 64) wide ? up_launch<T, 8, 64>(t, nt, s, st) : up_launch<T, 32, 64>(t, nt, s, st);
-  else if (mmax <= 128) wide ? up_launch<T, 8, 128>(t, nt, s, st) : up_launch<T, 32, 128>(t, nt, s, st);
-  else wide ? up_launch<T, 8, 256>(t, nt, s, st) : up_launch<T, 32, 256>(t, nt, s, st);
+  // staged elements: reflectors + L1, or the root's LU (whichever is larger)
+  const size_t want = std::max((size_t)mmax * kmax + (size_t)mkmax * mkmax, (size_t)mmax * mmax);
+  if (mmax <= 64) wide ? up_launch<T, 8, 64>(t, nt, s, want, st) : up_launch<T, 32, 64>(t, nt, s, want, st);
+  else if (mmax <= 128) wide ? up_launch<T, 8, 128>(t, nt, s, want, st) : up_launch<T, 32, 128>(t, nt, s, want, st);
+  else wide ? up_launch<T, 8, 256>(t, nt, s, want, st) : up_launch<T, 32, 256>(t, nt, s, want, st);
 }
 
 template <typename T>
-void launch_ulv_solve_down_reg(const Task* t, int64_t nt, const Slot* s, int nmax, int r, cudaStream_t st) {
+void launch_ulv_solve_down_reg(const Task* t, int64_t nt, const Slot* s, int nmax, int mkmax, int r,
+                               cudaStream_t st) {
   if (nt <= 0) return;
   const bool wide = r > 8;
-  if (nmax <= 64) wide ? down_launch<T, 8, 64>(t, nt, s, st) : down_launch<T, 32, 64>(t, nt, s, st);
-  else if (nmax <= 128) wide ? down_launch<T, 8, 128>(t, nt, s, st) : down_launch<T, 32, 128>(t, nt, s, st);
-  else wide ? down_launch<T, 8, 256>(t, nt, s, st) : down_launch<T, 32, 256>(t, nt, s, st);
+  const size_t want = (size_t)nmax * mkmax;
+  if (nmax <= 64) wide ? down_launch<T, 8, 64>(t, nt, s, want, st) : down_launch<T, 32, 64>(t, nt, s, want, st);
+  else if (nmax <= 128) wide ? down_launch<T, 8, 128>(t, nt, s, want, st) : down_launch<T, 32, 128>(t, nt, s, want, st);
+  else wide ? down_launch<T, 8, 256>(t, nt, s, want, st) : down_launch<T, 32, 256>(t, nt, s, want, st);
 }
 
-template void launch_ulv_solve_up_reg<double>(const Task*, int64_t, const Slot*, int, int, cudaStream_t);
-template void launch_ulv_solve_up_reg<float>(const Task*, int64_t, const Slot*, int, int, cudaStream_t);
-template void launch_ulv_solve_down_reg<double>(const Task*, int64_t, const Slot*, int, int, cudaStream_t);
-template void launch_ulv_solve_down_reg<float>(const Task*, int64_t, const Slot*, int, int, cudaStream_t);
+template void launch_ulv_solve_up_reg<double>(const Task*, int64_t, const Slot*, int, int, int, int, cudaStream_t);
+template void launch_ulv_solve_up_reg<float>(const Task*, int64_t, const Slot*, int, int, int, int, cudaStream_t);
+template void launch_ulv_solve_down_reg<double>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
+template void launch_ulv_solve_down_reg<float>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
 
 }  // namespace hss
