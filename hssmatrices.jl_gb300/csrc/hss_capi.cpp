@@ -105,6 +105,7 @@ struct Seg {
   int mmax = 0, nmax = 0, kumax = 0, kvmax = 0;   // largest node of the list
   int c1u = 0, c2u = 0, c1v = 0, c2v = 0;          // largest children's ranks (branches)
   int kmax = 0, mkmax = 0;                         // largest ULV k and m - k
+  int c1mr = 0, c2mr = 0, c1nr = 0, c2nr = 0;      // largest children's reduced sizes
 };
 
 inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
@@ -444,6 +445,10 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
             v[lv].c2u = std::max(v[lv].c2u, c2.ku);
             v[lv].c1v = std::max(v[lv].c1v, c1.kv);
             v[lv].c2v = std::max(v[lv].c2v, c2.kv);
+            v[lv].c1mr = std::max(v[lv].c1mr, c1.mr);
+            v[lv].c2mr = std::max(v[lv].c2mr, c2.mr);
+            v[lv].c1nr = std::max(v[lv].c1nr, c1.nr);
+            v[lv].c2nr = std::max(v[lv].c2nr, c2.nr);
           }
         }
       }
@@ -530,8 +535,13 @@ void run_factor(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
   for (size_t h = 0; h < P->by_h.size(); ++h) {
     const Seg& g = P->by_h[h];
     traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, g.cnt, st, [&] {
-      if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax))
-        launch_ulv_factor_fast<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, st);
+      // merge staging: converted generators, children's reduced U/V, T12/T21
+      const size_t extra = (size_t)g.c1u * g.c2v + (size_t)g.c2u * g.c1v + (size_t)(g.c1u + g.c2u) * g.kumax +
+                           (size_t)(g.c1v + g.c2v) * g.kvmax + (size_t)g.c1mr * g.c1u + (size_t)g.c2mr * g.c2u +
+                           (size_t)g.c1nr * g.c1v + (size_t)g.c2nr * g.c2v + (size_t)g.c1mr * g.c2v +
+                           (size_t)g.c2mr * g.c1v;
+      if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra))
+        launch_ulv_factor_fast<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, extra, st);
       else
         launch_ulv_factor<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
     });
@@ -629,6 +639,7 @@ int factor_impl(hss_factor_s* f, cudaStream_t st) {
 template <typename T>
 int solve_pass(hss_factor_s* f, const std::vector<Cols>& io, const double* scale,
                const int64_t* off, int mode, cudaStream_t st) {
+  const int64_t rtot = off[f->plan->ntrees];
   SlotTable& table = mode ? f->sv_slots_ref : f->sv_slots;
   hss_plan_s* P = f->plan;
   int64_t rmax = 0;
@@ -644,6 +655,7 @@ int solve_pass(hss_factor_s* f, const std::vector<Cols>& io, const double* scale
     x.ws = f->sv_ws.p; x.ldws = P->ws_sv;
     x.fbase = f->d_fac;
     x.colscale = scale ? scale + off[t] : nullptr;
+    x.colinv = scale ? scale + rtot + off[t] : nullptr;
     x.r = (int32_t)io[t].r;
     x.mode = mode;
     x.err = P->d_err;
@@ -685,7 +697,7 @@ int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t
   if (refine) {
     CUDA_TRY(f->bn2.ensure(rtot));
     CUDA_TRY(f->rn2.ensure(rtot));
-    CUDA_TRY(f->scale.ensure(rtot));
+    CUDA_TRY(f->scale.ensure(2 * rtot));
     CUDA_TRY(f->R.ensure(std::max<int64_t>(roff[P->ntrees], 1)));
     CUDA_TRY(f->h_bn2.ensure(rtot));
     CUDA_TRY(f->h_rn2.ensure(rtot));

@@ -17,6 +17,7 @@
 // The root block gets an LU with partial pivoting in shared memory instead.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include "hss_device.cuh"
 #include "hss_internal.h"
 #include "hss_launch.h"
 
@@ -53,16 +54,7 @@ __device__ __forceinline__ T bsum(T v, T* red) {
 
 template <typename T>
 __device__ __forceinline__ void larfg(T alpha, T ss, T& beta, T& tau, T& scal) {
-  if (ss == T(0)) {
-    tau = T(0);
-    beta = alpha;
-    scal = T(1);
-  } else {
-    const T xnorm = sqrt(ss);
-    beta = -copysign(hypot(alpha, xnorm), alpha);
-    tau = (beta - alpha) / beta;
-    scal = T(1) / (alpha - beta);
-  }
+  larfg_ss(alpha, ss, beta, tau, scal);
 }
 
 // padded index of the broadcast vector: 33 slots per 32 entries (no bank conflicts)
@@ -76,7 +68,7 @@ __device__ void lu_smem(T* A, int m, int ld, int32_t* piv, int32_t* err, T* bv, 
     T best = T(-1);
     int idx = m;
     for (int i = c + tid; i < m; i += FT) {
-      const T a = fabs(A[i + c * ld]);
+      const T a = dabs(A[i + c * ld]);
       if (a > best) { best = a; idx = i; }
     }
 #pragma unroll
@@ -138,7 +130,8 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
   T* sD = (T*)smraw;                                // m x n, ld LDD
   T* sU = sD + (size_t)LDD * nmax;                  // m x ku, ld LDD
   T* part = sU + (size_t)LDD * (kumax > 0 ? kumax : 1);
-  T* sv = part + 4 * PART_COLS;                     // padded broadcast vector
+  T* sv = part + 4 * PART_COLS;                     // padded broadcast vectors (2)
+  T* sx = sv + 2 * SVLEN;                           // merge staging (branches)
   T* gD = fb + nd.fD;
   T* gU = fb + nd.fU;
   T* gV = fb + nd.fV;
@@ -150,77 +143,111 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
     if (!nd.root)
       for (int e = tid; e < m * ku; e += FT) sU[(e % m) + (e / m) * LDD] = (T)nd.U[e];
   } else {
+    // Merge (src/ulvfactor.jl:74-79).  Generator blocks are converted to T
+    // once and, with the children's reduced U and V, staged in shared memory.
     const Node& c1 = nodes[nd.left];
     const Node& c2 = nodes[nd.right];
-    const T* D1 = fb + c1.fD + c1.mk + (int64_t)c1.nk * c1.m;
-    const T* D2 = fb + c2.fD + c2.mk + (int64_t)c2.nk * c2.m;
-    const T* U1 = fb + c1.fU + c1.mk;
-    const T* U2 = fb + c2.fU + c2.mk;
-    const T* V1 = fb + c1.fV + c1.nk;
-    const T* V2 = fb + c2.fV + c2.nk;
+    const int u1 = c1.ku, u2 = c2.ku, v1 = c1.kv, v2 = c2.kv;
+    const int mr1 = c1.mr, mr2 = c2.mr, nr1 = c1.nr, nr2 = c2.nr;
+    const int kuo = nd.root ? 0 : ku, kvo = nd.root ? 0 : kv;
+    T* gB12 = sx;                     // u1 x v2
+    T* gB21 = gB12 + u1 * v2;         // u2 x v1
+    T* gR1 = gB21 + u2 * v1;          // u1 x ku
+    T* gR2 = gR1 + u1 * kuo;          // u2 x ku
+    T* gW1 = gR2 + u2 * kuo;          // v1 x kv
+    T* gW2 = gW1 + v1 * kvo;          // v2 x kv
+    T* cU1 = gW2 + v2 * kvo;          // mr1 x u1 (tril applied when reduced)
+    T* cU2 = cU1 + mr1 * u1;          // mr2 x u2
+    T* cV1 = cU2 + mr2 * u2;          // nr1 x v1
+    T* cV2 = cV1 + nr1 * v1;          // nr2 x v2
+    T* sT12 = cV2 + nr2 * v2;         // mr1 x v2
+    T* sT21 = sT12 + mr1 * v2;        // mr2 x v1
+    for (int e = tid; e < u1 * v2; e += FT) gB12[e] = (T)nd.B12[e];
+    for (int e = tid; e < u2 * v1; e += FT) gB21[e] = (T)nd.B21[e];
+    for (int e = tid; e < u1 * kuo; e += FT) gR1[e] = (T)nd.R1[e];
+    for (int e = tid; e < u2 * kuo; e += FT) gR2[e] = (T)nd.R2[e];
+    for (int e = tid; e < v1 * kvo; e += FT) gW1[e] = (T)nd.W1[e];
+    for (int e = tid; e < v2 * kvo; e += FT) gW2[e] = (T)nd.W2[e];
+    {
+      const T* U1 = fb + c1.fU + c1.mk;   // ld c1.m
+      const T* U2 = fb + c2.fU + c2.mk;
+      const T* V1 = fb + c1.fV + c1.nk;   // ld c1.n
+      const T* V2 = fb + c2.fV + c2.nk;
+      for (int e = tid; e < mr1 * u1; e += FT) {
+        const int i = e % mr1, l = e / mr1;
+        cU1[e] = (c1.lower_u && l > i) ? T(0) : U1[i + (int64_t)l * c1.m];
+      }
+      for (int e = tid; e < mr2 * u2; e += FT) {
+        const int i = e % mr2, l = e / mr2;
+        cU2[e] = (c2.lower_u && l > i) ? T(0) : U2[i + (int64_t)l * c2.m];
+      }
+      for (int e = tid; e < nr1 * v1; e += FT) cV1[e] = V1[(e % nr1) + (int64_t)(e / nr1) * c1.n];
+      for (int e = tid; e < nr2 * v2; e += FT) cV2[e] = V2[(e % nr2) + (int64_t)(e / nr2) * c2.n];
+    }
+    __syncthreads();
     T* T12 = fb + nd.fT12;
     T* T21 = fb + nd.fT21;
-    for (int o = tid; o < c1.mr * c2.kv; o += FT) {
-      const int i = o % c1.mr, j = o / c1.mr;
-      const int lmax = c1.lower_u ? min(i + 1, c1.ku) : c1.ku;
+    for (int o = tid; o < mr1 * v2; o += FT) {
+      const int i = o % mr1, j = o / mr1;
       T s = T(0);
-      for (int l = 0; l < lmax; ++l) s += U1[i + (int64_t)l * c1.m] * (T)nd.B12[l + (int64_t)j * c1.ku];
-      T12[i + (int64_t)j * c1.mr] = s;
+      for (int l = 0; l < u1; ++l) s += cU1[i + l * mr1] * gB12[l + j * u1];
+      sT12[o] = s;
+      T12[o] = s;
     }
-    for (int o = tid; o < c2.mr * c1.kv; o += FT) {
-      const int i = o % c2.mr, j = o / c2.mr;
-      const int lmax = c2.lower_u ? min(i + 1, c2.ku) : c2.ku;
+    for (int o = tid; o < mr2 * v1; o += FT) {
+      const int i = o % mr2, j = o / mr2;
       T s = T(0);
-      for (int l = 0; l < lmax; ++l) s += U2[i + (int64_t)l * c2.m] * (T)nd.B21[l + (int64_t)j * c2.ku];
-      T21[i + (int64_t)j * c2.mr] = s;
+      for (int l = 0; l < u2; ++l) s += cU2[i + l * mr2] * gB21[l + j * u2];
+      sT21[o] = s;
+      T21[o] = s;
     }
     if (!nd.root) {
       for (int o = tid; o < m * ku; o += FT) {
         const int i = o % m, j = o / m;
         T s = T(0);
-        if (i < c1.mr) {
-          const int lmax = c1.lower_u ? min(i + 1, c1.ku) : c1.ku;
-          for (int l = 0; l < lmax; ++l) s += U1[i + (int64_t)l * c1.m] * (T)nd.R1[l + (int64_t)j * c1.ku];
+        if (i < mr1) {
+          for (int l = 0; l < u1; ++l) s += cU1[i + l * mr1] * gR1[l + j * u1];
         } else {
-          const int i2 = i - c1.mr;
-          const int lmax = c2.lower_u ? min(i2 + 1, c2.ku) : c2.ku;
-          for (int l = 0; l < lmax; ++l) s += U2[i2 + (int64_t)l * c2.m] * (T)nd.R2[l + (int64_t)j * c2.ku];
+          const int i2 = i - mr1;
+          for (int l = 0; l < u2; ++l) s += cU2[i2 + l * mr2] * gR2[l + j * u2];
         }
         sU[i + j * LDD] = s;
       }
       for (int o = tid; o < n * kv; o += FT) {
         const int i = o % n, j = o / n;
         T s = T(0);
-        if (i < c1.nr) {
-          for (int l = 0; l < c1.kv; ++l) s += V1[i + (int64_t)l * c1.n] * (T)nd.W1[l + (int64_t)j * c1.kv];
+        if (i < nr1) {
+          for (int l = 0; l < v1; ++l) s += cV1[i + l * nr1] * gW1[l + j * v1];
         } else {
-          const int i2 = i - c1.nr;
-          for (int l = 0; l < c2.kv; ++l) s += V2[i2 + (int64_t)l * c2.n] * (T)nd.W2[l + (int64_t)j * c2.kv];
+          const int i2 = i - nr1;
+          for (int l = 0; l < v2; ++l) s += cV2[i2 + l * nr2] * gW2[l + j * v2];
         }
         gV[i + (int64_t)j * n] = s;
       }
     }
-    __syncthreads();   // T12 / T21 (global) visible to the block
+    __syncthreads();
+    const T* D1 = fb + c1.fD + c1.mk + (int64_t)c1.nk * c1.m;
+    const T* D2 = fb + c2.fD + c2.mk + (int64_t)c2.nk * c2.m;
     for (int o = tid; o < m * n; o += FT) {
       const int i = o % m, j = o / m;
       T val;
-      if (i < c1.mr) {
-        if (j < c1.nr) {
+      if (i < mr1) {
+        if (j < nr1) {
           val = D1[i + (int64_t)j * c1.m];
         } else {
-          const int j2 = j - c1.nr;
+          const int j2 = j - nr1;
           T s = T(0);
-          for (int l = 0; l < c2.kv; ++l) s += T12[i + (int64_t)l * c1.mr] * V2[j2 + (int64_t)l * c2.n];
+          for (int l = 0; l < v2; ++l) s += sT12[i + l * mr1] * cV2[j2 + l * nr2];
           val = s;
         }
       } else {
-        const int i2 = i - c1.mr;
-        if (j < c1.nr) {
+        const int i2 = i - mr1;
+        if (j < nr1) {
           T s = T(0);
-          for (int l = 0; l < c1.kv; ++l) s += T21[i2 + (int64_t)l * c2.mr] * V1[j + (int64_t)l * c1.n];
+          for (int l = 0; l < v1; ++l) s += sT21[i2 + l * mr2] * cV1[j + l * nr1];
           val = s;
         } else {
-          val = D2[i2 + (int64_t)(j - c1.nr) * c2.m];
+          val = D2[i2 + (int64_t)(j - nr1) * c2.m];
         }
       }
       sD[i + j * LDD] = val;
@@ -485,22 +512,23 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
 }  // namespace
 
 template <typename T>
-size_t factor_fast_smem(int mmax, int nmax, int kumax) {
+size_t factor_fast_smem(int mmax, int nmax, int kumax, size_t extra) {
   const int LDD = mmax | 1;
-  return ((size_t)LDD * nmax + (size_t)LDD * (kumax > 0 ? kumax : 1) + 4 * PART_COLS + 2 * SVLEN) * sizeof(T);
+  return ((size_t)LDD * nmax + (size_t)LDD * (kumax > 0 ? kumax : 1) + 4 * PART_COLS + 2 * SVLEN + extra) *
+         sizeof(T);
 }
 
 template <typename T>
-bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax) {
+bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra) {
   return mmax <= FMAX && nmax <= FMAX && kumax <= FKMAX && kvmax <= FKMAX &&
-         factor_fast_smem<T>(mmax, nmax, kumax) <= kFastSmemCap;
+         factor_fast_smem<T>(mmax, nmax, kumax, extra) <= kFastSmemCap;
 }
 
 template <typename T>
 void launch_ulv_factor_fast(const Task* t, int64_t nt, const Slot* s, int mmax, int nmax, int kumax,
-                            cudaStream_t st) {
+                            size_t extra, cudaStream_t st) {
   if (nt <= 0) return;
-  const size_t smem = factor_fast_smem<T>(mmax, nmax, kumax);
+  const size_t smem = factor_fast_smem<T>(mmax, nmax, kumax, extra);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(ulv_factor_fast_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmemCap);
@@ -509,9 +537,9 @@ void launch_ulv_factor_fast(const Task* t, int64_t nt, const Slot* s, int mmax, 
   ulv_factor_fast_kernel<T><<<(unsigned)nt, FT, smem, st>>>(t, s, mmax | 1, nmax, kumax);
 }
 
-template bool factor_fast_fits<double>(int, int, int, int);
-template bool factor_fast_fits<float>(int, int, int, int);
-template void launch_ulv_factor_fast<double>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
-template void launch_ulv_factor_fast<float>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
+template bool factor_fast_fits<double>(int, int, int, int, size_t);
+template bool factor_fast_fits<float>(int, int, int, int, size_t);
+template void launch_ulv_factor_fast<double>(const Task*, int64_t, const Slot*, int, int, int, size_t, cudaStream_t);
+template void launch_ulv_factor_fast<float>(const Task*, int64_t, const Slot*, int, int, int, size_t, cudaStream_t);
 
 }  // namespace hss

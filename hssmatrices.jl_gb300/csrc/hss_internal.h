@@ -51,7 +51,8 @@ struct Slot {
   double alpha, beta;
   void* ws;         int64_t ldws;     // workspace (double for products, T for solves)
   void* fbase;                        // factor storage (T)
-  const double* colscale;             // solve: rhs column j is divided by colscale[j]
+  const double* colscale;             // solve: rhs column j is divided by colscale[j] ...
+  const double* colinv;               // ... i.e. multiplied by colinv[j] = 1 / colscale[j]
   double* colnorm2;                   // product: += sum_i C(i,j)^2 per column (nullable)
   int32_t r, mode;                    // solve: mode 0 x = s*d, 1 x += s*d
   int32_t* err;                       // device status word (nullable)

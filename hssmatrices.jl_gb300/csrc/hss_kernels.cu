@@ -17,6 +17,7 @@
 //     v = x / (alpha - beta); tau = 0 (H = I) when x == 0.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include "hss_device.cuh"
 #include "hss_internal.h"
 #include "hss_launch.h"
 
@@ -45,19 +46,9 @@ __device__ __forceinline__ T block_sum(T v, T* red) {
   return s;
 }
 
-// dlarfg from the squared norm of the tail.
 template <typename T>
 __device__ __forceinline__ void householder(T alpha, T ss, T& beta, T& tau, T& scal) {
-  if (ss == T(0)) {
-    tau = T(0);
-    beta = alpha;
-    scal = T(1);
-  } else {
-    const T xnorm = sqrt(ss);
-    beta = -copysign(hypot(alpha, xnorm), alpha);
-    tau = (beta - alpha) / beta;
-    scal = T(1) / (alpha - beta);
-  }
+  larfg_ss(alpha, ss, beta, tau, scal);
 }
 
 // ---------------------------------------------------------------------------
@@ -482,7 +473,7 @@ __device__ void lu_factor(T* A, int m, int32_t* piv, int32_t* err) {
     T best = T(-1);
     int idx = m;
     for (int i = c + tid; i < m; i += NT) {
-      const T a = fabs(A[i + (int64_t)c * m]);
+      const T a = dabs(A[i + (int64_t)c * m]);
       if (a > best) { best = a; idx = i; }
     }
 #pragma unroll
@@ -663,8 +654,8 @@ __global__ void __launch_bounds__(NT) ulv_solve_up_kernel(const Task* __restrict
   if (nd.leaf) {
     for (int o = tid; o < m * r; o += NT) {
       const int i = o % m, j = o / m;
-      const double s = sl.colscale ? sl.colscale[j] : 1.0;
-      b[i + j * ld] = (T)(sl.B[nd.row0 + i + (int64_t)j * sl.ldb] / s);
+      const double bv = sl.B[nd.row0 + i + (int64_t)j * sl.ldb];
+      b[i + j * ld] = sl.colinv ? (T)(bv * sl.colinv[j]) : (T)bv;
     }
   } else {
     // b = [b1; b2] - [U1 B12 u2; U2 B21 u1] (src/ulvfactor.jl:74)
@@ -865,7 +856,9 @@ __global__ void colnorm2_kernel(const double* __restrict__ B, int64_t ldb, int64
 __global__ void sqrt_scale_kernel(const double* __restrict__ n2, double* __restrict__ s, int64_t r) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < r; j += (int64_t)gridDim.x * blockDim.x) {
     const double v = n2[j];
-    s[j] = v > 0.0 ? sqrt(v) : 1.0;
+    const double sc = v > 0.0 ? sqrt(v) : 1.0;
+    s[j] = sc;
+    s[r + j] = 1.0 / sc;
   }
 }
 

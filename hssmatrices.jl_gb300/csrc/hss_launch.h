@@ -21,11 +21,12 @@ void launch_mv_down_staged(const Task* t, int64_t ntasks, const Slot* s, size_t 
 template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,
                        cudaStream_t st);
+// On-chip factor kernel (hss_factor_fast.cu); `extra` = merge staging elements.
 template <typename T>
-bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax);
+bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra);
 template <typename T>
 void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax,
-                            cudaStream_t st);
+                            size_t extra, cudaStream_t st);
 // Register-resident solve sweeps for nodes with m, n <= 256 (hss_solve.cu).
 bool solve_reg_fits(int mmax, int nmax);
 template <typename T>
@@ -42,7 +43,7 @@ void launch_ulv_solve_down(const Task* t, int64_t ntasks, const Slot* s, cudaStr
 // out[j] += sum_i B(i,j)^2 for i < n, j < r (out must be zeroed by the caller).
 void launch_colnorm2(const double* B, int64_t ldb, int64_t n, int64_t r, double* out,
                      cudaStream_t st);
-// s[j] = sqrt(n2[j]) (1 where n2[j] == 0).
+// s[j] = sqrt(n2[j]) (1 where n2[j] == 0) and s[r + j] = 1 / s[j]; s holds 2r values.
 void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st);
 
 }  // namespace hss

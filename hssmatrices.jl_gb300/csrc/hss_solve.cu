@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
         const int row = e % m, gg = e / m, j = j0 + gg;
         T val = T(0);
         if (j < r) {
-          const double s = sl.colscale ? sl.colscale[j] : 1.0;
-          val = (T)(sl.B[nd.row0 + row + (int64_t)j * sl.ldb] / s);
+          const double bv = sl.B[nd.row0 + row + (int64_t)j * sl.ldb];
+          val = sl.colinv ? (T)(bv * sl.colinv[j]) : (T)bv;
         }
         sb[row + gg * LDS] = val;
       }
