@@ -106,6 +106,7 @@ struct Seg {
   int c1u = 0, c2u = 0, c1v = 0, c2v = 0;          // largest children's ranks (branches)
   int kmax = 0, mkmax = 0;                         // largest ULV k and m - k
   int c1mr = 0, c2mr = 0, c1nr = 0, c2nr = 0;      // largest children's reduced sizes
+  int64_t sv_stage = 0;                            // largest upward-solve staging need
 };
 
 inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
@@ -438,6 +439,13 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
           v[lv].kvmax = std::max(v[lv].kvmax, x.kv);
           v[lv].kmax = std::max(v[lv].kmax, x.root ? 0 : x.k);
           v[lv].mkmax = std::max(v[lv].mkmax, x.mk);
+          {
+            const Node* a = x.leaf ? nullptr : &P->nodes[x.left];
+            const Node* b = x.leaf ? nullptr : &P->nodes[x.right];
+            v[lv].sv_stage = std::max(v[lv].sv_stage,
+                                      solve_up_stage_need(x.m, x.k, x.mk, x.nk, x.kv, x.leaf, x.root, a ? a->mr : 0,
+                                                          b ? b->mr : 0, a ? a->kv : 0, b ? b->kv : 0));
+          }
           if (!x.leaf) {
             const Node& c1 = P->nodes[x.left];
             const Node& c2 = P->nodes[x.right];
@@ -505,16 +513,16 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
 // launch sequences
 // ---------------------------------------------------------------------------
 
-void run_matvec(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
+void run_matvec(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
   const Task* T = P->d_tasks;
   constexpr size_t kStagedCap = 200 * 1024;
   traced(HSS_TRACE_MV_LEAF, P->leaves.cnt, st,
-         [&] { launch_mv_leaf(T + P->leaves.off, P->leaves.cnt, slots, st); });
+         [&] { launch_mv_leaf(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
   for (size_t h = 1; h < P->mv_up.size(); ++h) {
     const Seg& g = P->mv_up[h];
     traced(HSS_TRACE_MV_UP, g.cnt, st, [&] {
       const size_t sm = mv_up_staged_smem(g.kvmax, g.c1v, g.c2v);
-      if (sm <= kStagedCap) launch_mv_up_staged(T + g.off, g.cnt, slots, sm, st);
+      if (sm <= kStagedCap) launch_mv_up_staged(T + g.off, g.cnt, slots, sm, rmax, st);
       else launch_mv_up(T + g.off, g.cnt, slots, st);
     });
   }
@@ -522,12 +530,12 @@ void run_matvec(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
     const Seg& g = P->mv_dn[d];
     traced(HSS_TRACE_MV_DOWN, g.cnt, st, [&] {
       const size_t sm = mv_down_staged_smem(g.kumax, g.c1u, g.c2u, g.c1v, g.c2v);
-      if (sm <= kStagedCap) launch_mv_down_staged(T + g.off, g.cnt, slots, sm, st);
+      if (sm <= kStagedCap) launch_mv_down_staged(T + g.off, g.cnt, slots, sm, rmax, st);
       else launch_mv_down(T + g.off, g.cnt, slots, st);
     });
   }
   traced(HSS_TRACE_MV_FINAL, P->leaves.cnt, st,
-         [&] { launch_mv_leaf_final(T + P->leaves.off, P->leaves.cnt, slots, st); });
+         [&] { launch_mv_leaf_final(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
 }
 
 template <typename T>
@@ -554,7 +562,7 @@ void run_solve(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
     const Seg& g = P->by_h[h];
     traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
       if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
-        launch_ulv_solve_up_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.kmax, g.mkmax, rmax, st);
+        launch_ulv_solve_up_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.sv_stage, rmax, st);
       else
         launch_ulv_solve_up<T>(P->d_tasks + g.off, g.cnt, slots, st);
     });
@@ -616,7 +624,7 @@ int matmul_impl(hss_plan_s* P, const std::vector<Cols>& io, double alpha, double
     x.err = P->d_err;
   }
   CUDA_TRY(table.upload(s, st));
-  run_matvec(P, table.dev.p, st);
+  run_matvec(P, table.dev.p, (int)rmax, st);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -750,7 +758,7 @@ int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t
         x.err = P->d_err;
       }
       CUDA_TRY(f->mv_slots.upload(s, st));
-      run_matvec(P, f->mv_slots.dev.p, st);
+      run_matvec(P, f->mv_slots.dev.p, (int)rmax, st);
       CUDA_TRY(cudaGetLastError());
     }
     CUDA_TRY(cudaMemcpyAsync(f->h_rn2.p, f->rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));

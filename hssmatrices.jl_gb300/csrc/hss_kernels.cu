@@ -152,17 +152,20 @@ __device__ void block_rows_times_cols(const double* A, int m, int n, const doubl
 }
 
 // Leaves: Z = V^T B_leaf (src/matmul.jl:34) and C = alpha D B_leaf + beta Y (:46).
+// One thread block per (leaf, chunk of rc right-hand sides).
 __global__ void __launch_bounds__(NT) mv_leaf_kernel(const Task* __restrict__ tasks,
-                                                     const Slot* __restrict__ slots) {
+                                                     const Slot* __restrict__ slots, int rc, int nchunk) {
   __shared__ double Xs[256 * 8];
   __shared__ double part[NT * 8];
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.x / nchunk];
+  const int j0 = (blockIdx.x % nchunk) * rc;
   const Node& nd = tk.nodes[tk.node];
   const Slot& sl = slots[tk.slot];
-  const int m = nd.gm, n = nd.gn, kv = nd.kv, r = sl.r;
-  const double* Bl = sl.B + nd.col0;
+  if (j0 >= sl.r) return;
+  const int m = nd.gm, n = nd.gn, kv = nd.kv, r = min(rc, sl.r - j0);
+  const double* Bl = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
   if (kv > 0) {
-    double* Z = (double*)sl.ws + nd.wz;
+    double* Z = (double*)sl.ws + nd.wz + (int64_t)j0 * sl.ldws;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int o = warp; o < kv * r; o += NW) {
       const int c = o % kv, j = o / kv;
@@ -175,10 +178,11 @@ __global__ void __launch_bounds__(NT) mv_leaf_kernel(const Task* __restrict__ ta
     }
   }
   block_rows_times_cols(nd.D, m, n, Bl, sl.ldb, r, Xs, part, sl.alpha, sl.beta,
-                        sl.Y ? sl.Y + nd.row0 : nullptr, sl.ldy, sl.C + nd.row0, sl.ldc,
-                        false, nullptr);
+                        sl.Y ? sl.Y + nd.row0 + (int64_t)j0 * sl.ldy : nullptr, sl.ldy,
+                        sl.C + nd.row0 + (int64_t)j0 * sl.ldc, sl.ldc, false, nullptr);
 }
 
+// Generic (unstaged) sweeps for ranks whose staged blocks do not fit in shared memory.
 // Upsweep, non-root branch: Z = W1^T Z1 + W2^T Z2 (src/matmul.jl:39).
 __global__ void __launch_bounds__(NT) mv_up_kernel(const Task* __restrict__ tasks,
                                                    const Slot* __restrict__ slots) {
@@ -238,8 +242,7 @@ __global__ void __launch_bounds__(NT) mv_down_kernel(const Task* __restrict__ ta
 // Staged variants of the two translator sweeps: every operand of the node is
 // first copied into shared memory with all threads (independent, coalesced
 // loads), then the small products run out of shared memory.  Right-hand sides
-// are processed in chunks of MV_RC columns.
-constexpr int MV_RC = 32;
+// are processed in chunks (one thread block per node and chunk).
 
 __device__ __forceinline__ void stage(double* dst, const double* __restrict__ src, int64_t cnt) {
   for (int64_t e = threadIdx.x; e < cnt; e += NT) dst[e] = src[e];
@@ -260,104 +263,106 @@ __device__ __forceinline__ void stage_cols(double* dst, const double* __restrict
 }
 
 // Upsweep, non-root branch: Z = W1^T Z1 + W2^T Z2 (src/matmul.jl:39).
+// One thread block per (node, chunk of rc right-hand sides).
 __global__ void __launch_bounds__(NT) mv_up_staged_kernel(const Task* __restrict__ tasks,
-                                                          const Slot* __restrict__ slots) {
+                                                          const Slot* __restrict__ slots, int rc, int nchunk) {
   extern __shared__ __align__(16) double sm[];
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.x / nchunk];
+  const int j0 = (blockIdx.x % nchunk) * rc;
   const Node& nd = tk.nodes[tk.node];
   const Node& c1 = tk.nodes[nd.left];
   const Node& c2 = tk.nodes[nd.right];
   const Slot& sl = slots[tk.slot];
+  if (j0 >= sl.r) return;
+  const int nc = min(rc, sl.r - j0);
   const double* ws = (const double*)sl.ws;
   const int64_t ld = sl.ldws;
-  const int kv = nd.kv, k1 = c1.kv, k2 = c2.kv, r = sl.r;
+  const int kv = nd.kv, k1 = c1.kv, k2 = c2.kv;
   double* W1t = sm;                  // kv x k1 (transposed)
   double* W2t = W1t + kv * k1;       // kv x k2
-  double* Z1 = W2t + kv * k2;        // k1 x MV_RC
-  double* Z2 = Z1 + k1 * MV_RC;      // k2 x MV_RC
+  double* Z1 = W2t + kv * k2;        // k1 x rc
+  double* Z2 = Z1 + k1 * rc;         // k2 x rc
   stage_t(W1t, nd.W1, k1, kv);
   stage_t(W2t, nd.W2, k2, kv);
-  for (int j0 = 0; j0 < r; j0 += MV_RC) {
-    const int nc = min(MV_RC, r - j0);
-    stage_cols(Z1, ws + c1.wz + (int64_t)j0 * ld, k1, ld, nc);
-    stage_cols(Z2, ws + c2.wz + (int64_t)j0 * ld, k2, ld, nc);
-    __syncthreads();
-    double* Z = (double*)sl.ws + nd.wz + (int64_t)j0 * ld;
-    for (int o = threadIdx.x; o < kv * nc; o += NT) {
-      const int c = o % kv, j = o / kv;
-      double s = 0.0;
-      for (int l = 0; l < k1; ++l) s = fma(W1t[c + l * kv], Z1[l + j * k1], s);
-      for (int l = 0; l < k2; ++l) s = fma(W2t[c + l * kv], Z2[l + j * k2], s);
-      Z[c + (int64_t)j * ld] = s;
-    }
-    __syncthreads();
+  stage_cols(Z1, ws + c1.wz + (int64_t)j0 * ld, k1, ld, nc);
+  stage_cols(Z2, ws + c2.wz + (int64_t)j0 * ld, k2, ld, nc);
+  __syncthreads();
+  double* Z = (double*)sl.ws + nd.wz + (int64_t)j0 * ld;
+  for (int o = threadIdx.x; o < kv * nc; o += NT) {
+    const int c = o % kv, j = o / kv;
+    double s0 = 0.0, s1 = 0.0;
+    for (int l = 0; l < k1; ++l) s0 = fma(W1t[c + l * kv], Z1[l + j * k1], s0);
+    for (int l = 0; l < k2; ++l) s1 = fma(W2t[c + l * kv], Z2[l + j * k2], s1);
+    Z[c + (int64_t)j * ld] = s0 + s1;
   }
 }
 
 // Downsweep, branch: F1 = B12 Z2 + R1 F, F2 = B21 Z1 + R2 F (src/matmul.jl:50-56).
 __global__ void __launch_bounds__(NT) mv_down_staged_kernel(const Task* __restrict__ tasks,
-                                                            const Slot* __restrict__ slots) {
+                                                            const Slot* __restrict__ slots, int rc, int nchunk) {
   extern __shared__ __align__(16) double sm[];
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.x / nchunk];
+  const int j0 = (blockIdx.x % nchunk) * rc;
   const Node& nd = tk.nodes[tk.node];
   const Node& c1 = tk.nodes[nd.left];
   const Node& c2 = tk.nodes[nd.right];
   const Slot& sl = slots[tk.slot];
+  if (j0 >= sl.r) return;
+  const int nc = min(rc, sl.r - j0);
   double* ws = (double*)sl.ws;
   const int64_t ld = sl.ldws;
-  const int ku = nd.root ? 0 : nd.ku, u1 = c1.ku, u2 = c2.ku, v1 = c1.kv, v2 = c2.kv, r = sl.r;
+  const int ku = nd.root ? 0 : nd.ku, u1 = c1.ku, u2 = c2.ku, v1 = c1.kv, v2 = c2.kv;
   double* B12 = sm;                  // u1 x v2
   double* B21 = B12 + u1 * v2;       // u2 x v1
   double* R1 = B21 + u2 * v1;        // u1 x ku
   double* R2 = R1 + u1 * ku;         // u2 x ku
-  double* Z1 = R2 + u2 * ku;         // v1 x MV_RC
-  double* Z2 = Z1 + v1 * MV_RC;      // v2 x MV_RC
-  double* Fs = Z2 + v2 * MV_RC;      // ku x MV_RC
+  double* Z1 = R2 + u2 * ku;         // v1 x rc
+  double* Z2 = Z1 + v1 * rc;         // v2 x rc
+  double* Fs = Z2 + v2 * rc;         // ku x rc
   stage(B12, nd.B12, (int64_t)u1 * v2);
   stage(B21, nd.B21, (int64_t)u2 * v1);
   if (ku > 0) {
     stage(R1, nd.R1, (int64_t)u1 * ku);
     stage(R2, nd.R2, (int64_t)u2 * ku);
   }
-  for (int j0 = 0; j0 < r; j0 += MV_RC) {
-    const int nc = min(MV_RC, r - j0);
-    stage_cols(Z1, ws + c1.wz + (int64_t)j0 * ld, v1, ld, nc);
-    stage_cols(Z2, ws + c2.wz + (int64_t)j0 * ld, v2, ld, nc);
-    if (ku > 0) stage_cols(Fs, ws + nd.wf + (int64_t)j0 * ld, ku, ld, nc);
-    __syncthreads();
-    for (int o = threadIdx.x; o < (u1 + u2) * nc; o += NT) {
-      double s = 0.0;
-      if (o < u1 * nc) {
-        const int i = o % u1, j = o / u1;
-        for (int l = 0; l < v2; ++l) s = fma(B12[i + l * u1], Z2[l + j * v2], s);
-        for (int l = 0; l < ku; ++l) s = fma(R1[i + l * u1], Fs[l + j * ku], s);
-        ws[c1.wf + i + (int64_t)(j0 + j) * ld] = s;
-      } else {
-        const int o2 = o - u1 * nc;
-        const int i = o2 % u2, j = o2 / u2;
-        for (int l = 0; l < v1; ++l) s = fma(B21[i + l * u2], Z1[l + j * v1], s);
-        for (int l = 0; l < ku; ++l) s = fma(R2[i + l * u2], Fs[l + j * ku], s);
-        ws[c2.wf + i + (int64_t)(j0 + j) * ld] = s;
-      }
+  stage_cols(Z1, ws + c1.wz + (int64_t)j0 * ld, v1, ld, nc);
+  stage_cols(Z2, ws + c2.wz + (int64_t)j0 * ld, v2, ld, nc);
+  if (ku > 0) stage_cols(Fs, ws + nd.wf + (int64_t)j0 * ld, ku, ld, nc);
+  __syncthreads();
+  for (int o = threadIdx.x; o < (u1 + u2) * nc; o += NT) {
+    double s0 = 0.0, s1 = 0.0;
+    if (o < u1 * nc) {
+      const int i = o % u1, j = o / u1;
+      for (int l = 0; l < v2; ++l) s0 = fma(B12[i + l * u1], Z2[l + j * v2], s0);
+      for (int l = 0; l < ku; ++l) s1 = fma(R1[i + l * u1], Fs[l + j * ku], s1);
+      ws[c1.wf + i + (int64_t)(j0 + j) * ld] = s0 + s1;
+    } else {
+      const int o2 = o - u1 * nc;
+      const int i = o2 % u2, j = o2 / u2;
+      for (int l = 0; l < v1; ++l) s0 = fma(B21[i + l * u2], Z1[l + j * v1], s0);
+      for (int l = 0; l < ku; ++l) s1 = fma(R2[i + l * u2], Fs[l + j * ku], s1);
+      ws[c2.wf + i + (int64_t)(j0 + j) * ld] = s0 + s1;
     }
-    __syncthreads();
   }
 }
 
 // Leaves: C += alpha U F (src/matmul.jl:47), and per-column sums of squares.
 __global__ void __launch_bounds__(NT) mv_leaf_final_kernel(const Task* __restrict__ tasks,
-                                                           const Slot* __restrict__ slots) {
+                                                           const Slot* __restrict__ slots, int rc, int nchunk) {
   __shared__ double Xs[256 * 8];
   __shared__ double part[NT * 8];
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.x / nchunk];
+  const int j0 = (blockIdx.x % nchunk) * rc;
   const Node& nd = tk.nodes[tk.node];
   const Slot& sl = slots[tk.slot];
-  const int m = nd.gm, ku = nd.root ? 0 : nd.ku, r = sl.r;
-  double* Cl = sl.C + nd.row0;
+  if (j0 >= sl.r) return;
+  const int m = nd.gm, ku = nd.root ? 0 : nd.ku, r = min(rc, sl.r - j0);
+  double* Cl = sl.C + nd.row0 + (int64_t)j0 * sl.ldc;
+  double* cn = sl.colnorm2 ? sl.colnorm2 + j0 : nullptr;
   if (ku > 0) {
-    block_rows_times_cols(nd.U, m, ku, (const double*)sl.ws + nd.wf, sl.ldws, r, Xs, part,
-                          sl.alpha, 0.0, nullptr, 0, Cl, sl.ldc, true, sl.colnorm2);
-  } else if (sl.colnorm2 != nullptr) {
+    block_rows_times_cols(nd.U, m, ku, (const double*)sl.ws + nd.wf + (int64_t)j0 * sl.ldws, sl.ldws, r, Xs, part,
+                          sl.alpha, 0.0, nullptr, 0, Cl, sl.ldc, true, cn);
+  } else if (cn != nullptr) {
     for (int j = threadIdx.x >> 5; j < r; j += NW) {
       double s = 0.0;
       for (int i = threadIdx.x & 31; i < m; i += 32) {
@@ -365,7 +370,7 @@ __global__ void __launch_bounds__(NT) mv_leaf_final_kernel(const Task* __restric
         s = fma(c, c, s);
       }
       s = warp_sum(s);
-      if ((threadIdx.x & 31) == 0) atomicAdd(sl.colnorm2 + j, s);
+      if ((threadIdx.x & 31) == 0) atomicAdd(cn + j, s);
     }
   }
 }
@@ -866,8 +871,16 @@ __global__ void sqrt_scale_kernel(const double* __restrict__ n2, double* __restr
 // launch wrappers
 // ---------------------------------------------------------------------------
 
-void launch_mv_leaf(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
-  if (nt > 0) mv_leaf_kernel<<<(unsigned)nt, NT, 0, st>>>(t, s);
+// Leaf products: one thread block per (leaf, 8 right-hand sides) once r >= 16.
+static int leaf_chunk(int rmax) { return rmax >= 16 ? 8 : (rmax > 0 ? rmax : 1); }
+
+void launch_mv_leaf(const Task* t, int64_t nt, const Slot* s, int rmax, cudaStream_t st) {
+  const int rc = leaf_chunk(rmax), nchunk = (rmax + rc - 1) / rc;
+  if (nt > 0 && nchunk > 0) mv_leaf_kernel<<<(unsigned)(nt * nchunk), NT, 0, st>>>(t, s, rc, nchunk);
+}
+void launch_mv_leaf_final(const Task* t, int64_t nt, const Slot* s, int rmax, cudaStream_t st) {
+  const int rc = leaf_chunk(rmax), nchunk = (rmax + rc - 1) / rc;
+  if (nt > 0 && nchunk > 0) mv_leaf_final_kernel<<<(unsigned)(nt * nchunk), NT, 0, st>>>(t, s, rc, nchunk);
 }
 void launch_mv_up(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
   if (nt > 0) mv_up_kernel<<<(unsigned)nt, NT, 0, st>>>(t, s);
@@ -876,31 +889,34 @@ void launch_mv_down(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
   if (nt > 0) mv_down_kernel<<<(unsigned)nt, NT, 0, st>>>(t, s);
 }
 
+// Right-hand sides per thread block of the staged translator sweeps: small
+// chunks spread the few nodes of the upper levels over more SMs.
+constexpr int MV_RC_BLOCK = 8;
+
 size_t mv_up_staged_smem(int kv, int k1max, int k2max) {
-  return sizeof(double) * ((size_t)kv * (k1max + k2max) + (size_t)(k1max + k2max) * MV_RC);
+  return sizeof(double) * ((size_t)kv * (k1max + k2max) + (size_t)(k1max + k2max) * MV_RC_BLOCK);
 }
 size_t mv_down_staged_smem(int ku, int u1, int u2, int v1, int v2) {
   return sizeof(double) * ((size_t)u1 * v2 + (size_t)u2 * v1 + (size_t)(u1 + u2) * ku +
-                           (size_t)(v1 + v2 + ku) * MV_RC);
+                           (size_t)(v1 + v2 + ku) * MV_RC_BLOCK);
 }
-void launch_mv_up_staged(const Task* t, int64_t nt, const Slot* s, size_t smem, cudaStream_t st) {
+void launch_mv_up_staged(const Task* t, int64_t nt, const Slot* s, size_t smem, int rmax, cudaStream_t st) {
   static bool set = false;
   if (!set) {
     cudaFuncSetAttribute(mv_up_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     set = true;
   }
-  if (nt > 0) mv_up_staged_kernel<<<(unsigned)nt, NT, smem, st>>>(t, s);
+  const int nchunk = (rmax + MV_RC_BLOCK - 1) / MV_RC_BLOCK;
+  if (nt > 0 && nchunk > 0) mv_up_staged_kernel<<<(unsigned)(nt * nchunk), NT, smem, st>>>(t, s, MV_RC_BLOCK, nchunk);
 }
-void launch_mv_down_staged(const Task* t, int64_t nt, const Slot* s, size_t smem, cudaStream_t st) {
+void launch_mv_down_staged(const Task* t, int64_t nt, const Slot* s, size_t smem, int rmax, cudaStream_t st) {
   static bool set = false;
   if (!set) {
     cudaFuncSetAttribute(mv_down_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     set = true;
   }
-  if (nt > 0) mv_down_staged_kernel<<<(unsigned)nt, NT, smem, st>>>(t, s);
-}
-void launch_mv_leaf_final(const Task* t, int64_t nt, const Slot* s, cudaStream_t st) {
-  if (nt > 0) mv_leaf_final_kernel<<<(unsigned)nt, NT, 0, st>>>(t, s);
+  const int nchunk = (rmax + MV_RC_BLOCK - 1) / MV_RC_BLOCK;
+  if (nt > 0 && nchunk > 0) mv_down_staged_kernel<<<(unsigned)(nt * nchunk), NT, smem, st>>>(t, s, MV_RC_BLOCK, nchunk);
 }
 
 template <typename T>

@@ -6,16 +6,16 @@
 namespace hss {
 
 // HSS x dense product (reference src/matmul.jl:18-62), one launch per list.
-void launch_mv_leaf(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+void launch_mv_leaf(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
 void launch_mv_up(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
 void launch_mv_down(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
-void launch_mv_leaf_final(const Task* t, int64_t ntasks, const Slot* s, cudaStream_t st);
+void launch_mv_leaf_final(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
 // Shared-memory staged translator sweeps; smem from the *_smem helpers with the
 // level's largest ranks (children's and the node's own).
 size_t mv_up_staged_smem(int kv, int k1max, int k2max);
 size_t mv_down_staged_smem(int ku, int u1, int u2, int v1, int v2);
-void launch_mv_up_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, cudaStream_t st);
-void launch_mv_down_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, cudaStream_t st);
+void launch_mv_up_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, int rmax, cudaStream_t st);
+void launch_mv_down_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, int rmax, cudaStream_t st);
 
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>
@@ -30,8 +30,11 @@ void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mm
 // Register-resident solve sweeps for nodes with m, n <= 256 (hss_solve.cu).
 bool solve_reg_fits(int mmax, int nmax);
 template <typename T>
-void launch_ulv_solve_up_reg(const Task* t, int64_t ntasks, const Slot* s, int mmax, int kmax, int mkmax, int r,
+void launch_ulv_solve_up_reg(const Task* t, int64_t ntasks, const Slot* s, int mmax, int64_t stage, int r,
                              cudaStream_t st);
+// Shared-memory elements the upward solve stages for one node.
+int64_t solve_up_stage_need(int m, int k, int mk, int nk, int kv, bool leaf, bool root, int mr1, int mr2, int kv1,
+                            int kv2);
 template <typename T>
 void launch_ulv_solve_down_reg(const Task* t, int64_t ntasks, const Slot* s, int nmax, int mkmax, int r,
                                cudaStream_t st);

@@ -76,14 +76,29 @@ __device__ __forceinline__ void upper_solve(T (&b)[RPT], const T* __restrict__ A
   }
 }
 
+// Elements of shared memory the upward kernel stages for one node (beyond the
+// LDS x CPB right-hand-side block); the host sizes launches with the level's
+// largest value.
+__host__ __device__ inline int64_t solve_up_stage_elems(int m, int k, int mk, int nk, int kv, bool leaf, bool root,
+                                                       int mr1, int mr2, int kv1, int kv2, int cpb) {
+  int64_t e = 0;
+  if (root) e += (int64_t)m * m;
+  else if (mk > 0) e += (int64_t)m * k + (int64_t)mk * mk + (int64_t)k * nk + (int64_t)nk * kv;
+  if (!leaf) {
+    e += (int64_t)mr1 * kv2 + (int64_t)mr2 * kv1 + (int64_t)(kv1 + kv2) * cpb;
+    if (!root) e += (int64_t)(kv1 + kv2) * kv;
+  }
+  return e;
+}
+
 template <typename T, int TPC, int MR>
 __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ tasks,
-                                                       const Slot* __restrict__ slots, int stage_cap) {
+                                                       const Slot* __restrict__ slots, int64_t stage_cap) {
   constexpr int RPT = MR / TPC;
   constexpr int CPB = ST / TPC;
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* sb = (T*)smraw;   // LDS x CPB
-  T* sfac = sb + LDS * CPB;   // staged factor blocks (stage_cap elements)
+  T* sb = (T*)smraw;          // LDS x CPB right-hand sides
+  T* sx = sb + LDS * CPB;     // staged operands
   const Task tk = tasks[blockIdx.x];
   const Node* nodes = tk.nodes;
   const Node& nd = nodes[tk.node];
@@ -91,30 +106,59 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
   T* ws = (T*)sl.ws;
   const int64_t ld = sl.ldws;
   const T* fb = (const T*)sl.fbase;
-  const int m = nd.m, kv = nd.kv, r = sl.r;
+  const int m = nd.m, n = nd.n, kv = nd.kv, r = sl.r;
   const int tid = threadIdx.x, g = tid / TPC, gl = tid % TPC;
   const int k = nd.k, mk = nd.mk, nk = nd.nk;
   T* u = ws + nd.wu;
-  // Factor blocks read inside the sequential sweeps are copied on chip once:
-  // the QL reflectors (m x k) and L1 (mk x mk), or the root LU (m x m).
-  const T* Up = fb + nd.fU;     // ld m
-  const T* Lp = fb + nd.fD;     // ld m
-  int ldL = m;
-  if (nd.root) {
-    if (m * m <= stage_cap) {
-      for (int e = tid; e < m * m; e += ST) sfac[e] = Lp[e];
-      Lp = sfac;
+  const Node* c1 = nd.leaf ? nullptr : &nodes[nd.left];
+  const Node* c2 = nd.leaf ? nullptr : &nodes[nd.right];
+  const int mr1 = c1 ? c1->mr : 0, mr2 = c2 ? c2->mr : 0, kv1 = c1 ? c1->kv : 0, kv2 = c2 ? c2->kv : 0;
+  const bool staged = solve_up_stage_elems(m, k, mk, nk, kv, nd.leaf, nd.root, mr1, mr2, kv1, kv2, CPB) <= stage_cap;
+
+  // Every factor / generator block an inner loop reads is copied on chip once
+  // (bulk, coalesced), unless the level's blocks do not fit: then they are
+  // read from global memory in place.  Leading dimensions follow the copy.
+  const T* Up = fb + nd.fU;  int ldU = m;       // QL reflectors m x k
+  const T* Lp = fb + nd.fD;  int ldL = m;       // L1 (mk x mk) or the root LU (m x m)
+  const T* L2p = fb + nd.fD + mk;  int ldL2 = m;      // L2[:, 0:nk], k x nk
+  const T* Vap = fb + nd.fV; int ldVa = n;      // V[0:nk, :], nk x kv
+  const T* T12p = nd.leaf ? nullptr : fb + nd.fT12;   // mr1 x kv2
+  const T* T21p = nd.leaf ? nullptr : fb + nd.fT21;   // mr2 x kv1
+  T* sW1 = nullptr;  T* sW2 = nullptr;  T* su1 = nullptr;  T* su2 = nullptr;
+  if (staged) {
+    T* p = sx;
+    if (nd.root) {
+      for (int e = tid; e < m * m; e += ST) p[e] = Lp[e];
+      Lp = p; ldL = m; p += m * m;
+    } else if (mk > 0) {
+      T* q = p;
+      for (int e = tid; e < m * k; e += ST) q[e] = Up[e];
+      Up = q; ldU = m; q += m * k;
+      for (int e = tid; e < mk * mk; e += ST) q[e] = Lp[(e % mk) + (int64_t)(e / mk) * m];
+      Lp = q; ldL = mk; q += mk * mk;
+      for (int e = tid; e < k * nk; e += ST) q[e] = L2p[(e % k) + (int64_t)(e / k) * m];
+      L2p = q; ldL2 = k; q += k * nk;
+      for (int e = tid; e < nk * kv; e += ST) q[e] = Vap[(e % nk) + (int64_t)(e / nk) * n];
+      Vap = q; ldVa = nk; q += nk * kv;
+      p = q;
     }
-  } else if (mk > 0 && m * k + mk * mk <= stage_cap) {
-    T* sU = sfac;
-    T* sL = sfac + m * k;
-    for (int e = tid; e < m * k; e += ST) sU[e] = Up[e];
-    for (int e = tid; e < mk * mk; e += ST) sL[e] = Lp[(e % mk) + (int64_t)(e / mk) * m];
-    Up = sU;
-    Lp = sL;
-    ldL = mk;
+    if (!nd.leaf) {
+      for (int e = tid; e < mr1 * kv2; e += ST) p[e] = T12p[e];
+      T12p = p; p += mr1 * kv2;
+      for (int e = tid; e < mr2 * kv1; e += ST) p[e] = T21p[e];
+      T21p = p; p += mr2 * kv1;
+      if (!nd.root) {
+        sW1 = p; p += kv1 * kv;
+        sW2 = p; p += kv2 * kv;
+        for (int e = tid; e < kv1 * kv; e += ST) sW1[e] = (T)nd.W1[e];
+        for (int e = tid; e < kv2 * kv; e += ST) sW2[e] = (T)nd.W2[e];
+      }
+      su1 = p; p += kv1 * CPB;
+      su2 = p; p += kv2 * CPB;
+    }
   }
   for (int j0 = 0; j0 < r; j0 += CPB) {
+    const int ncol = min(CPB, r - j0);
     // ---- gather b for this chunk of columns into shared memory
     if (nd.leaf) {
       for (int e = tid; e < m * CPB; e += ST) {
@@ -127,37 +171,52 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
         sb[row + gg * LDS] = val;
       }
     } else {
-      const Node& c1 = nodes[nd.left];
-      const Node& c2 = nodes[nd.right];
-      const T* T12 = fb + nd.fT12;
-      const T* T21 = fb + nd.fT21;
+      // children's u for this chunk (kv1 x ncol, kv2 x ncol), then
+      // b = [b1; b2] - [T12 u2; T21 u1] (src/ulvfactor.jl:74)
+      const T* u1g = ws + c1->wu + (int64_t)j0 * ld;
+      const T* u2g = ws + c2->wu + (int64_t)j0 * ld;
+      const T* u1p = u1g;  int64_t ldu1 = ld;
+      const T* u2p = u2g;  int64_t ldu2 = ld;
+      if (staged) {
+        for (int e = tid; e < kv1 * ncol; e += ST) su1[e] = u1g[(e % kv1) + (int64_t)(e / kv1) * ld];
+        for (int e = tid; e < kv2 * ncol; e += ST) su2[e] = u2g[(e % kv2) + (int64_t)(e / kv2) * ld];
+        u1p = su1; ldu1 = kv1;
+        u2p = su2; ldu2 = kv2;
+        __syncthreads();
+      }
       for (int e = tid; e < m * CPB; e += ST) {
-        const int row = e % m, gg = e / m, j = j0 + gg;
+        const int row = e % m, gg = e / m;
         T val = T(0);
-        if (j < r) {
-          if (row < c1.mr) {
-            val = ws[c1.wb + c1.mk + row + (int64_t)j * ld];
-            const T* u2 = ws + c2.wu + (int64_t)j * ld;
-            for (int l = 0; l < c2.kv; ++l) val -= T12[row + (int64_t)l * c1.mr] * u2[l];
+        if (gg < ncol) {
+          const int64_t j = j0 + gg;
+          if (row < mr1) {
+            val = ws[c1->wb + c1->mk + row + j * ld];
+            const T* uu = u2p + (int64_t)gg * ldu2;
+            for (int l = 0; l < kv2; ++l) val -= T12p[row + l * mr1] * uu[l];
           } else {
-            const int i2 = row - c1.mr;
-            val = ws[c2.wb + c2.mk + i2 + (int64_t)j * ld];
-            const T* u1 = ws + c1.wu + (int64_t)j * ld;
-            for (int l = 0; l < c1.kv; ++l) val -= T21[i2 + (int64_t)l * c2.mr] * u1[l];
+            const int i2 = row - mr1;
+            val = ws[c2->wb + c2->mk + i2 + j * ld];
+            const T* uu = u1p + (int64_t)gg * ldu1;
+            for (int l = 0; l < kv1; ++l) val -= T21p[i2 + l * mr2] * uu[l];
           }
         }
         sb[row + gg * LDS] = val;
       }
       if (!nd.root) {
-        for (int e = tid; e < kv * CPB; e += ST) {
-          const int c = e % kv, j = j0 + e / kv;
-          if (j >= r) continue;
-          const T* u1 = ws + c1.wu + (int64_t)j * ld;
-          const T* u2 = ws + c2.wu + (int64_t)j * ld;
+        // u accumulates W1^T u1 + W2^T u2 (src/ulvfactor.jl:89)
+        for (int e = tid; e < kv * ncol; e += ST) {
+          const int c = e % kv, gg = e / kv;
+          const T* a1 = u1p + (int64_t)gg * ldu1;
+          const T* a2 = u2p + (int64_t)gg * ldu2;
           T s = T(0);
-          for (int l = 0; l < c1.kv; ++l) s += (T)nd.W1[l + (int64_t)c * c1.kv] * u1[l];
-          for (int l = 0; l < c2.kv; ++l) s += (T)nd.W2[l + (int64_t)c * c2.kv] * u2[l];
-          u[c + (int64_t)j * ld] = s;
+          if (staged) {
+            for (int l = 0; l < kv1; ++l) s += sW1[l + c * kv1] * a1[l];
+            for (int l = 0; l < kv2; ++l) s += sW2[l + c * kv2] * a2[l];
+          } else {
+            for (int l = 0; l < kv1; ++l) s += (T)nd.W1[l + (int64_t)c * kv1] * a1[l];
+            for (int l = 0; l < kv2; ++l) s += (T)nd.W2[l + (int64_t)c * kv2] * a2[l];
+          }
+          u[c + (int64_t)(j0 + gg) * ld] = s;
         }
       }
     }
@@ -180,8 +239,8 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
         const int row = gl + s * TPC;
         b[s] = row < m ? sb[row + g * LDS] : T(0);
       }
-      lower_solve<T, TPC, RPT, true>(b, A, m, m, gl);
-      upper_solve<T, TPC, RPT>(b, A, m, m, gl);
+      lower_solve<T, TPC, RPT, true>(b, A, ldL, m, gl);
+      upper_solve<T, TPC, RPT>(b, A, ldL, m, gl);
       if (j < r) {
         T* x = ws + nd.wx + (int64_t)j * ld;
 #pragma unroll
@@ -194,7 +253,6 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
       continue;
     }
     if (mk > 0) {
-      const T* Uf = Up;
       const T* tq = fb + nd.ftq;
       T b[RPT];
 #pragma unroll
@@ -207,15 +265,16 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
         const T tau = tq[c];
         if (tau == T(0)) continue;
         const int p = mk + c;
-        const T* v = Uf + (int64_t)c * m;
-        T dot = T(0);
+        const T* v = Up + (int64_t)c * ldU;
+        T d0 = T(0), d1 = T(0);
 #pragma unroll
         for (int s = 0; s < RPT; ++s) {
           const int row = gl + s * TPC;
           const T vr = row < p ? v[row] : (row == p ? T(1) : T(0));
-          dot += vr * b[s];
+          if (s & 1) d1 += vr * b[s];
+          else d0 += vr * b[s];
         }
-        dot = gsum<TPC>(dot) * tau;
+        const T dot = gsum<TPC>(d0 + d1) * tau;
 #pragma unroll
         for (int s = 0; s < RPT; ++s) {
           const int row = gl + s * TPC;
@@ -233,27 +292,33 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
     }
     __syncthreads();
     // ---- outputs: b_red (:49), u (:51, :89), x[0:mk] = zloc (:65)
-    const T* Df = fb + nd.fD;
-    const T* Vf = fb + nd.fV;
-    for (int e = tid; e < (m - mk) * CPB; e += ST) {
-      const int i = e % (m - mk), gg = e / (m - mk), jj = j0 + gg;
-      if (jj >= r) continue;
+    for (int e = tid; e < (m - mk) * ncol; e += ST) {
+      const int i = e % (m - mk), gg = e / (m - mk);
       const T* bb = sb + gg * LDS;
-      T s = bb[mk + i];
-      for (int l = 0; l < nk; ++l) s -= Df[mk + i + (int64_t)l * m] * bb[l];
-      ws[nd.wb + mk + i + (int64_t)jj * ld] = s;
+      T s0 = bb[mk + i], s1 = T(0);
+      int l = 0;
+      for (; l + 1 < nk; l += 2) {
+        s0 -= L2p[i + l * ldL2] * bb[l];
+        s1 -= L2p[i + (l + 1) * ldL2] * bb[l + 1];
+      }
+      if (l < nk) s0 -= L2p[i + l * ldL2] * bb[l];
+      ws[nd.wb + mk + i + (int64_t)(j0 + gg) * ld] = s0 + s1;
     }
-    for (int e = tid; e < kv * CPB; e += ST) {
-      const int c = e % kv, gg = e / kv, jj = j0 + gg;
-      if (jj >= r) continue;
+    for (int e = tid; e < kv * ncol; e += ST) {
+      const int c = e % kv, gg = e / kv;
       const T* bb = sb + gg * LDS;
-      T s = nd.leaf ? T(0) : u[c + (int64_t)jj * ld];
-      for (int l = 0; l < nk; ++l) s += Vf[l + (int64_t)c * nd.n] * bb[l];
-      u[c + (int64_t)jj * ld] = s;
+      T s0 = nd.leaf ? T(0) : u[c + (int64_t)(j0 + gg) * ld], s1 = T(0);
+      int l = 0;
+      for (; l + 1 < nk; l += 2) {
+        s0 += Vap[l + c * ldVa] * bb[l];
+        s1 += Vap[l + 1 + c * ldVa] * bb[l + 1];
+      }
+      if (l < nk) s0 += Vap[l + c * ldVa] * bb[l];
+      u[c + (int64_t)(j0 + gg) * ld] = s0 + s1;
     }
-    for (int e = tid; e < mk * CPB; e += ST) {
-      const int i = e % mk, gg = e / mk, jj = j0 + gg;
-      if (jj < r) ws[nd.wx + i + (int64_t)jj * ld] = sb[i + gg * LDS];
+    for (int e = tid; e < mk * ncol; e += ST) {
+      const int i = e % mk, gg = e / mk;
+      ws[nd.wx + i + (int64_t)(j0 + gg) * ld] = sb[i + gg * LDS];
     }
     __syncthreads();
   }
@@ -348,14 +413,14 @@ template <typename T, int TPC, int MR>
 void up_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStream_t st) {
   const size_t base = (size_t)LDS * (ST / TPC) * sizeof(T);
   size_t smem = base + want * sizeof(T);
-  if (smem > kSolveSmemCap) smem = base;   // factor blocks stay in global memory
+  if (smem > kSolveSmemCap) smem = base;   // operands stay in global memory
   static bool set = false;
   if (!set) {
     cudaFuncSetAttribute(ulv_solve_up_reg<T, TPC, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kSolveSmemCap);
     set = true;
   }
-  ulv_solve_up_reg<T, TPC, MR><<<(unsigned)nt, ST, smem, st>>>(t, s, (int)((smem - base) / sizeof(T)));
+  ulv_solve_up_reg<T, TPC, MR><<<(unsigned)nt, ST, smem, st>>>(t, s, (int64_t)((smem - base) / sizeof(T)));
 }
 
 template <typename T, int TPC, int MR>
@@ -375,13 +440,17 @@ void down_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStre
 
 bool solve_reg_fits(int mmax, int nmax) { return mmax <= 256 && nmax <= 256; }
 
+int64_t solve_up_stage_need(int m, int k, int mk, int nk, int kv, bool leaf, bool root, int mr1, int mr2, int kv1,
+                            int kv2) {
+  return solve_up_stage_elems(m, k, mk, nk, kv, leaf, root, mr1, mr2, kv1, kv2, ST / 8);
+}
+
 template <typename T>
-void launch_ulv_solve_up_reg(const Task* t, int64_t nt, const Slot* s, int mmax, int kmax, int mkmax, int r,
+void launch_ulv_solve_up_reg(const Task* t, int64_t nt, const Slot* s, int mmax, int64_t stage, int r,
                              cudaStream_t st) {
   if (nt <= 0) return;
   const bool wide = r > 8;
-  // staged elements: reflectors + L1, or the root's LU (whichever is larger)
-  const size_t want = std::max((size_t)mmax * kmax + (size_t)mkmax * mkmax, (size_t)mmax * mmax);
+  const size_t want = (size_t)stage;
   if (mmax <= 64) wide ? up_launch<T, 8, 64>(t, nt, s, want, st) : up_launch<T, 32, 64>(t, nt, s, want, st);
   else if (mmax <= 128) wide ? up_launch<T, 8, 128>(t, nt, s, want, st) : up_launch<T, 32, 128>(t, nt, s, want, st);
   else wide ? up_launch<T, 8, 256>(t, nt, s, want, st) : up_launch<T, 32, 256>(t, nt, s, want, st);
@@ -398,8 +467,8 @@ void launch_ulv_solve_down_reg(const Task* t, int64_t nt, const Slot* s, int nma
   else wide ? down_launch<T, 8, 256>(t, nt, s, want, st) : down_launch<T, 32, 256>(t, nt, s, want, st);
 }
 
-template void launch_ulv_solve_up_reg<double>(const Task*, int64_t, const Slot*, int, int, int, int, cudaStream_t);
-template void launch_ulv_solve_up_reg<float>(const Task*, int64_t, const Slot*, int, int, int, int, cudaStream_t);
+template void launch_ulv_solve_up_reg<double>(const Task*, int64_t, const Slot*, int, int64_t, int, cudaStream_t);
+template void launch_ulv_solve_up_reg<float>(const Task*, int64_t, const Slot*, int, int64_t, int, cudaStream_t);
 template void launch_ulv_solve_down_reg<double>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
 template void launch_ulv_solve_down_reg<float>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
 
