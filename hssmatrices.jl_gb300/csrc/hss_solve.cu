@@ -93,13 +93,15 @@ __host__ __device__ inline int64_t solve_up_stage_elems(int m, int k, int mk, in
 
 template <typename T, int TPC, int MR>
 __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ tasks,
-                                                       const Slot* __restrict__ slots, int64_t stage_cap) {
+                                                       const Slot* __restrict__ slots, int64_t stage_cap,
+                                                       int nchunk) {
   constexpr int RPT = MR / TPC;
   constexpr int CPB = ST / TPC;
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sb = (T*)smraw;          // LDS x CPB right-hand sides
   T* sx = sb + LDS * CPB;     // staged operands
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.x / nchunk];
+  const int jchunk = (blockIdx.x % nchunk) * CPB;   // this block's columns: jchunk .. jchunk+CPB-1
   const Node* nodes = tk.nodes;
   const Node& nd = nodes[tk.node];
   const Slot& sl = slots[tk.slot];
@@ -107,6 +109,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
   const int64_t ld = sl.ldws;
   const T* fb = (const T*)sl.fbase;
   const int m = nd.m, n = nd.n, kv = nd.kv, r = sl.r;
+  if (jchunk >= r) return;
   const int tid = threadIdx.x, g = tid / TPC, gl = tid % TPC;
   const int k = nd.k, mk = nd.mk, nk = nd.nk;
   T* u = ws + nd.wu;
@@ -138,8 +141,9 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
       Lp = q; ldL = mk; q += mk * mk;
       for (int e = tid; e < k * nk; e += ST) q[e] = L2p[(e % k) + (int64_t)(e / k) * m];
       L2p = q; ldL2 = k; q += k * nk;
-      for (int e = tid; e < nk * kv; e += ST) q[e] = Vap[(e % nk) + (int64_t)(e / nk) * n];
-      Vap = q; ldVa = nk; q += nk * kv;
+      // V[0:nk, :] transposed (element (l, c) at c + l*kv): consecutive threads read consecutive c
+      for (int e = tid; e < nk * kv; e += ST) q[(e / nk) + (e % nk) * kv] = Vap[(e % nk) + (int64_t)(e / nk) * n];
+      Vap = q; ldVa = -1; q += nk * kv;
       p = q;
     }
     if (!nd.leaf) {
@@ -150,14 +154,15 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
       if (!nd.root) {
         sW1 = p; p += kv1 * kv;
         sW2 = p; p += kv2 * kv;
-        for (int e = tid; e < kv1 * kv; e += ST) sW1[e] = (T)nd.W1[e];
-        for (int e = tid; e < kv2 * kv; e += ST) sW2[e] = (T)nd.W2[e];
+        // W1, W2 transposed (element (l, c) at c + l*kv)
+        for (int e = tid; e < kv1 * kv; e += ST) sW1[(e / kv1) + (e % kv1) * kv] = (T)nd.W1[e];
+        for (int e = tid; e < kv2 * kv; e += ST) sW2[(e / kv2) + (e % kv2) * kv] = (T)nd.W2[e];
       }
       su1 = p; p += kv1 * CPB;
       su2 = p; p += kv2 * CPB;
     }
   }
-  for (int j0 = 0; j0 < r; j0 += CPB) {
+  for (int j0 = jchunk; j0 < jchunk + CPB && j0 < r; j0 += CPB) {
     const int ncol = min(CPB, r - j0);
     // ---- gather b for this chunk of columns into shared memory
     if (nd.leaf) {
@@ -189,16 +194,28 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
         T val = T(0);
         if (gg < ncol) {
           const int64_t j = j0 + gg;
+          T acc0 = T(0), acc1 = T(0);
           if (row < mr1) {
             val = ws[c1->wb + c1->mk + row + j * ld];
             const T* uu = u2p + (int64_t)gg * ldu2;
-            for (int l = 0; l < kv2; ++l) val -= T12p[row + l * mr1] * uu[l];
+            int l = 0;
+            for (; l + 1 < kv2; l += 2) {
+              acc0 += T12p[row + l * mr1] * uu[l];
+              acc1 += T12p[row + (l + 1) * mr1] * uu[l + 1];
+            }
+            if (l < kv2) acc0 += T12p[row + l * mr1] * uu[l];
           } else {
             const int i2 = row - mr1;
             val = ws[c2->wb + c2->mk + i2 + j * ld];
             const T* uu = u1p + (int64_t)gg * ldu1;
-            for (int l = 0; l < kv1; ++l) val -= T21p[i2 + l * mr2] * uu[l];
+            int l = 0;
+            for (; l + 1 < kv1; l += 2) {
+              acc0 += T21p[i2 + l * mr2] * uu[l];
+              acc1 += T21p[i2 + (l + 1) * mr2] * uu[l + 1];
+            }
+            if (l < kv1) acc0 += T21p[i2 + l * mr2] * uu[l];
           }
+          val -= acc0 + acc1;
         }
         sb[row + gg * LDS] = val;
       }
@@ -210,8 +227,10 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
           const T* a2 = u2p + (int64_t)gg * ldu2;
           T s = T(0);
           if (staged) {
-            for (int l = 0; l < kv1; ++l) s += sW1[l + c * kv1] * a1[l];
-            for (int l = 0; l < kv2; ++l) s += sW2[l + c * kv2] * a2[l];
+            T s1 = T(0);
+            for (int l = 0; l < kv1; ++l) s += sW1[c + l * kv] * a1[l];
+            for (int l = 0; l < kv2; ++l) s1 += sW2[c + l * kv] * a2[l];
+            s += s1;
           } else {
             for (int l = 0; l < kv1; ++l) s += (T)nd.W1[l + (int64_t)c * kv1] * a1[l];
             for (int l = 0; l < kv2; ++l) s += (T)nd.W2[l + (int64_t)c * kv2] * a2[l];
@@ -308,12 +327,16 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
       const int c = e % kv, gg = e / kv;
       const T* bb = sb + gg * LDS;
       T s0 = nd.leaf ? T(0) : u[c + (int64_t)(j0 + gg) * ld], s1 = T(0);
-      int l = 0;
-      for (; l + 1 < nk; l += 2) {
-        s0 += Vap[l + c * ldVa] * bb[l];
-        s1 += Vap[l + 1 + c * ldVa] * bb[l + 1];
+      if (ldVa < 0) {   // staged transposed
+        int l = 0;
+        for (; l + 1 < nk; l += 2) {
+          s0 += Vap[c + l * kv] * bb[l];
+          s1 += Vap[c + (l + 1) * kv] * bb[l + 1];
+        }
+        if (l < nk) s0 += Vap[c + l * kv] * bb[l];
+      } else {
+        for (int l = 0; l < nk; ++l) s0 += Vap[l + c * ldVa] * bb[l];
       }
-      if (l < nk) s0 += Vap[l + c * ldVa] * bb[l];
       u[c + (int64_t)(j0 + gg) * ld] = s0 + s1;
     }
     for (int e = tid; e < mk * ncol; e += ST) {
@@ -326,12 +349,14 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
 
 template <typename T, int TPC, int MR>
 __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict__ tasks,
-                                                         const Slot* __restrict__ slots, int stage_cap) {
+                                                         const Slot* __restrict__ slots, int stage_cap,
+                                                         int nchunk) {
   constexpr int RPT = MR / TPC;
   constexpr int CPB = ST / TPC;
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sQ = (T*)smraw;
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.x / nchunk];
+  const int jchunk = (blockIdx.x % nchunk) * CPB;
   const Node* nodes = tk.nodes;
   const Node& nd = nodes[tk.node];
   const Slot& sl = slots[tk.slot];
@@ -339,6 +364,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
   const int64_t ld = sl.ldws;
   const T* fb = (const T*)sl.fbase;
   const int n = nd.n, r = sl.r;
+  if (jchunk >= r) return;
   const int tid = threadIdx.x, g = tid / TPC, gl = tid % TPC;
   const T* x = ws + nd.wx;
   const T* Qt = fb + nd.fQt;
@@ -347,7 +373,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
     Qt = sQ;
     __syncthreads();
   }
-  for (int j0 = 0; j0 < r; j0 += CPB) {
+  for (int j0 = jchunk; j0 < jchunk + CPB && j0 < r; j0 += CPB) {
     const int j = j0 + g;
     const bool act = j < r;
     T b[RPT];
@@ -410,7 +436,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
 constexpr size_t kSolveSmemCap = 200 * 1024;
 
 template <typename T, int TPC, int MR>
-void up_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStream_t st) {
+void up_launch(const Task* t, int64_t nt, const Slot* s, size_t want, int rmax, cudaStream_t st) {
   const size_t base = (size_t)LDS * (ST / TPC) * sizeof(T);
   size_t smem = base + want * sizeof(T);
   if (smem > kSolveSmemCap) smem = base;   // operands stay in global memory
@@ -420,11 +446,13 @@ void up_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStream
                          (int)kSolveSmemCap);
     set = true;
   }
-  ulv_solve_up_reg<T, TPC, MR><<<(unsigned)nt, ST, smem, st>>>(t, s, (int64_t)((smem - base) / sizeof(T)));
+  const int nchunk = (rmax + ST / TPC - 1) / (ST / TPC);
+  ulv_solve_up_reg<T, TPC, MR><<<(unsigned)(nt * nchunk), ST, smem, st>>>(t, s, (int64_t)((smem - base) / sizeof(T)),
+                                                                          nchunk);
 }
 
 template <typename T, int TPC, int MR>
-void down_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStream_t st) {
+void down_launch(const Task* t, int64_t nt, const Slot* s, size_t want, int rmax, cudaStream_t st) {
   size_t smem = want * sizeof(T);
   if (smem > kSolveSmemCap) smem = 0;
   static bool set = false;
@@ -433,7 +461,8 @@ void down_launch(const Task* t, int64_t nt, const Slot* s, size_t want, cudaStre
                          (int)kSolveSmemCap);
     set = true;
   }
-  ulv_solve_down_reg<T, TPC, MR><<<(unsigned)nt, ST, smem, st>>>(t, s, (int)(smem / sizeof(T)));
+  const int nchunk = (rmax + ST / TPC - 1) / (ST / TPC);
+  ulv_solve_down_reg<T, TPC, MR><<<(unsigned)(nt * nchunk), ST, smem, st>>>(t, s, (int)(smem / sizeof(T)), nchunk);
 }
 
 }  // namespace
@@ -442,29 +471,29 @@ bool solve_reg_fits(int mmax, int nmax) { return mmax <= 256 && nmax <= 256; }
 
 int64_t solve_up_stage_need(int m, int k, int mk, int nk, int kv, bool leaf, bool root, int mr1, int mr2, int kv1,
                             int kv2) {
-  return solve_up_stage_elems(m, k, mk, nk, kv, leaf, root, mr1, mr2, kv1, kv2, ST / 8);
+  return solve_up_stage_elems(m, k, mk, nk, kv, leaf, root, mr1, mr2, kv1, kv2, ST / 32);
 }
 
+// One warp per right-hand-side column, 8 columns per thread block; the grid
+// covers (node, column chunk) pairs so that few-node levels still fill SMs.
 template <typename T>
 void launch_ulv_solve_up_reg(const Task* t, int64_t nt, const Slot* s, int mmax, int64_t stage, int r,
                              cudaStream_t st) {
-  if (nt <= 0) return;
-  const bool wide = r > 8;
+  if (nt <= 0 || r <= 0) return;
   const size_t want = (size_t)stage;
-  if (mmax <= 64) wide ? up_launch<T, 8, 64>(t, nt, s, want, st) : up_launch<T, 32, 64>(t, nt, s, want, st);
-  else if (mmax <= 128) wide ? up_launch<T, 8, 128>(t, nt, s, want, st) : up_launch<T, 32, 128>(t, nt, s, want, st);
-  else wide ? up_launch<T, 8, 256>(t, nt, s, want, st) : up_launch<T, 32, 256>(t, nt, s, want, st);
+  if (mmax <= 64) up_launch<T, 32, 64>(t, nt, s, want, r, st);
+  else if (mmax <= 128) up_launch<T, 32, 128>(t, nt, s, want, r, st);
+  else up_launch<T, 32, 256>(t, nt, s, want, r, st);
 }
 
 template <typename T>
 void launch_ulv_solve_down_reg(const Task* t, int64_t nt, const Slot* s, int nmax, int mkmax, int r,
                                cudaStream_t st) {
-  if (nt <= 0) return;
-  const bool wide = r > 8;
+  if (nt <= 0 || r <= 0) return;
   const size_t want = (size_t)nmax * mkmax;
-  if (nmax <= 64) wide ? down_launch<T, 8, 64>(t, nt, s, want, st) : down_launch<T, 32, 64>(t, nt, s, want, st);
-  else if (nmax <= 128) wide ? down_launch<T, 8, 128>(t, nt, s, want, st) : down_launch<T, 32, 128>(t, nt, s, want, st);
-  else wide ? down_launch<T, 8, 256>(t, nt, s, want, st) : down_launch<T, 32, 256>(t, nt, s, want, st);
+  if (nmax <= 64) down_launch<T, 32, 64>(t, nt, s, want, r, st);
+  else if (nmax <= 128) down_launch<T, 32, 128>(t, nt, s, want, r, st);
+  else down_launch<T, 32, 256>(t, nt, s, want, r, st);
 }
 
 template void launch_ulv_solve_up_reg<double>(const Task*, int64_t, const Slot*, int, int64_t, int, cudaStream_t);
