@@ -115,6 +115,8 @@ inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
 int64_t g_launches = 0;
 // Forces the global-memory factor kernel for every level (parity tests of the two kernels).
 bool g_generic_factor = false;
+// Forces the native FP64 product for the refinement residual.
+bool g_residual_fp64 = false;
 struct TraceState {
   int kind = -1;
   std::vector<cudaEvent_t> pool;
@@ -169,6 +171,8 @@ struct hss_plan_s {
   SlotTable mv_slots;
   DBuf<double> hB, hC;                  // staging for the _host product
   hss_factor_s* fused[2] = {nullptr, nullptr};   // storage reused by hss_ulvfactsolve_host
+  int64_t gen_len = 0;                  // elements of d_gen
+  float2* d_gen_df = nullptr;           // generators as (hi, lo) float pairs, made on first use
   ~hss_plan_s();
 };
 
@@ -180,6 +184,7 @@ struct hss_factor_s {
   DBuf<char> sv_ws;
   SlotTable fac_slots, sv_slots, sv_slots_ref, mv_slots;
   DBuf<double> R, bn2, rn2, scale;
+  DBuf<float2> xs, tmp, ws2;            // double-float residual product buffers
   HBuf<double> h_bn2, h_rn2;
   DBuf<double> hB, hX;                  // staging for the _host solve
   ~hss_factor_s() {
@@ -190,6 +195,7 @@ struct hss_factor_s {
 hss_plan_s::~hss_plan_s() {
   delete fused[0];
   delete fused[1];
+  if (d_gen_df) cudaFree(d_gen_df);
   if (d_gen) cudaFree(d_gen);
   if (d_nodes) cudaFree(d_nodes);
   if (d_tasks) cudaFree(d_tasks);
@@ -485,6 +491,7 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
   // device phase
   CUDA_TRY(cudaGetDevice(&P->device));
   const int64_t total_gen = gbases.back();
+  P->gen_len = total_gen;
   CUDA_TRY(cudaMalloc((void**)&P->d_gen, std::max<int64_t>(total_gen, 1) * sizeof(double)));
   CUDA_TRY(cudaMalloc((void**)&P->d_err, sizeof(int32_t)));
   CUDA_TRY(cudaMemset(P->d_err, 0, sizeof(int32_t)));
@@ -536,6 +543,29 @@ void run_matvec(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
   }
   traced(HSS_TRACE_MV_FINAL, P->leaves.cnt, st,
          [&] { launch_mv_leaf_final(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
+}
+
+void run_matvec_df(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
+  const Task* T = P->d_tasks;
+  traced(HSS_TRACE_MV_LEAF, P->leaves.cnt, st,
+         [&] { launch_dfmv_leaf(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
+  for (size_t h = 1; h < P->mv_up.size(); ++h)
+    traced(HSS_TRACE_MV_UP, P->mv_up[h].cnt, st,
+           [&] { launch_dfmv_up(T + P->mv_up[h].off, P->mv_up[h].cnt, slots, rmax, st); });
+  for (size_t d = 0; d < P->mv_dn.size(); ++d)
+    traced(HSS_TRACE_MV_DOWN, P->mv_dn[d].cnt, st,
+           [&] { launch_dfmv_down(T + P->mv_dn[d].off, P->mv_dn[d].cnt, slots, rmax, st); });
+  traced(HSS_TRACE_MV_FINAL, P->leaves.cnt, st,
+         [&] { launch_dfmv_final(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
+}
+
+int ensure_df(hss_plan_s* P, cudaStream_t st) {
+  if (P->d_gen_df) return HSS_OK;
+  CUDA_TRY(cudaMalloc((void**)&P->d_gen_df, std::max<int64_t>(P->gen_len, 1) * sizeof(float2)));
+  launch_df_split(P->d_gen, P->d_gen_df, P->gen_len, st);
+  ++g_launches;
+  CUDA_TRY(cudaGetLastError());
+  return HSS_OK;
 }
 
 template <typename T>
@@ -740,10 +770,27 @@ int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t
   for (int32_t it = 0;; ++it) {
     CUDA_TRY(cudaMemsetAsync(f->rn2.p, 0, rtot * sizeof(double), st));
     {
-      // R = -A x + B
+      // R = -A x + B: double-float product on the FP32 pipe (FP32 factor), or
+      // the native FP64 product
+      const bool dfres = fp32 && !g_residual_fp64 && P->d_gen_df != nullptr;
       int64_t rmax = 0;
       for (auto& c : mvio) rmax = std::max(rmax, c.r);
-      CUDA_TRY(P->mv_ws.ensure((size_t)P->ws_mv * rmax));
+      std::vector<int64_t> xoff(P->ntrees + 1, 0), toff(P->ntrees + 1, 0);
+      for (int32_t t = 0; t < P->ntrees; ++t) {
+        xoff[t + 1] = xoff[t] + P->tree_n[t] * mvio[t].r;
+        toff[t + 1] = toff[t] + P->tree_m[t] * mvio[t].r;
+      }
+      if (dfres) {
+        CUDA_TRY(f->xs.ensure(std::max<int64_t>(xoff[P->ntrees], 1)));
+        CUDA_TRY(f->tmp.ensure(std::max<int64_t>(toff[P->ntrees], 1)));
+        CUDA_TRY(f->ws2.ensure((size_t)P->ws_mv * rmax));
+        for (int32_t t = 0; t < P->ntrees; ++t) {
+          launch_df_split_cols(mvio[t].B, mvio[t].ldb, P->tree_n[t], mvio[t].r, f->xs.p + xoff[t], st);
+          ++g_launches;
+        }
+      } else {
+        CUDA_TRY(P->mv_ws.ensure((size_t)P->ws_mv * rmax));
+      }
       std::vector<Slot> s(P->ntrees);
       for (int32_t t = 0; t < P->ntrees; ++t) {
         Slot& x = s[t];
@@ -756,9 +803,20 @@ int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t
         x.r = (int32_t)mvio[t].r;
         x.colnorm2 = f->rn2.p + off[t];
         x.err = P->d_err;
+        if (dfres) {
+          // per-tree pair buffers (row0/col0 are tree-local)
+          x.xs = f->xs.p + xoff[t];
+          x.ldx2 = P->tree_n[t];
+          x.tmp = f->tmp.p + toff[t];
+          x.ldt2 = P->tree_m[t];
+          x.ws2 = f->ws2.p;
+          x.gdf = P->d_gen_df;
+          x.gbase = P->d_gen;
+        }
       }
       CUDA_TRY(f->mv_slots.upload(s, st));
-      run_matvec(P, f->mv_slots.dev.p, (int)rmax, st);
+      if (dfres) run_matvec_df(P, f->mv_slots.dev.p, (int)rmax, st);
+      else run_matvec(P, f->mv_slots.dev.p, (int)rmax, st);
       CUDA_TRY(cudaGetLastError());
     }
     CUDA_TRY(cudaMemcpyAsync(f->h_rn2.p, f->rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -967,8 +1025,10 @@ int hss_ulvfactor(hss_handle h, int32_t precision, hss_factor* out, void* stream
     delete f;
     return cuda_fail(e, "cudaMalloc(factor)");
   }
-  int rc = precision == HSS_PREC_FP32 ? factor_impl<float>(f, (cudaStream_t)stream)
-                                      : factor_impl<double>(f, (cudaStream_t)stream);
+  int rc = precision == HSS_PREC_FP32 ? ensure_df(h, (cudaStream_t)stream) : HSS_OK;
+  if (!rc)
+    rc = precision == HSS_PREC_FP32 ? factor_impl<float>(f, (cudaStream_t)stream)
+                                    : factor_impl<double>(f, (cudaStream_t)stream);
   if (rc) { delete f; return rc; }
   *out = f;
   return HSS_OK;
@@ -1014,6 +1074,10 @@ int64_t hss_launch_counter(void) { return g_launches; }
 int hss_set_option(int32_t option, int64_t value) {
   if (option == HSS_OPT_GENERIC_FACTOR) {
     g_generic_factor = value != 0;
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_RESIDUAL_FP64) {
+    g_residual_fp64 = value != 0;
     return HSS_OK;
   }
   return fail(HSS_ERR_INVALID, "unknown option");

@@ -14,6 +14,7 @@
 // be mixed in one launch.
 #pragma once
 #include <cstdint>
+#include <vector_types.h>
 
 namespace hss {
 
@@ -56,6 +57,14 @@ struct Slot {
   double* colnorm2;                   // product: += sum_i C(i,j)^2 per column (nullable)
   int32_t r, mode;                    // solve: mode 0 x = s*d, 1 x += s*d
   int32_t* err;                       // device status word (nullable)
+  // double-float product: X split into (hi, lo) pairs, the D X partial
+  // products, pair workspace (same row offsets as ws), and the generators
+  // as pairs (gdf[e] pairs gbase[e]).
+  const float2* xs;  int64_t ldx2;
+  float2* tmp;       int64_t ldt2;
+  float2* ws2;
+  const float2* gdf;
+  const double* gbase;
 };
 
 // device status codes written into Slot::err

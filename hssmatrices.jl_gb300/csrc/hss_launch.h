@@ -17,6 +17,14 @@ size_t mv_down_staged_smem(int ku, int u1, int u2, int v1, int v2);
 void launch_mv_up_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, int rmax, cudaStream_t st);
 void launch_mv_down_staged(const Task* t, int64_t ntasks, const Slot* s, size_t smem, int rmax, cudaStream_t st);
 
+// Double-float (FP32 pair) product for the refinement residual (hss_matvec_df.cu).
+void launch_df_split(const double* src, float2* dst, int64_t cnt, cudaStream_t st);
+void launch_df_split_cols(const double* X, int64_t ldx, int64_t n, int64_t r, float2* Xs, cudaStream_t st);
+void launch_dfmv_leaf(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
+void launch_dfmv_up(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
+void launch_dfmv_down(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
+void launch_dfmv_final(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
+
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,

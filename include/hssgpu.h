@@ -173,8 +173,11 @@ int64_t hss_launch_counter(void);
 
 /* Process-wide switches.  HSS_OPT_GENERIC_FACTOR = 1 routes every ULV
  * factorization level to the global-memory kernel (used to test the on-chip
- * kernel against it); 0 (default) picks the on-chip kernel where it fits. */
-enum { HSS_OPT_GENERIC_FACTOR = 1 };
+ * kernel against it); 0 (default) picks the on-chip kernel where it fits.
+ * HSS_OPT_RESIDUAL_FP64 = 1 forms the refinement residual of an FP32 factor
+ * with the native FP64 product instead of the default double-float product
+ * on the FP32 pipe (~48-bit, made for GB300's low FP64 rate). */
+enum { HSS_OPT_GENERIC_FACTOR = 1, HSS_OPT_RESIDUAL_FP64 = 2 };
 int hss_set_option(int32_t option, int64_t value);
 
 const char* hss_last_error(void);

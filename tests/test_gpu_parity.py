@@ -186,3 +186,25 @@ def test_factor_kernels_agree(pkg, lib, orc, name):
     # unrefined FP32 solves: both within FP32 accuracy of the FP64 answer
     for generic in (0, 1):
         assert rel(out[generic, "fp32"], g["z"]) <= (1e-2 if name == "cauchy2001_compress" else 1e-4)
+
+
+@pytest.mark.parametrize("name", ["synthetic_perfect", "synthetic_uneven", "synthetic_earlyexit",
+                                  "cauchy2001_compress"])
+def test_refinement_residual_paths(pkg, lib, orc, name):
+    """FP32 factorization refined with the double-float residual product (default) and with
+    the native FP64 product: both reach 1e-10 in true (oracle, FP64) residual."""
+    g, h, A = _golden(pkg, orc, name)
+    Af = orc.full(h)
+    sols = []
+    for native in (0, 1):
+        assert lib.hss_set_option(2, native) == 0
+        try:
+            st = {}
+            z = pkg.ldiv(A, g["b"], precision="fp32", tol=1e-10, maxit=30, stats=st)
+        finally:
+            lib.hss_set_option(2, 0)
+        assert st["converged"]
+        res = np.linalg.norm(g["b"] - Af @ z, axis=0) / np.linalg.norm(g["b"], axis=0)
+        assert res.max() <= 2e-10, (native, res.max())
+        sols.append(z)
+    assert rel(sols[0], sols[1]) <= 1e-6
