@@ -31,7 +31,7 @@ constexpr int FMAX = 128;         // max m, n
 constexpr int FKMAX = 64;         // max ku, kv
 constexpr int PART_COLS = FMAX + FKMAX;
 constexpr size_t kFastSmemCap = 226 * 1024;   // dynamic part; the static part is < 1 KB
-constexpr int SVLEN = FMAX + FMAX / 32 + 8;     // padded broadcast vector
+constexpr int SVLEN = FMAX + (FMAX / 32) * 4 + 8;   // padded broadcast vector (16-byte multiple)
 
 template <typename T>
 __device__ __forceinline__ T wsum(T v) {
@@ -57,8 +57,43 @@ __device__ __forceinline__ void larfg(T alpha, T ss, T& beta, T& tau, T& scal) {
   larfg_ss(alpha, ss, beta, tau, scal);
 }
 
-// padded index of the broadcast vector: 33 slots per 32 entries (no bank conflicts)
-__device__ __forceinline__ int vp(int i) { return i + (i >> 5); }
+// padded index of the broadcast vector: 36 slots per 32 entries, so that each
+// 32-entry quarter starts 16-byte aligned and the four quarters a warp reads
+// with 128-bit loads sit in distinct banks
+__device__ __forceinline__ int vp(int i) { return i + ((i >> 5) << 2); }
+
+// v[0..31] = buf[36q .. 36q+31] with 128-bit shared loads
+template <typename T>
+__device__ __forceinline__ void load_quarter(T (&v)[32], const T* buf, int q) {
+  const T* b = buf + 36 * q;
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const float4 t = reinterpret_cast<const float4*>(b)[k];
+      v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const double2 t = reinterpret_cast<const double2*>(b)[k];
+      v[2 * k] = t.x; v[2 * k + 1] = t.y;
+    }
+  }
+}
+
+// sum_l a[l] * v[l] over 32 entries with four independent chains
+template <typename T>
+__device__ __forceinline__ T dot32(const T (&a)[32], const T (&v)[32]) {
+  T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+#pragma unroll
+  for (int l = 0; l < 32; l += 4) {
+    s0 += a[l] * v[l];
+    s1 += a[l + 1] * v[l + 1];
+    s2 += a[l + 2] * v[l + 2];
+    s3 += a[l + 3] * v[l + 3];
+  }
+  return (s0 + s1) + (s2 + s3);
+}
 
 // LU with partial pivoting of an m x m block in shared memory (ld = ld).
 template <typename T>
@@ -293,13 +328,14 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
     }
     auto ql_reflector = [&](int c, T* buf, int slot) {   // called by the 4 owners of U[:, c]
       const int p = mk + c;
-      T ss = T(0), mine = T(0);
+      T s4[4] = {T(0), T(0), T(0), T(0)}, mine = T(0);
 #pragma unroll
       for (int l = 0; l < 32; ++l) {
         const int row = r0 + l;
-        if (row < p) ss += uc[l] * uc[l];
+        if (row < p) s4[l & 3] += uc[l] * uc[l];
         if (row == p) mine = uc[l];
       }
+      T ss = (s4[0] + s4[1]) + (s4[2] + s4[3]);
       ss += __shfl_xor_sync(gm, ss, 1);
       ss += __shfl_xor_sync(gm, ss, 2);
       const T alpha = __shfl_sync(gm, mine, p >> 5, 4);
@@ -321,25 +357,23 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
       const T* svc = cur ? sv1 : sv0;
       const T tau = stau[cur];
       if (tau != T(0)) {
+        T vq[32];
+        load_quarter(vq, svc, q);
         if (cl < n) {
-          T w = T(0);
-#pragma unroll
-          for (int l = 0; l < 32; ++l) w += svc[vp(r0 + l)] * dc[l];
+          T w = dot32(dc, vq);
           w += __shfl_xor_sync(gm, w, 1);
           w += __shfl_xor_sync(gm, w, 2);
           w *= tau;
 #pragma unroll
-          for (int l = 0; l < 32; ++l) dc[l] -= w * svc[vp(r0 + l)];
+          for (int l = 0; l < 32; ++l) dc[l] -= w * vq[l];
         }
         if (cl < c) {
-          T w = T(0);
-#pragma unroll
-          for (int l = 0; l < 32; ++l) w += svc[vp(r0 + l)] * uc[l];
+          T w = dot32(uc, vq);
           w += __shfl_xor_sync(gm, w, 1);
           w += __shfl_xor_sync(gm, w, 2);
           w *= tau;
 #pragma unroll
-          for (int l = 0; l < 32; ++l) uc[l] -= w * svc[vp(r0 + l)];
+          for (int l = 0; l < 32; ++l) uc[l] -= w * vq[l];
         }
       }
       if (c >= 1 && cl == c - 1) ql_reflector(c - 1, cur ? sv0 : sv1, cur ^ 1);
@@ -426,13 +460,14 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
   }
   const int nl = min(mk, n);
   auto lq_reflector = [&](int i, T* buf, int slot) {   // called by the 4 owners of row i
-    T ss = T(0), mine = T(0);
+    T s4[4] = {T(0), T(0), T(0), T(0)}, mine = T(0);
 #pragma unroll
     for (int l = 0; l < 32; ++l) {
       const int col = c0 + l;
-      if (col > i) ss += d[l] * d[l];
+      if (col > i) s4[l & 3] += d[l] * d[l];
       if (col == i) mine = d[l];
     }
+    T ss = (s4[0] + s4[1]) + (s4[2] + s4[3]);
     ss += __shfl_xor_sync(gmask, ss, 1);
     ss += __shfl_xor_sync(gmask, ss, 2);
     const T alpha = __shfl_sync(gmask, mine, i >> 5, 4);
@@ -455,24 +490,40 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
     const T tau = stau[cur];
     if (tau != T(0)) {
       if (j > i && j < m) {
-        T w = T(0);
-#pragma unroll
-        for (int l = 0; l < 32; ++l) w += d[l] * svc[vp(c0 + l)];
+        T vq[32];
+        load_quarter(vq, svc, q);
+        T w = dot32(d, vq);
         w += __shfl_xor_sync(gmask, w, 1);
         w += __shfl_xor_sync(gmask, w, 2);
         w *= tau;
 #pragma unroll
-        for (int l = 0; l < 32; ++l) d[l] -= w * svc[vp(c0 + l)];
+        for (int l = 0; l < 32; ++l) d[l] -= w * vq[l];
       }
       {
         // every lane takes part (columns >= kv hold zeros): full-warp shuffles
-        T w0 = T(0), w1 = T(0);
+        T sr[8];
+        const T* vb = svc + vp(8 * vseg);   // 8 consecutive entries, 16-byte aligned
+        if constexpr (sizeof(T) == 4) {
+          const float4 a = reinterpret_cast<const float4*>(vb)[0];
+          const float4 b = reinterpret_cast<const float4*>(vb)[1];
+          sr[0] = a.x; sr[1] = a.y; sr[2] = a.z; sr[3] = a.w;
+          sr[4] = b.x; sr[5] = b.y; sr[6] = b.z; sr[7] = b.w;
+        } else {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-          const T sv_r = svc[vp(8 * vseg + r)];
-          w0 += sv_r * vv[0][r];
-          w1 += sv_r * vv[1][r];
+          for (int k = 0; k < 4; ++k) {
+            const double2 a = reinterpret_cast<const double2*>(vb)[k];
+            sr[2 * k] = a.x; sr[2 * k + 1] = a.y;
+          }
         }
+        T w0a = T(0), w0b = T(0), w1a = T(0), w1b = T(0);
+#pragma unroll
+        for (int r = 0; r < 8; r += 2) {
+          w0a += sr[r] * vv[0][r];
+          w0b += sr[r + 1] * vv[0][r + 1];
+          w1a += sr[r] * vv[1][r];
+          w1b += sr[r + 1] * vv[1][r + 1];
+        }
+        T w0 = w0a + w0b, w1 = w1a + w1b;
 #pragma unroll
         for (int o = 1; o < 16; o <<= 1) {
           w0 += __shfl_xor_sync(0xffffffffu, w0, o);
@@ -482,9 +533,8 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
         w1 *= tau;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          const T sv_r = svc[vp(8 * vseg + r)];
-          vv[0][r] -= w0 * sv_r;
-          vv[1][r] -= w1 * sv_r;
+          vv[0][r] -= w0 * sr[r];
+          vv[1][r] -= w1 * sr[r];
         }
       }
     }

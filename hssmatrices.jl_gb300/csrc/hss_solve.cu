@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
   const int tid = threadIdx.x, g = tid / TPC, gl = tid % TPC;
   const T* x = ws + nd.wx;
   const T* Qt = fb + nd.fQt;
-  if (!nd.root && nd.mk > 0 && nchunk == 1 && n * nd.mk <= stage_cap) {
+  if (!nd.root && nd.mk > 0 && n * nd.mk <= stage_cap) {
     for (int e = tid; e < n * nd.mk; e += ST) sQ[e] = Qt[e];
     Qt = sQ;
     __syncthreads();
@@ -454,8 +454,7 @@ void up_launch(const Task* t, int64_t nt, const Slot* s, size_t want, int rmax, 
 template <typename T, int TPC, int MR>
 void down_launch(const Task* t, int64_t nt, const Slot* s, size_t want, int rmax, cudaStream_t st) {
   size_t smem = want * sizeof(T);
-  // with several column chunks per node the reflectors are read through L1 instead
-  if (smem > kSolveSmemCap || rmax > ST / TPC) smem = 0;
+  if (smem > kSolveSmemCap) smem = 0;
   static bool set = false;
   if (!set) {
     cudaFuncSetAttribute(ulv_solve_down_reg<T, TPC, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
