@@ -32,6 +32,9 @@ constexpr int FKMAX = 64;         // max ku, kv
 constexpr int PART_COLS = FMAX + FKMAX;
 constexpr size_t kFastSmemCap = 226 * 1024;   // dynamic part; the static part is < 1 KB
 constexpr int SVLEN = FMAX + (FMAX / 32) * 4 + 8;   // padded broadcast vector (16-byte multiple)
+static_assert(SVLEN % 4 == 0 && PART_COLS % 4 == 0, "broadcast vectors must stay 16-byte aligned");
+
+__host__ __device__ constexpr size_t smem_align4(size_t e) { return (e + 3) & ~size_t(3); }
 
 template <typename T>
 __device__ __forceinline__ T wsum(T v) {
@@ -162,9 +165,11 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
   const Slot& sl = slots[tk.slot];
   T* fb = (T*)sl.fbase;
   const int m = nd.m, n = nd.n, ku = nd.ku, kv = nd.kv;
+  // region starts are rounded up to 4 elements: the broadcast vectors are
+  // read with 128-bit loads and must be 16-byte aligned
   T* sD = (T*)smraw;                                // m x n, ld LDD
-  T* sU = sD + (size_t)LDD * nmax;                  // m x ku, ld LDD
-  T* part = sU + (size_t)LDD * (kumax > 0 ? kumax : 1);
+  T* sU = sD + smem_align4((size_t)LDD * nmax);     // m x ku, ld LDD
+  T* part = sU + smem_align4((size_t)LDD * (kumax > 0 ? kumax : 1));
   T* sv = part + 4 * PART_COLS;                     // padded broadcast vectors (2)
   T* sx = sv + 2 * SVLEN;                           // merge staging (branches)
   T* gD = fb + nd.fD;
@@ -564,7 +569,8 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
 template <typename T>
 size_t factor_fast_smem(int mmax, int nmax, int kumax, size_t extra) {
   const int LDD = mmax | 1;
-  return ((size_t)LDD * nmax + (size_t)LDD * (kumax > 0 ? kumax : 1) + 4 * PART_COLS + 2 * SVLEN + extra) *
+  return (smem_align4((size_t)LDD * nmax) + smem_align4((size_t)LDD * (kumax > 0 ? kumax : 1)) + 4 * PART_COLS +
+          2 * SVLEN + extra) *
          sizeof(T);
 }
 
