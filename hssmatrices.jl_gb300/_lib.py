@@ -38,7 +38,7 @@ EXPORTS = [
     "hss_ulv_cols", "hss_matmul", "hss_matmul_host", "hss_matmul_batch", "hss_ulvfactor",
     "hss_factor_destroy", "hss_ulvsolve", "hss_ulvsolve_host", "hss_ulvsolve_batch",
     "hss_ulvfactsolve_host", "hss_factor_bytes", "hss_last_error", "hss_version", "hss_ulvrefactor",
-    "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option",
+    "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option", "hss_matmul_noalloc",
 ]
 
 
@@ -80,6 +80,7 @@ def _declare(lib):
         "hss_ulv_cols": (C.c_int, [P, I64, PI64, I64, PI64]),
         "hss_matmul": (C.c_int, [P, P, I64, I64, P, I64, D, D, P]),
         "hss_matmul_host": (C.c_int, [P, PD, I64, I64, PD, I64, D, D]),
+        "hss_matmul_noalloc": (C.c_int, [P, P, I64, I64, P, I64, D, D, P]),
         "hss_matmul_batch": (C.c_int, [P, C.POINTER(P), PI64, PI64, C.POINTER(P), PI64, D, D, P]),
         "hss_ulvfactor": (C.c_int, [P, I32, C.POINTER(P), P]),
         "hss_factor_destroy": (C.c_int, [P]),

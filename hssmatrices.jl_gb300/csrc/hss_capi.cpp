@@ -980,6 +980,42 @@ int hss_matmul(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* d
   return matmul_impl(h, io, alpha, beta, (cudaStream_t)stream, nullptr, nullptr, nullptr, h->mv_slots);
 }
 
+int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC, int64_t ldc,
+                       double alpha, double beta, void* stream) {
+  if (!h) return fail(HSS_ERR_INVALID, "null handle");
+  if (h->ntrees != 1) return fail(HSS_ERR_INVALID, "the allocation-free product takes a single matrix");
+  std::vector<Cols> io{Cols{dB, ldb, r, dC, ldc}};
+  int rc = check_cols(h, io, false);
+  if (rc) return rc;
+  if (r == 0) return HSS_OK;
+  if ((int64_t)h->ws_mv * r > noalloc_ws_capacity())
+    return fail(HSS_ERR_BAD_DIMS, "allocation-free product: workspace of " + std::to_string(h->ws_mv) + " rows x " +
+                                      std::to_string(r) + " right-hand sides exceeds the fixed scratch of " +
+                                      std::to_string(noalloc_ws_capacity()) + " doubles");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  double* ws = nullptr;
+  Slot* dslot = nullptr;
+  std::string err;
+  rc = noalloc_scratch(dev, &ws, &dslot, &err);
+  if (rc) return fail(rc, err);
+  Slot x;
+  std::memset(&x, 0, sizeof(Slot));
+  x.B = dB; x.ldb = ldb;
+  x.C = dC; x.ldc = ldc;
+  x.Y = dC; x.ldy = ldc;
+  x.alpha = alpha; x.beta = beta;
+  x.ws = ws; x.ldws = h->ws_mv;
+  x.r = (int32_t)r;
+  x.err = h->d_err;
+  cudaStream_t st = (cudaStream_t)stream;
+  // pageable source: staged by the driver before the call returns
+  CUDA_TRY(cudaMemcpyAsync(dslot, &x, sizeof(Slot), cudaMemcpyHostToDevice, st));
+  run_matvec(h, dslot, (int)r, st);
+  CUDA_TRY(cudaGetLastError());
+  return HSS_OK;
+}
+
 int hss_matmul_batch(hss_handle h, const double* const* dB, const int64_t* ldb, const int64_t* r,
                      double* const* dC, const int64_t* ldc, double alpha, double beta, void* stream) {
   if (!h || !dB || !ldb || !r || !dC || !ldc) return fail(HSS_ERR_INVALID, "bad batch arguments");

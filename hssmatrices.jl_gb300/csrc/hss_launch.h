@@ -1,6 +1,7 @@
 // Kernel launch wrappers (implemented in hss_kernels.cu, used by hss_capi.cpp).
 #pragma once
 #include <cuda_runtime.h>
+#include <string>
 #include "hss_internal.h"
 
 namespace hss {
@@ -56,5 +57,10 @@ void launch_colnorm2(const double* B, int64_t ldb, int64_t n, int64_t r, double*
                      cudaStream_t st);
 // s[j] = sqrt(n2[j]) (1 where n2[j] == 0) and s[r + j] = 1 / s[j]; s holds 2r values.
 void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st);
+
+// Fixed scratch of the allocation-free product (hss_noalloc.cu): device
+// addresses of the file-scope arrays on `device`, resolved once per device.
+int noalloc_scratch(int device, double** ws, Slot** slot, std::string* err);
+int64_t noalloc_ws_capacity();
 
 }  // namespace hss

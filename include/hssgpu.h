@@ -103,6 +103,20 @@ int hss_matmul(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* d
 int hss_matmul_host(hss_handle h, const double* B, int64_t ldb, int64_t r, double* C,
                     int64_t ldc, double alpha, double beta);
 
+/* hss_matmul without any memory allocation; no counterpart in the reference.
+ * For callers that cannot call cudaMalloc during a call (host callbacks,
+ * pre-allocated real-time loops, runtimes that forbid allocation after
+ * start-up).  The per-node workspace and the argument table live in fixed
+ * file-scope device arrays (8 MiB + one argument slot, held by every GPU that
+ * loads the library until the process exits): at most 2^20 doubles of workspace (workspace rows
+ * x r; e.g. n = 65536 at rank 32 allows r <= 16), larger calls return
+ * HSS_ERR_BAD_DIMS.  The arrays are shared by all calls on a device: calls
+ * that overlap on the GPU race; calls on one stream are ordered.  The first
+ * call on a device resolves the arrays' addresses (make it before any stream
+ * capture).  Same arguments and result as hss_matmul. */
+int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC,
+                       int64_t ldc, double alpha, double beta, void* stream);
+
 /* Batched product over a forest: matrix i uses dB[i], dC[i], r[i] (device). */
 int hss_matmul_batch(hss_handle h, const double* const* dB, const int64_t* ldb,
                      const int64_t* r, double* const* dC, const int64_t* ldc,
