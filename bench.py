@@ -251,6 +251,16 @@ def run_ours(args, rank, world, local_rank):
     k_ms, k_cnt = L.trace_end()
     times = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(times)
+    # per kernel kind: device time per mixed step (CUDA events around each
+    # launch of one kind at a time, a few extra steps per kind)
+    breakdown = {}
+    for kind in ("factor_leaf", "factor_merge", "solve_up", "solve_down", "mv_leaf", "mv_up", "mv_down",
+                 "mv_final"):
+        L.trace_begin(kind)
+        for _ in range(3):
+            step32()
+        kms, _kn = L.trace_end()
+        breakdown[kind] = kms / 3
     if dist:
         t = torch.tensor([total_ms], device="cuda")
         td.all_reduce(t, op=td.ReduceOp.MAX)
@@ -342,6 +352,7 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n * r,
                 "d2h_bytes_per_step": 8 * n * r, "ms_per_step": 1000.0 * e2e_total / args.steps},
         "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+        "breakdown_ms_per_step": breakdown,
         "factor_bytes": {"fp32": F32.nbytes(), "fp64": F64.nbytes()},
     }
     print(json.dumps(line), flush=True)
