@@ -39,6 +39,7 @@ EXPORTS = [
     "hss_factor_destroy", "hss_ulvsolve", "hss_ulvsolve_host", "hss_ulvsolve_batch",
     "hss_ulvfactsolve_host", "hss_factor_bytes", "hss_last_error", "hss_version", "hss_ulvrefactor",
     "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option", "hss_matmul_noalloc",
+    "hss_batcher_create", "hss_batcher_destroy", "hss_batcher_factor", "hss_batcher_solve",
 ]
 
 
@@ -95,6 +96,11 @@ def _declare(lib):
         "hss_trace_end": (C.c_int, [C.POINTER(D), PI64]),
         "hss_launch_counter": (C.c_int64, []),
         "hss_set_option": (C.c_int, [I32, I64]),
+        "hss_batcher_create": (C.c_int, [C.POINTER(P)]),
+        "hss_batcher_destroy": (C.c_int, [P]),
+        "hss_batcher_factor": (C.c_int, [P, I32, C.POINTER(P), I32, C.POINTER(P), P]),
+        "hss_batcher_solve": (C.c_int, [P, I32, C.POINTER(P), C.POINTER(P), PI64, PI64, C.POINTER(P), PI64, D, I32,
+                                        C.POINTER(SolveStats), P]),
         "hss_last_error": (C.c_char_p, []),
         "hss_version": (C.c_int32, []),
     }

@@ -173,7 +173,16 @@ struct hss_plan_s {
   hss_factor_s* fused[2] = {nullptr, nullptr};   // storage reused by hss_ulvfactsolve_host
   int64_t gen_len = 0;                  // elements of d_gen
   float2* d_gen_df = nullptr;           // generators as (hi, lo) float pairs, made on first use
+  std::vector<Task> h_tasks;            // host copy of the task lists (merged batches)
   ~hss_plan_s();
+};
+
+// Per-call buffers of a (batched) solve with refinement.
+struct SolveBufs {
+  DBuf<double> R, bn2, rn2, scale;
+  HBuf<double> h_bn2, h_rn2;
+  DBuf<float2> xs, tmp;
+  SlotTable sv0, sv1, mv;
 };
 
 struct hss_factor_s {
@@ -181,11 +190,10 @@ struct hss_factor_s {
   int prec = HSS_PREC_FP64;
   void* d_fac = nullptr;
   size_t fac_bytes = 0;
-  DBuf<char> sv_ws;
-  SlotTable fac_slots, sv_slots, sv_slots_ref, mv_slots;
-  DBuf<double> R, bn2, rn2, scale;
-  DBuf<float2> xs, tmp, ws2;            // double-float residual product buffers
-  HBuf<double> h_bn2, h_rn2;
+  DBuf<char> sv_ws;                     // solve workspace (this factor's plan layout)
+  DBuf<float2> ws2;                     // double-float product workspace
+  SlotTable fac_slots;
+  SolveBufs bufs;
   DBuf<double> hB, hX;                  // staging for the _host solve
   ~hss_factor_s() {
     if (d_fac) cudaFree(d_fac);
@@ -511,6 +519,7 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
   CUDA_TRY(cudaMalloc((void**)&P->d_nodes, total_nodes * sizeof(Node)));
   CUDA_TRY(cudaMemcpy(P->d_nodes, P->nodes.data(), total_nodes * sizeof(Node), cudaMemcpyHostToDevice));
   for (auto& t : tasks) t.nodes = P->d_nodes;
+  P->h_tasks = tasks;
   CUDA_TRY(cudaMalloc((void**)&P->d_tasks, std::max<size_t>(tasks.size(), 1) * sizeof(Task)));
   CUDA_TRY(cudaMemcpy(P->d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice));
   return HSS_OK;
@@ -520,43 +529,68 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
 // launch sequences
 // ---------------------------------------------------------------------------
 
-void run_matvec(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
-  const Task* T = P->d_tasks;
+// The task lists one launch sequence walks: a plan's own (slot = tree of the
+// forest) or lists merged over several single-tree plans (slot = item).
+struct Levels {
+  const Task* d_tasks = nullptr;
+  const std::vector<Seg>* by_h = nullptr;
+  const std::vector<Seg>* by_d = nullptr;
+  const std::vector<Seg>* mv_up = nullptr;
+  const std::vector<Seg>* mv_dn = nullptr;
+  Seg leaves;
+};
+
+Levels plan_levels(const hss_plan_s* P) {
+  Levels L;
+  L.d_tasks = P->d_tasks;
+  L.by_h = &P->by_h;
+  L.by_d = &P->by_d;
+  L.mv_up = &P->mv_up;
+  L.mv_dn = &P->mv_dn;
+  L.leaves = P->leaves;
+  return L;
+}
+
+void run_matvec(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
+  const Task* T = L.d_tasks;
   constexpr size_t kStagedCap = 200 * 1024;
-  traced(HSS_TRACE_MV_LEAF, P->leaves.cnt, st,
-         [&] { launch_mv_leaf(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
-  for (size_t h = 1; h < P->mv_up.size(); ++h) {
-    const Seg& g = P->mv_up[h];
+  traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st,
+         [&] { launch_mv_leaf(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
+  for (size_t h = 1; h < L.mv_up->size(); ++h) {
+    const Seg& g = (*L.mv_up)[h];
     traced(HSS_TRACE_MV_UP, g.cnt, st, [&] {
       const size_t sm = mv_up_staged_smem(g.kvmax, g.c1v, g.c2v);
       if (sm <= kStagedCap) launch_mv_up_staged(T + g.off, g.cnt, slots, sm, rmax, st);
       else launch_mv_up(T + g.off, g.cnt, slots, st);
     });
   }
-  for (size_t d = 0; d < P->mv_dn.size(); ++d) {
-    const Seg& g = P->mv_dn[d];
+  for (size_t d = 0; d < L.mv_dn->size(); ++d) {
+    const Seg& g = (*L.mv_dn)[d];
     traced(HSS_TRACE_MV_DOWN, g.cnt, st, [&] {
       const size_t sm = mv_down_staged_smem(g.kumax, g.c1u, g.c2u, g.c1v, g.c2v);
       if (sm <= kStagedCap) launch_mv_down_staged(T + g.off, g.cnt, slots, sm, rmax, st);
       else launch_mv_down(T + g.off, g.cnt, slots, st);
     });
   }
-  traced(HSS_TRACE_MV_FINAL, P->leaves.cnt, st,
-         [&] { launch_mv_leaf_final(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
+  traced(HSS_TRACE_MV_FINAL, L.leaves.cnt, st,
+         [&] { launch_mv_leaf_final(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
+}
+void run_matvec(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
+  run_matvec(plan_levels(P), slots, rmax, st);
 }
 
-void run_matvec_df(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
-  const Task* T = P->d_tasks;
-  traced(HSS_TRACE_MV_LEAF, P->leaves.cnt, st,
-         [&] { launch_dfmv_leaf(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
-  for (size_t h = 1; h < P->mv_up.size(); ++h)
-    traced(HSS_TRACE_MV_UP, P->mv_up[h].cnt, st,
-           [&] { launch_dfmv_up(T + P->mv_up[h].off, P->mv_up[h].cnt, slots, rmax, st); });
-  for (size_t d = 0; d < P->mv_dn.size(); ++d)
-    traced(HSS_TRACE_MV_DOWN, P->mv_dn[d].cnt, st,
-           [&] { launch_dfmv_down(T + P->mv_dn[d].off, P->mv_dn[d].cnt, slots, rmax, st); });
-  traced(HSS_TRACE_MV_FINAL, P->leaves.cnt, st,
-         [&] { launch_dfmv_final(T + P->leaves.off, P->leaves.cnt, slots, rmax, st); });
+void run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
+  const Task* T = L.d_tasks;
+  traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st,
+         [&] { launch_dfmv_leaf(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
+  for (size_t h = 1; h < L.mv_up->size(); ++h)
+    traced(HSS_TRACE_MV_UP, (*L.mv_up)[h].cnt, st,
+           [&] { launch_dfmv_up(T + (*L.mv_up)[h].off, (*L.mv_up)[h].cnt, slots, rmax, st); });
+  for (size_t d = 0; d < L.mv_dn->size(); ++d)
+    traced(HSS_TRACE_MV_DOWN, (*L.mv_dn)[d].cnt, st,
+           [&] { launch_dfmv_down(T + (*L.mv_dn)[d].off, (*L.mv_dn)[d].cnt, slots, rmax, st); });
+  traced(HSS_TRACE_MV_FINAL, L.leaves.cnt, st,
+         [&] { launch_dfmv_final(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
 }
 
 int ensure_df(hss_plan_s* P, cudaStream_t st) {
@@ -569,9 +603,9 @@ int ensure_df(hss_plan_s* P, cudaStream_t st) {
 }
 
 template <typename T>
-void run_factor(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
-  for (size_t h = 0; h < P->by_h.size(); ++h) {
-    const Seg& g = P->by_h[h];
+void run_factor(const Levels& L, const Slot* slots, cudaStream_t st) {
+  for (size_t h = 0; h < L.by_h->size(); ++h) {
+    const Seg& g = (*L.by_h)[h];
     traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, g.cnt, st, [&] {
       // merge staging: converted generators, children's reduced U/V, T12/T21
       const size_t extra = (size_t)g.c1u * g.c2v + (size_t)g.c2u * g.c1v + (size_t)(g.c1u + g.c2u) * g.kumax +
@@ -579,33 +613,109 @@ void run_factor(hss_plan_s* P, const Slot* slots, cudaStream_t st) {
                            (size_t)g.c1nr * g.c1v + (size_t)g.c2nr * g.c2v + (size_t)g.c1mr * g.c2v +
                            (size_t)g.c2mr * g.c1v;
       if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra))
-        launch_ulv_factor_fast<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, extra, st);
+        launch_ulv_factor_fast<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, extra, st);
       else
-        launch_ulv_factor<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
+        launch_ulv_factor<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
     });
   }
 }
 
 template <typename T>
-void run_solve(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
-  for (size_t h = 0; h < P->by_h.size(); ++h) {
-    const Seg& g = P->by_h[h];
+void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
+  for (size_t h = 0; h < L.by_h->size(); ++h) {
+    const Seg& g = (*L.by_h)[h];
     traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
       if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
-        launch_ulv_solve_up_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.mmax, g.sv_stage, rmax, st);
+        launch_ulv_solve_up_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.sv_stage, rmax, st);
       else
-        launch_ulv_solve_up<T>(P->d_tasks + g.off, g.cnt, slots, st);
+        launch_ulv_solve_up<T>(L.d_tasks + g.off, g.cnt, slots, st);
     });
   }
-  for (size_t d = 0; d < P->by_d.size(); ++d) {
-    const Seg& g = P->by_d[d];
+  for (size_t d = 0; d < L.by_d->size(); ++d) {
+    const Seg& g = (*L.by_d)[d];
     traced(HSS_TRACE_SOLVE_DOWN, g.cnt, st, [&] {
       if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
-        launch_ulv_solve_down_reg<T>(P->d_tasks + g.off, g.cnt, slots, g.nmax, g.mkmax, rmax, st);
+        launch_ulv_solve_down_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.nmax, g.mkmax, rmax, st);
       else
-        launch_ulv_solve_down<T>(P->d_tasks + g.off, g.cnt, slots, st);
+        launch_ulv_solve_down<T>(L.d_tasks + g.off, g.cnt, slots, st);
     });
   }
+}
+
+// Task lists merged over several single-tree plans, uploaded per call.
+struct MergedLevels {
+  std::vector<Seg> by_h, by_d, mv_up, mv_dn;
+  Seg leaves;
+  std::vector<Task> h;
+  DBuf<Task> d;
+  Levels view() const {
+    Levels L;
+    L.d_tasks = d.p;
+    L.by_h = &by_h;
+    L.by_d = &by_d;
+    L.mv_up = &mv_up;
+    L.mv_dn = &mv_dn;
+    L.leaves = leaves;
+    return L;
+  }
+};
+
+Seg merge_seg_dims(Seg a, const Seg& b) {
+  a.mmax = std::max(a.mmax, b.mmax); a.nmax = std::max(a.nmax, b.nmax);
+  a.kumax = std::max(a.kumax, b.kumax); a.kvmax = std::max(a.kvmax, b.kvmax);
+  a.c1u = std::max(a.c1u, b.c1u); a.c2u = std::max(a.c2u, b.c2u);
+  a.c1v = std::max(a.c1v, b.c1v); a.c2v = std::max(a.c2v, b.c2v);
+  a.kmax = std::max(a.kmax, b.kmax); a.mkmax = std::max(a.mkmax, b.mkmax);
+  a.c1mr = std::max(a.c1mr, b.c1mr); a.c2mr = std::max(a.c2mr, b.c2mr);
+  a.c1nr = std::max(a.c1nr, b.c1nr); a.c2nr = std::max(a.c2nr, b.c2nr);
+  a.sv_stage = std::max(a.sv_stage, b.sv_stage);
+  return a;
+}
+
+int merge_levels(const std::vector<hss_plan_s*>& plans, MergedLevels& M, cudaStream_t st) {
+  M.h.clear();
+  auto merge = [&](std::vector<Seg>& out, std::vector<Seg> hss_plan_s::*field) {
+    size_t nlev = 0;
+    for (auto* P : plans) nlev = std::max(nlev, (P->*field).size());
+    out.assign(nlev, Seg{});
+    for (size_t lv = 0; lv < nlev; ++lv) {
+      Seg g;
+      g.off = (int64_t)M.h.size();
+      for (size_t i = 0; i < plans.size(); ++i) {
+        const hss_plan_s* P = plans[i];
+        if (lv >= (P->*field).size()) continue;
+        const Seg& s = (P->*field)[lv];
+        for (int64_t t = 0; t < s.cnt; ++t) {
+          Task x = P->h_tasks[s.off + t];
+          x.slot = (int32_t)i;
+          M.h.push_back(x);
+        }
+        g = merge_seg_dims(g, s);
+      }
+      g.cnt = (int64_t)M.h.size() - g.off;
+      out[lv] = g;
+    }
+  };
+  merge(M.by_h, &hss_plan_s::by_h);
+  merge(M.by_d, &hss_plan_s::by_d);
+  merge(M.mv_up, &hss_plan_s::mv_up);
+  merge(M.mv_dn, &hss_plan_s::mv_dn);
+  M.leaves = Seg{};
+  M.leaves.off = (int64_t)M.h.size();
+  for (size_t i = 0; i < plans.size(); ++i) {
+    const hss_plan_s* P = plans[i];
+    for (int64_t t = 0; t < P->leaves.cnt; ++t) {
+      Task x = P->h_tasks[P->leaves.off + t];
+      x.slot = (int32_t)i;
+      M.h.push_back(x);
+    }
+  }
+  M.leaves.cnt = (int64_t)M.h.size() - M.leaves.off;
+  CUDA_TRY(M.d.ensure(std::max<size_t>(M.h.size(), 1)));
+  // pageable source: staged before the call returns; stream order protects
+  // the previous batch's reads of the same buffer
+  CUDA_TRY(cudaMemcpyAsync(M.d.p, M.h.data(), M.h.size() * sizeof(Task), cudaMemcpyHostToDevice, st));
+  return HSS_OK;
 }
 
 struct Cols {   // per-tree product / solve operands
@@ -659,47 +769,66 @@ int matmul_impl(hss_plan_s* P, const std::vector<Cols>& io, double alpha, double
   return HSS_OK;
 }
 
+// One factorization of a launch sequence: slot i of the sequence.
 template <typename T>
-int factor_impl(hss_factor_s* f, cudaStream_t st) {
-  hss_plan_s* P = f->plan;
-  std::vector<Slot> s(P->ntrees);
-  for (auto& x : s) {
+int factor_items(const std::vector<hss_factor_s*>& fs, const Levels& L, SlotTable& table, cudaStream_t st) {
+  std::vector<Slot> s(fs.size());
+  for (size_t i = 0; i < fs.size(); ++i) {
+    Slot& x = s[i];
     std::memset(&x, 0, sizeof(Slot));
-    x.fbase = f->d_fac;
-    x.err = P->d_err;
+    x.fbase = fs[i]->d_fac;
+    x.err = fs[i]->plan->d_err;
   }
-  CUDA_TRY(f->fac_slots.upload(s, st));
-  run_factor<T>(P, f->fac_slots.dev.p, st);
+  CUDA_TRY(table.upload(s, st));
+  run_factor<T>(L, table.dev.p, st);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
 
 template <typename T>
-int solve_pass(hss_factor_s* f, const std::vector<Cols>& io, const double* scale,
-               const int64_t* off, int mode, cudaStream_t st) {
-  const int64_t rtot = off[f->plan->ntrees];
-  SlotTable& table = mode ? f->sv_slots_ref : f->sv_slots;
+int factor_impl(hss_factor_s* f, cudaStream_t st) {
   hss_plan_s* P = f->plan;
+  std::vector<hss_factor_s*> fs(P->ntrees, f);   // every tree of a forest shares the storage
+  return factor_items<T>(fs, plan_levels(P), f->fac_slots, st);
+}
+
+// One solve operand set: tree `tree` of item.f's plan, slot i of the sequence.
+struct Item {
+  hss_factor_s* f;
+  int32_t tree;
+  Cols io;
+};
+
+template <typename T>
+int solve_pass(const std::vector<Item>& items, const Levels& L, const double* scale, const int64_t* off,
+               int64_t rtot, int mode, bool residual_input, const int64_t* roff, double* R, SlotTable& table,
+               cudaStream_t st) {
   int64_t rmax = 0;
-  for (auto& c : io) rmax = std::max(rmax, c.r);
+  for (auto& it : items) rmax = std::max(rmax, it.io.r);
   if (rmax == 0) return HSS_OK;
-  CUDA_TRY(f->sv_ws.ensure((size_t)P->ws_sv * rmax * sizeof(T)));
-  std::vector<Slot> s(P->ntrees);
-  for (int32_t t = 0; t < P->ntrees; ++t) {
-    Slot& x = s[t];
+  std::vector<Slot> s(items.size());
+  for (size_t i = 0; i < items.size(); ++i) {
+    const Item& it = items[i];
+    hss_plan_s* P = it.f->plan;
+    CUDA_TRY(it.f->sv_ws.ensure((size_t)P->ws_sv * rmax * sizeof(T)));
+    Slot& x = s[i];
     std::memset(&x, 0, sizeof(Slot));
-    x.B = io[t].B; x.ldb = io[t].ldb;
-    x.C = io[t].C; x.ldc = io[t].ldc;
-    x.ws = f->sv_ws.p; x.ldws = P->ws_sv;
-    x.fbase = f->d_fac;
-    x.colscale = scale ? scale + off[t] : nullptr;
-    x.colinv = scale ? scale + rtot + off[t] : nullptr;
-    x.r = (int32_t)io[t].r;
+    if (residual_input) {
+      x.B = R + roff[i]; x.ldb = P->tree_m[it.tree];
+    } else {
+      x.B = it.io.B; x.ldb = it.io.ldb;
+    }
+    x.C = it.io.C; x.ldc = it.io.ldc;
+    x.ws = it.f->sv_ws.p; x.ldws = P->ws_sv;
+    x.fbase = it.f->d_fac;
+    x.colscale = scale ? scale + off[i] : nullptr;
+    x.colinv = scale ? scale + rtot + off[i] : nullptr;
+    x.r = (int32_t)it.io.r;
     x.mode = mode;
     x.err = P->d_err;
   }
   CUDA_TRY(table.upload(s, st));
-  run_solve<T>(P, table.dev.p, (int)rmax, st);
+  run_solve<T>(L, table.dev.p, (int)rmax, st);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -715,135 +844,146 @@ int read_dev_err(hss_plan_s* P, cudaStream_t st) {
   return HSS_OK;
 }
 
+// Solve every item, then refine (FP32 factors, or FP64 with tol > 0) until the
+// largest relative residual over all columns of all items is <= tol.
+int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, double tol, int32_t maxit,
+                hss_solve_stats* stats, cudaStream_t st) {
+  if (items.empty()) return HSS_OK;
+  const int prec = items[0].f->prec;
+  for (auto& it : items)
+    if (it.f->prec != prec) return fail(HSS_ERR_INVALID, "a batched solve needs factorizations of one precision");
+  const bool fp32 = prec == HSS_PREC_FP32;
+  // tol < 0: a single solve in the factor's precision, no residual
+  const bool refine = tol >= 0.0 && (fp32 || tol > 0.0);
+  if (stats) { stats->iterations = 0; stats->converged = refine ? 0 : 1; stats->residual = -1.0; }
+  const size_t ni = items.size();
+  std::vector<int64_t> off(ni + 1, 0), roff(ni + 1, 0), xoff(ni + 1, 0);
+  for (size_t i = 0; i < ni; ++i) {
+    hss_plan_s* P = items[i].f->plan;
+    off[i + 1] = off[i] + items[i].io.r;
+    roff[i + 1] = roff[i] + items[i].io.r * P->tree_m[items[i].tree];
+    xoff[i + 1] = xoff[i] + items[i].io.r * P->tree_n[items[i].tree];
+  }
+  const int64_t rtot = off[ni];
+  if (rtot == 0) { if (stats) stats->converged = 1; return HSS_OK; }
+  int64_t rmax = 0;
+  for (auto& it : items) rmax = std::max(rmax, it.io.r);
+  const double* scale = nullptr;
+  if (refine) {
+    CUDA_TRY(B.bn2.ensure(rtot));
+    CUDA_TRY(B.rn2.ensure(rtot));
+    CUDA_TRY(B.scale.ensure(2 * rtot));
+    CUDA_TRY(B.R.ensure(std::max<int64_t>(roff[ni], 1)));
+    CUDA_TRY(B.h_bn2.ensure(rtot));
+    CUDA_TRY(B.h_rn2.ensure(rtot));
+    CUDA_TRY(cudaMemsetAsync(B.bn2.p, 0, rtot * sizeof(double), st));
+    for (size_t i = 0; i < ni; ++i) {
+      const Item& it = items[i];
+      launch_colnorm2(it.io.B, it.io.ldb, it.f->plan->tree_m[it.tree], it.io.r, B.bn2.p + off[i], st);
+      ++g_launches;
+    }
+    if (fp32) {
+      launch_sqrt_scale(B.bn2.p, B.scale.p, rtot, st);
+      ++g_launches;
+      scale = B.scale.p;
+    }
+    CUDA_TRY(cudaMemcpyAsync(B.h_bn2.p, B.bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  int rc = fp32 ? solve_pass<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st)
+                : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st);
+  if (rc) return rc;
+  if (!refine) return HSS_OK;
+  // refinement: R = b - A x (double-float product for FP32 factors unless
+  // the FP64 product is forced), x += A_f^{-1} R
+  bool dfres = fp32 && !g_residual_fp64;
+  for (auto& it : items) dfres = dfres && it.f->plan->d_gen_df != nullptr;
+  if (dfres) {
+    CUDA_TRY(B.xs.ensure(std::max<int64_t>(xoff[ni], 1)));
+    CUDA_TRY(B.tmp.ensure(std::max<int64_t>(roff[ni], 1)));
+  }
+  std::vector<Slot> ms(ni);
+  for (size_t i = 0; i < ni; ++i) {
+    const Item& it = items[i];
+    hss_plan_s* P = it.f->plan;
+    Slot& x = ms[i];
+    std::memset(&x, 0, sizeof(Slot));
+    x.B = it.io.C; x.ldb = it.io.ldc;                  // current solution
+    x.C = B.R.p + roff[i]; x.ldc = P->tree_m[it.tree]; // residual
+    x.Y = it.io.B; x.ldy = it.io.ldb;                  // right-hand side
+    x.alpha = -1.0; x.beta = 1.0;
+    x.r = (int32_t)it.io.r;
+    x.colnorm2 = B.rn2.p + off[i];
+    x.err = P->d_err;
+    if (dfres) {
+      CUDA_TRY(it.f->ws2.ensure((size_t)P->ws_mv * rmax));
+      x.xs = B.xs.p + xoff[i];
+      x.ldx2 = P->tree_n[it.tree];
+      x.tmp = B.tmp.p + roff[i];
+      x.ldt2 = P->tree_m[it.tree];
+      x.ws2 = it.f->ws2.p;
+      x.ldws = P->ws_mv;
+      x.gdf = P->d_gen_df;
+      x.gbase = P->d_gen;
+    } else {
+      CUDA_TRY(P->mv_ws.ensure((size_t)P->ws_mv * rmax));
+      x.ws = P->mv_ws.p;
+      x.ldws = P->ws_mv;
+    }
+  }
+  double res = 0.0;
+  for (int32_t iter = 0;; ++iter) {
+    CUDA_TRY(cudaMemsetAsync(B.rn2.p, 0, rtot * sizeof(double), st));
+    if (dfres)
+      for (size_t i = 0; i < ni; ++i) {
+        const Item& it = items[i];
+        launch_df_split_cols(it.io.C, it.io.ldc, it.f->plan->tree_n[it.tree], it.io.r, B.xs.p + xoff[i], st);
+        ++g_launches;
+      }
+    CUDA_TRY(B.mv.upload(ms, st));
+    if (dfres) run_matvec_df(L, B.mv.dev.p, (int)rmax, st);
+    else run_matvec(L, B.mv.dev.p, (int)rmax, st);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(B.h_rn2.p, B.rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    res = 0.0;
+    for (int64_t j = 0; j < rtot; ++j) {
+      const double bn = std::sqrt(B.h_bn2.p[j]);
+      const double rn = std::sqrt(B.h_rn2.p[j]);
+      const double rel = bn > 0.0 ? rn / bn : rn;
+      if (!(rel <= res)) res = rel;   // NaN propagates
+    }
+    if (stats) { stats->iterations = iter; stats->residual = res; }
+    if (res <= tol) {
+      if (stats) stats->converged = 1;
+      for (auto& it : items) {
+        rc = read_dev_err(it.f->plan, st);
+        if (rc) return rc;
+      }
+      return HSS_OK;
+    }
+    if (iter >= maxit || std::isnan(res)) break;
+    launch_sqrt_scale(B.rn2.p, B.scale.p, rtot, st);
+    ++g_launches;
+    rc = fp32 ? solve_pass<float>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st)
+              : solve_pass<double>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st);
+    if (rc) return rc;
+  }
+  for (auto& it : items) {
+    rc = read_dev_err(it.f->plan, st);
+    if (rc) return rc;
+  }
+  return fail(HSS_ERR_NO_CONVERGENCE, "iterative refinement did not reach the tolerance (residual " +
+                                          std::to_string(res) + ")");
+}
+
 int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t maxit,
                hss_solve_stats* stats, cudaStream_t st) {
   hss_plan_s* P = f->plan;
   int rc = check_cols(P, io, true);
   if (rc) return rc;
-  const bool fp32 = f->prec == HSS_PREC_FP32;
-  // tol < 0: a single solve in the factor's precision, no residual
-  const bool refine = tol >= 0.0 && (fp32 || tol > 0.0);
-  if (stats) { stats->iterations = 0; stats->converged = refine ? 0 : 1; stats->residual = -1.0; }
-  std::vector<int64_t> off(P->ntrees + 1, 0), roff(P->ntrees + 1, 0);
-  for (int32_t t = 0; t < P->ntrees; ++t) {
-    off[t + 1] = off[t] + io[t].r;
-    roff[t + 1] = roff[t] + io[t].r * P->tree_m[t];
-  }
-  const int64_t rtot = off[P->ntrees];
-  if (rtot == 0) { if (stats) stats->converged = 1; return HSS_OK; }
-  const double* scale = nullptr;
-  if (refine) {
-    CUDA_TRY(f->bn2.ensure(rtot));
-    CUDA_TRY(f->rn2.ensure(rtot));
-    CUDA_TRY(f->scale.ensure(2 * rtot));
-    CUDA_TRY(f->R.ensure(std::max<int64_t>(roff[P->ntrees], 1)));
-    CUDA_TRY(f->h_bn2.ensure(rtot));
-    CUDA_TRY(f->h_rn2.ensure(rtot));
-    CUDA_TRY(cudaMemsetAsync(f->bn2.p, 0, rtot * sizeof(double), st));
-    for (int32_t t = 0; t < P->ntrees; ++t) {
-      launch_colnorm2(io[t].B, io[t].ldb, P->tree_m[t], io[t].r, f->bn2.p + off[t], st);
-      ++g_launches;
-    }
-    if (fp32) {
-      launch_sqrt_scale(f->bn2.p, f->scale.p, rtot, st);
-      ++g_launches;
-      scale = f->scale.p;
-    }
-    CUDA_TRY(cudaMemcpyAsync(f->h_bn2.p, f->bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
-  }
-  rc = fp32 ? solve_pass<float>(f, io, scale, off.data(), 0, st)
-            : solve_pass<double>(f, io, scale, off.data(), 0, st);
-  if (rc) return rc;
-  if (!refine) return HSS_OK;
-  // iterative refinement: r = b - A x (FP64 HSS product), x += A_f^{-1} r
-  std::vector<Cols> rio(P->ntrees), xin(P->ntrees);
-  std::vector<const double*> Y(P->ntrees);
-  for (int32_t t = 0; t < P->ntrees; ++t) {
-    xin[t] = Cols{io[t].C, io[t].ldc, io[t].r, f->R.p + roff[t], P->tree_m[t]};
-    rio[t] = Cols{f->R.p + roff[t], P->tree_m[t], io[t].r, io[t].C, io[t].ldc};
-    Y[t] = io[t].B;
-  }
-  // the product's beta term reads B with B's leading dimension
-  std::vector<Cols> mvio(P->ntrees);
-  for (int32_t t = 0; t < P->ntrees; ++t) mvio[t] = xin[t];
-  double res = 0.0;
-  for (int32_t it = 0;; ++it) {
-    CUDA_TRY(cudaMemsetAsync(f->rn2.p, 0, rtot * sizeof(double), st));
-    {
-      // R = -A x + B: double-float product on the FP32 pipe (FP32 factor), or
-      // the native FP64 product
-      const bool dfres = fp32 && !g_residual_fp64 && P->d_gen_df != nullptr;
-      int64_t rmax = 0;
-      for (auto& c : mvio) rmax = std::max(rmax, c.r);
-      std::vector<int64_t> xoff(P->ntrees + 1, 0), toff(P->ntrees + 1, 0);
-      for (int32_t t = 0; t < P->ntrees; ++t) {
-        xoff[t + 1] = xoff[t] + P->tree_n[t] * mvio[t].r;
-        toff[t + 1] = toff[t] + P->tree_m[t] * mvio[t].r;
-      }
-      if (dfres) {
-        CUDA_TRY(f->xs.ensure(std::max<int64_t>(xoff[P->ntrees], 1)));
-        CUDA_TRY(f->tmp.ensure(std::max<int64_t>(toff[P->ntrees], 1)));
-        CUDA_TRY(f->ws2.ensure((size_t)P->ws_mv * rmax));
-        for (int32_t t = 0; t < P->ntrees; ++t) {
-          launch_df_split_cols(mvio[t].B, mvio[t].ldb, P->tree_n[t], mvio[t].r, f->xs.p + xoff[t], st);
-          ++g_launches;
-        }
-      } else {
-        CUDA_TRY(P->mv_ws.ensure((size_t)P->ws_mv * rmax));
-      }
-      std::vector<Slot> s(P->ntrees);
-      for (int32_t t = 0; t < P->ntrees; ++t) {
-        Slot& x = s[t];
-        std::memset(&x, 0, sizeof(Slot));
-        x.B = mvio[t].B; x.ldb = mvio[t].ldb;
-        x.C = mvio[t].C; x.ldc = mvio[t].ldc;
-        x.Y = io[t].B; x.ldy = io[t].ldb;
-        x.alpha = -1.0; x.beta = 1.0;
-        x.ws = P->mv_ws.p; x.ldws = P->ws_mv;
-        x.r = (int32_t)mvio[t].r;
-        x.colnorm2 = f->rn2.p + off[t];
-        x.err = P->d_err;
-        if (dfres) {
-          // per-tree pair buffers (row0/col0 are tree-local)
-          x.xs = f->xs.p + xoff[t];
-          x.ldx2 = P->tree_n[t];
-          x.tmp = f->tmp.p + toff[t];
-          x.ldt2 = P->tree_m[t];
-          x.ws2 = f->ws2.p;
-          x.gdf = P->d_gen_df;
-          x.gbase = P->d_gen;
-        }
-      }
-      CUDA_TRY(f->mv_slots.upload(s, st));
-      if (dfres) run_matvec_df(P, f->mv_slots.dev.p, (int)rmax, st);
-      else run_matvec(P, f->mv_slots.dev.p, (int)rmax, st);
-      CUDA_TRY(cudaGetLastError());
-    }
-    CUDA_TRY(cudaMemcpyAsync(f->h_rn2.p, f->rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    res = 0.0;
-    for (int64_t j = 0; j < rtot; ++j) {
-      const double bn = std::sqrt(f->h_bn2.p[j]);
-      const double rn = std::sqrt(f->h_rn2.p[j]);
-      const double rel = bn > 0.0 ? rn / bn : rn;
-      if (!(rel <= res)) res = rel;   // NaN propagates
-    }
-    if (stats) { stats->iterations = it; stats->residual = res; }
-    if (res <= tol) {
-      if (stats) stats->converged = 1;
-      return read_dev_err(P, st);
-    }
-    if (it >= maxit || std::isnan(res)) break;
-    launch_sqrt_scale(f->rn2.p, f->scale.p, rtot, st);
-    ++g_launches;
-    rc = fp32 ? solve_pass<float>(f, rio, f->scale.p, off.data(), 1, st)
-              : solve_pass<double>(f, rio, f->scale.p, off.data(), 1, st);
-    if (rc) return rc;
-  }
-  rc = read_dev_err(P, st);
-  if (rc) return rc;
-  return fail(HSS_ERR_NO_CONVERGENCE, "iterative refinement did not reach the tolerance (residual " +
-                                          std::to_string(res) + ")");
+  std::vector<Item> items;
+  for (int32_t t = 0; t < P->ntrees; ++t) items.push_back(Item{f, t, io[t]});
+  return solve_items(items, plan_levels(P), f->bufs, tol, maxit, stats, st);
 }
 
 int copy_in(DBuf<double>& d, const double* h, int64_t rows, int64_t ld, int64_t r, cudaStream_t st) {
@@ -858,6 +998,27 @@ int copy_out(double* h, int64_t ld, const double* d, int64_t rows, int64_t r, cu
   if (rows * r > 0)
     CUDA_TRY(cudaMemcpy2DAsync(h, ld * sizeof(double), d, rows * sizeof(double), rows * sizeof(double), r,
                                cudaMemcpyDeviceToHost, st));
+  return HSS_OK;
+}
+
+}  // namespace
+
+// A reusable executor for batches over several independently created plans
+// (the serving form): merged task lists and per-call buffers.
+struct hss_batcher_s {
+  MergedLevels M;
+  std::vector<hss_plan_s*> last;   // plans of the merged lists on the device
+  SolveBufs bufs;
+  SlotTable fac_slots;
+};
+
+namespace {
+
+int batcher_levels(hss_batcher_s* b, const std::vector<hss_plan_s*>& plans, cudaStream_t st) {
+  if (plans == b->last && b->M.d.p) return HSS_OK;
+  int rc = merge_levels(plans, b->M, st);
+  if (rc) return rc;
+  b->last = plans;
   return HSS_OK;
 }
 
@@ -1175,6 +1336,76 @@ int hss_ulvfactsolve_host(hss_handle h, int32_t precision, const double* B, int6
   else rc = hss_ulvrefactor(f, nullptr);
   if (rc) return rc;
   return hss_ulvsolve_host(f, B, ldb, r, X, ldx, tol, maxit, stats);
+}
+
+int hss_batcher_create(hss_batcher* out) {
+  if (!out) return fail(HSS_ERR_INVALID, "null output");
+  *out = new hss_batcher_s();
+  return HSS_OK;
+}
+
+int hss_batcher_destroy(hss_batcher b) {
+  delete b;
+  return HSS_OK;
+}
+
+int hss_batcher_factor(hss_batcher b, int32_t count, const hss_handle* hs, int32_t precision, hss_factor* out,
+                       void* stream) {
+  if (!b || !hs || !out || count <= 0) return fail(HSS_ERR_INVALID, "bad batch arguments");
+  if (precision != HSS_PREC_FP64 && precision != HSS_PREC_FP32)
+    return fail(HSS_ERR_INVALID, "precision must be HSS_PREC_FP64 or HSS_PREC_FP32");
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<hss_plan_s*> plans(count);
+  std::vector<hss_factor_s*> fs(count, nullptr);
+  for (int32_t i = 0; i < count; ++i) {
+    out[i] = nullptr;
+    if (!hs[i] || hs[i]->ntrees != 1) return fail(HSS_ERR_INVALID, "batched factorization takes single-tree plans");
+    plans[i] = hs[i];
+  }
+  int rc = HSS_OK;
+  const size_t es = precision == HSS_PREC_FP32 ? sizeof(float) : sizeof(double);
+  for (int32_t i = 0; i < count && !rc; ++i) {
+    auto* f = new hss_factor_s();
+    f->plan = plans[i];
+    f->prec = precision;
+    f->fac_bytes = (size_t)plans[i]->fac_elems * es;
+    cudaError_t e = cudaMalloc(&f->d_fac, f->fac_bytes);
+    if (e != cudaSuccess) { delete f; rc = cuda_fail(e, "cudaMalloc(factor)"); break; }
+    fs[i] = f;
+    if (precision == HSS_PREC_FP32) rc = ensure_df(plans[i], st);
+  }
+  if (!rc) rc = batcher_levels(b, plans, st);
+  if (!rc)
+    rc = precision == HSS_PREC_FP32 ? factor_items<float>(fs, b->M.view(), b->fac_slots, st)
+                                    : factor_items<double>(fs, b->M.view(), b->fac_slots, st);
+  if (rc) {
+    for (auto* f : fs) delete f;
+    return rc;
+  }
+  for (int32_t i = 0; i < count; ++i) out[i] = fs[i];
+  return HSS_OK;
+}
+
+int hss_batcher_solve(hss_batcher b, int32_t count, const hss_factor* fs, const double* const* dB,
+                      const int64_t* ldb, const int64_t* r, double* const* dX, const int64_t* ldx, double tol,
+                      int32_t maxit, hss_solve_stats* stats, void* stream) {
+  if (!b || !fs || !dB || !ldb || !r || !dX || !ldx || count <= 0) return fail(HSS_ERR_INVALID, "bad batch arguments");
+  std::vector<hss_plan_s*> plans(count);
+  std::vector<Item> items(count);
+  for (int32_t i = 0; i < count; ++i) {
+    if (!fs[i] || fs[i]->plan->ntrees != 1) return fail(HSS_ERR_INVALID, "batched solve takes single-tree factors");
+    for (int32_t j = 0; j < i; ++j)
+      if (fs[j] == fs[i])
+        return fail(HSS_ERR_INVALID, "a factorization appears twice in one batch: join its right-hand sides");
+    plans[i] = fs[i]->plan;
+    items[i] = Item{fs[i], 0, Cols{dB[i], ldb[i], r[i], dX[i], ldx[i]}};
+    int rc = check_cols(plans[i], {items[i].io}, true);
+    if (rc) return rc;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = batcher_levels(b, plans, st);
+  if (rc) return rc;
+  return solve_items(items, b->M.view(), b->bufs, tol, maxit, stats, st);
 }
 
 }  // extern "C"

@@ -19,7 +19,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import check, dptr, iptr
-from .packing import pack
+from .packing import pack, pack_cached
 
 PREC = {"fp64": _lib.HSS_PREC_FP64, "fp32": _lib.HSS_PREC_FP32,
         _lib.HSS_PREC_FP64: _lib.HSS_PREC_FP64, _lib.HSS_PREC_FP32: _lib.HSS_PREC_FP32}
@@ -63,7 +63,7 @@ class DeviceHss:
         if _handle is not None:
             self.handle = _handle
         else:
-            table, packed = pack(h)
+            table, packed = pack_cached(h)
             check(self.lib.hss_create(table.shape[0], iptr(table), dptr(packed), packed.size,
                                       C.byref(self.handle)))
         n = C.c_int32()

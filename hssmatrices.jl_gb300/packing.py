@@ -88,3 +88,15 @@ def pack(h):
                 table[i, 14] = put(x.W2)
     packed = np.concatenate(chunks) if chunks else np.zeros(0)
     return np.ascontiguousarray(table), np.ascontiguousarray(packed)
+
+
+def pack_cached(h):
+    """``pack`` once per tree object (the serving loop uploads the same matrices again)."""
+    cached = getattr(h, "_packed", None)
+    if cached is None:
+        cached = pack(h)
+        try:
+            h._packed = cached
+        except AttributeError:
+            pass
+    return cached

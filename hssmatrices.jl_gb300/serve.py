@@ -1,0 +1,318 @@
+"""Serving form: a request loop with resident factorizations and continuous batching.
+
+Requests are either *factor* requests (a new HSS matrix: upload its generators,
+factorize, keep the factorization resident) or *solve* requests (right-hand
+sides against a resident factorization).  ``HssServer.step()`` takes every
+request that has arrived, admits factor requests while the HBM budget allows
+(evicting least-recently-used factorizations that no queued request needs),
+factorizes all admitted matrices in one batched launch sequence
+(``hss_batcher_factor``), joins the right-hand sides of all solve requests per
+matrix and solves every matrix of the batch in one launch sequence per tree
+level with FP64-accurate refinement (``hss_batcher_solve``).  Requests that
+arrive while a batch runs join the next one.  Results of a request are the
+same alone and in any mix: every matrix of a batch is an independent slot of
+the same kernels (the refinement of a batch stops when all its columns meet
+the tolerance, so a column may get an extra correction).
+
+There is no CPU path: every step runs the CUDA library.
+"""
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .linalg import DeviceHss, PREC, _stream
+
+
+class Batcher:
+    """Owner of an ``hss_batcher`` (merged task lists + buffers), one per stream."""
+
+    def __init__(self):
+        self.lib = _lib.load()
+        self.handle = C.c_void_p()
+        check(self.lib.hss_batcher_create(C.byref(self.handle)))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.lib.hss_batcher_destroy(self.handle)
+                self.handle = C.c_void_p()
+        except Exception:
+            pass
+
+    def factor(self, devs, precision="fp32", stream=None):
+        """Factorize several single-matrix plans in one launch sequence; returns factor handles."""
+        k = len(devs)
+        hs = (C.c_void_p * k)(*[d.handle for d in devs])
+        out = (C.c_void_p * k)()
+        check(self.lib.hss_batcher_factor(self.handle, k, hs, PREC[precision], out, _stream(stream)))
+        return [ResidentFactor(self.lib, C.c_void_p(out[i]), PREC[precision]) for i in range(k)]
+
+    def solve(self, factors, dBs, dXs, rows, rs, tol=1e-10, maxit=20, stream=None):
+        """Solve factors[i] against dBs[i] (rows[i] x rs[i], column-major device buffers)."""
+        k = len(factors)
+        fs = (C.c_void_p * k)(*[f.handle for f in factors])
+        B = (C.c_void_p * k)(*[_ptr(x) for x in dBs])
+        X = (C.c_void_p * k)(*[_ptr(x) for x in dXs])
+        ld = np.asarray(rows, dtype=np.int64)
+        r = np.asarray(rs, dtype=np.int64)
+        st = _lib.SolveStats()
+        check(self.lib.hss_batcher_solve(self.handle, k, fs, B, _lib.iptr(ld), _lib.iptr(r), X, _lib.iptr(ld),
+                                         float(tol), int(maxit), C.byref(st), _stream(stream)))
+        return st
+
+
+def _ptr(x):
+    return x if isinstance(x, int) else x.data_ptr()
+
+
+class ResidentFactor:
+    def __init__(self, lib, handle, prec):
+        self.lib = lib
+        self.handle = handle
+        self.prec = prec
+
+    def nbytes(self):
+        b = C.c_int64()
+        check(self.lib.hss_factor_bytes(self.handle, C.byref(b)))
+        return b.value
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.lib.hss_factor_destroy(self.handle)
+                self.handle = C.c_void_p()
+        except Exception:
+            pass
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str                      # "factor" or "solve"
+    arrival: float                 # seconds on the server's clock
+    matrix: int                    # matrix id
+    hss: object = None             # factor: the HssMatrix (host generators)
+    rhs: object = None             # solve: torch tensor r x n (column-major n x r)
+    done: Optional[float] = None
+    out: object = None
+    batch: int = -1
+    nbytes: int = 0
+
+
+@dataclass
+class Resident:
+    dev: DeviceHss
+    factor: ResidentFactor
+    nbytes: int
+    n: int
+    last_use: float = 0.0
+
+
+class HssServer:
+    """Continuous-batching HSS factor/solve server on one GPU."""
+
+    def __init__(self, budget_bytes=150 * 10**9, precision="fp32", tol=1e-10, maxit=20,
+                 max_factor_batch=32, stream=None):
+        import torch
+        self.torch = torch
+        self.budget = int(budget_bytes)
+        self.precision = precision
+        self.tol = tol
+        self.maxit = maxit
+        self.max_factor_batch = max_factor_batch
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        self.batcher = Batcher()
+        self.resident: "collections.OrderedDict[int, Resident]" = collections.OrderedDict()
+        self.pending_factor: "collections.deque[Request]" = collections.deque()
+        self.pending_solve: "list[Request]" = []
+        self.used = 0
+        self.batches = 0
+        self.evictions = 0
+        self.reloads = 0
+        self.matrices = {}             # matrix id -> host HssMatrix (re-admission after eviction)
+
+    # -- accounting --------------------------------------------------------
+    @staticmethod
+    def estimate_bytes(hss, precision):
+        """Generators (+ their FP32-pair copy) + factor storage + workspaces, from the sizes."""
+        from .packing import pack_cached
+        _table, packed = pack_cached(hss)
+        gen = packed.size * 8
+        m = hss.size()[0]
+        fac_elems = 2 * packed.size + 8 * m     # factor blocks, reflector copies, tau vectors
+        item = 4 if precision == "fp32" else 8
+        extra = gen if precision == "fp32" else 0
+        return gen + extra + fac_elems * item + 64 * m * 8
+
+    def _evict_for(self, need, keep):
+        while self.used + need > self.budget:
+            victim = None
+            for mid, res in self.resident.items():    # least recently used first
+                if mid not in keep:
+                    victim = mid
+                    break
+            if victim is None:
+                return False
+            res = self.resident.pop(victim)
+            self.used -= res.nbytes
+            self.evictions += 1
+        return True
+
+    # -- request intake ------------------------------------------------------
+    def submit(self, req: Request):
+        if req.kind == "factor":
+            self.matrices[req.matrix] = req.hss
+            self.pending_factor.append(req)
+        else:
+            self.pending_solve.append(req)
+
+    # -- one batch -----------------------------------------------------------
+    def step(self, now_fn):
+        """Run one batch of factor and solve work; returns the completed requests."""
+        torch = self.torch
+        completed = []
+        keep = {r.matrix for r in self.pending_solve}
+        # a matrix evicted while solves for it were still to come is loaded again
+        queued = {r.matrix for r in self.pending_factor}
+        for mid in keep:
+            if mid not in self.resident and mid not in queued and mid in self.matrices:
+                self.pending_factor.appendleft(Request(-1, "factor", now_fn(), mid, hss=self.matrices[mid]))
+                queued.add(mid)
+                self.reloads += 1
+        admitted = []
+        while self.pending_factor and len(admitted) < self.max_factor_batch:
+            req = self.pending_factor[0]
+            need = self.estimate_bytes(req.hss, self.precision)
+            if need > self.budget:
+                raise MemoryError(f"matrix {req.matrix} needs {need} bytes, above the budget {self.budget}")
+            if not self._evict_for(need, keep | {r.matrix for r in admitted}):
+                break
+            self.pending_factor.popleft()
+            self.used += need
+            req.nbytes = need
+            admitted.append(req)
+        if admitted:
+            devs = [DeviceHss(r.hss) for r in admitted]
+            factors = self.batcher.factor(devs, self.precision, stream=self.stream)
+            for r, d, f in zip(admitted, devs, factors):
+                self.resident[r.matrix] = Resident(d, f, r.nbytes, d.n, now_fn())
+                self.resident.move_to_end(r.matrix)
+        # solves: every request whose matrix is resident, joined per matrix
+        ready = [r for r in self.pending_solve if r.matrix in self.resident]
+        if ready:
+            self.pending_solve = [r for r in self.pending_solve if r.matrix not in self.resident]
+            groups = collections.OrderedDict()
+            for r in ready:
+                groups.setdefault(r.matrix, []).append(r)
+            facs, dBs, dXs, rows, rs = [], [], [], [], []
+            for mid, reqs in groups.items():
+                res = self.resident[mid]
+                res.last_use = now_fn()
+                self.resident.move_to_end(mid)
+                B = torch.cat([q.rhs for q in reqs], dim=0) if len(reqs) > 1 else reqs[0].rhs
+                X = torch.empty_like(B)
+                facs.append(res.factor)
+                dBs.append(B)
+                dXs.append(X)
+                rows.append(res.n)
+                rs.append(B.shape[0])
+            self.batcher.solve(facs, dBs, dXs, rows, rs, tol=self.tol, maxit=self.maxit, stream=self.stream)
+            self.stream.synchronize()
+            t = now_fn()
+            for (mid, reqs), X in zip(groups.items(), dXs):
+                c0 = 0
+                for q in reqs:
+                    q.out = X[c0:c0 + q.rhs.shape[0]]
+                    c0 += q.rhs.shape[0]
+                    q.done = t
+                    q.batch = self.batches
+                    completed.append(q)
+        if admitted:
+            self.stream.synchronize()
+            t = now_fn()
+            for r in admitted:
+                if r.rid < 0:
+                    continue   # internal re-admission
+                r.done = t
+                r.batch = self.batches
+                completed.append(r)
+        self.batches += 1
+        return completed
+
+    def idle(self):
+        return not self.pending_factor and not self.pending_solve
+
+
+def run_stream(server, requests, time_scale=1.0, poll=0.0):
+    """Replay requests (sorted by arrival, seconds) in real time against ``server``;
+    returns the completed requests with arrival/done on one clock."""
+    t0 = time.perf_counter()
+
+    def now():
+        return (time.perf_counter() - t0) / time_scale
+
+    i = 0
+    out = []
+    n = len(requests)
+    while len(out) < n:
+        t = now()
+        while i < n and requests[i].arrival <= t:
+            server.submit(requests[i])
+            i += 1
+        if server.idle():
+            if i < n:
+                wait = (requests[i].arrival - now()) * time_scale
+                if wait > 0:
+                    time.sleep(min(wait, 0.001))
+            continue
+        done = server.step(now)
+        out.extend(done)
+        if poll:
+            time.sleep(poll)
+    return out
+
+
+def synthetic_requests(n_requests=10000, seed=3, rate=2000.0, factor_frac=0.2, n_range=(2048, 65536),
+                       k_range=(16, 48), leafsize=128, r_range=(1, 32), pool_size=32, recent=16,
+                       device="cuda"):
+    """The serving workload: Poisson arrivals at `rate` per second; `factor_frac` are
+    factor requests for a new matrix (n log-uniform in n_range, rank uniform in
+    k_range, `leafsize`), the rest solve requests with r uniform in r_range against
+    one of the `recent` most recently factored matrices.  Matrices come from a
+    seeded pool of `pool_size` synthetic trees (each factor request gets a new
+    matrix id and uploads its pool entry); right-hand sides are N(0,1) on the device.
+    The first request is a factor request."""
+    import torch
+    from .synthetic import synthetic_hss
+    rng = np.random.default_rng(seed)
+    pool = []
+    for _ in range(pool_size):
+        n = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
+        k = int(rng.integers(k_range[0], k_range[1] + 1))
+        pool.append(synthetic_hss(n, leafsize, k, rng))
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    t = 0.0
+    reqs = []
+    factored = []
+    for i in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        if i == 0 or rng.random() < factor_frac:
+            mid = len(factored)
+            h = pool[mid % pool_size]
+            factored.append((mid, h.size()[0]))
+            reqs.append(Request(i, "factor", t, mid, hss=h))
+        else:
+            mid, n = factored[-1 - int(rng.integers(0, min(recent, len(factored))))]
+            r = int(rng.integers(r_range[0], r_range[1] + 1))
+            rhs = torch.randn((r, n), dtype=torch.float64, device=device, generator=gen)
+            reqs.append(Request(i, "solve", t, mid, rhs=rhs))
+    return reqs, pool

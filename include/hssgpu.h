@@ -162,6 +162,22 @@ int hss_ulvfactsolve_host(hss_handle h, int32_t precision, const double* B, int6
                           int64_t r, double* X, int64_t ldx, double tol, int32_t maxit,
                           hss_solve_stats* stats);
 
+/* Batches over independently created single-tree plans (the serving form):
+ * one launch per tree level covers every matrix of the batch.  A batcher owns
+ * the merged task lists and per-call buffers; use one batcher per stream. */
+typedef struct hss_batcher_s* hss_batcher;
+int hss_batcher_create(hss_batcher* out);
+int hss_batcher_destroy(hss_batcher b);
+/* Factor `count` plans in one set of launches; out[i] receives a new
+ * factorization of hs[i] (release with hss_factor_destroy). */
+int hss_batcher_factor(hss_batcher b, int32_t count, const hss_handle* hs, int32_t precision,
+                       hss_factor* out, void* stream);
+/* Solve (and refine, as hss_ulvsolve) distinct factorizations fs[i] of one
+ * precision with right-hand sides dB[i] (r[i] columns) into dX[i]. */
+int hss_batcher_solve(hss_batcher b, int32_t count, const hss_factor* fs, const double* const* dB,
+                      const int64_t* ldb, const int64_t* r, double* const* dX, const int64_t* ldx,
+                      double tol, int32_t maxit, hss_solve_stats* stats, void* stream);
+
 /* Device memory held by a factorization (bytes). */
 int hss_factor_bytes(hss_factor f, int64_t* bytes);
 
