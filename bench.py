@@ -51,6 +51,12 @@ def parse():
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--roofline-kernel", default="factor_leaf")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch"])
+    p.add_argument("--requests", type=int, default=10000)
+    p.add_argument("--rate", type=float, default=1000.0)
+    p.add_argument("--pool", type=int, default=32)
+    p.add_argument("--budget-gb", type=float, default=150.0)
+    p.add_argument("--matrices", type=int, default=256)
     return p.parse_args()
 
 
@@ -359,6 +365,163 @@ def run_ours(args, rank, world, local_rank):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# serving workload (Poisson request stream) and batched workload
+# ---------------------------------------------------------------------------
+
+
+def _pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))]
+
+
+def run_serve(args):
+    """Serving: Poisson stream of factor (20%) and solve (80%) requests; the
+    continuous-batching FP32+refinement server vs plain FP64 one at a time."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    from hssmatrices_gb300 import serve
+    reqs, pool = serve.synthetic_requests(n_requests=args.requests, seed=3, rate=args.rate,
+                                          pool_size=args.pool)
+    budget = int(args.budget_gb * 1e9)
+    # warm-up: factor and solve one pool matrix with both paths
+    w = serve.HssServer(budget_bytes=budget, precision="fp32", tol=args.tol)
+    serve.run_stream(w, [serve.Request(0, "factor", 0.0, 0, hss=pool[0]),
+                         serve.Request(1, "solve", 0.0, 0, rhs=torch.randn((4, pool[0].size()[0]),
+                                                                            dtype=torch.float64, device="cuda"))])
+    del w
+    torch.cuda.synchronize()
+    srv = serve.HssServer(budget_bytes=budget, precision="fp32", tol=args.tol)
+    clocks = Clocks(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    done = serve.run_stream(srv, reqs)
+    makespan = time.perf_counter() - t0
+    clk = clocks.stop()
+    lat = [1000.0 * (r.done - r.arrival) for r in done]
+    slat = [1000.0 * (r.done - r.arrival) for r in done if r.kind == "solve"]
+    flat = [1000.0 * (r.done - r.arrival) for r in done if r.kind == "factor"]
+    nsolve = sum(1 for r in done if r.kind == "solve")
+    nrhs = sum(r.rhs.shape[0] for r in done if r.kind == "solve")
+    # accuracy: true residuals of a sample of served solves (FP64 product on the GPU)
+    worst = 0.0
+    for r in [q for q in done if q.kind == "solve"][:64]:
+        A = srv.matrices[r.matrix]
+        b = r.rhs.cpu().numpy().T
+        x = r.out.cpu().numpy().T
+        res = np.linalg.norm(b - pkg.matmul(pkg.HssMatrix.from_tree(A), x), axis=0) / np.linalg.norm(b, axis=0)
+        worst = max(worst, float(res.max()))
+    # plain FP64, one request at a time in arrival order (same arrival clock)
+    t0 = time.perf_counter()
+    res64 = {}
+    lat64 = []
+    for r in reqs:
+        now = time.perf_counter() - t0
+        if r.arrival > now:
+            time.sleep(r.arrival - now)
+        if r.kind == "factor":
+            dev = pkg.linalg.DeviceHss(r.hss)
+            res64[r.matrix] = (dev, dev.ulvfactor("fp64"))
+            torch.cuda.synchronize()
+        else:
+            dev, F = res64[r.matrix]
+            X = torch.empty_like(r.rhs)
+            F.solve_device(r.rhs, dev.n, r.rhs.shape[0], X, dev.n, tol=0.0)
+            torch.cuda.synchronize()
+        lat64.append(1000.0 * (time.perf_counter() - t0 - r.arrival))
+        if len(res64) > 256:
+            res64.pop(next(iter(res64)))
+    makespan64 = time.perf_counter() - t0
+    line = {
+        "metric": METRIC, "value": nsolve / makespan, "unit": UNIT, "n_gpus": 1, "steps": len(reqs),
+        "warmup": 1, "ms_per_step": 1000.0 * makespan / len(reqs), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+        "config": {"workload": (f"serving: {len(reqs)} Poisson requests at {args.rate:g}/s (seed 3), 20% factor "
+                                f"(n log-uniform 2048..65536, k 16..48, leafsize 128, pool of {args.pool} "
+                                f"matrices), 80% solve (r 1..32) against resident factorizations; "
+                                f"{args.budget_gb:g} GB HBM budget"),
+                   "tol": args.tol},
+        "p50_ms": _pct(lat, 0.5), "p99_ms": _pct(lat, 0.99),
+        "solve_p50_ms": _pct(slat, 0.5), "solve_p99_ms": _pct(slat, 0.99),
+        "factor_p50_ms": _pct(flat, 0.5), "factor_p99_ms": _pct(flat, 0.99),
+        "rhs_per_s": nrhs / makespan, "batches": srv.batches, "evictions": srv.evictions,
+        "reloads": srv.reloads, "max_residual_sampled": worst, "clocks": clk,
+        "fp64_one_at_a_time": {"solves_per_s": nsolve / makespan64, "p50_ms": _pct(lat64, 0.5),
+                               "p99_ms": _pct(lat64, 0.99), "makespan_s": makespan64},
+        "makespan_s": makespan,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batch(args):
+    """Batching: many independent HSS matrices of uneven sizes, leaf sizes and ranks
+    in one forest, factored and solved with one launch per tree level; FP64 and
+    FP32+refinement vs looping plain FP64 per matrix."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    rng = np.random.default_rng(2)
+    trees, rs = [], []
+    for _ in range(args.matrices):
+        n = int(rng.integers(1024 // 128, 16384 // 128 + 1)) * 128
+        ls = int(rng.choice([64, 128, 256]))
+        k = int(rng.integers(8, 49))
+        trees.append(pkg.synthetic_hss(n, ls, k, rng))
+        rs.append(int(rng.integers(1, 17)))
+    forest = pkg.DeviceHss.from_trees(trees)
+    Bs = [torch.randn((r, t.size()[0]), dtype=torch.float64, device="cuda") for t, r in zip(trees, rs)]
+    Xs = [torch.empty_like(b) for b in Bs]
+    ns = [t.size()[0] for t in trees]
+    out = {}
+    for prec, tol in (("fp64", 0.0), ("fp32", args.tol)):
+        F = forest.ulvfactor(prec)
+        for _ in range(max(1, args.warmup)):
+            F.refactor()
+            F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=tol, maxit=20)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            F.refactor()
+            F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=tol, maxit=20)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        out[prec] = {"ms_per_step": 1000.0 * statistics.mean(times), "p50_ms": 1000.0 * statistics.median(times)}
+        del F
+    # looping plain FP64 per matrix (separate plans, one matrix at a time)
+    devs = [pkg.linalg.DeviceHss(t) for t in trees]
+    facs = [d.ulvfactor("fp64") for d in devs]
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for d, f, b, x, r in zip(devs, facs, Bs, Xs, rs):
+            f.refactor()
+            f.solve_device(b, d.n, r, x, d.n, tol=0.0)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    loop_ms = 1000.0 * statistics.mean(times)
+    m32 = out["fp32"]["ms_per_step"]
+    line = {
+        "metric": METRIC, "value": 1000.0 * args.matrices / m32, "unit": "matrix solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": m32, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+        "config": {"workload": (f"batching: {args.matrices} matrices, n uniform 1024..16384 step 128 (seed 2), "
+                                f"leafsize in {{64,128,256}}, k 8..48, r 1..16; step = factor + solve of all, "
+                                f"FP32 ULV + refinement to {args.tol:g}")},
+        "fp64_batched_ms": out["fp64"]["ms_per_step"], "fp64_loop_ms": loop_ms,
+        "speedup_vs_fp64_loop": loop_ms / m32, "total_rhs": sum(rs),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -366,6 +529,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "serve":
+        return run_serve(args) if rank == 0 else 0
+    if args.workload == "batch":
+        return run_batch(args) if rank == 0 else 0
     if world > 1:
         import torch
         import torch.distributed as td
