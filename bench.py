@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--roofline-kernel", default="factor_leaf")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch"])
+    p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch", "compress"])
+    p.add_argument("--compress-n", type=int, default=16384)
     p.add_argument("--requests", type=int, default=10000)
     p.add_argument("--rate", type=float, default=1000.0)
     p.add_argument("--pool", type=int, default=32)
@@ -522,6 +523,122 @@ def run_batch(args):
     return 0
 
 
+def cauchy_device(n):
+    """A_ij = 1/(x_i - x_j), 1 on the diagonal, x = n uniform points in [-1, 1], built
+    on the device as its column-major storage (the (n, n) row-major tensor of A^T)."""
+    import torch
+    x = torch.linspace(-1.0, 1.0, n, dtype=torch.float64, device="cuda")
+    t = x[None, :] - x[:, None]          # t[j, i] = x_i - x_j = A_ij
+    t.reciprocal_()
+    t.diagonal().fill_(1.0)
+    return t
+
+
+def run_compress(args):
+    """Config 2: randcompress_adaptive of the Cauchy kernel matrix (n = 16384,
+    leafsize 128, kest 10, atol = rtol = 1e-9, noversampling 10, stepsize 20),
+    then a 64-RHS product and a 64-RHS FP64 ULV factor + solve of the result."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    from hssmatrices_gb300 import compression as CP
+    n = args.compress_n
+    tol = 1e-9
+    Ad = CP.DenseDevice.__new__(CP.DenseDevice)
+    Ad.t, Ad.m, Ad.n, Ad.lda = cauchy_device(n), n, n, n
+    cl = pkg.bisection_cluster(n, 128)
+    flops_per_col = 2.0 * n * n
+
+    def compress(stats=None):
+        return pkg.randcompress_adaptive(Ad, cl, cl, kest=10, atol=tol, rtol=tol, noversampling=10, stepsize=20,
+                                         rng=np.random.default_rng(1), stats=stats, device=True)
+
+    for _ in range(max(1, args.warmup)):
+        dev = compress()
+    torch.cuda.synchronize()
+    # sample-product kernel alone: A * Omega with 20 columns (one test round's product)
+    Om = torch.randn((20, n), dtype=torch.float64, device="cuda")
+    out = torch.empty_like(Om)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ts = []
+    for _ in range(5):
+        e0.record()
+        CP.sample(Ad, Om, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    gemm_ms = statistics.median(ts)
+    clocks = Clocks(0)
+    clocks.start()
+    times = []
+    st = {}
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev = compress(st)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    ck = clocks.stop()
+    ms = 1000.0 * statistics.median(times)
+    h = dev.to_host()
+    # the compressed matrix on the hot path: 64-RHS product and FP64 ULV solve
+    rng = np.random.default_rng(1)
+    Bh = rng.standard_normal((n, 64))
+    dB = torch.from_numpy(np.ascontiguousarray(Bh.T)).cuda()
+    dC = torch.empty_like(dB)
+    dev.matmul_device(dB, n, 64, dC, n)
+    F = dev.ulvfactor("fp64")
+    dX = torch.empty_like(dB)
+    F.solve_device(dB, n, 64, dX, n, tol=0.0)
+    torch.cuda.synchronize()
+    tm, tf = [], []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        dev.matmul_device(dB, n, 64, dC, n)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        F.refactor()
+        F.solve_device(dB, n, 64, dX, n, tol=0.0)
+        torch.cuda.synchronize()
+        tm.append(t1 - t0)
+        tf.append(time.perf_counter() - t1)
+    # accuracy against the dense matrix (on the device)
+    At = Ad.t   # column-major A
+    AX = (dX @ At)                      # (64, n) row-major = columns of A X
+    solve_res = float(torch.linalg.norm(AX - dB) / torch.linalg.norm(dB))
+    Ay = (dB @ At)
+    mv_err = float(torch.linalg.norm(dC - Ay) / torch.linalg.norm(Ay))
+    samples = st.get("samples", 0)
+    cols = 2 * samples + 2 * 20 * st.get("rounds", 0)   # initial samples + every test round
+    line = {
+        "metric": "randcompress_adaptive compressions/s (config 2)", "value": 1000.0 / ms,
+        "unit": "compressions/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": (f"compress: Cauchy kernel 1/(x_i-x_j) on {n} points in [-1,1], dense FP64 "
+                                f"resident; bisection_cluster leafsize 128; randcompress_adaptive kest 10, "
+                                f"atol=rtol=1e-9, noversampling 10, stepsize 20, Omega from default_rng(1)")},
+        "rounds": st.get("rounds"), "k": st.get("k"), "hssrank": int(pkg.hssrank(h)),
+        "sample_gemm": {"ms_20cols": gemm_ms, "tflops": flops_per_col * 20 / (gemm_ms * 1e-3) / 1e12,
+                        "fp64_peak_tflops_measured": 1.204},
+        "sample_columns_per_compression": cols,
+        "matvec64_ms": 1000.0 * statistics.median(tm), "matvec_rel_err_vs_dense": mv_err,
+        "ulv64_fp64_ms": 1000.0 * statistics.median(tf), "ulv_rel_residual_vs_dense": solve_res,
+        "clocks": ck,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import hss_oracle as orc
+        A = orc.cauchy_matrix(n)
+        ocl = orc.bisection_cluster(n, 128)
+        t0 = time.perf_counter()
+        orc.randcompress_adaptive(A, ocl, ocl, 10, tol, tol, 10, 20, rng=np.random.default_rng(1))
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "compressions/s", "cores": os.cpu_count(),
+                                "kind": "port", "sample": "1 randcompress_adaptive of the same matrix"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -533,6 +650,8 @@ def main():
         return run_serve(args) if rank == 0 else 0
     if args.workload == "batch":
         return run_batch(args) if rank == 0 else 0
+    if args.workload == "compress":
+        return run_compress(args) if rank == 0 else 0
     if world > 1:
         import torch
         import torch.distributed as td

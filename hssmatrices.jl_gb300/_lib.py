@@ -30,6 +30,7 @@ HSS_PREC_FP64 = 0
 HSS_PREC_FP32 = 1
 
 NODE_FIELDS = 16
+CLUSTER_FIELDS = 6
 INFO_FIELDS = 13
 
 # every symbol include/hssgpu.h declares
@@ -40,6 +41,8 @@ EXPORTS = [
     "hss_ulvfactsolve_host", "hss_factor_bytes", "hss_last_error", "hss_version", "hss_ulvrefactor",
     "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option", "hss_matmul_noalloc",
     "hss_batcher_create", "hss_batcher_destroy", "hss_batcher_factor", "hss_batcher_solve",
+    "hss_sample", "hss_sumsq", "hss_rc_create", "hss_rc_destroy", "hss_rc_size", "hss_rc_compress",
+    "hss_rc_ranks", "hss_export_size", "hss_export",
 ]
 
 
@@ -101,6 +104,15 @@ def _declare(lib):
         "hss_batcher_factor": (C.c_int, [P, I32, C.POINTER(P), I32, C.POINTER(P), P]),
         "hss_batcher_solve": (C.c_int, [P, I32, C.POINTER(P), C.POINTER(P), PI64, PI64, C.POINTER(P), PI64, D, I32,
                                         C.POINTER(SolveStats), P]),
+        "hss_sample": (C.c_int, [P, I64, I64, I64, I32, P, I64, I64, P, I64, D, D, P]),
+        "hss_sumsq": (C.c_int, [P, I64, I64, I64, PD, P]),
+        "hss_rc_create": (C.c_int, [I64, PI64, C.POINTER(P)]),
+        "hss_rc_destroy": (C.c_int, [P]),
+        "hss_rc_size": (C.c_int, [P, PI64, PI64]),
+        "hss_rc_compress": (C.c_int, [P, P, I64, P, I64, P, I64, P, I64, P, I64, I64, D, D, C.POINTER(P), P]),
+        "hss_rc_ranks": (C.c_int, [P, C.POINTER(I32)]),
+        "hss_export_size": (C.c_int, [P, PI64, PI64]),
+        "hss_export": (C.c_int, [P, PI64, PD]),
         "hss_last_error": (C.c_char_p, []),
         "hss_version": (C.c_int32, []),
     }

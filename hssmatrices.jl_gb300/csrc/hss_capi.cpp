@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "hss_host.h"
 #include "hss_internal.h"
 #include "hss_launch.h"
 
@@ -35,53 +36,6 @@ int cuda_fail(cudaError_t e, const char* what) {
     cudaError_t e_ = (x);                             \
     if (e_ != cudaSuccess) return cuda_fail(e_, #x);  \
   } while (0)
-
-// Grow-only device buffer.
-template <typename T>
-struct DBuf {
-  T* p = nullptr;
-  size_t cap = 0;
-  DBuf() = default;
-  DBuf(const DBuf&) = delete;
-  DBuf& operator=(const DBuf&) = delete;
-  ~DBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  cudaError_t ensure(size_t n) {
-    if (n <= cap && p) return cudaSuccess;
-    release();
-    size_t want = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
-    if (e == cudaSuccess) cap = want;
-    else p = nullptr;
-    return e;
-  }
-};
-
-// Pinned host buffer.
-template <typename T>
-struct HBuf {
-  T* p = nullptr;
-  size_t cap = 0;
-  HBuf() = default;
-  HBuf(const HBuf&) = delete;
-  HBuf& operator=(const HBuf&) = delete;
-  ~HBuf() {
-    if (p) cudaFreeHost(p);
-  }
-  cudaError_t ensure(size_t n) {
-    if (n <= cap && p) return cudaSuccess;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    cap = 0;
-    cudaError_t e = cudaMallocHost((void**)&p, std::max<size_t>(n, 1) * sizeof(T));
-    if (e == cudaSuccess) cap = std::max<size_t>(n, 1);
-    return e;
-  }
-};
 
 // Slot table on the device, re-uploaded only when its contents change.
 struct SlotTable {
@@ -174,6 +128,8 @@ struct hss_plan_s {
   int64_t gen_len = 0;                  // elements of d_gen
   float2* d_gen_df = nullptr;           // generators as (hi, lo) float pairs, made on first use
   std::vector<Task> h_tasks;            // host copy of the task lists (merged batches)
+  std::vector<int64_t> h_table;         // node table of a single-tree plan (hss_export)
+  int64_t h_npacked = 0;                // its packed generator length
   ~hss_plan_s();
 };
 
@@ -488,9 +444,10 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
   return HSS_OK;
 }
 
-int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
+// device_fill: the generator buffer is left for the caller to write on the device.
+int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill = false) {
   for (auto& t : trees)
-    if (t.npacked > 0 && t.packed == nullptr) return fail(HSS_ERR_INVALID, "null packed buffer");
+    if (t.npacked > 0 && t.packed == nullptr && !device_fill) return fail(HSS_ERR_INVALID, "null packed buffer");
   std::vector<GenOffsets> go;
   std::vector<Task> tasks;
   std::vector<int64_t> gbases;
@@ -504,9 +461,14 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees) {
   CUDA_TRY(cudaMalloc((void**)&P->d_err, sizeof(int32_t)));
   CUDA_TRY(cudaMemset(P->d_err, 0, sizeof(int32_t)));
   for (size_t ti = 0; ti < trees.size(); ++ti)
-    if (trees[ti].npacked > 0)
+    if (trees[ti].npacked > 0 && !device_fill)
       CUDA_TRY(cudaMemcpy(P->d_gen + gbases[ti], trees[ti].packed, trees[ti].npacked * sizeof(double),
                           cudaMemcpyHostToDevice));
+  if (trees.size() == 1)
+  {
+    P->h_table.assign(trees[0].table, trees[0].table + trees[0].nnodes * HSS_NODE_FIELDS);
+    P->h_npacked = trees[0].npacked;
+  }
   auto gp = [&](int64_t off) -> const double* { return off < 0 ? nullptr : P->d_gen + off; };
   for (size_t i = 0; i < P->nodes.size(); ++i) {
     Node& x = P->nodes[i];
@@ -1028,6 +990,27 @@ int batcher_levels(hss_batcher_s* b, const std::vector<hss_plan_s*>& plans, cuda
 // C ABI
 // ---------------------------------------------------------------------------
 
+namespace hss {
+
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+int set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+void count_launches(int64_t n) { g_launches += n; }
+
+int plan_create_device(int64_t nnodes, const int64_t* table, int64_t npacked, hss_plan_s** out, double** d_gen) {
+  *out = nullptr;
+  *d_gen = nullptr;
+  auto* P = new hss_plan_s();
+  int rc = build_plan(P, {TreeIn{nnodes, table, nullptr, npacked}}, true);
+  if (rc) { delete P; return rc; }
+  *out = P;
+  *d_gen = P->d_gen;
+  return HSS_OK;
+}
+
+void plan_destroy(hss_plan_s* p) { delete p; }
+
+}  // namespace hss
+
 extern "C" {
 
 const char* hss_last_error(void) { return g_err.c_str(); }
@@ -1077,6 +1060,22 @@ int hss_inspect(int64_t nnodes, const int64_t* nodes, int64_t npacked, int64_t* 
 
 int hss_destroy(hss_handle h) {
   delete h;
+  return HSS_OK;
+}
+
+int hss_export_size(hss_handle h, int64_t* nnodes, int64_t* npacked) {
+  if (!h || h->ntrees != 1 || h->h_table.empty()) return fail(HSS_ERR_INVALID, "export needs a single-tree handle");
+  if (nnodes) *nnodes = (int64_t)h->h_table.size() / HSS_NODE_FIELDS;
+  if (npacked) *npacked = h->h_npacked;
+  return HSS_OK;
+}
+
+int hss_export(hss_handle h, int64_t* nodes, double* packed) {
+  if (!h || h->ntrees != 1 || h->h_table.empty()) return fail(HSS_ERR_INVALID, "export needs a single-tree handle");
+  CUDA_TRY(cudaSetDevice(h->device));
+  if (nodes) std::memcpy(nodes, h->h_table.data(), h->h_table.size() * sizeof(int64_t));
+  if (packed && h->h_npacked > 0)
+    CUDA_TRY(cudaMemcpy(packed, h->d_gen, h->h_npacked * sizeof(double), cudaMemcpyDeviceToHost));
   return HSS_OK;
 }
 

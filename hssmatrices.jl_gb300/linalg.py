@@ -101,6 +101,24 @@ class DeviceHss:
             pass
 
     # -- bookkeeping ------------------------------------------------------
+    def export(self):
+        """Node table and packed generators (host copies) of a single-tree handle."""
+        nn, npk = C.c_int64(), C.c_int64()
+        check(self.lib.hss_export_size(self.handle, C.byref(nn), C.byref(npk)))
+        table = np.zeros((nn.value, _lib.NODE_FIELDS), dtype=np.int64)
+        packed = np.zeros(max(npk.value, 1), dtype=np.float64)
+        check(self.lib.hss_export(self.handle, iptr(table), dptr(packed)))
+        return table, packed[:npk.value]
+
+    def to_host(self):
+        """The ``HssMatrix`` of this handle, keeping this upload as its device copy."""
+        from .packing import unpack
+        table, packed = self.export()
+        h = unpack(table, packed)
+        h._device = self
+        h._packed = (table, packed)
+        return h
+
     def node_info(self, node):
         f = np.zeros(_lib.INFO_FIELDS, dtype=np.int64)
         check(self.lib.hss_node_info(self.handle, node, iptr(f)))

@@ -100,3 +100,36 @@ def pack_cached(h):
         except AttributeError:
             pass
     return cached
+
+
+def unpack(table, packed):
+    """Inverse of ``pack``: the ``HssMatrix`` of a node table + packed buffer
+    (e.g. exported from the device after randomized compression)."""
+    from .hssmatrix import HssMatrix
+    table = np.asarray(table, dtype=np.int64)
+    packed = np.asarray(packed, dtype=np.float64)
+
+    def blk(off, r, c):
+        if r * c == 0:
+            return np.zeros((r, c))
+        return packed[off:off + r * c].reshape((r, c), order="F").copy()
+
+    def build(i, root):
+        t = table[i]
+        if t[0] < 0:
+            D = blk(t[6], t[2], t[3])
+            if root:
+                return HssMatrix.leaf(D, rootnode=True)
+            return HssMatrix.leaf(D, blk(t[7], t[2], t[4]), blk(t[8], t[3], t[5]))
+        l, r = int(t[0]), int(t[1])
+        A11, A22 = build(l, False), build(r, False)
+        ku1, kv1 = table[l, 4], table[l, 5]
+        ku2, kv2 = table[r, 4], table[r, 5]
+        B12, B21 = blk(t[9], ku1, kv2), blk(t[10], ku2, kv1)
+        if root:
+            return HssMatrix.branch(A11, A22, B12, B21, rootnode=True)
+        ku, kv = t[4], t[5]
+        return HssMatrix.branch(A11, A22, B12, B21, blk(t[11], ku1, ku), blk(t[13], kv1, kv),
+                                blk(t[12], ku2, ku), blk(t[14], kv2, kv), rootnode=False)
+
+    return build(0, True)

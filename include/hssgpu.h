@@ -213,6 +213,55 @@ int hss_set_option(int32_t option, int64_t value);
 const char* hss_last_error(void);
 int32_t hss_version(void);
 
+/* ---- randomized compression (reference src/compression.jl:278-444) ----
+ *
+ * The dense matrix A (m x n, column-major, lda) lives on the device.  The
+ * reference's `randcompress(A, rcl, ccl, kest)` (:278) and
+ * `randcompress_adaptive(A, rcl, ccl; kest)` (:312) become, on the host:
+ * draw Omega_col (n x s), Omega_row (m x s); S_col = A * Omega_col and
+ * S_row = A^T * Omega_row with hss_sample; hss_rc_compress; for the adaptive
+ * form, test with fresh samples through hss_sample, hss_matmul and hss_sumsq
+ * and repeat with more columns (the loop of :330-352). */
+
+/* S = alpha * op(A) * X + beta * S (op(A) = A if trans == 0, A^T if 1):
+ * A * Omega and A' * Omega of src/compression.jl:290-291, :326-327, :336-337.
+ * X has n (trans 0) or m (trans 1) rows and r columns.  FP64. */
+int hss_sample(const double* dA, int64_t lda, int64_t m, int64_t n, int32_t trans, const double* dX, int64_t ldx,
+               int64_t r, double* dY, int64_t ldy, double alpha, double beta, void* stream);
+
+/* *out = sum of squares of the m x r device matrix B (the `norm(...)^2` of
+ * src/compression.jl:340-341); synchronises `stream`. */
+int hss_sumsq(const double* dB, int64_t ldb, int64_t m, int64_t r, double* out, void* stream);
+
+/* Row and column cluster trees, which must be compatible (`compatible`,
+ * src/clustertree.jl): one table of nnodes rows of 6 int64 -- left child,
+ * right child (-1 for leaves), row range [rlo, rhi), column range [clo, chi),
+ * 0-based -- with the root in row 0 covering [0, m) x [0, n). */
+typedef struct hss_rc_s* hss_rc;
+#define HSS_CLUSTER_FIELDS 6
+int hss_rc_create(int64_t nnodes, const int64_t* clusters, hss_rc* out);
+int hss_rc_destroy(hss_rc rc);
+int hss_rc_size(hss_rc rc, int64_t* m, int64_t* n);
+
+/* `_randcompress!(hss_blkdiag(A, rcl, ccl), A, Scol, Srow, Ocol, Orow, 0, 0,
+ * atol, rtol; rootnode = true)` (src/compression.jl:358-430, `_interpolate`
+ * :433-444): from the s samples S_col = A * Omega_col (m x s) and
+ * S_row = A^T * Omega_row (n x s), builds the HSS approximation of A as a new
+ * handle (node numbering = the cluster table's, generators on the device).
+ * Rank decisions (QR with column pivoting) are FP64 on the GPU; the call
+ * synchronises `stream` once to read the ranks.  Samples are not modified. */
+int hss_rc_compress(hss_rc rc, const double* dA, int64_t lda, const double* dScol, int64_t ldscol,
+                    const double* dSrow, int64_t ldsrow, const double* dOcol, int64_t ldocol, const double* dOrow,
+                    int64_t ldorow, int64_t s, double atol, double rtol, hss_handle* out, void* stream);
+/* Ranks of the last hss_rc_compress: 2 per cluster node (column side = U/R
+ * rank, row side = V/W rank); 0 for the root. */
+int hss_rc_ranks(hss_rc rc, int32_t* ranks);
+
+/* Node table (nnodes x HSS_NODE_FIELDS, the hss_create format) and packed
+ * generators of a single-tree handle, e.g. to rebuild the host HssMatrix. */
+int hss_export_size(hss_handle h, int64_t* nnodes, int64_t* npacked);
+int hss_export(hss_handle h, int64_t* nodes, double* packed);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,3 +120,56 @@ def test_synthetic_generator_matches_oracle(pkg, orc):
     tb, pb = pkg.pack(pkg.HssMatrix.from_tree(b))
     assert np.array_equal(ta, tb) and np.array_equal(pa, pb)
     assert pkg.generator_entries(a) == orc.generator_entries(b) == pa.size
+
+
+def test_cluster_table_and_validation(pkg, lib):
+    """Cluster table of two compatible trees (pre-order, 0-based half-open), and
+    hss_rc_create's host-side checks (no GPU needed: they run before any CUDA call)."""
+    import ctypes as C
+    rcl = pkg.bisection_cluster(10, 3)
+    t = pkg.cluster_table(rcl, rcl)
+    expect = [[1, 4, 0, 10, 0, 10], [2, 3, 0, 5, 0, 5], [-1, -1, 0, 3, 0, 3], [-1, -1, 3, 5, 3, 5],
+              [5, 6, 5, 10, 5, 10], [-1, -1, 5, 8, 5, 8], [-1, -1, 8, 10, 8, 10]]
+    assert t.tolist() == expect
+    # rectangular: rows and columns from different trees of the same shape
+    t2 = pkg.cluster_table(pkg.bisection_cluster(10, 3), pkg.bisection_cluster(12, 3))
+    assert t2[0].tolist() == [1, 4, 0, 10, 0, 12]
+    with pytest.raises(ValueError):
+        pkg.cluster_table(pkg.bisection_cluster(10, 3), pkg.bisection_cluster(10, 5))
+
+    def create(tab):
+        tab = np.ascontiguousarray(np.asarray(tab, dtype=np.int64))
+        h = C.c_void_p()
+        return lib.hss_rc_create(tab.shape[0], tab.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(h))
+
+    bad = [r[:] for r in expect]
+    bad[1][3] = 4                      # left child does not end where the right one starts
+    assert create(bad) == pkg._lib.HSS_ERR_BAD_DIMS
+    bad = [r[:] for r in expect]
+    bad[0][1] = -1                     # one child only
+    assert create(bad) == pkg._lib.HSS_ERR_BAD_DIMS
+    bad = [r[:] for r in expect]
+    bad[4][0] = 2                      # node 2 with two parents
+    assert create(bad) == pkg._lib.HSS_ERR_BAD_DIMS
+    bad = [r[:] for r in expect]
+    bad[2][3] = 0                      # empty leaf
+    assert create(bad) == pkg._lib.HSS_ERR_BAD_DIMS
+
+
+def test_sample_argument_checks(pkg, lib):
+    import ctypes as C
+    # leading dimensions below the sizes are rejected before any device access
+    assert lib.hss_sample(None, 5, 10, 4, 0, None, 4, 2, None, 10, 1.0, 0.0, None) == pkg._lib.HSS_ERR_BAD_DIMS
+    assert lib.hss_sample(None, 10, 10, 4, 1, None, 4, 2, None, 4, 1.0, 0.0, None) == pkg._lib.HSS_ERR_BAD_DIMS
+    assert lib.hss_sample(None, 10, 10, 4, 2, None, 4, 2, None, 10, 1.0, 0.0, None) == pkg._lib.HSS_ERR_BAD_DIMS
+    out = C.c_double()
+    assert lib.hss_sumsq(None, 3, 5, 1, C.byref(out), None) == pkg._lib.HSS_ERR_BAD_DIMS
+
+
+def test_unpack_inverts_pack(pkg, orc):
+    rng = np.random.default_rng(12)
+    h = pkg.HssMatrix.from_tree(orc.synthetic_hss(777, 64, 9, rng))
+    table, packed = pkg.pack(h)
+    h2 = pkg.unpack(table, packed)
+    t2, p2 = pkg.pack(h2)
+    assert np.array_equal(table, t2) and np.array_equal(packed, p2)
