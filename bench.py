@@ -51,7 +51,7 @@ def parse():
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--roofline-kernel", default="factor_leaf")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch", "compress"])
+    p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch", "compress", "matvec"])
     p.add_argument("--compress-n", type=int, default=16384)
     p.add_argument("--requests", type=int, default=10000)
     p.add_argument("--rate", type=float, default=1000.0)
@@ -639,6 +639,77 @@ def run_compress(args):
     return 0
 
 
+def run_matvec_workload(args):
+    """HSS x dense product (``hss_matmul``, FP64) on the precision workload's tree
+    (n = 65536, leafsize 128, k = 32): r = 1, where the product is bound by HBM
+    bandwidth and GB300's FP64 rate, and r = --rhs.  The persistent product (one
+    cooperative launch) is timed beside the level-by-level kernels.  L2 is flushed
+    (512 MB write) before every timed call; CUDA events on the launching stream."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    from hssmatrices_gb300 import synthetic as S
+    n = args.n
+    A = pkg.synthetic_hss(n, args.leafsize, args.rank, np.random.default_rng(args.seed))
+    dev = A.device()
+    lib = dev.lib
+    entries = S.generator_entries(A)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peak_src = "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    out = {}
+    clocks = Clocks(0)
+    clocks.start()
+    for r in sorted({1, args.rhs}):
+        dB = torch.randn((r, n), dtype=torch.float64, device="cuda")
+        dC = torch.empty_like(dB)
+        alg = 8 * entries + 8 * r * (2 * n)     # generators + B read + C written
+        res = {}
+        for level in (0, 1):
+            assert lib.hss_set_option(3, level) == 0
+            try:
+                for _ in range(max(3, args.warmup)):
+                    dev.matmul_device(dB, n, r, dC, n, stream=stream)
+                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                      for _ in range(args.steps)]
+                torch.cuda.synchronize()
+                for a, b in ev:
+                    flush.zero_()
+                    a.record(stream)
+                    dev.matmul_device(dB, n, r, dC, n, stream=stream)
+                    b.record(stream)
+                torch.cuda.synchronize()
+                t = sorted(x.elapsed_time(y) for x, y in ev)
+                res["level" if level else "persistent"] = {
+                    "us_median": 1000.0 * statistics.median(t), "us_min": 1000.0 * t[0],
+                    "gbs": alg / (statistics.median(t) * 1e-3) / 1e9}
+                res["C" if not level else "C_level"] = dC.cpu().numpy()
+            finally:
+                lib.hss_set_option(3, 0)
+        diff = float(np.linalg.norm(res.pop("C") - res.pop("C_level")))
+        out[r] = dict(res, algorithmic_bytes=alg, paths_rel_diff=diff / max(1e-300, float(torch.linalg.norm(dC))))
+    clk = clocks.stop()
+    g1 = out[1]["persistent"]["gbs"]
+    line = {
+        "metric": "HSS matvec GB/s (FP64 hss_matmul, r=1)", "value": g1, "unit": "GB/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": out[1]["persistent"]["us_median"] / 1000.0,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": (f"matvec: synthetic HSS n={n}, perfect tree leafsize {args.leafsize}, k={args.rank}; "
+                                f"C = A B with r = 1 and r = {args.rhs}; algorithmic bytes = 8 x generator entries "
+                                f"({entries}) + 16 n r"), "l2": "flushed before every timed call (512 MB write)"},
+        "roofline": {"kernel": "pmv_kernel<PF64>", "bound": "hbm", "achieved": g1, "peak": peak, "unit": "GB/s",
+                     "frac": g1 / peak, "peak_source": peak_src},
+        "by_rhs": {str(r): v for r, v in out.items()}, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -652,6 +723,8 @@ def main():
         return run_batch(args) if rank == 0 else 0
     if args.workload == "compress":
         return run_compress(args) if rank == 0 else 0
+    if args.workload == "matvec":
+        return run_matvec_workload(args) if rank == 0 else 0
     if world > 1:
         import torch
         import torch.distributed as td

@@ -37,10 +37,25 @@ int cuda_fail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, #x);  \
   } while (0)
 
-// Slot table on the device, re-uploaded only when its contents change.
+// Slot table on the device, re-uploaded only when its contents change, and
+// the launch state of the persistent product run with it.
 struct SlotTable {
   DBuf<Slot> dev;
   std::vector<Slot> last;
+  DBuf<uint32_t> pstate;   // counters + queue tags: zero between launches
+  DBuf<int2> pq;           // queue entries
+  uint32_t epoch = 0;      // tag of the last persistent launch on pstate
+  cudaError_t ensure_pmv(int64_t entries, cudaStream_t st) {
+    const size_t words = (size_t)pmv_state_words(entries);
+    if (pstate.p && pstate.cap >= words && pq.p && pq.cap >= (size_t)std::max<int64_t>(entries, 1) && epoch != ~0u)
+      return cudaSuccess;
+    pstate.release();
+    cudaError_t e = pstate.ensure(words);
+    if (e == cudaSuccess) e = cudaMemsetAsync(pstate.p, 0, pstate.cap * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = pq.ensure((size_t)std::max<int64_t>(entries, 1));
+    epoch = 0;
+    return e;
+  }
   cudaError_t upload(const std::vector<Slot>& s, cudaStream_t st) {
     if (s.size() == last.size() && dev.p &&
         std::memcmp(s.data(), last.data(), s.size() * sizeof(Slot)) == 0)
@@ -71,6 +86,8 @@ int64_t g_launches = 0;
 bool g_generic_factor = false;
 // Forces the native FP64 product for the refinement residual.
 bool g_residual_fp64 = false;
+// Forces the level-by-level product kernels instead of the persistent one.
+bool g_level_product = false;
 struct TraceState {
   int kind = -1;
   std::vector<cudaEvent_t> pool;
@@ -127,6 +144,9 @@ struct hss_plan_s {
   hss_factor_s* fused[2] = {nullptr, nullptr};   // storage reused by hss_ulvfactsolve_host
   int64_t gen_len = 0;                  // elements of d_gen
   float2* d_gen_df = nullptr;           // generators as (hi, lo) float pairs, made on first use
+  int32_t* d_sync = nullptr;            // per-node arrival counters of the persistent product
+  int pmv_nleaf = 0, pmv_mleaf = 0, pmv_kmax = 0;   // largest leaf columns / rows, largest rank
+  int64_t tr_lo = 0, tr_hi = 0;         // element range of d_gen holding every translator (B, R, W)
   std::vector<Task> h_tasks;            // host copy of the task lists (merged batches)
   std::vector<int64_t> h_table;         // node table of a single-tree plan (hss_export)
   int64_t h_npacked = 0;                // its packed generator length
@@ -164,6 +184,7 @@ hss_plan_s::~hss_plan_s() {
   if (d_nodes) cudaFree(d_nodes);
   if (d_tasks) cudaFree(d_tasks);
   if (d_err) cudaFree(d_err);
+  if (d_sync) cudaFree(d_sync);
 }
 
 
@@ -460,6 +481,16 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill
   CUDA_TRY(cudaMalloc((void**)&P->d_gen, std::max<int64_t>(total_gen, 1) * sizeof(double)));
   CUDA_TRY(cudaMalloc((void**)&P->d_err, sizeof(int32_t)));
   CUDA_TRY(cudaMemset(P->d_err, 0, sizeof(int32_t)));
+  const size_t nsync = std::max<size_t>(P->nodes.size(), 1) * pmv_sync_chunks();
+  CUDA_TRY(cudaMalloc((void**)&P->d_sync, nsync * sizeof(int32_t)));
+  CUDA_TRY(cudaMemset(P->d_sync, 0, nsync * sizeof(int32_t)));
+  for (const Node& x : P->nodes) {
+    if (x.leaf) {
+      P->pmv_nleaf = std::max(P->pmv_nleaf, x.gn);
+      P->pmv_mleaf = std::max(P->pmv_mleaf, x.gm);
+    }
+    P->pmv_kmax = std::max(P->pmv_kmax, std::max(x.ku, x.kv));
+  }
   for (size_t ti = 0; ti < trees.size(); ++ti)
     if (trees[ti].npacked > 0 && !device_fill)
       CUDA_TRY(cudaMemcpy(P->d_gen + gbases[ti], trees[ti].packed, trees[ti].npacked * sizeof(double),
@@ -468,6 +499,31 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill
   {
     P->h_table.assign(trees[0].table, trees[0].table + trees[0].nnodes * HSS_NODE_FIELDS);
     P->h_npacked = trees[0].npacked;
+  }
+  {
+    // translator range (prefetched into L2 by the persistent product); kept only
+    // when it is not much larger than the translators themselves
+    int64_t lo = INT64_MAX, hi = 0, tot = 0;
+    for (size_t i = 0; i < P->nodes.size(); ++i) {
+      const Node& x = P->nodes[i];
+      if (x.leaf) continue;
+      const Node& c1 = P->nodes[x.left];
+      const Node& c2 = P->nodes[x.right];
+      const GenOffsets& o = go[i];
+      const int64_t offs[6] = {o.B12, o.B21, o.R1, o.R2, o.W1, o.W2};
+      const int64_t lens[6] = {(int64_t)c1.ku * c2.kv, (int64_t)c2.ku * c1.kv, (int64_t)c1.ku * x.ku,
+                               (int64_t)c2.ku * x.ku, (int64_t)c1.kv * x.kv, (int64_t)c2.kv * x.kv};
+      for (int j = 0; j < 6; ++j)
+        if (offs[j] >= 0 && lens[j] > 0) {
+          lo = std::min(lo, offs[j]);
+          hi = std::max(hi, offs[j] + lens[j]);
+          tot += lens[j];
+        }
+    }
+    if (tot > 0 && hi - lo <= 2 * tot) {
+      P->tr_lo = lo;
+      P->tr_hi = hi;
+    }
   }
   auto gp = [&](int64_t off) -> const double* { return off < 0 ? nullptr : P->d_gen + off; };
   for (size_t i = 0; i < P->nodes.size(); ++i) {
@@ -500,6 +556,14 @@ struct Levels {
   const std::vector<Seg>* mv_up = nullptr;
   const std::vector<Seg>* mv_dn = nullptr;
   Seg leaves;
+  // persistent product: largest leaf columns / rows, largest rank, non-root nodes
+  int nleaf = 0, mleaf = 0, kmax = 0;
+  int64_t ntasks = 0;
+  int device = 0;
+  // translators to prefetch into L2 (FP64 and pair copies; null: none)
+  const double* pf64 = nullptr;
+  const float2* pfdf = nullptr;
+  int64_t pf_elems = 0;
 };
 
 Levels plan_levels(const hss_plan_s* P) {
@@ -510,10 +574,44 @@ Levels plan_levels(const hss_plan_s* P) {
   L.mv_up = &P->mv_up;
   L.mv_dn = &P->mv_dn;
   L.leaves = P->leaves;
+  L.nleaf = P->pmv_nleaf;
+  L.mleaf = P->pmv_mleaf;
+  L.kmax = P->pmv_kmax;
+  L.ntasks = (int64_t)P->nodes.size() - P->ntrees;
+  L.device = P->device;
+  if (P->tr_hi > P->tr_lo) {
+    L.pf64 = P->d_gen + P->tr_lo;
+    L.pfdf = P->d_gen_df ? P->d_gen_df + P->tr_lo : nullptr;
+    L.pf_elems = P->tr_hi - P->tr_lo;
+  }
   return L;
 }
 
-void run_matvec(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
+// The persistent product runs when a launch state is given, it is not
+// switched off, and the forest's leaves and ranks fit its shared memory.
+bool use_pmv(const Levels& L, const SlotTable* pm, bool pairs, int rmax) {
+  return pm != nullptr && !g_level_product && L.leaves.cnt > 0 && pmv_fits(L.nleaf, L.mleaf, L.kmax) &&
+         pmv_chunks(pairs, rmax) > 0;
+}
+
+int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable& pm, cudaStream_t st) {
+  CUDA_TRY(pm.ensure_pmv(L.ntasks * pmv_chunks(pairs, rmax), st));
+  ++pm.epoch;
+  cudaError_t e = cudaSuccess;
+  traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st, [&] {
+    const void* pf = pairs ? (const void*)L.pfdf : (const void*)L.pf64;
+    e = launch_pmv(pairs, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, L.ntasks, rmax, L.nleaf, L.kmax, pm.pstate.p,
+                   pm.pq.p, pm.epoch, pf, pf ? L.pf_elems * 8 : 0, L.device, st);
+  });
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_fail(e, "persistent product launch");
+  }
+  return HSS_OK;
+}
+
+int run_matvec(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, SlotTable* pm = nullptr) {
+  if (use_pmv(L, pm, false, rmax)) return run_pmv(L, slots, rmax, false, *pm, st);
   const Task* T = L.d_tasks;
   constexpr size_t kStagedCap = 200 * 1024;
   traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st,
@@ -536,12 +634,14 @@ void run_matvec(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
   }
   traced(HSS_TRACE_MV_FINAL, L.leaves.cnt, st,
          [&] { launch_mv_leaf_final(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
+  return HSS_OK;
 }
-void run_matvec(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st) {
-  run_matvec(plan_levels(P), slots, rmax, st);
+int run_matvec(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st, SlotTable* pm = nullptr) {
+  return run_matvec(plan_levels(P), slots, rmax, st, pm);
 }
 
-void run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
+int run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, SlotTable* pm = nullptr) {
+  if (use_pmv(L, pm, true, rmax)) return run_pmv(L, slots, rmax, true, *pm, st);
   const Task* T = L.d_tasks;
   traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st,
          [&] { launch_dfmv_leaf(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
@@ -553,6 +653,7 @@ void run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st
            [&] { launch_dfmv_down(T + (*L.mv_dn)[d].off, (*L.mv_dn)[d].cnt, slots, rmax, st); });
   traced(HSS_TRACE_MV_FINAL, L.leaves.cnt, st,
          [&] { launch_dfmv_final(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
+  return HSS_OK;
 }
 
 int ensure_df(hss_plan_s* P, cudaStream_t st) {
@@ -610,6 +711,8 @@ struct MergedLevels {
   Seg leaves;
   std::vector<Task> h;
   DBuf<Task> d;
+  int nleaf = 0, mleaf = 0, kmax = 0, device = 0;
+  int64_t ntasks = 0;
   Levels view() const {
     Levels L;
     L.d_tasks = d.p;
@@ -618,6 +721,11 @@ struct MergedLevels {
     L.mv_up = &mv_up;
     L.mv_dn = &mv_dn;
     L.leaves = leaves;
+    L.nleaf = nleaf;
+    L.mleaf = mleaf;
+    L.kmax = kmax;
+    L.ntasks = ntasks;
+    L.device = device;
     return L;
   }
 };
@@ -673,6 +781,15 @@ int merge_levels(const std::vector<hss_plan_s*>& plans, MergedLevels& M, cudaStr
     }
   }
   M.leaves.cnt = (int64_t)M.h.size() - M.leaves.off;
+  M.nleaf = M.mleaf = M.kmax = 0;
+  M.ntasks = 0;
+  for (auto* P : plans) {
+    M.nleaf = std::max(M.nleaf, P->pmv_nleaf);
+    M.mleaf = std::max(M.mleaf, P->pmv_mleaf);
+    M.kmax = std::max(M.kmax, P->pmv_kmax);
+    M.ntasks += (int64_t)P->nodes.size() - P->ntrees;
+  }
+  M.device = plans.empty() ? 0 : plans[0]->device;
   CUDA_TRY(M.d.ensure(std::max<size_t>(M.h.size(), 1)));
   // pageable source: staged before the call returns; stream order protects
   // the previous batch's reads of the same buffer
@@ -724,9 +841,12 @@ int matmul_impl(hss_plan_s* P, const std::vector<Cols>& io, double alpha, double
     x.r = (int32_t)io[t].r;
     x.colnorm2 = colnorm2 ? colnorm2 + cn_off[t] : nullptr;
     x.err = P->d_err;
+    x.nodes = P->d_nodes;
+    x.sync = P->d_sync;
   }
   CUDA_TRY(table.upload(s, st));
-  run_matvec(P, table.dev.p, (int)rmax, st);
+  int rc = run_matvec(P, table.dev.p, (int)rmax, st, &table);
+  if (rc) return rc;
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -803,6 +923,14 @@ int read_dev_err(hss_plan_s* P, cudaStream_t st) {
     cudaMemsetAsync(P->d_err, 0, sizeof(int32_t), st);
     return fail(HSS_ERR_SINGULAR, "root block of the ULV factorization is singular");
   }
+  if (e == DEV_TIMEOUT || e == DEV_BAD) {
+    // a persistent launch gave up: its per-node counters may be left non-zero
+    cudaMemsetAsync(P->d_sync, 0, std::max<size_t>(P->nodes.size(), 1) * pmv_sync_chunks() * sizeof(int32_t), st);
+    cudaMemsetAsync(P->d_err, 0, sizeof(int32_t), st);
+    cudaStreamSynchronize(st);
+    return e == DEV_TIMEOUT ? fail(HSS_ERR_TIMEOUT, "persistent product: no ready work within the poll limit")
+                            : fail(HSS_ERR_CUDA, "persistent product: more downsweep tasks than tree nodes");
+  }
   return HSS_OK;
 }
 
@@ -876,6 +1004,8 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     x.r = (int32_t)it.io.r;
     x.colnorm2 = B.rn2.p + off[i];
     x.err = P->d_err;
+    x.nodes = P->d_nodes;
+    x.sync = P->d_sync;
     if (dfres) {
       CUDA_TRY(it.f->ws2.ensure((size_t)P->ws_mv * rmax));
       x.xs = B.xs.p + xoff[i];
@@ -892,18 +1022,19 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
       x.ldws = P->ws_mv;
     }
   }
+  const bool persistent = use_pmv(L, &B.mv, dfres, (int)rmax);
   double res = 0.0;
   for (int32_t iter = 0;; ++iter) {
     CUDA_TRY(cudaMemsetAsync(B.rn2.p, 0, rtot * sizeof(double), st));
-    if (dfres)
+    if (dfres && !persistent)   // the persistent product splits B itself
       for (size_t i = 0; i < ni; ++i) {
         const Item& it = items[i];
         launch_df_split_cols(it.io.C, it.io.ldc, it.f->plan->tree_n[it.tree], it.io.r, B.xs.p + xoff[i], st);
         ++g_launches;
       }
     CUDA_TRY(B.mv.upload(ms, st));
-    if (dfres) run_matvec_df(L, B.mv.dev.p, (int)rmax, st);
-    else run_matvec(L, B.mv.dev.p, (int)rmax, st);
+    rc = dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, &B.mv) : run_matvec(L, B.mv.dev.p, (int)rmax, st, &B.mv);
+    if (rc) return rc;
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(B.h_rn2.p, B.rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
@@ -1171,7 +1302,7 @@ int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, d
   cudaStream_t st = (cudaStream_t)stream;
   // pageable source: staged by the driver before the call returns
   CUDA_TRY(cudaMemcpyAsync(dslot, &x, sizeof(Slot), cudaMemcpyHostToDevice, st));
-  run_matvec(h, dslot, (int)r, st);
+  run_matvec(h, dslot, (int)r, st);   // level kernels: the persistent product's state would be allocated
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -1274,6 +1405,10 @@ int hss_set_option(int32_t option, int64_t value) {
   }
   if (option == HSS_OPT_RESIDUAL_FP64) {
     g_residual_fp64 = value != 0;
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_LEVEL_PRODUCT) {
+    g_level_product = value != 0;
     return HSS_OK;
   }
   return fail(HSS_ERR_INVALID, "unknown option");

@@ -65,9 +65,13 @@ struct Slot {
   float2* ws2;
   const float2* gdf;
   const double* gbase;
+  // persistent product (hss_pmv.cu): the node array of this slot's plan and
+  // its per-node arrival counters (zero between launches)
+  const Node* nodes;
+  int32_t* sync;
 };
 
 // device status codes written into Slot::err
-enum { DEV_OK = 0, DEV_SINGULAR = 1, DEV_BAD = 2 };
+enum { DEV_OK = 0, DEV_SINGULAR = 1, DEV_BAD = 2, DEV_TIMEOUT = 3 };
 
 }  // namespace hss

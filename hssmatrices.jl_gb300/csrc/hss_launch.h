@@ -26,6 +26,28 @@ void launch_dfmv_up(const Task* t, int64_t ntasks, const Slot* s, int rmax, cuda
 void launch_dfmv_down(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
 void launch_dfmv_final(const Task* t, int64_t ntasks, const Slot* s, int rmax, cudaStream_t st);
 
+// Persistent product (hss_pmv.cu): the whole product of a forest in one
+// cooperative launch, FP64 (pairs = false) or double-float (pairs = true).
+// Shared-memory elements for leaves of <= nleaf columns and ranks <= kmax;
+// *mcap gets the part available for staged translators.
+size_t pmv_smem_elems(int nleaf, int kmax, int* mcap);
+bool pmv_fits(int nleaf, int mleaf, int kmax);
+// Column chunks of a product with rmax right-hand sides (0: too many for the
+// persistent product).  Tasks are (node, chunk) pairs: a launch over ntasks
+// non-root nodes has ntasks * chunks queue entries.
+int pmv_chunks(bool pairs, int rmax);
+// 32-bit words of launch state for that many queue entries (the caller zeroes
+// them once; the kernel leaves them zero; int2 entries are separate).
+int64_t pmv_state_words(int64_t entries);
+// Per-node counters: a plan holds nodes * pmv_sync_chunks() of them, zeroed.
+int pmv_sync_chunks();
+// ntasks = non-root nodes of all trees; the slots' nodes/sync must be set and
+// every sync counter zero; epoch must differ from every earlier launch on state.
+// [prefetch, prefetch + prefetch_bytes) (nullable) is brought into L2 first.
+cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks, int rmax,
+                       int nleaf, int kmax, uint32_t* state, int2* qtask, uint32_t epoch, const void* prefetch,
+                       int64_t prefetch_bytes, int device, cudaStream_t st);
+
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,

@@ -15,6 +15,7 @@
 //   final   C = alpha (P + U F) + beta Y  (rounded to FP64 once), column norms
 #include <cuda_runtime.h>
 #include <cstdint>
+#include "hss_df.cuh"
 #include "hss_internal.h"
 #include "hss_launch.h"
 
@@ -24,39 +25,6 @@ namespace {
 
 constexpr int DT = 256;
 constexpr int DRC = 8;    // right-hand sides per thread block
-
-// acc += a * x in double-float (no contraction: every step is rounded once).
-__device__ __forceinline__ void df_fma(float& sh, float& sl, float2 a, float2 x) {
-  const float p = __fmul_rn(a.x, x.x);
-  float e = __fmaf_rn(a.x, x.x, -p);
-  e = __fmaf_rn(a.x, x.y, e);
-  e = __fmaf_rn(a.y, x.x, e);
-  const float t = __fadd_rn(sh, p);
-  const float bp = __fsub_rn(t, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-  sh = t;
-  sl = __fadd_rn(sl, __fadd_rn(err, e));
-}
-
-// (sh, sl) += (bh, bl)
-__device__ __forceinline__ void df_add(float& sh, float& sl, float bh, float bl) {
-  const float t = __fadd_rn(sh, bh);
-  const float bp = __fsub_rn(t, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(bh, bp));
-  sh = t;
-  sl = __fadd_rn(sl, __fadd_rn(err, bl));
-}
-
-__device__ __forceinline__ float2 df_norm(float sh, float sl) {
-  const float s = __fadd_rn(sh, sl);
-  return make_float2(s, __fsub_rn(sl, __fsub_rn(s, sh)));
-}
-
-__device__ __forceinline__ float2 split_d(double x) {
-  const float h = __double2float_rn(x);
-  const float l = __double2float_rn(x - (double)h);
-  return make_float2(h, l);
-}
 
 __device__ __forceinline__ const float2* dfp(const Slot& sl, const double* p) {
   return sl.gdf + (p - sl.gbase);

@@ -206,8 +206,11 @@ int64_t hss_launch_counter(void);
  * kernel against it); 0 (default) picks the on-chip kernel where it fits.
  * HSS_OPT_RESIDUAL_FP64 = 1 forms the refinement residual of an FP32 factor
  * with the native FP64 product instead of the default double-float product
- * on the FP32 pipe (~48-bit, made for GB300's low FP64 rate). */
-enum { HSS_OPT_GENERIC_FACTOR = 1, HSS_OPT_RESIDUAL_FP64 = 2 };
+ * on the FP32 pipe (~48-bit, made for GB300's low FP64 rate).
+ * HSS_OPT_LEVEL_PRODUCT = 1 runs every product with one kernel launch per
+ * tree level instead of the default single persistent launch (leaves up to
+ * 512 columns, ranks up to 64); used to test the two against each other. */
+enum { HSS_OPT_GENERIC_FACTOR = 1, HSS_OPT_RESIDUAL_FP64 = 2, HSS_OPT_LEVEL_PRODUCT = 3 };
 int hss_set_option(int32_t option, int64_t value);
 
 const char* hss_last_error(void);

@@ -1,0 +1,136 @@
+"""GPU: the persistent product (one cooperative launch per product) against the
+level-by-level product and the CPU oracle.
+
+Tolerances: FP64 products 1e-12 relative (2-norm) against the oracle and 1e-13
+between the two GPU paths (same arithmetic, different summation order); the
+persistent product is deterministic, so repeated calls agree bit for bit.  The
+double-float refinement residual of an FP32 factorization must bring the true
+(oracle) residual to 1e-10 with either product.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, unpack_tree
+
+pytestmark = pytest.mark.gpu
+
+HSS_OPT_LEVEL_PRODUCT = 3
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _tree(pkg, orc, name):
+    g = load_golden(name)
+    h = unpack_tree(g["table"], g["packed"], orc)
+    return g, h, pkg.HssMatrix.from_tree(h)
+
+
+def _both(lib, fn):
+    """fn() with the persistent product (default) and with the level product."""
+    out = []
+    for level in (0, 1):
+        assert lib.hss_set_option(HSS_OPT_LEVEL_PRODUCT, level) == 0
+        try:
+            out.append(fn())
+        finally:
+            lib.hss_set_option(HSS_OPT_LEVEL_PRODUCT, 0)
+    return out
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("r", [1, 3, 8, 13, 40])
+def test_products_agree(pkg, lib, orc, name, r):
+    g, h, A = _tree(pkg, orc, name)
+    n = g["x"].shape[0]
+    x = np.random.default_rng(r).standard_normal((n, r))
+    ref = orc.matmul(h, x)
+    p, l = _both(lib, lambda: pkg.matmul(A, x))
+    assert rel(p, ref) <= 1e-12
+    assert rel(p, l) <= 1e-13
+
+
+@pytest.mark.parametrize("name", ["synthetic_uneven", "synthetic_unbalanced", "single_leaf"])
+def test_alpha_beta_agree(pkg, lib, orc, name):
+    """mul!(C, hssA, B, alpha, beta) (src/matmul.jl:18-28) on both paths."""
+    g, h, A = _tree(pkg, orc, name)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((g["x"].shape[0], 9))
+    C0 = np.asfortranarray(rng.standard_normal((g["y"].shape[0], 9)))
+    ref = orc.matmul(h, x, 0.5, -2.0, C0)
+
+    def run():
+        C = C0.copy(order="F")
+        pkg.mul(C, A, x, 0.5, -2.0)
+        return C
+
+    p, l = _both(lib, run)
+    assert rel(p, ref) <= 1e-12 and rel(p, l) <= 1e-13
+
+
+def test_repeated_calls_bitwise(pkg, lib, orc):
+    """Launch state resets itself: ten products in a row give identical bits, and
+    each product is one kernel launch."""
+    g, h, A = _tree(pkg, orc, "synthetic_perfect")
+    dev = A.device()
+    x = np.random.default_rng(0).standard_normal((g["x"].shape[0], 5))
+    first = dev.matmul_host(x)
+    c0 = lib.hss_launch_counter()
+    for _ in range(10):
+        assert np.array_equal(dev.matmul_host(x), first)
+    assert lib.hss_launch_counter() - c0 == 10
+    assert rel(first, orc.matmul(h, x)) <= 1e-12
+
+
+def test_forest_agrees(pkg, lib, orc):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(4)
+    trees = [orc.synthetic_hss(n, ls, k, rng) for n, ls, k in
+             [(1152, 64, 48), (640, 128, 20), (2001, 64, 16), (129, 64, 8), (64, 64, 8)]]
+    dev = pkg.DeviceHss.from_trees([pkg.HssMatrix.from_tree(t) for t in trees])
+    rs = [1, 4, 0, 11, 3]
+    xs = [rng.standard_normal((t.size()[1], r)) for t, r in zip(trees, rs)]
+
+    def run():
+        dX = [torch.from_numpy(np.ascontiguousarray(x.T)).cuda() for x in xs]
+        dY = [torch.zeros((x.shape[1], t.size()[0]), dtype=torch.float64, device="cuda") for x, t in zip(xs, trees)]
+        dev.matmul_batch_device(dX, [x.shape[0] for x in xs], rs, dY, [t.size()[0] for t in trees])
+        torch.cuda.synchronize()
+        return [y.cpu().numpy().T for y in dY]
+
+    p, l = _both(lib, run)
+    for t, x, a, b in zip(trees, xs, p, l):
+        if x.shape[1] == 0:
+            continue
+        ref = orc.matmul(t, x)
+        assert rel(a, ref) <= 1e-12 and rel(a, b) <= 1e-13
+
+
+@pytest.mark.parametrize("name", ["synthetic_perfect", "synthetic_uneven", "cauchy2001_compress"])
+def test_refinement_with_both_products(pkg, lib, orc, name):
+    g, h, A = _tree(pkg, orc, name)
+    Af = orc.full(h)
+
+    def run():
+        st = {}
+        z = pkg.ldiv(A, g["b"], precision="fp32", tol=1e-10, maxit=30, stats=st)
+        return z, st
+
+    for z, st in _both(lib, run):
+        assert st["converged"] and st["residual"] <= 1e-10
+        res = np.linalg.norm(g["b"] - Af @ z, axis=0) / np.linalg.norm(g["b"], axis=0)
+        assert res.max() <= 2e-10
+
+
+def test_full_size_r1(pkg, lib, orc):
+    """n = 65536, leafsize 128, k = 32 at one right-hand side (the bandwidth-bound
+    product): oracle agreement and linearity."""
+    rng = np.random.default_rng(3)
+    A = pkg.synthetic_hss(65536, 128, 32, rng)
+    h = orc.synthetic_hss(65536, 128, 32, np.random.default_rng(3))
+    x = rng.standard_normal((65536, 1))
+    y = rng.standard_normal((65536, 1))
+    Ax = pkg.matmul(A, x)
+    assert rel(Ax, orc.matmul(h, x)) <= 1e-12
+    assert rel(pkg.matmul(A, x - 3 * y), Ax - 3 * pkg.matmul(A, y)) <= 1e-13
