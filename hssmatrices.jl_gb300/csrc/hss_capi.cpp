@@ -676,7 +676,7 @@ void run_factor(const Levels& L, const Slot* slots, cudaStream_t st) {
                            (size_t)g.c1nr * g.c1v + (size_t)g.c2nr * g.c2v + (size_t)g.c1mr * g.c2v +
                            (size_t)g.c2mr * g.c1v;
       if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra))
-        launch_ulv_factor_fast<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, extra, st);
+        launch_ulv_factor_fast<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, g.kvmax, extra, st);
       else
         launch_ulv_factor<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
     });

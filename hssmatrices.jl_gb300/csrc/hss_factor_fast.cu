@@ -149,10 +149,443 @@ __device__ void lu_smem(T* A, int m, int ld, int32_t* piv, int32_t* err, T* bv, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Blocked FP32 reduction (P1 + P2 of the FP32 factorization)
+//
+// The same reflectors, in the same order, as the unblocked path above (up to
+// rounding), but each reflector touches only its panel of BP columns (QL) or
+// rows (LQ); the rest of the block is updated once per panel with the compact
+// WY form of the panel's product, H(a) H(a+1) ... H(b-1) = I - Y T Y^T, as
+// shared-memory FP32 GEMMs.  T (forward xLARFT) is never formed: for orthogonal
+// reflectors (tau_j = 2 / y_j^T y_j) its inverse is S = diag(1/tau) + the
+// strictly upper part of the Gram matrix Y^T Y, so every product with T or T^T
+// is a triangular substitution with S (a zero tau gives a zero row, as in T):
+//   QL (geqlf!/ormql!, src/ulvfactor.jl:39-42): Q^T C = H(c0) ... H(c1-1) C
+//       (generation order c = c1-1 .. c0) = C - Y (T (Y^T C)) for C = D and the
+//       U columns left of the panel;
+//   LQ (gelqf!/ormlq!, :44-50): C Q^T over rows i0..i1-1 = C H(i0) ... H(i1-1)
+//       = C - (C Y^T) T Y for the rows below the panel, and Q V =
+//       H(i1-1) ... H(i0) V = V - Y^T (T^T (Y V)).
+// Panel threads: a half-warp per column (QL) or row (LQ), 8 entries per thread,
+// so every reduction of a reflector step is a 16-lane shuffle; one barrier per
+// step (the owner of the next reflector applies the current one first).
+// ---------------------------------------------------------------------------
+
+constexpr int BP = 32;                    // panel width
+constexpr int YP = 132;                   // ld of the reflector-major copy of Y (>= 128, multiple of 4)
+constexpr int KP = 36;                    // ld of the row-major copy of Y (>= BP, multiple of 4)
+constexpr int XP = 132;                   // ld of the GEMM intermediate
+constexpr int GP = 33;                    // ld of the Gram matrix and T
+constexpr size_t kBlkElems = (size_t)BP * YP + (size_t)FMAX * KP + (size_t)BP * XP + 2 * (size_t)BP * GP + 2 * BP;
+
+// xLARFG from alpha and the squared tail norm, FP32 panels: the norm as
+// sqrt(alpha^2 + ss) (hypot only when that overflows) and correctly rounded
+// reciprocals instead of divisions.
+__device__ __forceinline__ void larfg_f32(float alpha, float ss, float& beta, float& tau, float& scal) {
+  if (ss == 0.f) {
+    tau = 0.f;
+    beta = alpha;
+    scal = 1.f;
+    return;
+  }
+  const float t = fmaf(alpha, alpha, ss);
+  const float nrm = t <= 3.0e38f ? sqrtf(t) : hypotf(alpha, sqrtf(ss));
+  beta = -copysignf(nrm, alpha);
+  tau = (beta - alpha) * __frcp_rn(beta);
+  scal = __frcp_rn(alpha - beta);
+}
+
+__device__ __forceinline__ float hsum(float v, unsigned m) {
+  v += __shfl_xor_sync(m, v, 8);
+  v += __shfl_xor_sync(m, v, 4);
+  v += __shfl_xor_sync(m, v, 2);
+  v += __shfl_xor_sync(m, v, 1);
+  return v;
+}
+
+__device__ __forceinline__ void ld8(float (&v)[8], const float* p) {   // p 16-byte aligned
+  const float4 a = reinterpret_cast<const float4*>(p)[0];
+  const float4 b = reinterpret_cast<const float4*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void st8(float* p, const float (&v)[8]) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+  reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+// Strictly upper part of the Gram matrix: G(a, b) = sum_{r < len} Yt[r*KP + a] Yt[r*KP + b]
+// for a < b < nb.  Ends with a barrier.
+__device__ void blk_gram(int nb, int len, const float* Yt, float* G) {
+  for (int o = threadIdx.x; o < nb * nb; o += FT) {
+    const int b = o % nb, a = o / nb;
+    if (a >= b) continue;
+    float s0 = 0.f, s1 = 0.f;
+    int r = 0;
+    for (; r + 1 < len; r += 2) {
+      s0 = fmaf(Yt[r * KP + a], Yt[r * KP + b], s0);
+      s1 = fmaf(Yt[(r + 1) * KP + a], Yt[(r + 1) * KP + b], s1);
+    }
+    if (r < len) s0 = fmaf(Yt[r * KP + a], Yt[r * KP + b], s0);
+    G[a * GP + b] = s0 + s1;
+  }
+  __syncthreads();
+}
+
+// x <- T x: back substitution S x' = x, S = diag(1/tau) + strictly upper G.
+__device__ __forceinline__ void t_times(float (&x)[BP], int nb, const float* G, const float* tau) {
+#pragma unroll
+  for (int i = BP - 1; i >= 0; --i) {
+    if (i < nb) {
+      float s = x[i];
+#pragma unroll
+      for (int l = i + 1; l < BP; ++l)
+        if (l < nb) s = fmaf(-G[i * GP + l], x[l], s);
+      x[i] = s * tau[i];
+    }
+  }
+}
+
+// x <- T^T x (equivalently a row vector times T): forward substitution S^T x' = x.
+__device__ __forceinline__ void tt_times(float (&x)[BP], int nb, const float* G, const float* tau) {
+#pragma unroll
+  for (int a = 0; a < BP; ++a) {
+    if (a < nb) {
+      float s = x[a];
+#pragma unroll
+      for (int l = 0; l < a; ++l) s = fmaf(-G[l * GP + a], x[l], s);
+      x[a] = s * tau[a];
+    }
+  }
+}
+
+// C (rows 0..m-1, N columns, ld ldc) <- C - Y (T (Y^T C)), Y = Yc (reflector-major,
+// nb x m) / Yt (row-major, m x nb).  Ends with a barrier.
+__device__ void blk_apply_left(float* C, int ldc, int m, int N, int nb, const float* Yc, const float* Yt,
+                               const float* G, const float* tau, float* X) {
+  const int tid = threadIdx.x;
+  const int j = tid & 127, cb = tid >> 7;   // column, block of 8 reflectors
+  // X = Y^T C (nb x N)
+  if (j < N && cb * 8 < nb) {
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int r = 0; r < m; ++r) {
+      const float c = C[r + j * ldc];
+      float y[8];
+      ld8(y, Yt + r * KP + cb * 8);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = fmaf(y[q], c, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (cb * 8 + q < nb) X[(cb * 8 + q) * XP + j] = acc[q];
+  }
+  __syncthreads();
+  // X = T X, column by column
+  if (j < N && cb == 0) {
+    float x[BP];
+#pragma unroll
+    for (int c = 0; c < BP; ++c) x[c] = c < nb ? X[c * XP + j] : 0.f;
+    t_times(x, nb, G, tau);
+#pragma unroll
+    for (int c = 0; c < BP; ++c)
+      if (c < nb) X[c * XP + j] = x[c];
+  }
+  __syncthreads();
+  // C -= Y X
+  if (j < N) {
+    for (int r0 = cb * 8; r0 < m; r0 += 32) {
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int c = 0; c < nb; ++c) {
+        const float xv = X[c * XP + j];
+        float y[8];
+        ld8(y, Yc + c * YP + r0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = fmaf(y[q], xv, acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (r0 + q < m) C[r0 + q + j * ldc] -= acc[q];
+    }
+  }
+  __syncthreads();
+}
+
+// Rows r0..m-1 of C (n columns, ld ldc) <- C - (C Y^T) T Y with Y = Yc (nb x n,
+// reflector-major) / Yt (n x nb).  Ends with a barrier.
+__device__ void blk_apply_right(float* C, int ldc, int r0, int m, int n, int nb, const float* Yc, const float* Yt,
+                                const float* G, const float* tau, float* X) {
+  const int tid = threadIdx.x;
+  const int r = r0 + (tid & 127), ab = tid >> 7;
+  const bool act = r < m && ab * 8 < nb;
+  // X = C Y^T ((m - r0) x nb), stored reflector-major
+  if (act) {
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int col = 0; col < n; ++col) {
+      const float c = C[r + col * ldc];
+      float y[8];
+      ld8(y, Yt + col * KP + ab * 8);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = fmaf(c, y[q], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (ab * 8 + q < nb) X[(ab * 8 + q) * XP + (r - r0)] = acc[q];
+  }
+  __syncthreads();
+  // X = X T, row by row
+  if (r < m && ab == 0) {
+    float x[BP];
+#pragma unroll
+    for (int a = 0; a < BP; ++a) x[a] = a < nb ? X[a * XP + (r - r0)] : 0.f;
+    tt_times(x, nb, G, tau);
+#pragma unroll
+    for (int a = 0; a < BP; ++a)
+      if (a < nb) X[a * XP + (r - r0)] = x[a];
+  }
+  __syncthreads();
+  // C -= X Y
+  if (r < m) {
+    for (int col0 = ab * 8; col0 < n; col0 += 32) {
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int a = 0; a < nb; ++a) {
+        const float xv = X[a * XP + (r - r0)];
+        float y[8];
+        ld8(y, Yc + a * YP + col0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = fmaf(xv, y[q], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (col0 + q < n) C[r + (col0 + q) * ldc] -= acc[q];
+    }
+  }
+  __syncthreads();
+}
+
+// V (n x kv, ld ldv) <- V - Y^T (T^T (Y V)).  Ends with a barrier.
+__device__ void blk_apply_v(float* V, int ldv, int n, int kv, int nb, const float* Yc, const float* Yt,
+                            const float* G, const float* tau, float* X) {
+  const int tid = threadIdx.x;
+  // Z = Y V (nb x kv): thread (column c, block of 4 reflectors)
+  for (int o = tid; o < kv * 8; o += FT) {
+    const int c = o % kv, ab = o / kv;
+    if (ab * 4 >= nb) continue;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int col = 0; col < n; ++col) {
+      const float v = V[col + c * ldv];
+      const float4 y = *reinterpret_cast<const float4*>(Yt + col * KP + ab * 4);
+      acc[0] = fmaf(y.x, v, acc[0]);
+      acc[1] = fmaf(y.y, v, acc[1]);
+      acc[2] = fmaf(y.z, v, acc[2]);
+      acc[3] = fmaf(y.w, v, acc[3]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (ab * 4 + q < nb) X[(ab * 4 + q) * XP + c] = acc[q];
+  }
+  __syncthreads();
+  // Z = T^T Z, column by column
+  if (tid < kv) {
+    float z[BP];
+#pragma unroll
+    for (int a = 0; a < BP; ++a) z[a] = a < nb ? X[a * XP + tid] : 0.f;
+    tt_times(z, nb, G, tau);
+#pragma unroll
+    for (int a = 0; a < BP; ++a)
+      if (a < nb) X[a * XP + tid] = z[a];
+  }
+  __syncthreads();
+  // V -= Y^T Z: thread (row col, block of 8 columns of V)
+  const int col = tid & 127, cb = tid >> 7;
+  if (col < n) {
+    for (int c0 = cb * 8; c0 < kv; c0 += 32) {
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int a = 0; a < nb; ++a) {
+        const float y = Yc[a * YP + col];
+        float z[8];
+        ld8(z, X + a * XP + c0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = fmaf(y, z[q], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (c0 + q < kv) V[col + (c0 + q) * ldv] -= acc[q];
+    }
+  }
+  __syncthreads();
+}
+
+// P1 + P2 of one node in FP32 (see above).  In: sD (m x n) and sU (m x ku),
+// ld LDD, and sV (n x kv, ld LDV) in shared memory.  Out: the same blocks in
+// shared memory plus tau vectors and the transposed LQ reflectors in global
+// memory (tq, tl, gQt).
+__device__ void ulv_reduce_blocked(const Node& nd, float* sD, float* sU, int LDD, float* sV, int LDV, float* sv,
+                                   float* stau, float* blk, float* tq, float* tl, float* gQt) {
+  const int m = nd.m, n = nd.n, k = nd.k, mk = nd.mk, kv = nd.kv;
+  const int tid = threadIdx.x;
+  const unsigned hm = 0xFFFFu << (tid & 16);   // this thread's half-warp
+  const int hl = tid & 16;                     // its first lane
+  float* Yc = blk;                             // BP x YP
+  float* Yt = Yc + BP * YP;                    // FMAX x KP
+  float* X = Yt + FMAX * KP;                   // BP x XP
+  float* G = X + BP * XP;                      // BP x GP (strictly upper part used)
+  float* ptau = G + 2 * BP * GP;               // BP taus of the panel
+
+  // ---- P1: QL of U, panels of BP columns from the last -----------------------
+  {
+    const int cc = tid >> 4, rs = tid & 15, r0 = rs * 8;
+    for (int c1 = k; c1 > 0; c1 -= BP) {
+      const int c0 = max(0, c1 - BP), nb = c1 - c0;
+      const int col = c0 + cc;
+      float u[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) u[l] = (cc < nb && r0 + l < m) ? sU[r0 + l + col * LDD] : 0.f;
+      auto gen = [&](int c, int buf) {   // the 16 threads of column c
+        const int p = mk + c;
+        float ss = 0.f, mine = 0.f;
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const int row = r0 + l;
+          if (row < p) ss = fmaf(u[l], u[l], ss);
+          if (row == p) mine = u[l];
+        }
+        ss = hsum(ss, hm);
+        const float alpha = __shfl_sync(hm, mine, hl + (p >> 3));
+        float beta, tau, sc;
+        larfg_f32(alpha, ss, beta, tau, sc);
+        float v[8];
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const int row = r0 + l;
+          if (row < p && tau != 0.f) u[l] *= sc;
+          if (row == p) u[l] = beta;
+          v[l] = row < p ? u[l] : (row == p ? 1.f : 0.f);
+        }
+        st8(sv + buf * SVLEN + r0, v);
+        if (rs == 0) {
+          stau[buf] = tau;
+          ptau[c - c0] = tau;
+          tq[c] = tau;
+        }
+      };
+      if (cc == nb - 1) gen(c1 - 1, 0);
+      __syncthreads();
+      for (int c = c1 - 1; c >= c0; --c) {
+        const int cur = (c1 - 1 - c) & 1;
+        const float tau = stau[cur];
+        if (cc < c - c0 && tau != 0.f) {
+          float v[8];
+          ld8(v, sv + cur * SVLEN + r0);
+          float w = 0.f;
+#pragma unroll
+          for (int l = 0; l < 8; ++l) w = fmaf(v[l], u[l], w);
+          w = hsum(w, hm) * tau;
+#pragma unroll
+          for (int l = 0; l < 8; ++l) u[l] = fmaf(-w, v[l], u[l]);
+        }
+        if (c > c0 && cc == c - 1 - c0) gen(c - 1, cur ^ 1);
+        __syncthreads();
+      }
+      // write back the panel and its reflectors (Y zero below each pivot)
+      if (cc < nb) {
+        const int p = mk + col;
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const int row = r0 + l;
+          if (row < m) {
+            sU[row + col * LDD] = u[l];
+            const float y = row < p ? u[l] : (row == p ? 1.f : 0.f);
+            Yc[cc * YP + row] = y;
+            Yt[row * KP + cc] = y;
+          }
+        }
+      }
+      __syncthreads();
+      blk_gram(nb, m, Yt, G);
+      blk_apply_left(sD, LDD, m, n, nb, Yc, Yt, G, ptau, X);
+      if (c0 > 0) blk_apply_left(sU, LDD, m, c0, nb, Yc, Yt, G, ptau, X);
+    }
+  }
+
+  // ---- P2: LQ of D[0:mk, :], panels of BP rows ------------------------------
+  {
+    const int rr = tid >> 4, cs = tid & 15, q0 = cs * 8;
+    for (int i0 = 0; i0 < mk; i0 += BP) {
+      const int i1 = min(mk, i0 + BP), nb = i1 - i0;
+      const int row = i0 + rr;
+      float d[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) d[l] = (rr < nb && q0 + l < n) ? sD[row + (q0 + l) * LDD] : 0.f;
+      auto gen = [&](int i, int buf) {   // the 16 threads of row i
+        float ss = 0.f, mine = 0.f;
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const int col = q0 + l;
+          if (col > i) ss = fmaf(d[l], d[l], ss);
+          if (col == i) mine = d[l];
+        }
+        ss = hsum(ss, hm);
+        const float alpha = __shfl_sync(hm, mine, hl + (i >> 3));
+        float beta, tau, sc;
+        larfg_f32(alpha, ss, beta, tau, sc);
+        float v[8];
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const int col = q0 + l;
+          if (col > i && tau != 0.f) d[l] *= sc;
+          if (col == i) d[l] = beta;
+          v[l] = col < i ? 0.f : (col == i ? 1.f : d[l]);
+        }
+        st8(sv + buf * SVLEN + q0, v);
+        if (cs == 0) {
+          stau[buf] = tau;
+          ptau[i - i0] = tau;
+          tl[i] = tau;
+        }
+      };
+      if (rr == 0) gen(i0, 0);
+      __syncthreads();
+      for (int i = i0; i < i1; ++i) {
+        const int cur = (i - i0) & 1;
+        const float tau = stau[cur];
+        if (rr > i - i0 && rr < nb && tau != 0.f) {
+          float v[8];
+          ld8(v, sv + cur * SVLEN + q0);
+          float w = 0.f;
+#pragma unroll
+          for (int l = 0; l < 8; ++l) w = fmaf(v[l], d[l], w);
+          w = hsum(w, hm) * tau;
+#pragma unroll
+          for (int l = 0; l < 8; ++l) d[l] = fmaf(-w, v[l], d[l]);
+        }
+        if (i + 1 < i1 && rr == i + 1 - i0) gen(i + 1, cur ^ 1);
+        __syncthreads();
+      }
+      if (rr < nb) {
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const int col = q0 + l;
+          if (col < n) {
+            sD[row + col * LDD] = d[l];
+            const float y = col < row ? 0.f : (col == row ? 1.f : d[l]);
+            Yc[rr * YP + col] = y;
+            Yt[col * KP + rr] = y;
+            gQt[col + (int64_t)row * n] = y;
+          }
+        }
+      }
+      __syncthreads();
+      blk_gram(nb, n, Yt, G);
+      if (i1 < m) blk_apply_right(sD, LDD, i1, m, n, nb, Yc, Yt, G, ptau, X);
+      if (kv > 0) blk_apply_v(sV, LDV, n, kv, nb, Yc, Yt, G, ptau, X);
+    }
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __restrict__ tasks,
                                                                 const Slot* __restrict__ slots,
-                                                                int LDD, int nmax, int kumax) {
+                                                                int LDD, int nmax, int kumax, int kvmax,
+                                                                int extra) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ T red[FW];
   __shared__ T scal3[3];
@@ -179,9 +612,22 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
 
   // ---- P0: load or assemble the node's block --------------------------------
   if (nd.leaf) {
-    for (int e = tid; e < m * n; e += FT) sD[(e % m) + (e / m) * LDD] = (T)nd.D[e];
+    // column j by warp, rows by lane: coalesced, no index division
+    const int lane = tid & 31, warp = tid >> 5;
+    const double* gD0 = nd.D;
+    const double* gU0 = nd.U;
+#pragma unroll 2
+    for (int j = warp; j < n; j += FW) {
+      const double* col = gD0 + (int64_t)j * m;
+#pragma unroll 4
+      for (int i = lane; i < m; i += 32) sD[i + j * LDD] = (T)__ldg(col + i);
+    }
     if (!nd.root)
-      for (int e = tid; e < m * ku; e += FT) sU[(e % m) + (e / m) * LDD] = (T)nd.U[e];
+      for (int j = warp; j < ku; j += FW) {
+        const double* col = gU0 + (int64_t)j * m;
+#pragma unroll 4
+        for (int i = lane; i < m; i += 32) sU[i + j * LDD] = (T)__ldg(col + i);
+      }
   } else {
     // Merge (src/ulvfactor.jl:74-79).  Generator blocks are converted to T
     // once and, with the children's reduced U and V, staged in shared memory.
@@ -313,85 +759,33 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
   T* tq = fb + nd.ftq;
   T* tl = fb + nd.ftl;
 
+  if constexpr (sizeof(T) == 4) {
+    // FP32: blocked reduction with the block and V in shared memory
+    const int LDV = nmax | 1;
+    T* sVb = sx + smem_align4((size_t)extra);
+    T* blk = sVb + smem_align4((size_t)LDV * (kvmax > 0 ? kvmax : 1));
+    {
+      const int lane = tid & 31, warp = tid >> 5;
+      const double* gV0 = nd.V;
+      for (int c = warp; c < kv; c += FW)
+#pragma unroll 4
+        for (int row = lane; row < n; row += 32)
+          sVb[row + c * LDV] = nd.leaf ? (T)__ldg(gV0 + row + (int64_t)c * n) : gV[row + (int64_t)c * n];
+    }
+    __syncthreads();
+    ulv_reduce_blocked(nd, sD, sU, LDD, sVb, LDV, sv, stau, blk, tq, tl, fb + nd.fQt);
+    for (int e = tid; e < m * n; e += FT) gD[e] = sD[(e % m) + (e / m) * LDD];
+    for (int e = tid; e < m * ku; e += FT) gU[e] = sU[(e % m) + (e / m) * LDD];
+    for (int e = tid; e < n * kv; e += FT) gV[e] = sVb[(e % n) + (e / n) * LDV];
+  } else {
+
   // ---- P1: QL of U, Q^T applied to D -------------------------------------------
   // Broadcast vectors are double-buffered: while every thread applies reflector
   // c, the owner of the next column (already updated) builds reflector c-1, so
   // each step needs one barrier.
   T* sv0 = sv;
   T* sv1 = sv + SVLEN;
-  if constexpr (sizeof(T) == 4) {
-    // FP32: column-owner registers.  Thread (column cl, quarter q) holds rows
-    // 32q..32q+31 of D[:, cl] and, for cl < ku, of U[:, cl].
-    const int cl = tid >> 2, q = tid & 3, r0 = q * 32;
-    const unsigned gm = 0xFu << ((tid & 31) & ~3);
-    T dc[32], uc[32];
-#pragma unroll
-    for (int l = 0; l < 32; ++l) {
-      const int row = r0 + l;
-      dc[l] = (row < m && cl < n) ? sD[row + cl * LDD] : T(0);
-      uc[l] = (row < m && cl < ku) ? sU[row + cl * LDD] : T(0);
-    }
-    auto ql_reflector = [&](int c, T* buf, int slot) {   // called by the 4 owners of U[:, c]
-      const int p = mk + c;
-      T s4[4] = {T(0), T(0), T(0), T(0)}, mine = T(0);
-#pragma unroll
-      for (int l = 0; l < 32; ++l) {
-        const int row = r0 + l;
-        if (row < p) s4[l & 3] += uc[l] * uc[l];
-        if (row == p) mine = uc[l];
-      }
-      T ss = (s4[0] + s4[1]) + (s4[2] + s4[3]);
-      ss += __shfl_xor_sync(gm, ss, 1);
-      ss += __shfl_xor_sync(gm, ss, 2);
-      const T alpha = __shfl_sync(gm, mine, p >> 5, 4);
-      T beta, tau, sc;
-      larfg(alpha, ss, beta, tau, sc);
-#pragma unroll
-      for (int l = 0; l < 32; ++l) {
-        const int row = r0 + l;
-        if (row < p && tau != T(0)) uc[l] *= sc;
-        if (row == p) uc[l] = beta;
-        buf[vp(row)] = row < p ? uc[l] : (row == p ? T(1) : T(0));
-      }
-      if (q == 0) { stau[slot] = tau; tq[c] = tau; }
-    };
-    if (cl == k - 1) ql_reflector(k - 1, sv0, 0);
-    __syncthreads();
-    for (int c = k - 1; c >= 0; --c) {
-      const int cur = (k - 1 - c) & 1;
-      const T* svc = cur ? sv1 : sv0;
-      const T tau = stau[cur];
-      if (tau != T(0)) {
-        T vq[32];
-        load_quarter(vq, svc, q);
-        if (cl < n) {
-          T w = dot32(dc, vq);
-          w += __shfl_xor_sync(gm, w, 1);
-          w += __shfl_xor_sync(gm, w, 2);
-          w *= tau;
-#pragma unroll
-          for (int l = 0; l < 32; ++l) dc[l] -= w * vq[l];
-        }
-        if (cl < c) {
-          T w = dot32(uc, vq);
-          w += __shfl_xor_sync(gm, w, 1);
-          w += __shfl_xor_sync(gm, w, 2);
-          w *= tau;
-#pragma unroll
-          for (int l = 0; l < 32; ++l) uc[l] -= w * vq[l];
-        }
-      }
-      if (c >= 1 && cl == c - 1) ql_reflector(c - 1, cur ? sv0 : sv1, cur ^ 1);
-      __syncthreads();
-    }
-#pragma unroll
-    for (int l = 0; l < 32; ++l) {
-      const int row = r0 + l;
-      if (row < m && cl < ku) gU[row + (int64_t)cl * m] = uc[l];
-      if (row < m && cl < n) sD[row + cl * LDD] = dc[l];
-    }
-    __syncthreads();
-  } else {
+  {
     // FP64: the working block stays in shared memory; one thread per column
     // and row quarter, partial dot products combined through shared memory.
     const int cs = tid & 127, rq = tid >> 7, r0 = rq * 32;
@@ -562,40 +956,44 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
       if (c < kv && row < n) gV[row + (int64_t)c * n] = vv[h][r];
     }
   }
+  }
 }
 
 }  // namespace
 
 template <typename T>
-size_t factor_fast_smem(int mmax, int nmax, int kumax, size_t extra) {
+size_t factor_fast_smem(int mmax, int nmax, int kumax, int kvmax, size_t extra) {
   const int LDD = mmax | 1;
-  return (smem_align4((size_t)LDD * nmax) + smem_align4((size_t)LDD * (kumax > 0 ? kumax : 1)) + 4 * PART_COLS +
-          2 * SVLEN + extra) *
-         sizeof(T);
+  size_t e = smem_align4((size_t)LDD * nmax) + smem_align4((size_t)LDD * (kumax > 0 ? kumax : 1)) + 4 * PART_COLS +
+             2 * SVLEN + smem_align4(extra);
+  if (sizeof(T) == 4) e += smem_align4((size_t)(nmax | 1) * (kvmax > 0 ? kvmax : 1)) + kBlkElems;
+  return e * sizeof(T);
 }
 
 template <typename T>
 bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra) {
   return mmax <= FMAX && nmax <= FMAX && kumax <= FKMAX && kvmax <= FKMAX &&
-         factor_fast_smem<T>(mmax, nmax, kumax, extra) <= kFastSmemCap;
+         factor_fast_smem<T>(mmax, nmax, kumax, kvmax, extra) <= kFastSmemCap;
 }
 
 template <typename T>
-void launch_ulv_factor_fast(const Task* t, int64_t nt, const Slot* s, int mmax, int nmax, int kumax,
+void launch_ulv_factor_fast(const Task* t, int64_t nt, const Slot* s, int mmax, int nmax, int kumax, int kvmax,
                             size_t extra, cudaStream_t st) {
   if (nt <= 0) return;
-  const size_t smem = factor_fast_smem<T>(mmax, nmax, kumax, extra);
+  const size_t smem = factor_fast_smem<T>(mmax, nmax, kumax, kvmax, extra);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(ulv_factor_fast_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmemCap);
     attr_set = true;
   }
-  ulv_factor_fast_kernel<T><<<(unsigned)nt, FT, smem, st>>>(t, s, mmax | 1, nmax, kumax);
+  ulv_factor_fast_kernel<T><<<(unsigned)nt, FT, smem, st>>>(t, s, mmax | 1, nmax, kumax, kvmax, (int)extra);
 }
 
 template bool factor_fast_fits<double>(int, int, int, int, size_t);
 template bool factor_fast_fits<float>(int, int, int, int, size_t);
-template void launch_ulv_factor_fast<double>(const Task*, int64_t, const Slot*, int, int, int, size_t, cudaStream_t);
-template void launch_ulv_factor_fast<float>(const Task*, int64_t, const Slot*, int, int, int, size_t, cudaStream_t);
+template void launch_ulv_factor_fast<double>(const Task*, int64_t, const Slot*, int, int, int, int, size_t,
+                                             cudaStream_t);
+template void launch_ulv_factor_fast<float>(const Task*, int64_t, const Slot*, int, int, int, int, size_t,
+                                            cudaStream_t);
 
 }  // namespace hss

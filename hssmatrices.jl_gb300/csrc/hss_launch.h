@@ -56,7 +56,7 @@ void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, 
 template <typename T>
 bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra);
 template <typename T>
-void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax,
+void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax, int kvmax,
                             size_t extra, cudaStream_t st);
 // Register-resident solve sweeps for nodes with m, n <= 256 (hss_solve.cu).
 bool solve_reg_fits(int mmax, int nmax);
