@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -124,6 +125,7 @@ void traced(int kind, int64_t cnt, cudaStream_t st, F&& launch) {
 }  // namespace
 
 struct hss_plan_s {
+  uint64_t serial = 0;                  // unique per plan for the life of the process (cache key)
   int device = 0;
   int32_t ntrees = 0;
   std::vector<Node> nodes;              // host copy, device pointers inside
@@ -164,6 +166,7 @@ struct SolveBufs {
 struct hss_factor_s {
   hss_plan_s* plan = nullptr;
   int prec = HSS_PREC_FP64;
+  bool blocked = false;                 // FP32 factors of the blocked reduction on every level
   void* d_fac = nullptr;
   size_t fac_bytes = 0;
   DBuf<char> sv_ws;                     // solve workspace (this factor's plan layout)
@@ -409,6 +412,11 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
         x.fT21 = fac; fac += align16((int64_t)c2.mr * c1.kv);
       }
       if (x.root) { x.fpiv = fac; fac += align16(x.m); }
+      if (!x.root && x.mk > 0) {
+        x.fTq = fac; fac += align16((int64_t)((x.k + 31) / 32) * 1024);
+        x.fTl = fac; fac += align16((int64_t)((x.mk + 31) / 32) * 1024);
+        x.fLi = fac; fac += align16((int64_t)((x.mk + 31) / 32) * 1024);
+      }
     }
     nbase += nn;
   }
@@ -465,8 +473,13 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
   return HSS_OK;
 }
 
+// Serial numbers of plans: a freed plan's address can be reused by a new one,
+// so caches keyed on plans use these instead of pointers.
+std::atomic<uint64_t> g_plan_serial{0};
+
 // device_fill: the generator buffer is left for the caller to write on the device.
 int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill = false) {
+  P->serial = ++g_plan_serial;
   for (auto& t : trees)
     if (t.npacked > 0 && t.packed == nullptr && !device_fill) return fail(HSS_ERR_INVALID, "null packed buffer");
   std::vector<GenOffsets> go;
@@ -665,8 +678,11 @@ int ensure_df(hss_plan_s* P, cudaStream_t st) {
   return HSS_OK;
 }
 
+// Returns true when every level ran the on-chip kernel (for FP32 the blocked
+// reduction, whose factors also carry the panel T matrices and L1 block inverses).
 template <typename T>
-void run_factor(const Levels& L, const Slot* slots, cudaStream_t st) {
+bool run_factor(const Levels& L, const Slot* slots, cudaStream_t st) {
+  bool all_fast = true;
   for (size_t h = 0; h < L.by_h->size(); ++h) {
     const Seg& g = (*L.by_h)[h];
     traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, g.cnt, st, [&] {
@@ -675,20 +691,37 @@ void run_factor(const Levels& L, const Slot* slots, cudaStream_t st) {
                            (size_t)(g.c1v + g.c2v) * g.kvmax + (size_t)g.c1mr * g.c1u + (size_t)g.c2mr * g.c2u +
                            (size_t)g.c1nr * g.c1v + (size_t)g.c2nr * g.c2v + (size_t)g.c1mr * g.c2v +
                            (size_t)g.c2mr * g.c1v;
-      if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra))
+      if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra)) {
         launch_ulv_factor_fast<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, g.kvmax, extra, st);
-      else
+      } else {
         launch_ulv_factor<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
+        all_fast = false;
+      }
     });
   }
+  return all_fast;
 }
 
+// Largest rank a level's blocked solve stages (its own and its children's).
+inline int seg_kmax(const Seg& g) { return std::max({g.kmax, g.kumax, g.c1mr, g.c2mr, 1}); }
+inline int seg_kvmax(const Seg& g) { return std::max({g.kvmax, g.c1v, g.c2v, 1}); }
+
+// The blocked solve (GEMM steps, one block per 32 right-hand sides) wins on
+// levels of large nodes; the register kernels (one warp per right-hand side)
+// win on levels of small nodes (64 x 64 merges, the root).
+inline bool use_bsolve(bool blocked, const Seg& g) {
+  return blocked && std::max(g.mmax, g.nmax) > 64 && bsolve_fits(g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g));
+}
+
+// blocked: the factors come from the blocked FP32 reduction (T = float only).
 template <typename T>
-void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
+void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, bool blocked = false) {
   for (size_t h = 0; h < L.by_h->size(); ++h) {
     const Seg& g = (*L.by_h)[h];
     traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
-      if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
+      if (use_bsolve(blocked, g))
+        launch_bsolve_up(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g), rmax, st);
+      else if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
         launch_ulv_solve_up_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.sv_stage, rmax, st);
       else
         launch_ulv_solve_up<T>(L.d_tasks + g.off, g.cnt, slots, st);
@@ -697,7 +730,9 @@ void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st) {
   for (size_t d = 0; d < L.by_d->size(); ++d) {
     const Seg& g = (*L.by_d)[d];
     traced(HSS_TRACE_SOLVE_DOWN, g.cnt, st, [&] {
-      if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
+      if (use_bsolve(blocked, g))
+        launch_bsolve_down(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g), rmax, st);
+      else if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
         launch_ulv_solve_down_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.nmax, g.mkmax, rmax, st);
       else
         launch_ulv_solve_down<T>(L.d_tasks + g.off, g.cnt, slots, st);
@@ -862,7 +897,8 @@ int factor_items(const std::vector<hss_factor_s*>& fs, const Levels& L, SlotTabl
     x.err = fs[i]->plan->d_err;
   }
   CUDA_TRY(table.upload(s, st));
-  run_factor<T>(L, table.dev.p, st);
+  const bool fast = run_factor<T>(L, table.dev.p, st);
+  for (auto* f : fs) f->blocked = fast && sizeof(T) == sizeof(float);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -910,7 +946,9 @@ int solve_pass(const std::vector<Item>& items, const Levels& L, const double* sc
     x.err = P->d_err;
   }
   CUDA_TRY(table.upload(s, st));
-  run_solve<T>(L, table.dev.p, (int)rmax, st);
+  bool blocked = true;
+  for (auto& it : items) blocked = blocked && it.f->blocked;
+  run_solve<T>(L, table.dev.p, (int)rmax, st, blocked);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -1100,7 +1138,7 @@ int copy_out(double* h, int64_t ld, const double* d, int64_t rows, int64_t r, cu
 // (the serving form): merged task lists and per-call buffers.
 struct hss_batcher_s {
   MergedLevels M;
-  std::vector<hss_plan_s*> last;   // plans of the merged lists on the device
+  std::vector<uint64_t> last;      // serial numbers of the plans of the merged lists
   SolveBufs bufs;
   SlotTable fac_slots;
 };
@@ -1108,10 +1146,13 @@ struct hss_batcher_s {
 namespace {
 
 int batcher_levels(hss_batcher_s* b, const std::vector<hss_plan_s*>& plans, cudaStream_t st) {
-  if (plans == b->last && b->M.d.p) return HSS_OK;
+  std::vector<uint64_t> ids(plans.size());
+  for (size_t i = 0; i < plans.size(); ++i) ids[i] = plans[i]->serial;
+  if (ids == b->last && b->M.d.p) return HSS_OK;
+  b->last.clear();
   int rc = merge_levels(plans, b->M, st);
   if (rc) return rc;
-  b->last = plans;
+  b->last = ids;
   return HSS_OK;
 }
 

@@ -156,10 +156,10 @@ __device__ void lu_smem(T* A, int m, int ld, int32_t* piv, int32_t* err, T* bv, 
 // rounding), but each reflector touches only its panel of BP columns (QL) or
 // rows (LQ); the rest of the block is updated once per panel with the compact
 // WY form of the panel's product, H(a) H(a+1) ... H(b-1) = I - Y T Y^T, as
-// shared-memory FP32 GEMMs.  T (forward xLARFT) is never formed: for orthogonal
-// reflectors (tau_j = 2 / y_j^T y_j) its inverse is S = diag(1/tau) + the
-// strictly upper part of the Gram matrix Y^T Y, so every product with T or T^T
-// is a triangular substitution with S (a zero tau gives a zero row, as in T):
+// shared-memory FP32 GEMMs.  T (forward xLARFT) is formed from its inverse: for
+// orthogonal reflectors (tau_j = 2 / y_j^T y_j) T^{-1} = S = diag(1/tau) + the
+// strictly upper part of the Gram matrix Y^T Y, so each column of T is one
+// independent back substitution (a zero tau gives a zero row, as in T):
 //   QL (geqlf!/ormql!, src/ulvfactor.jl:39-42): Q^T C = H(c0) ... H(c1-1) C
 //       (generation order c = c1-1 .. c0) = C - Y (T (Y^T C)) for C = D and the
 //       U columns left of the panel;
@@ -177,6 +177,7 @@ constexpr int KP = 36;                    // ld of the row-major copy of Y (>= B
 constexpr int XP = 132;                   // ld of the GEMM intermediate
 constexpr int GP = 33;                    // ld of the Gram matrix and T
 constexpr size_t kBlkElems = (size_t)BP * YP + (size_t)FMAX * KP + (size_t)BP * XP + 2 * (size_t)BP * GP + 2 * BP;
+static_assert((size_t)BP * XP >= 4 * (size_t)BP * GP, "the L1 block inverses use X as scratch");
 
 // xLARFG from alpha and the squared tail norm, FP32 panels: the norm as
 // sqrt(alpha^2 + ss) (hypot only when that overflows) and correctly rounded
@@ -231,37 +232,62 @@ __device__ void blk_gram(int nb, int len, const float* Yt, float* G) {
   __syncthreads();
 }
 
-// x <- T x: back substitution S x' = x, S = diag(1/tau) + strictly upper G.
-__device__ __forceinline__ void t_times(float (&x)[BP], int nb, const float* G, const float* tau) {
-#pragma unroll
-  for (int i = BP - 1; i >= 0; --i) {
-    if (i < nb) {
-      float s = x[i];
-#pragma unroll
-      for (int l = i + 1; l < BP; ++l)
-        if (l < nb) s = fmaf(-G[i * GP + l], x[l], s);
-      x[i] = s * tau[i];
+// T = S^{-1} explicitly (S = diag(1/tau) + strictly upper G), one column per
+// thread of warp 0: T(b,b) = tau_b, T(a,b) = -tau_a sum_{a<l<=b} G(a,l) T(l,b).
+// Tm is row-major (ld GP), zero outside the upper triangle; also written to Tg
+// (32 x 32, column-major) for the solve.  Ends with a barrier.
+__device__ void blk_tmat(int nb, const float* G, const float* tau, float* Tm, float* Tg) {
+  if (threadIdx.x < 32) {
+    const int b = threadIdx.x;
+    for (int a = b + 1; a < BP; ++a) Tm[a * GP + b] = 0.f;
+    if (b < nb) {
+      Tm[b * GP + b] = tau[b];
+      for (int a = b - 1; a >= 0; --a) {
+        float s0 = 0.f, s1 = 0.f;
+        int l = a + 1;
+        for (; l + 1 <= b; l += 2) {
+          s0 = fmaf(G[a * GP + l], Tm[l * GP + b], s0);
+          s1 = fmaf(G[a * GP + l + 1], Tm[(l + 1) * GP + b], s1);
+        }
+        if (l <= b) s0 = fmaf(G[a * GP + l], Tm[l * GP + b], s0);
+        Tm[a * GP + b] = -tau[a] * (s0 + s1);
+      }
+    } else {
+      for (int a = 0; a <= b; ++a) Tm[a * GP + b] = 0.f;
     }
   }
+  __syncthreads();
+  for (int e = threadIdx.x; e < BP * BP; e += FT) Tg[e] = Tm[(e % BP) * GP + e / BP];
 }
 
-// x <- T^T x (equivalently a row vector times T): forward substitution S^T x' = x.
-__device__ __forceinline__ void tt_times(float (&x)[BP], int nb, const float* G, const float* tau) {
-#pragma unroll
-  for (int a = 0; a < BP; ++a) {
-    if (a < nb) {
-      float s = x[a];
-#pragma unroll
-      for (int l = 0; l < a; ++l) s = fmaf(-G[l * GP + a], x[l], s);
-      x[a] = s * tau[a];
+// Inverses of the 32 x 32 diagonal blocks of L1 = lower part of D[0:mk, 0:mk]
+// (ld LDD), block p by warp p, column b by lane b (forward substitution),
+// written column-major to Lg + 1024 p.  `scr` holds 4 x 32 x 33 floats.
+__device__ void blk_linv(int mk, const float* sD, int LDD, float* scr, float* Lg) {
+  const int w = threadIdx.x >> 5, b = threadIdx.x & 31;
+  const int i0 = w * BP;
+  if (i0 < mk && w < 4) {
+    const int nb = min(BP, mk - i0);
+    float* x = scr + w * BP * GP;   // row-major a*GP + b
+    for (int a = 0; a < BP; ++a) x[a * GP + b] = 0.f;
+    if (b < nb) {
+      x[b * GP + b] = __frcp_rn(sD[(i0 + b) + (i0 + b) * LDD]);
+      for (int a = b + 1; a < nb; ++a) {
+        float s = 0.f;
+        for (int l = b; l < a; ++l) s = fmaf(sD[(i0 + a) + (i0 + l) * LDD], x[l * GP + b], s);
+        x[a * GP + b] = -s * __frcp_rn(sD[(i0 + a) + (i0 + a) * LDD]);
+      }
     }
+    __syncwarp();
+    for (int e = b; e < BP * BP; e += 32) Lg[w * 1024 + e] = x[(e % BP) * GP + e / BP];
   }
+  __syncthreads();
 }
 
 // C (rows 0..m-1, N columns, ld ldc) <- C - Y (T (Y^T C)), Y = Yc (reflector-major,
 // nb x m) / Yt (row-major, m x nb).  Ends with a barrier.
 __device__ void blk_apply_left(float* C, int ldc, int m, int N, int nb, const float* Yc, const float* Yt,
-                               const float* G, const float* tau, float* X) {
+                               const float* Tm, float* X) {
   const int tid = threadIdx.x;
   const int j = tid & 127, cb = tid >> 7;   // column, block of 8 reflectors
   // X = Y^T C (nb x N)
@@ -279,15 +305,22 @@ __device__ void blk_apply_left(float* C, int ldc, int m, int N, int nb, const fl
       if (cb * 8 + q < nb) X[(cb * 8 + q) * XP + j] = acc[q];
   }
   __syncthreads();
-  // X = T X, column by column
-  if (j < N && cb == 0) {
-    float x[BP];
+  // X = T X (T upper)
+  float nx[8];
+  if (j < N && cb * 8 < nb) {
 #pragma unroll
-    for (int c = 0; c < BP; ++c) x[c] = c < nb ? X[c * XP + j] : 0.f;
-    t_times(x, nb, G, tau);
+    for (int q = 0; q < 8; ++q) nx[q] = 0.f;
+    for (int c2 = cb * 8; c2 < nb; ++c2) {
+      const float xv = X[c2 * XP + j];
 #pragma unroll
-    for (int c = 0; c < BP; ++c)
-      if (c < nb) X[c * XP + j] = x[c];
+      for (int q = 0; q < 8; ++q) nx[q] = fmaf(Tm[(cb * 8 + q) * GP + c2], xv, nx[q]);
+    }
+  }
+  __syncthreads();
+  if (j < N && cb * 8 < nb) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (cb * 8 + q < nb) X[(cb * 8 + q) * XP + j] = nx[q];
   }
   __syncthreads();
   // C -= Y X
@@ -312,7 +345,7 @@ __device__ void blk_apply_left(float* C, int ldc, int m, int N, int nb, const fl
 // Rows r0..m-1 of C (n columns, ld ldc) <- C - (C Y^T) T Y with Y = Yc (nb x n,
 // reflector-major) / Yt (n x nb).  Ends with a barrier.
 __device__ void blk_apply_right(float* C, int ldc, int r0, int m, int n, int nb, const float* Yc, const float* Yt,
-                                const float* G, const float* tau, float* X) {
+                                const float* Tm, float* X) {
   const int tid = threadIdx.x;
   const int r = r0 + (tid & 127), ab = tid >> 7;
   const bool act = r < m && ab * 8 < nb;
@@ -331,15 +364,23 @@ __device__ void blk_apply_right(float* C, int ldc, int r0, int m, int n, int nb,
       if (ab * 8 + q < nb) X[(ab * 8 + q) * XP + (r - r0)] = acc[q];
   }
   __syncthreads();
-  // X = X T, row by row
-  if (r < m && ab == 0) {
-    float x[BP];
+  // X = X T (T upper)
+  float nx[8];
+  if (act) {
 #pragma unroll
-    for (int a = 0; a < BP; ++a) x[a] = a < nb ? X[a * XP + (r - r0)] : 0.f;
-    tt_times(x, nb, G, tau);
+    for (int q = 0; q < 8; ++q) nx[q] = 0.f;
+    const int hi = min(nb, ab * 8 + 8);
+    for (int a2 = 0; a2 < hi; ++a2) {
+      const float xv = X[a2 * XP + (r - r0)];
 #pragma unroll
-    for (int a = 0; a < BP; ++a)
-      if (a < nb) X[a * XP + (r - r0)] = x[a];
+      for (int q = 0; q < 8; ++q) nx[q] = fmaf(xv, Tm[a2 * GP + ab * 8 + q], nx[q]);
+    }
+  }
+  __syncthreads();
+  if (act) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (ab * 8 + q < nb) X[(ab * 8 + q) * XP + (r - r0)] = nx[q];
   }
   __syncthreads();
   // C -= X Y
@@ -363,7 +404,7 @@ __device__ void blk_apply_right(float* C, int ldc, int r0, int m, int n, int nb,
 
 // V (n x kv, ld ldv) <- V - Y^T (T^T (Y V)).  Ends with a barrier.
 __device__ void blk_apply_v(float* V, int ldv, int n, int kv, int nb, const float* Yc, const float* Yt,
-                            const float* G, const float* tau, float* X) {
+                            const float* Tm, float* X) {
   const int tid = threadIdx.x;
   // Z = Y V (nb x kv): thread (column c, block of 4 reflectors)
   for (int o = tid; o < kv * 8; o += FT) {
@@ -383,15 +424,25 @@ __device__ void blk_apply_v(float* V, int ldv, int n, int kv, int nb, const floa
       if (ab * 4 + q < nb) X[(ab * 4 + q) * XP + c] = acc[q];
   }
   __syncthreads();
-  // Z = T^T Z, column by column
-  if (tid < kv) {
-    float z[BP];
+  // Z = T^T Z
+  {
+    float nz[4] = {0.f, 0.f, 0.f, 0.f};
+    const int c = tid % kv, ab = tid / kv;   // kv * 8 <= 512 threads
+    const bool act = tid < kv * 8 && ab * 4 < nb;
+    if (act) {
+      const int hi = min(nb, ab * 4 + 4);
+      for (int a2 = 0; a2 < hi; ++a2) {
+        const float zv = X[a2 * XP + c];
 #pragma unroll
-    for (int a = 0; a < BP; ++a) z[a] = a < nb ? X[a * XP + tid] : 0.f;
-    tt_times(z, nb, G, tau);
+        for (int q = 0; q < 4; ++q) nz[q] = fmaf(Tm[a2 * GP + ab * 4 + q], zv, nz[q]);
+      }
+    }
+    __syncthreads();
+    if (act) {
 #pragma unroll
-    for (int a = 0; a < BP; ++a)
-      if (a < nb) X[a * XP + tid] = z[a];
+      for (int q = 0; q < 4; ++q)
+        if (ab * 4 + q < nb) X[(ab * 4 + q) * XP + c] = nz[q];
+    }
   }
   __syncthreads();
   // V -= Y^T Z: thread (row col, block of 8 columns of V)
@@ -419,7 +470,8 @@ __device__ void blk_apply_v(float* V, int ldv, int n, int kv, int nb, const floa
 // shared memory plus tau vectors and the transposed LQ reflectors in global
 // memory (tq, tl, gQt).
 __device__ void ulv_reduce_blocked(const Node& nd, float* sD, float* sU, int LDD, float* sV, int LDV, float* sv,
-                                   float* stau, float* blk, float* tq, float* tl, float* gQt) {
+                                   float* stau, float* blk, float* tq, float* tl, float* gQt, float* gTq, float* gTl,
+                                   float* gLi) {
   const int m = nd.m, n = nd.n, k = nd.k, mk = nd.mk, kv = nd.kv;
   const int tid = threadIdx.x;
   const unsigned hm = 0xFFFFu << (tid & 16);   // this thread's half-warp
@@ -428,7 +480,8 @@ __device__ void ulv_reduce_blocked(const Node& nd, float* sD, float* sU, int LDD
   float* Yt = Yc + BP * YP;                    // FMAX x KP
   float* X = Yt + FMAX * KP;                   // BP x XP
   float* G = X + BP * XP;                      // BP x GP (strictly upper part used)
-  float* ptau = G + 2 * BP * GP;               // BP taus of the panel
+  float* Tm = G + BP * GP;                     // BP x GP, row-major T of the panel
+  float* ptau = Tm + BP * GP;                  // BP taus of the panel
 
   // ---- P1: QL of U, panels of BP columns from the last -----------------------
   {
@@ -501,8 +554,9 @@ __device__ void ulv_reduce_blocked(const Node& nd, float* sD, float* sU, int LDD
       }
       __syncthreads();
       blk_gram(nb, m, Yt, G);
-      blk_apply_left(sD, LDD, m, n, nb, Yc, Yt, G, ptau, X);
-      if (c0 > 0) blk_apply_left(sU, LDD, m, c0, nb, Yc, Yt, G, ptau, X);
+      blk_tmat(nb, G, ptau, Tm, gTq + (int64_t)((k - c1) / BP) * 1024);
+      blk_apply_left(sD, LDD, m, n, nb, Yc, Yt, Tm, X);
+      if (c0 > 0) blk_apply_left(sU, LDD, m, c0, nb, Yc, Yt, Tm, X);
     }
   }
 
@@ -575,10 +629,13 @@ __device__ void ulv_reduce_blocked(const Node& nd, float* sD, float* sU, int LDD
       }
       __syncthreads();
       blk_gram(nb, n, Yt, G);
-      if (i1 < m) blk_apply_right(sD, LDD, i1, m, n, nb, Yc, Yt, G, ptau, X);
-      if (kv > 0) blk_apply_v(sV, LDV, n, kv, nb, Yc, Yt, G, ptau, X);
+      blk_tmat(nb, G, ptau, Tm, gTl + (int64_t)(i0 / BP) * 1024);
+      if (i1 < m) blk_apply_right(sD, LDD, i1, m, n, nb, Yc, Yt, Tm, X);
+      if (kv > 0) blk_apply_v(sV, LDV, n, kv, nb, Yc, Yt, Tm, X);
     }
   }
+  // inverses of L1's diagonal blocks for the solve (X is free now)
+  blk_linv(mk, sD, LDD, X, gLi);
 }
 
 template <typename T>
@@ -773,7 +830,8 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
           sVb[row + c * LDV] = nd.leaf ? (T)__ldg(gV0 + row + (int64_t)c * n) : gV[row + (int64_t)c * n];
     }
     __syncthreads();
-    ulv_reduce_blocked(nd, sD, sU, LDD, sVb, LDV, sv, stau, blk, tq, tl, fb + nd.fQt);
+    ulv_reduce_blocked(nd, sD, sU, LDD, sVb, LDV, sv, stau, blk, tq, tl, fb + nd.fQt, fb + nd.fTq, fb + nd.fTl,
+                       fb + nd.fLi);
     for (int e = tid; e < m * n; e += FT) gD[e] = sD[(e % m) + (e / m) * LDD];
     for (int e = tid; e < m * ku; e += FT) gU[e] = sU[(e % m) + (e / m) * LDD];
     for (int e = tid; e < n * kv; e += FT) gV[e] = sVb[(e % n) + (e / n) * LDV];

@@ -37,6 +37,10 @@ struct Node {
   // V (n x kv), tau_ql (k), tau_lq (mk), T12 (mr1 x kv2), T21 (mr2 x kv1), pivots (root),
   // Qt (n x mk): the LQ reflectors as columns (explicit 1 on the diagonal, 0 above)
   int64_t fD, fU, fV, ftq, ftl, fT12, fT21, fpiv, fQt;
+  // blocked FP32 solve: per panel of 32 reflectors the compact-WY T (32 x 32,
+  // column-major) of the QL (fTq, ceil(k/32) panels) and LQ (fTl, ceil(mk/32))
+  // reflectors, and the inverses of L1's 32 x 32 diagonal blocks (fLi)
+  int64_t fTq, fTl, fLi;
 };
 
 struct Task {

@@ -58,6 +58,13 @@ bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra);
 template <typename T>
 void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax, int kvmax,
                             size_t extra, cudaStream_t st);
+// Blocked FP32 solve sweeps (hss_bsolve.cu) over factors of the blocked FP32
+// reduction: sizes are the level's largest node and children's ranks.
+bool bsolve_fits(int mmax, int nmax, int kmax, int kvmax);
+void launch_bsolve_up(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kmax, int kvmax, int r,
+                      cudaStream_t st);
+void launch_bsolve_down(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kmax, int kvmax, int r,
+                        cudaStream_t st);
 // Register-resident solve sweeps for nodes with m, n <= 256 (hss_solve.cu).
 bool solve_reg_fits(int mmax, int nmax);
 template <typename T>
