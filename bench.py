@@ -40,7 +40,7 @@ UNIT = "solves/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=65536)
@@ -173,6 +173,18 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+
+
+def profiled_traffic(name):
+    """DRAM bytes per launch (read + write) recorded from an ncu capture in
+    profiles/<name>.md ("traffic_bytes_per_launch: N"), or None."""
+    try:
+        for ln in open(os.path.join(ROOT, "profiles", name + ".md")):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return int(ln.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
 
 
 def factor_leaf_bytes(A, factor_itemsize):
@@ -335,8 +347,10 @@ def run_ours(args, rank, world, local_rank):
         peak, peak_src = 6800.0, "fallback"
     alg_bytes = factor_leaf_bytes(A, 4) if args.roofline_kernel == "factor_leaf" else None
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9 if alg_bytes and per_launch_ms > 0 else None
+    traffic = profiled_traffic("ulv_factor_fast_leaf_f32_n65536") if args.roofline_kernel == "factor_leaf" else None
     roof = {"kernel": args.roofline_kernel, "bound": "hbm", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+            "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+            "traffic_source": "profiles/ulv_factor_fast_leaf_f32_n65536.md (ncu, one launch)" if traffic else None,
             "peak_source": peak_src, "launch_ms": per_launch_ms, "launches": k_cnt,
             "algorithmic_bytes": alg_bytes}
     cpu = None
