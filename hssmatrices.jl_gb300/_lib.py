@@ -38,7 +38,7 @@ EXPORTS = [
     "hss_create", "hss_create_batch", "hss_inspect", "hss_destroy", "hss_size", "hss_ntrees", "hss_node_info",
     "hss_ulv_cols", "hss_matmul", "hss_matmul_host", "hss_matmul_batch", "hss_ulvfactor",
     "hss_factor_destroy", "hss_ulvsolve", "hss_ulvsolve_host", "hss_ulvsolve_batch",
-    "hss_ulvfactsolve_host", "hss_factor_bytes", "hss_last_error", "hss_version", "hss_ulvrefactor",
+    "hss_ulvfactsolve_host", "hss_factor_bytes", "hss_autotune", "hss_autotune_info", "hss_last_error", "hss_version", "hss_ulvrefactor",
     "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option", "hss_matmul_noalloc",
     "hss_batcher_create", "hss_batcher_destroy", "hss_batcher_factor", "hss_batcher_solve",
     "hss_sample", "hss_sumsq", "hss_rc_create", "hss_rc_destroy", "hss_rc_size", "hss_rc_compress",
@@ -94,6 +94,9 @@ def _declare(lib):
                                          C.POINTER(SolveStats), P]),
         "hss_ulvfactsolve_host": (C.c_int, [P, I32, PD, I64, I64, PD, I64, D, I32, C.POINTER(SolveStats)]),
         "hss_factor_bytes": (C.c_int, [P, PI64]),
+        "hss_autotune": (C.c_int, [P, I64, P]),
+        "hss_autotune_info": (C.c_int, [P, C.POINTER(C.c_int32), C.c_char_p, C.POINTER(C.c_int32), C.c_char_p,
+                                        C.POINTER(C.c_int32)]),
         "hss_ulvrefactor": (C.c_int, [P, P]),
         "hss_trace_begin": (C.c_int, [I32]),
         "hss_trace_end": (C.c_int, [C.POINTER(D), PI64]),

@@ -89,6 +89,9 @@ bool g_generic_factor = false;
 bool g_residual_fp64 = false;
 // Forces the level-by-level product kernels instead of the persistent one.
 bool g_level_product = false;
+// Autotuner: forces every solve level to the register (0) or the blocked (1)
+// kernel where the blocked one is eligible; -1 leaves the choice to the factor.
+int g_pick_force = -1;
 struct TraceState {
   int kind = -1;
   std::vector<cudaEvent_t> pool;
@@ -167,6 +170,10 @@ struct hss_factor_s {
   hss_plan_s* plan = nullptr;
   int prec = HSS_PREC_FP64;
   bool blocked = false;                 // FP32 factors of the blocked reduction on every level
+  // autotuned kernel per tree level (hss_autotune): 1 blocked solve, 0 register
+  // solve, -1 (or empty) the built-in rule; residual product 1 persistent, 0 per level
+  std::vector<int8_t> tune_up, tune_down;
+  int tune_pmv = -1;
   void* d_fac = nullptr;
   size_t fac_bytes = 0;
   DBuf<char> sv_ws;                     // solve workspace (this factor's plan layout)
@@ -713,13 +720,27 @@ inline bool use_bsolve(bool blocked, const Seg& g) {
   return blocked && std::max(g.mmax, g.nmax) > 64 && bsolve_fits(g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g));
 }
 
-// blocked: the factors come from the blocked FP32 reduction (T = float only).
+// Kernel of one solve level: the autotuner's forced choice, else the factor's
+// tuned choice (tuned[level] of the plan's own lists), else the rule above.
+inline bool pick_bsolve(bool blocked, const Seg& g, const std::vector<int8_t>* tuned, size_t level) {
+  const bool eligible = blocked && bsolve_fits(g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g));
+  if (!eligible) return false;
+  if (g_pick_force >= 0) return g_pick_force == 1;
+  if (tuned && level < tuned->size() && (*tuned)[level] >= 0) return (*tuned)[level] == 1;
+  return use_bsolve(blocked, g);
+}
+
+// blocked: the factors come from the blocked FP32 reduction (T = float only);
+// tf: the factor whose tuned choices apply (the plan's own task lists), or null.
 template <typename T>
-void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, bool blocked = false) {
+void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, bool blocked = false,
+               const hss_factor_s* tf = nullptr) {
+  const std::vector<int8_t>* tup = tf ? &tf->tune_up : nullptr;
+  const std::vector<int8_t>* tdn = tf ? &tf->tune_down : nullptr;
   for (size_t h = 0; h < L.by_h->size(); ++h) {
     const Seg& g = (*L.by_h)[h];
     traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
-      if (use_bsolve(blocked, g))
+      if (pick_bsolve(blocked, g, tup, h))
         launch_bsolve_up(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g), rmax, st);
       else if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
         launch_ulv_solve_up_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.sv_stage, rmax, st);
@@ -730,7 +751,7 @@ void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, bo
   for (size_t d = 0; d < L.by_d->size(); ++d) {
     const Seg& g = (*L.by_d)[d];
     traced(HSS_TRACE_SOLVE_DOWN, g.cnt, st, [&] {
-      if (use_bsolve(blocked, g))
+      if (pick_bsolve(blocked, g, tdn, d))
         launch_bsolve_down(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g), rmax, st);
       else if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
         launch_ulv_solve_down_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.nmax, g.mkmax, rmax, st);
@@ -920,7 +941,7 @@ struct Item {
 template <typename T>
 int solve_pass(const std::vector<Item>& items, const Levels& L, const double* scale, const int64_t* off,
                int64_t rtot, int mode, bool residual_input, const int64_t* roff, double* R, SlotTable& table,
-               cudaStream_t st) {
+               cudaStream_t st, const hss_factor_s* tf = nullptr) {
   int64_t rmax = 0;
   for (auto& it : items) rmax = std::max(rmax, it.io.r);
   if (rmax == 0) return HSS_OK;
@@ -948,7 +969,7 @@ int solve_pass(const std::vector<Item>& items, const Levels& L, const double* sc
   CUDA_TRY(table.upload(s, st));
   bool blocked = true;
   for (auto& it : items) blocked = blocked && it.f->blocked;
-  run_solve<T>(L, table.dev.p, (int)rmax, st, blocked);
+  run_solve<T>(L, table.dev.p, (int)rmax, st, blocked, tf);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -975,7 +996,7 @@ int read_dev_err(hss_plan_s* P, cudaStream_t st) {
 // Solve every item, then refine (FP32 factors, or FP64 with tol > 0) until the
 // largest relative residual over all columns of all items is <= tol.
 int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, double tol, int32_t maxit,
-                hss_solve_stats* stats, cudaStream_t st) {
+                hss_solve_stats* stats, cudaStream_t st, const hss_factor_s* tf = nullptr) {
   if (items.empty()) return HSS_OK;
   const int prec = items[0].f->prec;
   for (auto& it : items)
@@ -1017,8 +1038,8 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     }
     CUDA_TRY(cudaMemcpyAsync(B.h_bn2.p, B.bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
-  int rc = fp32 ? solve_pass<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st)
-                : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st);
+  int rc = fp32 ? solve_pass<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf)
+                : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf);
   if (rc) return rc;
   if (!refine) return HSS_OK;
   // refinement: R = b - A x (double-float product for FP32 factors unless
@@ -1060,7 +1081,9 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
       x.ldws = P->ws_mv;
     }
   }
-  const bool persistent = use_pmv(L, &B.mv, dfres, (int)rmax);
+  // the tuned residual product of this factor, else the persistent one where it fits
+  SlotTable* pm = (tf && tf->tune_pmv == 0) ? nullptr : &B.mv;
+  const bool persistent = use_pmv(L, pm, dfres, (int)rmax);
   double res = 0.0;
   for (int32_t iter = 0;; ++iter) {
     CUDA_TRY(cudaMemsetAsync(B.rn2.p, 0, rtot * sizeof(double), st));
@@ -1071,7 +1094,7 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
         ++g_launches;
       }
     CUDA_TRY(B.mv.upload(ms, st));
-    rc = dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, &B.mv) : run_matvec(L, B.mv.dev.p, (int)rmax, st, &B.mv);
+    rc = dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, pm) : run_matvec(L, B.mv.dev.p, (int)rmax, st, pm);
     if (rc) return rc;
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(B.h_rn2.p, B.rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1095,8 +1118,8 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     if (iter >= maxit || std::isnan(res)) break;
     launch_sqrt_scale(B.rn2.p, B.scale.p, rtot, st);
     ++g_launches;
-    rc = fp32 ? solve_pass<float>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st)
-              : solve_pass<double>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st);
+    rc = fp32 ? solve_pass<float>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st, tf)
+              : solve_pass<double>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st, tf);
     if (rc) return rc;
   }
   for (auto& it : items) {
@@ -1114,7 +1137,105 @@ int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t
   if (rc) return rc;
   std::vector<Item> items;
   for (int32_t t = 0; t < P->ntrees; ++t) items.push_back(Item{f, t, io[t]});
-  return solve_items(items, plan_levels(P), f->bufs, tol, maxit, stats, st);
+  return solve_items(items, plan_levels(P), f->bufs, tol, maxit, stats, st, f);
+}
+
+// Per-launch times (ms) of the traced kind since hss_trace_begin, in launch order.
+std::vector<double> trace_pairs() {
+  std::vector<double> t;
+  for (size_t i = 0; i + 1 < g_trace.used; i += 2) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(g_trace.pool[i + 1]) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, g_trace.pool[i], g_trace.pool[i + 1]) != cudaSuccess)
+      ms = 0.f;
+    t.push_back(ms);
+  }
+  g_trace.kind = -1;
+  g_trace.used = 0;
+  return t;
+}
+
+// The autotuner (hss_autotune): times the kernel variants of every solve level
+// and the two residual products on scratch right-hand sides (r columns of
+// zeros: the kernels' time does not depend on the values) and keeps the
+// faster per level in the factor.
+int autotune_impl(hss_factor_s* f, int64_t r, cudaStream_t st) {
+  hss_plan_s* P = f->plan;
+  const Levels L = plan_levels(P);
+  int64_t mtot = 0, ntot = 0;
+  for (int32_t t = 0; t < P->ntrees; ++t) {
+    mtot += P->tree_m[t];
+    ntot += P->tree_n[t];
+  }
+  DBuf<double> Bs, Xs;
+  CUDA_TRY(Bs.ensure((size_t)mtot * r));
+  CUDA_TRY(Xs.ensure((size_t)ntot * r));
+  CUDA_TRY(cudaMemsetAsync(Bs.p, 0, (size_t)mtot * r * sizeof(double), st));
+  std::vector<Item> items;
+  int64_t mo = 0, no = 0;
+  for (int32_t t = 0; t < P->ntrees; ++t) {
+    items.push_back(Item{f, t, Cols{Bs.p + mo, P->tree_m[t], r, Xs.p + no, P->tree_n[t]}});
+    mo += P->tree_m[t] * r;
+    no += P->tree_n[t] * r;
+  }
+  f->tune_up.clear();
+  f->tune_down.clear();
+  f->tune_pmv = -1;
+  constexpr int kReps = 3;
+  int rc = HSS_OK;
+  auto per_level = [&](int kind, int force, const std::vector<Seg>& segs, std::vector<double>& out) -> int {
+    g_pick_force = force;
+    int e = solve_items(items, L, f->bufs, -1.0, 0, nullptr, st, f);   // warm-up
+    if (!e) {
+      hss_trace_begin(kind);
+      for (int i = 0; i < kReps && !e; ++i) e = solve_items(items, L, f->bufs, -1.0, 0, nullptr, st, f);
+      const std::vector<double> t = trace_pairs();
+      out.assign(segs.size(), 0.0);
+      size_t li = 0;
+      for (int i = 0; i < kReps; ++i)
+        for (size_t lv = 0; lv < segs.size(); ++lv)
+          if (segs[lv].cnt > 0 && li < t.size()) out[lv] += t[li++];
+    }
+    g_pick_force = -1;
+    return e;
+  };
+  if (f->prec == HSS_PREC_FP32 && f->blocked) {
+    std::vector<double> up0, up1, dn0, dn1;
+    if ((rc = per_level(HSS_TRACE_SOLVE_UP, 0, P->by_h, up0))) return rc;
+    if ((rc = per_level(HSS_TRACE_SOLVE_UP, 1, P->by_h, up1))) return rc;
+    if ((rc = per_level(HSS_TRACE_SOLVE_DOWN, 0, P->by_d, dn0))) return rc;
+    if ((rc = per_level(HSS_TRACE_SOLVE_DOWN, 1, P->by_d, dn1))) return rc;
+    f->tune_up.resize(P->by_h.size());
+    f->tune_down.resize(P->by_d.size());
+    for (size_t h = 0; h < P->by_h.size(); ++h) f->tune_up[h] = up1[h] < up0[h] ? 1 : 0;
+    for (size_t d = 0; d < P->by_d.size(); ++d) f->tune_down[d] = dn1[d] < dn0[d] ? 1 : 0;
+  }
+  // residual product: one refinement step (solve, residual, correction,
+  // residual) with each product; only the product differs between the two
+  if (f->prec == HSS_PREC_FP32) {
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    double best[2] = {0.0, 0.0};
+    for (int v = 1; v >= 0; --v) {
+      f->tune_pmv = v;
+      solve_items(items, L, f->bufs, 0.0, 1, nullptr, st, f);   // warm-up (ends without convergence)
+      cudaEventRecord(a, st);
+      for (int i = 0; i < kReps; ++i) solve_items(items, L, f->bufs, 0.0, 1, nullptr, st, f);
+      cudaEventRecord(b, st);
+      float ms = 0.f;
+      cudaEventSynchronize(b);
+      cudaEventElapsedTime(&ms, a, b);
+      best[v] = ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    f->tune_pmv = best[1] <= best[0] ? 1 : 0;
+    g_err.clear();
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  CUDA_TRY(cudaGetLastError());
+  return HSS_OK;
 }
 
 int copy_in(DBuf<double>& d, const double* h, int64_t rows, int64_t ld, int64_t r, cudaStream_t st) {
@@ -1453,6 +1574,22 @@ int hss_set_option(int32_t option, int64_t value) {
     return HSS_OK;
   }
   return fail(HSS_ERR_INVALID, "unknown option");
+}
+
+int hss_autotune(hss_factor f, int64_t r, void* stream) {
+  if (!f) return fail(HSS_ERR_INVALID, "null factor");
+  if (r <= 0 || r > (1 << 16)) return fail(HSS_ERR_BAD_DIMS, "autotune needs 1 <= r <= 65536 right-hand sides");
+  return autotune_impl(f, r, (cudaStream_t)stream);
+}
+
+int hss_autotune_info(hss_factor f, int32_t* nup, int8_t* up, int32_t* ndown, int8_t* down, int32_t* pmv) {
+  if (!f) return fail(HSS_ERR_INVALID, "null factor");
+  if (nup) *nup = (int32_t)f->tune_up.size();
+  if (ndown) *ndown = (int32_t)f->tune_down.size();
+  if (up) std::memcpy(up, f->tune_up.data(), f->tune_up.size());
+  if (down) std::memcpy(down, f->tune_down.data(), f->tune_down.size());
+  if (pmv) *pmv = f->tune_pmv;
+  return HSS_OK;
 }
 
 int hss_factor_bytes(hss_factor f, int64_t* bytes) {

@@ -16,6 +16,7 @@
 //       strips per column.
 // The root block gets an LU with partial pivoting in shared memory instead.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 #include "hss_device.cuh"
 #include "hss_internal.h"
@@ -817,9 +818,10 @@ __global__ void __launch_bounds__(FT, 1) ulv_factor_fast_kernel(const Task* __re
   T* tl = fb + nd.ftl;
 
   if constexpr (sizeof(T) == 4) {
-    // FP32: blocked reduction with the block and V in shared memory
+    // FP32: blocked reduction with the block and V in shared memory; its
+    // buffers reuse the merge staging region (dead after the assembly)
     const int LDV = nmax | 1;
-    T* sVb = sx + smem_align4((size_t)extra);
+    T* sVb = sx;
     T* blk = sVb + smem_align4((size_t)LDV * (kvmax > 0 ? kvmax : 1));
     {
       const int lane = tid & 31, warp = tid >> 5;
@@ -1023,8 +1025,10 @@ template <typename T>
 size_t factor_fast_smem(int mmax, int nmax, int kumax, int kvmax, size_t extra) {
   const int LDD = mmax | 1;
   size_t e = smem_align4((size_t)LDD * nmax) + smem_align4((size_t)LDD * (kumax > 0 ? kumax : 1)) + 4 * PART_COLS +
-             2 * SVLEN + smem_align4(extra);
-  if (sizeof(T) == 4) e += smem_align4((size_t)(nmax | 1) * (kvmax > 0 ? kvmax : 1)) + kBlkElems;
+             2 * SVLEN;
+  // the FP32 blocked buffers (V and the panel workspace) overlay the merge staging
+  const size_t blk = sizeof(T) == 4 ? smem_align4((size_t)(nmax | 1) * (kvmax > 0 ? kvmax : 1)) + kBlkElems : 0;
+  e += std::max(smem_align4(extra), blk);
   return e * sizeof(T);
 }
 

@@ -187,6 +187,24 @@ class UlvFactor:
         """Recompute the factorization in place (no allocation)."""
         check(self.lib.hss_ulvrefactor(self.handle, _stream(stream)))
 
+    def autotune(self, r, stream=None):
+        """Time the solve kernel variants of every tree level and the residual
+        products on scratch right-hand sides (r columns); later solves of this
+        factorization use the faster per level.  Returns the choices."""
+        check(self.lib.hss_autotune(self.handle, int(r), _stream(stream)))
+        return self.tuning()
+
+    def tuning(self):
+        """{"up": [...], "down": [...], "product": p}: per level 1 blocked solve,
+        0 register solve, -1 not tuned; product 1 persistent, 0 per level."""
+        nu, nd, pm = C.c_int32(), C.c_int32(), C.c_int32()
+        check(self.lib.hss_autotune_info(self.handle, C.byref(nu), None, C.byref(nd), None, C.byref(pm)))
+        up = C.create_string_buffer(max(nu.value, 1))
+        dn = C.create_string_buffer(max(nd.value, 1))
+        check(self.lib.hss_autotune_info(self.handle, C.byref(nu), up, C.byref(nd), dn, C.byref(pm)))
+        sgn = lambda b: [x - 256 if x > 127 else x for x in b]
+        return {"up": sgn(up.raw[:nu.value]), "down": sgn(dn.raw[:nd.value]), "product": pm.value}
+
     def nbytes(self):
         b = C.c_int64()
         check(self.lib.hss_factor_bytes(self.handle, C.byref(b)))

@@ -181,6 +181,19 @@ int hss_batcher_solve(hss_batcher b, int32_t count, const hss_factor* fs, const 
 /* Device memory held by a factorization (bytes). */
 int hss_factor_bytes(hss_factor f, int64_t* bytes);
 
+/* Autotuner (new; the reference has no GPU kernels to choose between).  Times,
+ * on scratch right-hand sides with r columns, the two solve kernels of every
+ * tree level of this factorization -- a warp per right-hand side ("register")
+ * and a block per 32 right-hand sides with GEMM steps ("blocked", FP32 factors)
+ * -- and the two refinement residual products (one persistent launch, one
+ * launch per level), and keeps the faster per level in the factorization for
+ * its later solves (hss_ulvsolve*; a batcher's merged solves use the built-in
+ * rule).  Synchronises the stream.  hss_autotune_info reads the choices back:
+ * per level 1 blocked, 0 register, -1 not tuned; product 1 persistent, 0 per
+ * level, -1 not tuned (arrays of *nup / *ndown entries; null to query sizes). */
+int hss_autotune(hss_factor f, int64_t r, void* stream);
+int hss_autotune_info(hss_factor f, int32_t* nup, int8_t* up, int32_t* ndown, int8_t* down, int32_t* pmv);
+
 /* Profiling aid: bracket every launch of one kernel kind with CUDA events on
  * its stream (-1 disables), then read the summed device time and the number
  * of launches (hss_trace_end synchronises on the recorded events). */

@@ -134,3 +134,31 @@ def test_full_size_r1(pkg, lib, orc):
     Ax = pkg.matmul(A, x)
     assert rel(Ax, orc.matmul(h, x)) <= 1e-12
     assert rel(pkg.matmul(A, x - 3 * y), Ax - 3 * pkg.matmul(A, y)) <= 1e-13
+
+
+def test_autotune_keeps_results(pkg, orc):
+    """The autotuner only changes which kernels run: refined solves before and
+    after tuning agree with the oracle, on a forest with uneven sizes and ranks."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    trees = [orc.synthetic_hss(n, ls, k, rng) for n, ls, k in [(2048, 128, 32), (1536, 128, 48), (640, 128, 20)]]
+    dev = pkg.DeviceHss.from_trees([pkg.HssMatrix.from_tree(t) for t in trees])
+    F = dev.ulvfactor("fp32")
+    rs = [3, 8, 5]
+    bs = [rng.standard_normal((t.size()[0], r)) for t, r in zip(trees, rs)]
+    dB = [torch.from_numpy(np.ascontiguousarray(b.T)).cuda() for b in bs]
+
+    def solve():
+        dX = [torch.zeros_like(b) for b in dB]
+        F.solve_batch_device(dB, [b.shape[0] for b in bs], rs, dX, [b.shape[0] for b in bs], tol=1e-10, maxit=20)
+        torch.cuda.synchronize()
+        return [x.cpu().numpy().T for x in dX]
+
+    before = solve()
+    tune = F.autotune(8)
+    assert len(tune["up"]) > 0 and len(tune["down"]) > 0 and tune["product"] in (0, 1)
+    assert all(v in (0, 1) for v in tune["up"] + tune["down"])
+    after = solve()
+    for t, b, x0, x1 in zip(trees, bs, before, after):
+        ref = orc.ulvfactsolve(t, b)
+        assert rel(x0, ref) <= 1e-8 and rel(x1, ref) <= 1e-8
