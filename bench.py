@@ -488,26 +488,35 @@ def run_batch(args):
         trees.append(pkg.synthetic_hss(n, ls, k, rng))
         rs.append(int(rng.integers(1, 17)))
     forest = pkg.DeviceHss.from_trees(trees)
-    Bs = [torch.randn((r, t.size()[0]), dtype=torch.float64, device="cuda") for t, r in zip(trees, rs)]
-    Xs = [torch.empty_like(b) for b in Bs]
+    stream = torch.cuda.Stream()   # graphs need a non-default stream
+    with torch.cuda.stream(stream):
+        Bs = [torch.randn((r, t.size()[0]), dtype=torch.float64, device="cuda") for t, r in zip(trees, rs)]
+        Xs = [torch.empty_like(b) for b in Bs]
+    stream.synchronize()
     ns = [t.size()[0] for t in trees]
+    lib = forest.lib
+    assert lib.hss_set_option(4, 1) == 0   # HSS_OPT_GRAPHS: factor and solve launch sequences as CUDA graphs
     out = {}
+    tuning = None
     for prec, tol in (("fp64", 0.0), ("fp32", args.tol)):
-        F = forest.ulvfactor(prec)
-        for _ in range(max(1, args.warmup)):
-            F.refactor()
-            F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=tol, maxit=20)
-        torch.cuda.synchronize()
+        F = forest.ulvfactor(prec, stream=stream)
+        if prec == "fp32":
+            tuning = F.autotune(max(rs), stream=stream)   # per-level kernel choice, timed once
+        for _ in range(max(2, args.warmup)):   # the second identical call is captured
+            F.refactor(stream=stream)
+            F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=tol, maxit=20, stream=stream)
+        stream.synchronize()
         times = []
         for _ in range(args.steps):
-            torch.cuda.synchronize()
+            stream.synchronize()
             t0 = time.perf_counter()
-            F.refactor()
-            F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=tol, maxit=20)
-            torch.cuda.synchronize()
+            F.refactor(stream=stream)
+            F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=tol, maxit=20, stream=stream)
+            stream.synchronize()
             times.append(time.perf_counter() - t0)
         out[prec] = {"ms_per_step": 1000.0 * statistics.mean(times), "p50_ms": 1000.0 * statistics.median(times)}
         del F
+    lib.hss_set_option(4, 0)
     # looping plain FP64 per matrix (separate plans, one matrix at a time)
     devs = [pkg.linalg.DeviceHss(t) for t in trees]
     facs = [d.ulvfactor("fp64") for d in devs]
@@ -529,7 +538,10 @@ def run_batch(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
         "config": {"workload": (f"batching: {args.matrices} matrices, n uniform 1024..16384 step 128 (seed 2), "
                                 f"leafsize in {{64,128,256}}, k 8..48, r 1..16; step = factor + solve of all, "
-                                f"FP32 ULV + refinement to {args.tol:g}")},
+                                f"FP32 ULV + refinement to {args.tol:g}; one forest plan, one launch per tree "
+                                f"level across all matrices, factor/solve sequences replayed as CUDA graphs, "
+                                f"solve kernels autotuned per level")},
+        "autotune": tuning,
         "fp64_batched_ms": out["fp64"]["ms_per_step"], "fp64_loop_ms": loop_ms,
         "speedup_vs_fp64_loop": loop_ms / m32, "total_rhs": sum(rs),
     }

@@ -40,9 +40,28 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 // Slot table on the device, re-uploaded only when its contents change, and
 // the launch state of the persistent product run with it.
+// A launch sequence captured as a CUDA graph, replayed while its key (the
+// task lists, slot table, sizes and kernel choices that shaped it) is unchanged.
+struct GraphCache {
+  uint64_t key = 0, seen = 0;     // seen: key of the last uncaptured run
+  cudaGraphExec_t exec = nullptr;
+  int64_t launches = 0;           // kernel launches inside the graph
+  bool flag = false;              // a result of the captured run (factor: every level fast)
+  GraphCache() = default;
+  GraphCache(const GraphCache&) = delete;
+  GraphCache& operator=(const GraphCache&) = delete;
+  ~GraphCache() { reset(); }
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    key = 0;
+  }
+};
+
 struct SlotTable {
   DBuf<Slot> dev;
   std::vector<Slot> last;
+  GraphCache graph;
   DBuf<uint32_t> pstate;   // counters + queue tags: zero between launches
   DBuf<int2> pq;           // queue entries
   uint32_t epoch = 0;      // tag of the last persistent launch on pstate
@@ -89,6 +108,8 @@ bool g_generic_factor = false;
 bool g_residual_fp64 = false;
 // Forces the level-by-level product kernels instead of the persistent one.
 bool g_level_product = false;
+// Replays factor and solve launch sequences as CUDA graphs (non-default streams).
+bool g_graphs = false;
 // Autotuner: forces every solve level to the register (0) or the blocked (1)
 // kernel where the blocked one is eligible; -1 leaves the choice to the factor.
 int g_pick_force = -1;
@@ -907,6 +928,65 @@ int matmul_impl(hss_plan_s* P, const std::vector<Cols>& io, double alpha, double
   return HSS_OK;
 }
 
+inline uint64_t fnv(uint64_t h, uint64_t v) {
+  for (int i = 0; i < 8; ++i) {
+    h ^= (v >> (8 * i)) & 0xffu;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+// Key of a launch sequence over task lists L with the device slot table `slots`.
+uint64_t levels_key(const Levels& L, const void* slots, int64_t extra) {
+  uint64_t h = 1469598103934665603ull;
+  h = fnv(h, (uint64_t)(uintptr_t)L.d_tasks);
+  h = fnv(h, (uint64_t)(uintptr_t)slots);
+  h = fnv(h, (uint64_t)extra);
+  for (const std::vector<Seg>* v : {L.by_h, L.by_d})
+    for (const Seg& g : *v) {
+      const int64_t f[] = {g.off, g.cnt, g.mmax, g.nmax, g.kumax, g.kvmax, g.c1u, g.c2u, g.c1v, g.c2v,
+                           g.kmax, g.mkmax, g.c1mr, g.c2mr, g.c1nr, g.c2nr, g.sv_stage};
+      for (int64_t x : f) h = fnv(h, (uint64_t)x);
+    }
+  return h;
+}
+
+// Runs `launch` (which issues kernels on st and returns a flag) directly or,
+// with graphs enabled on a non-default stream, as a replayed CUDA graph: the
+// second run with an unchanged key is captured and every later one replays it.
+template <typename F>
+int graphed(GraphCache& gc, uint64_t key, cudaStream_t st, bool& flag, F&& launch) {
+  const bool can = g_graphs && st != nullptr && g_trace.kind < 0 && g_pick_force < 0;
+  if (!can || (gc.key != key && gc.seen != key)) {
+    if (can) gc.seen = key;
+    flag = launch();
+    return HSS_OK;
+  }
+  if (gc.key != key) {
+    gc.reset();
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = g_launches;
+    const bool fl = launch();
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    const cudaError_t ie = cudaGraphInstantiate(&gc.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      gc.exec = nullptr;
+      return cuda_fail(ie, "cudaGraphInstantiate");
+    }
+    gc.key = key;
+    gc.launches = g_launches - l0;
+    gc.flag = fl;
+    g_launches = l0;
+  }
+  CUDA_TRY(cudaGraphLaunch(gc.exec, st));
+  g_launches += gc.launches;
+  flag = gc.flag;
+  return HSS_OK;
+}
+
 // One factorization of a launch sequence: slot i of the sequence.
 template <typename T>
 int factor_items(const std::vector<hss_factor_s*>& fs, const Levels& L, SlotTable& table, cudaStream_t st) {
@@ -918,7 +998,10 @@ int factor_items(const std::vector<hss_factor_s*>& fs, const Levels& L, SlotTabl
     x.err = fs[i]->plan->d_err;
   }
   CUDA_TRY(table.upload(s, st));
-  const bool fast = run_factor<T>(L, table.dev.p, st);
+  bool fast = false;
+  const uint64_t key = levels_key(L, table.dev.p, (int64_t)sizeof(T) + (g_generic_factor ? 16 : 0));
+  int rc = graphed(table.graph, key, st, fast, [&] { return run_factor<T>(L, table.dev.p, st); });
+  if (rc) return rc;
   for (auto* f : fs) f->blocked = fast && sizeof(T) == sizeof(float);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
@@ -969,7 +1052,16 @@ int solve_pass(const std::vector<Item>& items, const Levels& L, const double* sc
   CUDA_TRY(table.upload(s, st));
   bool blocked = true;
   for (auto& it : items) blocked = blocked && it.f->blocked;
-  run_solve<T>(L, table.dev.p, (int)rmax, st, blocked, tf);
+  uint64_t key = levels_key(L, table.dev.p, rmax * 64 + (blocked ? 1 : 0) + (sizeof(T) == 4 ? 2 : 0));
+  if (tf)
+    for (const std::vector<int8_t>* v : {&tf->tune_up, &tf->tune_down})
+      for (int8_t c : *v) key = fnv(key, (uint64_t)(c + 2));
+  bool unused = false;
+  int rc = graphed(table.graph, key, st, unused, [&] {
+    run_solve<T>(L, table.dev.p, (int)rmax, st, blocked, tf);
+    return true;
+  });
+  if (rc) return rc;
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -1571,6 +1663,10 @@ int hss_set_option(int32_t option, int64_t value) {
   }
   if (option == HSS_OPT_LEVEL_PRODUCT) {
     g_level_product = value != 0;
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_GRAPHS) {
+    g_graphs = value != 0;
     return HSS_OK;
   }
   return fail(HSS_ERR_INVALID, "unknown option");

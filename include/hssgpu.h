@@ -222,8 +222,12 @@ int64_t hss_launch_counter(void);
  * on the FP32 pipe (~48-bit, made for GB300's low FP64 rate).
  * HSS_OPT_LEVEL_PRODUCT = 1 runs every product with one kernel launch per
  * tree level instead of the default single persistent launch (leaves up to
- * 512 columns, ranks up to 64); used to test the two against each other. */
-enum { HSS_OPT_GENERIC_FACTOR = 1, HSS_OPT_RESIDUAL_FP64 = 2, HSS_OPT_LEVEL_PRODUCT = 3 };
+ * 512 columns, ranks up to 64); used to test the two against each other.
+ * HSS_OPT_GRAPHS = 1 replays the per-level launch sequences of factorizations
+ * and solve passes issued on a non-default stream as CUDA graphs: the second
+ * call with unchanged task lists, buffers and sizes is captured, later ones
+ * replay the graph (no capture on the legacy default stream). */
+enum { HSS_OPT_GENERIC_FACTOR = 1, HSS_OPT_RESIDUAL_FP64 = 2, HSS_OPT_LEVEL_PRODUCT = 3, HSS_OPT_GRAPHS = 4 };
 int hss_set_option(int32_t option, int64_t value);
 
 const char* hss_last_error(void);
