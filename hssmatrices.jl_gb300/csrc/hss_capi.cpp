@@ -62,17 +62,18 @@ struct SlotTable {
   DBuf<Slot> dev;
   std::vector<Slot> last;
   GraphCache graph;
-  DBuf<uint32_t> pstate;   // counters + queue tags: zero between launches
-  DBuf<int2> pq;           // queue entries
-  uint32_t epoch = 0;      // tag of the last persistent launch on pstate
+  DBuf<uint32_t> pstate;             // launch counters: zero between launches
+  DBuf<unsigned long long> pq;       // queue entries, tagged with the epoch of their launch
+  uint32_t epoch = 0;                // tag of the last persistent launch on pq
   cudaError_t ensure_pmv(int64_t entries, cudaStream_t st) {
-    const size_t words = (size_t)pmv_state_words(entries);
-    if (pstate.p && pstate.cap >= words && pq.p && pq.cap >= (size_t)std::max<int64_t>(entries, 1) && epoch != ~0u)
-      return cudaSuccess;
+    const size_t words = (size_t)pmv_state_words(), ents = (size_t)std::max<int64_t>(entries, 1);
+    if (pstate.p && pstate.cap >= words && pq.p && pq.cap >= ents && epoch < pmv_epoch_limit()) return cudaSuccess;
     pstate.release();
+    pq.release();
     cudaError_t e = pstate.ensure(words);
     if (e == cudaSuccess) e = cudaMemsetAsync(pstate.p, 0, pstate.cap * sizeof(uint32_t), st);
-    if (e == cudaSuccess) e = pq.ensure((size_t)std::max<int64_t>(entries, 1));
+    if (e == cudaSuccess) e = pq.ensure(ents);
+    if (e == cudaSuccess) e = cudaMemsetAsync(pq.p, 0, pq.cap * sizeof(unsigned long long), st);
     epoch = 0;
     return e;
   }
@@ -172,6 +173,7 @@ struct hss_plan_s {
   float2* d_gen_df = nullptr;           // generators as (hi, lo) float pairs, made on first use
   int32_t* d_sync = nullptr;            // per-node arrival counters of the persistent product
   int pmv_nleaf = 0, pmv_mleaf = 0, pmv_kmax = 0;   // largest leaf columns / rows, largest rank
+  int64_t pmv_ninner = 0;                           // branches that are not roots
   int64_t tr_lo = 0, tr_hi = 0;         // element range of d_gen holding every translator (B, R, W)
   std::vector<Task> h_tasks;            // host copy of the task lists (merged batches)
   std::vector<int64_t> h_table;         // node table of a single-tree plan (hss_export)
@@ -446,6 +448,18 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
         x.fLi = fac; fac += align16((int64_t)((x.mk + 31) / 32) * 1024);
       }
     }
+    for (int32_t i : pre) {
+      Node& x = N[i];
+      if (x.leaf) continue;
+      for (int c = 0; c < 2; ++c) {
+        const Node& y = N[F(i, c)];
+        x.cku[c] = y.ku;
+        x.ckv[c] = y.kv;
+        x.cleaf[c] = y.leaf;
+        x.cwz[c] = y.wz;
+        x.cwf[c] = y.wf;
+      }
+    }
     nbase += nn;
   }
   P->ws_mv = std::max<int64_t>(ws_mv, 1);
@@ -531,6 +545,7 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill
       P->pmv_mleaf = std::max(P->pmv_mleaf, x.gm);
     }
     P->pmv_kmax = std::max(P->pmv_kmax, std::max(x.ku, x.kv));
+    if (!x.leaf && !x.root) ++P->pmv_ninner;
   }
   for (size_t ti = 0; ti < trees.size(); ++ti)
     if (trees[ti].npacked > 0 && !device_fill)
@@ -600,6 +615,8 @@ struct Levels {
   // persistent product: largest leaf columns / rows, largest rank, non-root nodes
   int nleaf = 0, mleaf = 0, kmax = 0;
   int64_t ntasks = 0;
+  int64_t nodes_max = 0, nslots = 0;   // largest node array of a slot's plan; slots
+  int64_t ninner = 0;                  // non-root branches
   int device = 0;
   // translators to prefetch into L2 (FP64 and pair copies; null: none)
   const double* pf64 = nullptr;
@@ -619,6 +636,9 @@ Levels plan_levels(const hss_plan_s* P) {
   L.mleaf = P->pmv_mleaf;
   L.kmax = P->pmv_kmax;
   L.ntasks = (int64_t)P->nodes.size() - P->ntrees;
+  L.nodes_max = (int64_t)P->nodes.size();
+  L.nslots = P->ntrees;
+  L.ninner = P->pmv_ninner;
   L.device = P->device;
   if (P->tr_hi > P->tr_lo) {
     L.pf64 = P->d_gen + P->tr_lo;
@@ -632,16 +652,17 @@ Levels plan_levels(const hss_plan_s* P) {
 // switched off, and the forest's leaves and ranks fit its shared memory.
 bool use_pmv(const Levels& L, const SlotTable* pm, bool pairs, int rmax) {
   return pm != nullptr && !g_level_product && L.leaves.cnt > 0 && pmv_fits(L.nleaf, L.mleaf, L.kmax) &&
-         pmv_chunks(pairs, rmax) > 0;
+         pmv_chunks(pairs, rmax) > 0 && pmv_queue_fits(L.nodes_max, L.nslots);
 }
 
 int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable& pm, cudaStream_t st) {
-  CUDA_TRY(pm.ensure_pmv(L.ntasks * pmv_chunks(pairs, rmax), st));
+  CUDA_TRY(pm.ensure_pmv(pmv_queue_entries(L.ntasks, L.ninner, pmv_chunks(pairs, rmax)), st));
   ++pm.epoch;
   cudaError_t e = cudaSuccess;
   traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st, [&] {
     const void* pf = pairs ? (const void*)L.pfdf : (const void*)L.pf64;
-    e = launch_pmv(pairs, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, L.ntasks, rmax, L.nleaf, L.kmax, pm.pstate.p,
+    e = launch_pmv(pairs, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, L.ntasks, L.ninner, rmax, L.nleaf, L.kmax,
+                   pm.pstate.p,
                    pm.pq.p, pm.epoch, pf, pf ? L.pf_elems * 8 : 0, L.device, st);
   });
   if (e != cudaSuccess) {
@@ -789,7 +810,7 @@ struct MergedLevels {
   std::vector<Task> h;
   DBuf<Task> d;
   int nleaf = 0, mleaf = 0, kmax = 0, device = 0;
-  int64_t ntasks = 0;
+  int64_t ntasks = 0, nodes_max = 0, nslots = 0, ninner = 0;
   Levels view() const {
     Levels L;
     L.d_tasks = d.p;
@@ -802,6 +823,9 @@ struct MergedLevels {
     L.mleaf = mleaf;
     L.kmax = kmax;
     L.ntasks = ntasks;
+    L.nodes_max = nodes_max;
+    L.nslots = nslots;
+    L.ninner = ninner;
     L.device = device;
     return L;
   }
@@ -860,12 +884,17 @@ int merge_levels(const std::vector<hss_plan_s*>& plans, MergedLevels& M, cudaStr
   M.leaves.cnt = (int64_t)M.h.size() - M.leaves.off;
   M.nleaf = M.mleaf = M.kmax = 0;
   M.ntasks = 0;
+  M.nodes_max = 0;
+  M.ninner = 0;
   for (auto* P : plans) {
     M.nleaf = std::max(M.nleaf, P->pmv_nleaf);
     M.mleaf = std::max(M.mleaf, P->pmv_mleaf);
     M.kmax = std::max(M.kmax, P->pmv_kmax);
     M.ntasks += (int64_t)P->nodes.size() - P->ntrees;
+    M.nodes_max = std::max<int64_t>(M.nodes_max, (int64_t)P->nodes.size());
+    M.ninner += P->pmv_ninner;
   }
+  M.nslots = (int64_t)plans.size();
   M.device = plans.empty() ? 0 : plans[0]->device;
   CUDA_TRY(M.d.ensure(std::max<size_t>(M.h.size(), 1)));
   // pageable source: staged before the call returns; stream order protects

@@ -41,7 +41,12 @@ struct Node {
   // column-major) of the QL (fTq, ceil(k/32) panels) and LQ (fTl, ceil(mk/32))
   // reflectors, and the inverses of L1's 32 x 32 diagonal blocks (fLi)
   int64_t fTq, fTl, fLi;
+  // the children's ranks, leaf flags and product workspace offsets (left, right),
+  // so that a product task reads one descriptor
+  int32_t cku[2], ckv[2], cleaf[2];
+  int64_t cwz[2], cwf[2];
 };
+static_assert(sizeof(Node) % 8 == 0, "Node is copied as 8-byte words");
 
 struct Task {
   const Node* nodes;   // node array the index refers to
@@ -70,7 +75,7 @@ struct Slot {
   const float2* gdf;
   const double* gbase;
   // persistent product (hss_pmv.cu): the node array of this slot's plan and
-  // its per-node arrival counters (zero between launches)
+  // its per-node event counters (even between launches)
   const Node* nodes;
   int32_t* sync;
 };

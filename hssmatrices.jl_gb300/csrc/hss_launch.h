@@ -34,19 +34,27 @@ size_t pmv_smem_elems(int nleaf, int kmax, int* mcap);
 bool pmv_fits(int nleaf, int mleaf, int kmax);
 // Column chunks of a product with rmax right-hand sides (0: too many for the
 // persistent product).  Tasks are (node, chunk) pairs: a launch over ntasks
-// non-root nodes has ntasks * chunks queue entries.
+// non-root nodes, ninner of them branches, has (ntasks + ninner) * chunks
+// queue entries (downsweep / final tasks and B-term tasks).
 int pmv_chunks(bool pairs, int rmax);
-// 32-bit words of launch state for that many queue entries (the caller zeroes
-// them once; the kernel leaves them zero; int2 entries are separate).
-int64_t pmv_state_words(int64_t entries);
+int64_t pmv_queue_entries(int64_t ntasks, int64_t ninner, int chunks);
+// 32-bit words of launch state (the caller zeroes them once; the kernel leaves
+// them zero).  Queue entries are separate 64-bit words, zeroed when allocated;
+// each carries the epoch of the launch that wrote it, so epochs must grow from
+// 1 and stay <= pmv_epoch_limit() (then: zero the entries and start again).
+int64_t pmv_state_words();
+uint32_t pmv_epoch_limit();
+// Queue entries hold node indices below 2^20 and slot indices below 2^16.
+bool pmv_queue_fits(int64_t nodes, int64_t slots);
 // Per-node counters: a plan holds nodes * pmv_sync_chunks() of them, zeroed.
 int pmv_sync_chunks();
-// ntasks = non-root nodes of all trees; the slots' nodes/sync must be set and
-// every sync counter zero; epoch must differ from every earlier launch on state.
+// ntasks = non-root nodes of all trees, ninner = non-root branches; the slots' nodes/sync must be set and
+// every sync counter even (zeroed at allocation); epoch must differ from every earlier launch on state.
 // [prefetch, prefetch + prefetch_bytes) (nullable) is brought into L2 first.
-cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks, int rmax,
-                       int nleaf, int kmax, uint32_t* state, int2* qtask, uint32_t epoch, const void* prefetch,
-                       int64_t prefetch_bytes, int device, cudaStream_t st);
+cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks,
+                       int64_t ninner, int rmax,
+                       int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
+                       const void* prefetch, int64_t prefetch_bytes, int device, cudaStream_t st);
 
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>

@@ -8,17 +8,18 @@
 //
 //   1. upsweep by climbing: for each (leaf, column chunk) pair a block forms
 //      Z = V^T B (matmul.jl:34) and arrives at the parent's counter of that chunk.  The second
-//      child to arrive computes the parent, Z = W1^T Z1 + W2^T Z2 (:39), together
-//      with the B-terms of the parent's children, G1 = B12 Z2 and G2 = B21 Z1
-//      (:51, :55), then climbs on.  No block waits.  The block that completes a
-//      root starts the downsweep of that tree (F of the root's children = G).
+//      child to arrive computes the parent, Z = W1^T Z1 + W2^T Z2 (:39), and
+//      climbs on; no block waits.  The B-terms of a branch's children, G1 = B12 Z2
+//      and G2 = B21 Z1 (:51, :55), are a separate queue task, off the climb's
+//      critical path.  The block that reaches a root forms the root's B-terms
+//      and starts the downsweep of that tree (F of the root's children = G).
 //   2. the leaf products D B (:46) are bulk units; upsweep and bulk units are
 //      taken, upsweep first, from one global counter whenever no tree task is ready;
 //   3. downsweep tasks go through a ready queue: the task of an internal node p,
-//      enqueued once F_p is final, forms F_c = G_c + R_c F_p (:50-56) for both
-//      children and enqueues them; the final task of a leaf (C += U F, :47) is
-//      enqueued by whichever of its prerequisites (F of the leaf, every bulk
-//      unit of the leaf) completes last.
+//      enqueued once F_p is final and the B-terms of p's children are done, forms
+//      F_c = G_c + R_c F_p (:50-56) for both children; the final task of a leaf
+//      (C += U F, :47) is enqueued once F of the leaf is final and the leaf's bulk
+//      unit is done.  Each pair of prerequisites meets on a per-node counter.
 // A block claims a queue entry by taking a ticket (one atomicAdd, never
 // retried) whenever produced entries are unclaimed, and then polls only its
 // own entry's tag; between bulk units it looks for unclaimed entries first, so
@@ -26,8 +27,8 @@
 // Once the bulk units are gone every block takes a ticket or leaves.  Waits
 // are bounded: a block whose entry does not appear within the poll limit
 // records DEV_TIMEOUT and exits.  The last block to finish resets the launch
-// counters, and the per-node counters reset themselves, so consecutive
-// launches need no clearing.  Small products (upsweep, translators, downsweep)
+// counters; the per-node counters are even between launches (each launch adds
+// an even number), so consecutive launches need no clearing.  Small products (upsweep, translators, downsweep)
 // are split over all warps of the block, because GB300's FP64 units issue a
 // warp instruction only every 64 cycles per SM sub-partition.
 //
@@ -55,19 +56,25 @@ constexpr int LCH = 64;                      // rows of V staged per pass (leaf 
 constexpr uint32_t kIdleLimit = 1u << 22;    // polls of an idle block before it gives up
 constexpr int PART_ELEMS = PT * 4;           // split-K partials (8-byte accumulators)
 
-// launch counters, one 128-byte line each, then one epoch tag per queue entry
+// launch counters, one 128-byte line each
 enum { ST_HEAD = 0, ST_TAIL = 32, ST_BULK = 64, ST_DONE = 96, ST_WORDS = 128 };
+
+// A queue entry is one 64-bit word, so that a consumer reads the task and its
+// tag in one load: epoch (21 bits) | kind (1) | slot (16) | node (20) | column
+// chunk (6).  Kinds: the node's downsweep task (a leaf's final task), or the
+// B-terms of the node's children.
+constexpr int QE_EPOCH = 43, QE_KIND = 42, QE_SLOT = 26, QE_NODE = 6;
+enum { TK_DOWN = 0, TK_BTERM = 1 };
 
 struct PmvArgs {
   const Task* leaves;
   const Slot* slots;
-  uint32_t* state;       // launch counters and queue tags
-  int2* qtask;           // queue entries: (slot, node)
+  uint32_t* state;       // launch counters
+  unsigned long long* qent;   // queue entries
   const char* pf;        // translator generators, prefetched into L2 at the start
   int64_t pf_bytes;
   int32_t nleaves, ntasks, nchunk, nbulk;
   int32_t cw;            // columns per chunk (<= RC)
-  int32_t mcap;          // shared elements available for the staged translators
   uint32_t epoch;
 };
 
@@ -114,37 +121,89 @@ __device__ __forceinline__ int32_t* counter(const Slot& sl, int node, int ch) {
   return sl.sync + (int64_t)node * kSyncChunks + ch;
 }
 
-// Appends task (slot, node, chunk) to the ready queue (one thread; the caller
-// fenced its data).
-__device__ void push(const PmvArgs& a, int slot, int node, int ch, const Slot& sl) {
-  const uint32_t idx = atomicAdd(&a.state[ST_TAIL], 1u);
-  if (idx >= (uint32_t)a.ntasks) {   // more tasks than the host counted: the tree tables disagree
-    set_err(sl, DEV_BAD);
-    return;
-  }
-  a.qtask[idx] = make_int2(slot, node * kSyncChunks + ch);
-  __threadfence();
-  atomicExch(&a.state[ST_WORDS + idx], a.epoch);
+__device__ __forceinline__ unsigned long long qentry(uint32_t epoch, int kind, int slot, int node, int ch) {
+  return ((unsigned long long)epoch << QE_EPOCH) | ((unsigned long long)kind << QE_KIND) |
+         ((unsigned long long)slot << QE_SLOT) | ((unsigned long long)node << QE_NODE) | (unsigned long long)ch;
 }
 
-// One of the two prerequisites of a leaf chunk's final task is done (F of the
-// leaf, or the leaf's bulk unit); the second one enqueues the task.
-__device__ void leaf_event(const PmvArgs& a, int slot, const Slot& sl, int leaf, int ch) {
-  int32_t* c = counter(sl, leaf, ch);
-  if (atomicAdd(c, 1) == 1) {
-    atomicExch(c, 0);
-    push(a, slot, leaf, ch, sl);
+// Appends np <= 2 tasks (kind[i], slot, node[i], chunk) to the ready queue: one
+// thread, after a barrier of the block and a fence that published the tasks' data.
+__device__ void push(const PmvArgs& a, int slot, const int* node, const int* kind, int np, int ch, const Slot& sl) {
+  if (np == 0) return;
+  const uint32_t idx = atomicAdd(&a.state[ST_TAIL], (uint32_t)np);
+  for (int i = 0; i < np; ++i) {
+    if (idx + i >= (uint32_t)a.ntasks) {   // more tasks than the host counted: the tree tables disagree
+      set_err(sl, DEV_BAD);
+      return;
+    }
+    *(volatile unsigned long long*)&a.qent[idx + i] = qentry(a.epoch, kind[i], slot, node[i], ch);
   }
 }
 
-// Releases the children of node p, whose F of chunk ch is now final.
-__device__ void release_children(const PmvArgs& a, int slot, const Slot& sl, const Node* nodes, const Node& p,
-                                 int ch) {
+// Every non-root node's downsweep task (a leaf: its final task) has two
+// prerequisites: its F is final, and either the B-terms of its children
+// (branch) or its bulk unit (leaf) are done.  The second of the two events on
+// the node's counter enqueues the task.  Counters are never reset: a launch
+// adds an even number to each (a branch: two arrivals, then two events; a
+// leaf: two events), so the second event of a pair is the one that reads an
+// odd value.
+__device__ void node_event(const PmvArgs& a, int slot, const Slot& sl, int node, int ch) {
+  int32_t* c = counter(sl, node, ch);
+  if (atomicAdd(c, 1) & 1) {
+    // the first event's writes, observed through the counter, are published
+    // with the entry (fence between observing and enqueueing)
+    __threadfence();
+    const int k = TK_DOWN;
+    push(a, slot, &node, &k, 1, ch, sl);
+  }
+}
+
+// F of both children of p (chunk ch) is final (thread 0, after the block's
+// barrier and a fence): both counter updates are in flight together and the
+// queue slots are taken with one atomic.
+__device__ void release_children(const PmvArgs& a, int slot, const Slot& sl, const Node& p, int ch) {
   const int cs[2] = {p.left, p.right};
-  for (int i = 0; i < 2; ++i) {
-    if (nodes[cs[i]].leaf) leaf_event(a, slot, sl, cs[i], ch);
-    else push(a, slot, cs[i], ch, sl);
-  }
+  int old[2];
+  for (int i = 0; i < 2; ++i) old[i] = atomicAdd(counter(sl, cs[i], ch), 1);
+  int go[2], kd[2] = {TK_DOWN, TK_DOWN}, np = 0;
+  for (int i = 0; i < 2; ++i)
+    if (old[i] & 1) go[np++] = cs[i];
+  if (np == 0) return;
+  __threadfence();   // as in node_event: the other events' writes go out with the entries
+  push(a, slot, go, kd, np, ch, sl);
+}
+
+// ---- staging into shared memory ---------------------------------------------
+
+// Asynchronous 8-byte copies global -> shared (cp.async), all of a phase in
+// flight at once.  Only for data that no block writes during the launch (the
+// generators): the copies go through L1.
+__device__ __forceinline__ void cp8(void* s, const void* g) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// rows x cols column-major block (global ld ldg) into shared memory (ld lds):
+// warps take columns, lanes rows.
+template <class E>
+__device__ __forceinline__ void stage_gen(E* s, int lds, const E* g, int64_t ldg, int rows, int cols) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c = w; c < cols; c += PT / 32)
+    for (int l = lane; l < rows; l += 32) cp8(s + l + c * lds, g + l + (int64_t)c * ldg);
+}
+
+// The same for workspace blocks written by other blocks of this launch: loads
+// that bypass L1 (an SM may hold a stale line of a neighbouring block).
+template <class E>
+__device__ __forceinline__ void stage_ws(E* s, int lds, const E* g, int64_t ldg, int rows, int cols) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c = w; c < cols; c += PT / 32)
+    for (int l = lane; l < rows; l += 32) s[l + c * lds] = __ldcg(g + l + (int64_t)c * ldg);
 }
 
 // ---- per-node work (one column chunk: columns j0 .. j0 + nc - 1) -------------
@@ -183,7 +242,8 @@ __device__ void sdot(int nout, int K, typename P::Acc* part, Term term, Epi epi)
 }
 
 // Z = V^T B for one leaf (matmul.jl:34).  B is staged, V in passes of LCH rows
-// (ld LCH + 1); thread (output slot, group) keeps its partial sums over the passes.
+// (ld LCH + 1) through two buffers, the next pass's copies in flight while one
+// is used; thread (output slot, group) keeps its partial sums over the passes.
 template <class P>
 __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename P::Acc* part,
                         typename P::E* sm) {
@@ -193,23 +253,30 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
   if (kv == 0 || nc <= 0) return;
   const E* V = P::gen(sl, nd.V);
   E* ws = P::ws(sl);
-  E* Xs = sm;                       // n x RC
-  E* Vs = sm + n * RC;              // LCH x kv, ld LCH + 1
+  E* Xs = sm;                                      // n x RC
+  E* Vb[2] = {sm + n * RC, sm + n * RC + (LCH + 1) * kv};   // LCH x kv each, ld LCH + 1
+  const int npass = (n + LCH - 1) / LCH;
+  auto issue = [&](int ps) {
+    const int l0 = ps * LCH;
+    stage_gen(Vb[ps & 1], LCH + 1, V + l0, n, min(LCH, n - l0), kv);
+    cp_commit();
+  };
+  issue(0);
+  if (npass > 1) issue(1);
   const int nout = kv * nc, op = out_slots(nout), G = PT / op;
   const int slot = threadIdx.x % op, g = threadIdx.x / op;
   const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
-  for (int e = threadIdx.x; e < n * nc; e += PT) {
-    const int l = e % n, q = e / n;
-    Xs[l + q * n] = P::xin(__ldg(X + l + (int64_t)q * sl.ldb));
+  {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int q = w; q < nc; q += PT / 32)
+      for (int l = lane; l < n; l += 32) Xs[l + q * n] = P::xin(__ldg(X + l + (int64_t)q * sl.ldb));
   }
   Acc acc[2] = {P::zero(), P::zero()};   // nout <= 512 = 2 PT
-  for (int l0 = 0; l0 < n; l0 += LCH) {
-    const int nl = min(LCH, n - l0);
-    __syncthreads();
-    for (int e = threadIdx.x; e < nl * kv; e += PT) {
-      const int l = e % nl, c = e / nl;
-      Vs[l + c * (LCH + 1)] = __ldg(V + l0 + l + (int64_t)c * n);
-    }
+  for (int ps = 0; ps < npass; ++ps) {
+    const int l0 = ps * LCH, nl = min(LCH, n - l0);
+    const E* Vs = Vb[ps & 1];
+    if (ps + 1 < npass) cp_wait<1>();
+    else cp_wait<0>();
     __syncthreads();
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
@@ -221,6 +288,10 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
 #pragma unroll 4
         for (int l = g; l < nl; l += G) P::fma(acc[s], v[l], x[l]);
       }
+    }
+    if (ps + 2 < npass) {
+      __syncthreads();   // every thread is done with this buffer
+      issue(ps + 2);
     }
   }
 #pragma unroll
@@ -237,59 +308,62 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
   }
 }
 
-// Climb step at branch p once both children's Z are final: Z_p = W1^T Z1 + W2^T Z2
-// (matmul.jl:39; not for a root) and the B-terms G1 = B12 Z2, G2 = B21 Z1
-// (:51, :55) into the children's F slots.
+// Climb step at a non-root branch p once both children's Z are final:
+// Z_p = W1^T Z1 + W2^T Z2 (matmul.jl:39).  The children's sizes and offsets come
+// from p's descriptor (here a copy in shared memory).
 template <class P>
-__device__ void climb_node(const PmvArgs& a, const Slot& sl, const Node* nodes, const Node& p, int j0, int nc,
-                           typename P::Acc* part, typename P::E* sm) {
+__device__ void z_node(const Slot& sl, const Node& p, int j0, int nc, typename P::Acc* part, typename P::E* sm) {
+  using E = typename P::E;
+  using Acc = typename P::Acc;
+  const int v1 = p.ckv[0], v2 = p.ckv[1], kv = p.kv;
+  if (nc <= 0 || kv == 0) return;
+  E* ws = P::ws(sl);
+  const int64_t ld = sl.ldws;
+  // W1, W2 column-major with odd leading dimensions (lanes take columns in the product)
+  const int ld1 = v1 | 1, ld2 = v2 | 1;
+  E* Z1 = sm;
+  E* Z2 = Z1 + v1 * RC;
+  E* W1s = Z2 + v2 * RC;
+  E* W2s = W1s + ld1 * kv;
+  stage_gen(W1s, ld1, P::gen(sl, p.W1), v1, v1, kv);
+  stage_gen(W2s, ld2, P::gen(sl, p.W2), v2, v2, kv);
+  cp_commit();
+  stage_ws(Z1, v1, ws + p.cwz[0] + (int64_t)j0 * ld, ld, v1, nc);
+  stage_ws(Z2, v2, ws + p.cwz[1] + (int64_t)j0 * ld, ld, v2, nc);
+  cp_wait<0>();
+  __syncthreads();
+  sdot<P>(kv * nc, v1 + v2, part,
+          [&](int o, int l, Acc& s) {
+            const int c = o % kv, q = o / kv;
+            if (l < v1) P::fma(s, W1s[l + c * ld1], Z1[l + q * v1]);
+            else P::fma(s, W2s[(l - v1) + c * ld2], Z2[(l - v1) + q * v2]);
+          },
+          [&](int o, const Acc& s) { ws[p.wz + (o % kv) + (int64_t)(j0 + o / kv) * ld] = P::fin(s); });
+}
+
+// B-terms of branch p's children, G1 = B12 Z2 and G2 = B21 Z1 (matmul.jl:51,
+// :55), into the children's F slots.  Off the upsweep's critical path: a queue
+// task (the root's inline, its children's downsweep waits for them).
+template <class P>
+__device__ void bterm_node(const Slot& sl, const Node& p, int j0, int nc, typename P::Acc* part,
+                           typename P::E* sm) {
   using E = typename P::E;
   using Acc = typename P::Acc;
   if (nc <= 0) return;
-  const Node& c1 = nodes[p.left];
-  const Node& c2 = nodes[p.right];
-  const int v1 = c1.kv, v2 = c2.kv, u1 = c1.ku, u2 = c2.ku, kv = p.root ? 0 : p.kv;
+  const int v1 = p.ckv[0], v2 = p.ckv[1], u1 = p.cku[0], u2 = p.cku[1];
   E* ws = P::ws(sl);
   const int64_t ld = sl.ldws;
-  const int ldw = kv | 1;
   E* Z1 = sm;
   E* Z2 = Z1 + v1 * RC;
-  E* M = Z2 + v2 * RC;
-  const int needW = kv > 0 ? ldw * (v1 + v2) : 0, needB = u1 * v2 + u2 * v1;
-  const bool together = needW + needB <= a.mcap;
-  E* W1t = M;
-  E* W2t = M + ldw * v1;
-  E* B12 = together ? M + needW : M;
+  E* B12 = Z2 + v2 * RC;
   E* B21 = B12 + u1 * v2;
-  const E* gB12 = P::gen(sl, p.B12);
-  const E* gB21 = P::gen(sl, p.B21);
-  for (int e = threadIdx.x; e < v1 * nc; e += PT) Z1[e] = __ldcg(ws + c1.wz + (e % v1) + (int64_t)(j0 + e / v1) * ld);
-  for (int e = threadIdx.x; e < v2 * nc; e += PT) Z2[e] = __ldcg(ws + c2.wz + (e % v2) + (int64_t)(j0 + e / v2) * ld);
-  if (kv > 0) {
-    const E* gW1 = P::gen(sl, p.W1);
-    const E* gW2 = P::gen(sl, p.W2);
-    for (int e = threadIdx.x; e < v1 * kv; e += PT) W1t[(e / v1) + (e % v1) * ldw] = __ldg(gW1 + e);
-    for (int e = threadIdx.x; e < v2 * kv; e += PT) W2t[(e / v2) + (e % v2) * ldw] = __ldg(gW2 + e);
-  }
-  auto stageB = [&]() {
-    for (int e = threadIdx.x; e < u1 * v2; e += PT) B12[e] = __ldg(gB12 + e);
-    for (int e = threadIdx.x; e < u2 * v1; e += PT) B21[e] = __ldg(gB21 + e);
-  };
-  if (together) stageB();
+  stage_gen(B12, u1, P::gen(sl, p.B12), u1, u1, v2);
+  stage_gen(B21, u2, P::gen(sl, p.B21), u2, u2, v1);
+  cp_commit();
+  stage_ws(Z1, v1, ws + p.cwz[0] + (int64_t)j0 * ld, ld, v1, nc);
+  stage_ws(Z2, v2, ws + p.cwz[1] + (int64_t)j0 * ld, ld, v2, nc);
+  cp_wait<0>();
   __syncthreads();
-  if (kv > 0)
-    sdot<P>(kv * nc, v1 + v2, part,
-            [&](int o, int l, Acc& s) {
-              const int c = o % kv, q = o / kv;
-              if (l < v1) P::fma(s, W1t[c + l * ldw], Z1[l + q * v1]);
-              else P::fma(s, W2t[c + (l - v1) * ldw], Z2[(l - v1) + q * v2]);
-            },
-            [&](int o, const Acc& s) { ws[p.wz + (o % kv) + (int64_t)(j0 + o / kv) * ld] = P::fin(s); });
-  if (!together) {
-    __syncthreads();
-    stageB();
-    __syncthreads();
-  }
   sdot<P>((u1 + u2) * nc, max(v1, v2), part,
           [&](int o, int l, Acc& s) {
             if (o < u1 * nc) {
@@ -302,65 +376,85 @@ __device__ void climb_node(const PmvArgs& a, const Slot& sl, const Node* nodes, 
             }
           },
           [&](int o, const Acc& s) {
-            if (o < u1 * nc) ws[c1.wf + (o % u1) + (int64_t)(j0 + o / u1) * ld] = P::fin(s);
-            else ws[c2.wf + ((o - u1 * nc) % u2) + (int64_t)(j0 + (o - u1 * nc) / u2) * ld] = P::fin(s);
+            if (o < u1 * nc) ws[p.cwf[0] + (o % u1) + (int64_t)(j0 + o / u1) * ld] = P::fin(s);
+            else ws[p.cwf[1] + ((o - u1 * nc) % u2) + (int64_t)(j0 + (o - u1 * nc) / u2) * ld] = P::fin(s);
           });
 }
 
-// Arrival of a finished node (chunk ch) at its parent; the second child to arrive climbs.
+// Arrival of a finished node x (its Z of chunk ch written by this block) at its
+// parent; the second child to arrive climbs.  While thread 0 fences and
+// arrives, warp 1 enqueues the B-term task of x (a branch) and warp 2 copies
+// the parent's descriptor into shared memory, so the next step reads no
+// descriptor from global memory.  At the root the block forms the root's
+// B-terms, which are F of the root's children, and releases them.
 template <class P>
 __device__ void climb_from(const PmvArgs& a, int slot, const Slot& sl, const Node* nodes, int node, int ch,
                            typename P::Acc* part, typename P::E* sm) {
   __shared__ int s_go;
+  __shared__ Node s_node;
   const int j0 = ch * a.cw, nc = min(a.cw, sl.r - j0);
+  const Node* x = &nodes[node];
   for (;;) {
-    const Node& x = nodes[node];
-    if (x.root) return;
-    __threadfence();   // every thread publishes its writes of x's Z / B-terms
-    __syncthreads();
+    const int xpar = x->parent;
+    const bool xroot = x->root != 0, xbranch = !x->leaf;
+    __syncthreads();   // x's Z is written; nobody reads s_node any more
+    if (xroot) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-      int32_t* c = counter(sl, x.parent, ch);
-      const int old = atomicAdd(c, 1);
-      s_go = old == 1;
-      if (old == 1) atomicExch(c, 0);
+      __threadfence();   // publishes the block's writes (cumulative over the barrier)
+      const int old = atomicAdd(counter(sl, xpar, ch), 1);
+      s_go = old & 1;
+      if (old & 1) __threadfence();   // acquire: the sibling's Z is read after the barrier below
+    } else if (threadIdx.x == 32 && xbranch) {
+      __threadfence();
+      const int k = TK_BTERM;
+      push(a, slot, &node, &k, 1, ch, sl);
+    } else if (w == 2) {
+      const unsigned long long* src = (const unsigned long long*)&nodes[xpar];
+      unsigned long long* dst = (unsigned long long*)&s_node;
+      for (int i = lane; i < (int)(sizeof(Node) / 8); i += 32) dst[i] = src[i];
     }
     __syncthreads();
     if (!s_go) return;
-    __threadfence();
-    const Node& p = nodes[x.parent];
-    climb_node<P>(a, sl, nodes, p, j0, nc, part, sm);
+    const Node& p = s_node;
+    node = xpar;
     if (p.root) {
-      // F of the root's children is their B-term (the root has no F)
-      __threadfence();
+      bterm_node<P>(sl, p, j0, nc, part, sm);
       __syncthreads();
-      if (threadIdx.x == 0) release_children(a, slot, sl, nodes, p, ch);
+      if (threadIdx.x == 0) {
+        __threadfence();
+        release_children(a, slot, sl, p, ch);
+      }
       return;
     }
-    node = x.parent;
+    z_node<P>(sl, p, j0, nc, part, sm);
+    x = &s_node;
   }
 }
 
-// Downsweep task of a non-root branch p (F_p final):
-// F_c = G_c + R_c F_p for both children (matmul.jl:50-56), in place over G_c.
+// Downsweep task of a non-root branch p (F_p final, its children's B-terms G_c
+// done): F_c = G_c + R_c F_p for both children (matmul.jl:50-56), in place over G_c.
 template <class P>
-__device__ void down_node(const Slot& sl, const Node* nodes, const Node& p, int j0, int nc, typename P::Acc* part,
-                          typename P::E* sm) {
+__device__ void down_node(const Slot& sl, const Node& p, int j0, int nc, typename P::Acc* part, typename P::E* sm) {
   using E = typename P::E;
   using Acc = typename P::Acc;
   if (nc <= 0) return;
-  const Node& c1 = nodes[p.left];
-  const Node& c2 = nodes[p.right];
-  const int u1 = c1.ku, u2 = c2.ku, kp = p.ku;
+  const int u1 = p.cku[0], u2 = p.cku[1], kp = p.ku;
+  const int64_t f1 = p.cwf[0], f2 = p.cwf[1];
   E* ws = P::ws(sl);
   const int64_t ld = sl.ldws;
   E* Fp = sm;                 // kp x RC
   E* R1 = Fp + kp * RC;       // u1 x kp
   E* R2 = R1 + u1 * kp;       // u2 x kp
-  const E* gR1 = P::gen(sl, p.R1);
-  const E* gR2 = P::gen(sl, p.R2);
-  for (int e = threadIdx.x; e < kp * nc; e += PT) Fp[e] = __ldcg(ws + p.wf + (e % kp) + (int64_t)(j0 + e / kp) * ld);
-  for (int e = threadIdx.x; e < u1 * kp; e += PT) R1[e] = __ldg(gR1 + e);
-  for (int e = threadIdx.x; e < u2 * kp; e += PT) R2[e] = __ldg(gR2 + e);
+  E* G1 = R2 + u2 * kp;       // u1 x RC: the children's B-terms
+  E* G2 = G1 + u1 * RC;       // u2 x RC
+  stage_gen(R1, u1, P::gen(sl, p.R1), u1, u1, kp);
+  stage_gen(R2, u2, P::gen(sl, p.R2), u2, u2, kp);
+  cp_commit();
+  stage_ws(Fp, kp, ws + p.wf + (int64_t)j0 * ld, ld, kp, nc);
+  stage_ws(G1, u1, ws + f1 + (int64_t)j0 * ld, ld, u1, nc);
+  stage_ws(G2, u2, ws + f2 + (int64_t)j0 * ld, ld, u2, nc);
+  cp_wait<0>();
   __syncthreads();
   sdot<P>((u1 + u2) * nc, kp, part,
           [&](int o, int l, Acc& s) {
@@ -371,10 +465,9 @@ __device__ void down_node(const Slot& sl, const Node* nodes, const Node& p, int 
             const bool first = o < u1 * nc;
             const int o2 = first ? o : o - u1 * nc;
             const int uc = first ? u1 : u2;
-            E* f = ws + (first ? c1.wf : c2.wf) + (o2 % uc) + (int64_t)(j0 + o2 / uc) * ld;
             Acc t = s;
-            P::addE(t, __ldcg(f));
-            *f = P::fin(t);
+            P::addE(t, (first ? G1 : G2)[o2]);   // G[i + q uc] with i = o2 % uc, q = o2 / uc
+            ws[(first ? f1 : f2) + (o2 % uc) + (int64_t)(j0 + o2 / uc) * ld] = P::fin(t);
           });
 }
 
@@ -470,6 +563,13 @@ __device__ void bulk_unit(const PmvArgs& a, int u, typename P::Acc* part, typena
   const Slot& sl = a.slots[tk.slot];
   const Node& nd = tk.nodes[tk.node];
   const int j0 = ch * a.cw;
+  if (ch == 0 && !nd.root && nd.ku > 0) {
+    // U is read by the leaf's final tasks at the end of the downsweep: into L2 now
+    const char* ub = (const char*)P::gen(sl, nd.U);
+    const int64_t bytes = (int64_t)nd.gm * nd.ku * (int64_t)sizeof(E);
+    for (int64_t off = (int64_t)threadIdx.x * 128; off < bytes; off += PT * 128)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(ub + off));
+  }
   if (j0 < sl.r) {
     const int nc = min(a.cw, sl.r - j0), m = nd.gm, n = nd.gn;
     E* Xs = sm;
@@ -502,9 +602,11 @@ __device__ void bulk_unit(const PmvArgs& a, int u, typename P::Acc* part, typena
     }
   }
   if (!nd.root) {
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) leaf_event(a, tk.slot, sl, tk.node, ch);
+    if (threadIdx.x == 0) {
+      __threadfence();
+      node_event(a, tk.slot, sl, tk.node, ch);
+    }
   }
 }
 
@@ -523,7 +625,7 @@ __device__ void final_leaf(const Slot& sl, const Node& nd, int j0, int nc, typen
   E* Fs = sm;                              // ku x RC
   const E* U = P::gen(sl, nd.U);
   __syncthreads();
-  for (int e = threadIdx.x; e < ku * nc; e += PT) Fs[e] = __ldcg(ws + nd.wf + (e % ku) + (int64_t)(j0 + e / ku) * sl.ldws);
+  stage_ws(Fs, ku, ws + nd.wf + (int64_t)j0 * sl.ldws, sl.ldws, ku, nc);
   __syncthreads();
   double* C = sl.C + nd.row0 + (int64_t)j0 * sl.ldc;
   double* cn = sl.colnorm2 ? sl.colnorm2 + j0 : nullptr;
@@ -555,7 +657,7 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
   extern __shared__ __align__(16) unsigned char pmv_smem[];
   Acc* part = (Acc*)pmv_smem;                    // PART_ELEMS split-K partials
   E* sm = (E*)pmv_smem + PART_ELEMS;             // per-phase staging
-  __shared__ int s_cmd, s_x, s_y;
+  __shared__ int s_cmd, s_x, s_y, s_k;
 
   // the translators are read by the tree chain: have them in L2 before it starts
   for (int64_t off = ((int64_t)blockIdx.x * PT + threadIdx.x) * 128; off < a.pf_bytes;
@@ -592,13 +694,16 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
           }
         }
       }
-      if (ticket >= 0 && ld_vol(&a.state[ST_WORDS + ticket]) == a.epoch) {
-        __threadfence();
-        const int2 q = __ldcg(&a.qtask[ticket]);
-        s_x = q.x;
-        s_y = q.y;
-        cmd = 1;
-        ticket = -1;
+      if (ticket >= 0) {
+        const unsigned long long w = *(const volatile unsigned long long*)&a.qent[ticket];
+        if ((uint32_t)(w >> QE_EPOCH) == a.epoch) {
+          __threadfence();   // acquire: the task's inputs are read after the barrier below
+          s_x = (int)((w >> QE_SLOT) & 0xffffu);
+          s_y = (int)(w & ((1u << QE_SLOT) - 1));   // node * kSyncChunks + chunk
+          s_k = (int)((w >> QE_KIND) & 1u);
+          cmd = 1;
+          ticket = -1;
+        }
       }
       if (cmd == 0) {
         if (++idle > kIdleLimit) {
@@ -621,13 +726,22 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
       const Node* nodes = sl.nodes;
       const Node& x = nodes[node];
       const int j0 = ch * a.cw, nc = min(a.cw, sl.r - j0);
-      if (x.leaf) {
+      if (s_k == TK_BTERM) {
+        bterm_node<P>(sl, x, j0, nc, part, sm);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          __threadfence();
+          node_event(a, slot, sl, node, ch);
+        }
+      } else if (x.leaf) {
         final_leaf<P>(sl, x, j0, nc, part, sm);
       } else {
-        down_node<P>(sl, nodes, x, j0, nc, part, sm);
-        __threadfence();
+        down_node<P>(sl, x, j0, nc, part, sm);
         __syncthreads();
-        if (threadIdx.x == 0) release_children(a, slot, sl, nodes, x, ch);
+        if (threadIdx.x == 0) {
+          __threadfence();
+          release_children(a, slot, sl, x, ch);
+        }
       }
     } else if (cmd == 2) {
       const int u = s_x;
@@ -690,18 +804,14 @@ int resident_blocks(size_t smem, int device) {
 // available for staged translators.
 size_t pmv_smem_elems(int nleaf, int kmax, int* mcap) {
   const size_t k = kmax > 0 ? kmax : 1;
-  const size_t up = (size_t)nleaf * RC + (size_t)(LCH + 1) * k;
+  const size_t up = (size_t)nleaf * RC + 2 * (size_t)(LCH + 1) * k;   // X + two V buffers
   const size_t bulk = (size_t)nleaf * RC;
   const size_t fin = k * RC;
-  const size_t down = k * RC + 2 * k * k;
-  const size_t zst = 2 * k * RC;
-  const size_t two = std::max((k | 1) * 2 * k, 2 * k * k);
-  const size_t all = (k | 1) * 2 * k + 2 * k * k;
-  const size_t need = std::max(std::max(up, bulk), std::max(fin, down));
-  // stage all four translators at once when the whole buffer stays within 48 KB
-  const size_t with_all = PART_ELEMS + std::max(need, zst + all);
-  const size_t total = with_all * 8 <= 48 * 1024 ? with_all : PART_ELEMS + std::max(need, zst + two);
-  if (mcap) *mcap = (int)(total - PART_ELEMS - zst);
+  const size_t down = 3 * k * RC + 2 * k * k;                         // F_p, R1, R2, G1, G2
+  const size_t climb = 2 * k * RC + 2 * (k | 1) * k;                  // Z1, Z2, W1, W2
+  const size_t bterm = 2 * k * RC + 2 * k * k;                        // Z1, Z2, B12, B21
+  const size_t total = PART_ELEMS + std::max(std::max(std::max(up, bulk), std::max(fin, down)), std::max(climb, bterm));
+  if (mcap) *mcap = (int)(total - PART_ELEMS);
   return total;
 }
 
@@ -714,27 +824,32 @@ int pmv_chunks(bool pairs, int rmax) {
   const int nc = std::max(1, (rmax + cw - 1) / cw);
   return nc <= kSyncChunks ? nc : 0;
 }
-int64_t pmv_state_words(int64_t entries) { return ST_WORDS + entries; }
+int64_t pmv_queue_entries(int64_t ntasks, int64_t ninner, int chunks) { return (ntasks + ninner) * chunks; }
+int64_t pmv_state_words() { return ST_WORDS; }
+uint32_t pmv_epoch_limit() { return (1u << (64 - QE_EPOCH)) - 1; }
+bool pmv_queue_fits(int64_t nodes, int64_t slots) {
+  return nodes <= (int64_t(1) << (QE_SLOT - QE_NODE)) && slots <= (int64_t(1) << (QE_EPOCH - QE_SLOT));
+}
 int pmv_sync_chunks() { return kSyncChunks; }
 
-cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks, int rmax,
-                       int nleaf, int kmax, uint32_t* state, int2* qtask, uint32_t epoch, const void* prefetch,
+cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks,
+                       int64_t ninner, int rmax,
+                       int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
+                       const void* prefetch,
                        int64_t prefetch_bytes, int device, cudaStream_t st) {
   if (nleaves <= 0) return cudaSuccess;
-  int mcap = 0;
-  const size_t smem = pmv_smem_elems(nleaf, kmax, &mcap) * 8;
+  const size_t smem = pmv_smem_elems(nleaf, kmax, nullptr) * 8;
   PmvArgs a;
   a.leaves = leaves;
   a.slots = slots;
   a.state = state;
-  a.qtask = qtask;
+  a.qent = qent;
   a.nleaves = (int32_t)nleaves;
   a.cw = pairs ? RC : 4;   // FP64: narrower chunks spread the slow FP64 work over more SMs
   a.nchunk = pmv_chunks(pairs, rmax);
   if (a.nchunk == 0) return cudaErrorInvalidValue;
   a.nbulk = (int32_t)(nleaves * a.nchunk);
-  a.ntasks = (int32_t)(ntasks * a.nchunk);
-  a.mcap = mcap;
+  a.ntasks = (int32_t)pmv_queue_entries(ntasks, ninner, a.nchunk);
   a.epoch = epoch;
   a.pf = (const char*)prefetch;
   a.pf_bytes = prefetch ? prefetch_bytes : 0;
