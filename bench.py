@@ -576,9 +576,10 @@ def run_compress(args):
     cl = pkg.bisection_cluster(n, 128)
     flops_per_col = 2.0 * n * n
 
-    def compress(stats=None):
+    def compress(stats=None, prec="fp64"):
         return pkg.randcompress_adaptive(Ad, cl, cl, kest=10, atol=tol, rtol=tol, noversampling=10, stepsize=20,
-                                         rng=np.random.default_rng(1), stats=stats, device=True)
+                                         rng=np.random.default_rng(1), stats=stats, device=True,
+                                         sample_precision=prec)
 
     for _ in range(max(1, args.warmup)):
         dev = compress()
@@ -595,6 +596,18 @@ def run_compress(args):
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     gemm_ms = statistics.median(ts)
+    # the same product in double-float arithmetic (the mixed-precision form)
+    ref20 = out.clone()
+    with CP._SamplePrecision(Ad, "df"):
+        ts = []
+        for _ in range(5):
+            e0.record()
+            CP.sample(Ad, Om, out=out)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+    gemm_df_ms = statistics.median(ts)
+    gemm_df_err = float(torch.linalg.norm(out - ref20) / torch.linalg.norm(ref20))
     clocks = Clocks(0)
     clocks.start()
     times = []
@@ -607,6 +620,17 @@ def run_compress(args):
         times.append(time.perf_counter() - t0)
     ck = clocks.stop()
     ms = 1000.0 * statistics.median(times)
+    # mixed form: double-float sample products, FP64 rank decisions
+    st_df = {}
+    dev_df = compress(st_df, "df")
+    times_df = []
+    for _ in range(min(args.steps, 50)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_df = compress(st_df, "df")
+        torch.cuda.synchronize()
+        times_df.append(time.perf_counter() - t0)
+    ms_df = 1000.0 * statistics.median(times_df)
     h = dev.to_host()
     # the compressed matrix on the hot path: 64-RHS product and FP64 ULV solve
     rng = np.random.default_rng(1)
@@ -635,6 +659,8 @@ def run_compress(args):
     solve_res = float(torch.linalg.norm(AX - dB) / torch.linalg.norm(dB))
     Ay = (dB @ At)
     mv_err = float(torch.linalg.norm(dC - Ay) / torch.linalg.norm(Ay))
+    dev_df.matmul_device(dB, n, 64, dC, n)
+    mv_err_df = float(torch.linalg.norm(dC - Ay) / torch.linalg.norm(Ay))
     samples = st.get("samples", 0)
     cols = 2 * samples + 2 * 20 * st.get("rounds", 0)   # initial samples + every test round
     line = {
@@ -648,6 +674,12 @@ def run_compress(args):
         "sample_gemm": {"ms_20cols": gemm_ms, "tflops": flops_per_col * 20 / (gemm_ms * 1e-3) / 1e12,
                         "fp64_peak_tflops_measured": 1.204},
         "sample_columns_per_compression": cols,
+        "mixed_df_sampling": {
+            "ms_per_compression": ms_df, "compressions_per_s": 1000.0 / ms_df, "speedup_vs_fp64": ms / ms_df,
+            "rounds": st_df.get("rounds"), "k": st_df.get("k"), "hssrank": int(pkg.hssrank(dev_df.to_host())),
+            "matvec_rel_err_vs_dense": mv_err_df,
+            "sample_gemm_ms_20cols": gemm_df_ms, "sample_gemm_rel_diff_vs_fp64": gemm_df_err,
+            "sample_gemm_fp64_equiv_tflops": flops_per_col * 20 / (gemm_df_ms * 1e-3) / 1e12},
         "matvec64_ms": 1000.0 * statistics.median(tm), "matvec_rel_err_vs_dense": mv_err,
         "ulv64_fp64_ms": 1000.0 * statistics.median(tf), "ulv_rel_residual_vs_dense": solve_res,
         "clocks": ck,

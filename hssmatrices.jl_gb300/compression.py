@@ -7,7 +7,10 @@
 
 The dense matrix is held on the device once (``DenseDevice``, column-major
 FP64); the sample products ``A * Omega``, ``A' * Omega`` and the test product
-``hssA * Omega`` run there.  The test matrices are drawn on the host with a
+``hssA * Omega`` run there.  ``sample_precision="df"`` computes the sample
+products in double-float arithmetic on the FP32 pipe (the mixed-precision
+form: ~2^-47 relative per operation, several times the FP64 rate of GB300;
+rank decisions stay FP64); "fp64" (default) matches the reference's Float64.  The test matrices are drawn on the host with a
 NumPy ``Generator`` (``rng``), in the reference's order -- Omega_col, then
 Omega_row, then per test round Omega_col_test, Omega_row_test -- so that a
 seeded run is repeatable.  The result is an ``HssMatrix`` whose uploaded copy
@@ -118,6 +121,7 @@ class Compressor:
     def __init__(self, rcl, ccl):
         self.lib = _lib.load()
         self.table = cluster_table(rcl, ccl)
+        self.m, self.n = int(self.table[0, 3]), int(self.table[0, 5])
         self.handle = C.c_void_p()
         check(self.lib.hss_rc_create(self.table.shape[0], iptr(self.table), C.byref(self.handle)))
 
@@ -143,6 +147,23 @@ class Compressor:
                                        C.byref(h), _stream(stream)))
         return DeviceHss(_handle=h)
 
+    def sample(self, A: DenseDevice, X, trans=False, stream=None):
+        """``A * X`` (``A' * X``) through ``hss_rc_sample``: with double-float
+        sampling on, A's diagonal leaf blocks are multiplied in FP64 and the
+        rest in double-float, so the corrected sample ``S - D * X`` keeps its
+        own relative accuracy; otherwise the FP64 product of ``sample``."""
+        rows, inner = (A.n, A.m) if trans else (A.m, A.n)
+        if (A.m, A.n) != (self.m, self.n):
+            raise ValueError("DimensionMismatch: matrix and clusters")
+        if X.shape[1] != inner:
+            raise ValueError(f"DimensionMismatch: expected {inner} rows, got {X.shape[1]}")
+        r = X.shape[0]
+        out = _torch().empty((r, rows), dtype=X.dtype, device=X.device)
+        check(self.lib.hss_rc_sample(self.handle, C.c_void_p(A.ptr()), A.lda, int(bool(trans)),
+                                     C.c_void_p(X.data_ptr()), max(inner, 1), r, C.c_void_p(out.data_ptr()),
+                                     max(rows, 1), _stream(stream)))
+        return out
+
     def ranks(self):
         """(column-side, row-side) rank per cluster node of the last compression."""
         out = np.zeros(2 * self.table.shape[0], dtype=np.int32)
@@ -155,7 +176,32 @@ def _opts(opts, kw):
     return opts.copy(**kw).check()
 
 
-def randcompress(A, rcl, ccl, kest, opts=None, rng=None, device=False, **kw):
+HSS_OPT_SAMPLE_DF = 5
+
+
+class _SamplePrecision:
+    """Sets the library's sample arithmetic for the duration of one compression.
+    Double-float holds entries within float's exponent range; a matrix whose
+    largest entry lies outside [2^-60, 2^100] is sampled in FP64."""
+
+    def __init__(self, A: DenseDevice, precision):
+        if precision not in ("fp64", "df"):
+            raise ValueError(f"sample_precision must be 'fp64' or 'df', not {precision!r}")
+        self.df = precision == "df"
+        if self.df and A.t.numel() > 0:
+            amax = float(A.t.abs().max())
+            self.df = 2.0 ** -60 <= amax <= 2.0 ** 100
+
+    def __enter__(self):
+        check(_lib.load().hss_set_option(HSS_OPT_SAMPLE_DF, int(self.df)))
+        return self
+
+    def __exit__(self, *exc):
+        _lib.load().hss_set_option(HSS_OPT_SAMPLE_DF, 0)
+        return False
+
+
+def randcompress(A, rcl, ccl, kest, opts=None, rng=None, device=False, sample_precision="fp64", **kw):
     """``randcompress(A, rcl, ccl, kest)`` (src/compression.jl:278-294): one
     compression from kest + noversampling samples."""
     opts = _opts(opts, kw)
@@ -166,13 +212,15 @@ def randcompress(A, rcl, ccl, kest, opts=None, rng=None, device=False, **kw):
     s = kest + opts.noversampling
     Ocol = _cols_to_device(rng.standard_normal((n, s)))
     Orow = _cols_to_device(rng.standard_normal((m, s)))
-    Scol = sample(Ad, Ocol)
-    Srow = sample(Ad, Orow, trans=True)
+    with _SamplePrecision(Ad, sample_precision):
+        Scol = comp.sample(Ad, Ocol)
+        Srow = comp.sample(Ad, Orow, trans=True)
     dev = comp.compress(Ad, Scol, Srow, Ocol, Orow, opts.atol, opts.rtol)
     return dev if device else dev.to_host()
 
 
-def randcompress_adaptive(A, rcl, ccl, opts=None, kest=10, rng=None, stats=None, device=False, **kw):
+def randcompress_adaptive(A, rcl, ccl, opts=None, kest=10, rng=None, stats=None, device=False,
+                          sample_precision="fp64", **kw):
     """``randcompress_adaptive(A, rcl, ccl; kest)`` (src/compression.jl:312-355):
     compress, test the approximation on ``stepsize`` fresh samples
     (``sqrt(1/bs) * norm(Scol_test - hssA * Omega_test)`` against atol and
@@ -186,10 +234,12 @@ def randcompress_adaptive(A, rcl, ccl, opts=None, kest=10, rng=None, stats=None,
     maxrank = n
     comp = Compressor(rcl, ccl)
     k, r, bs = kest, opts.noversampling, opts.stepsize
+    sp = _SamplePrecision(Ad, sample_precision)
     Ocol = _cols_to_device(rng.standard_normal((n, k + r)))
     Orow = _cols_to_device(rng.standard_normal((m, k + r)))
-    Scol = sample(Ad, Ocol)
-    Srow = sample(Ad, Orow, trans=True)
+    with sp:
+        Scol = comp.sample(Ad, Ocol)
+        Srow = comp.sample(Ad, Orow, trans=True)
     failed = True
     rounds = 0
     dev = None
@@ -197,8 +247,9 @@ def randcompress_adaptive(A, rcl, ccl, opts=None, kest=10, rng=None, stats=None,
         dev = comp.compress(Ad, Scol, Srow, Ocol, Orow, opts.atol, opts.rtol)
         Ocol_t = _cols_to_device(rng.standard_normal((n, bs)))
         Orow_t = _cols_to_device(rng.standard_normal((m, bs)))
-        Scol_t = sample(Ad, Ocol_t)
-        Srow_t = sample(Ad, Orow_t, trans=True)
+        with sp:
+            Scol_t = comp.sample(Ad, Ocol_t)
+            Srow_t = comp.sample(Ad, Orow_t, trans=True)
         nrm = math.sqrt(1.0 / bs) * math.sqrt(sumsq(Scol_t))
         E = Scol_t.clone()
         dev.matmul_device(Ocol_t, n, bs, E, m, alpha=-1.0, beta=1.0)

@@ -15,6 +15,7 @@
 #include "hss_host.h"
 #include "hss_internal.h"
 #include "hss_launch.h"
+#include "hss_sample.h"
 
 using namespace hss;
 
@@ -1696,6 +1697,10 @@ int hss_set_option(int32_t option, int64_t value) {
   }
   if (option == HSS_OPT_GRAPHS) {
     g_graphs = value != 0;
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_SAMPLE_DF) {
+    g_sample_df = value != 0;
     return HSS_OK;
   }
   return fail(HSS_ERR_INVALID, "unknown option");

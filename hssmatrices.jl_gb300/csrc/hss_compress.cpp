@@ -18,6 +18,8 @@
 
 using namespace hss;
 
+bool hss::g_sample_df = false;
+
 namespace {
 
 #define RC_TRY(x)                                             \
@@ -56,6 +58,7 @@ struct hss_rc_s {
   DBuf<int32_t> d_lists;
   std::vector<int64_t> list_off;              // offsets of each level's list (levels, then root)
   DBuf<int64_t> d_leafdims;                   // row0, rows, col0, cols of the leaves
+  DBuf<int32_t> d_leafof;                     // leaf index of every row (m), then of every column (n)
   DBuf<double> scorr;                         // corrected samples: m x s then n x s
   DBuf<double> gscratch;
   DBuf<CopyTask> d_tasks;
@@ -224,6 +227,16 @@ int hss_rc_create(int64_t nnodes, const int64_t* clusters, hss_rc* out) {
   if ((e = cudaMemcpy(R->d_leafdims.p, dims.data(), dims.size() * sizeof(int64_t), cudaMemcpyHostToDevice)) !=
       cudaSuccess)
     return cfail(e, "cudaMemcpy");
+  std::vector<int32_t> leafof(R->m + R->n, 0);
+  for (int64_t k = 0; k < nl; ++k) {
+    const int32_t i = R->leaves[k];
+    for (int64_t q = R->F(i, 2); q < R->F(i, 3); ++q) leafof[q] = (int32_t)k;
+    for (int64_t q = R->F(i, 4); q < R->F(i, 5); ++q) leafof[R->m + q] = (int32_t)k;
+  }
+  if ((e = R->d_leafof.ensure(leafof.size())) != cudaSuccess) return cfail(e, "cudaMalloc");
+  if ((e = cudaMemcpy(R->d_leafof.p, leafof.data(), leafof.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return cfail(e, "cudaMemcpy");
   (void)rc;
   *out = R;
   return HSS_OK;
@@ -256,8 +269,47 @@ int hss_sample(const double* dA, int64_t lda, int64_t m, int64_t n, int32_t tran
   // split-K partial sums: stream-ordered scratch, so calls on different streams do not share it
   double* partial = nullptr;
   if (nsplit > 1) RC_TRY(cudaMallocAsync((void**)&partial, (size_t)nsplit * rows * r * sizeof(double), st));
-  launch_sample_gemm(dA, lda, rows, inner, trans, dX, ldx, r, dY, ldy, alpha, beta, nsplit, partial, st);
+  launch_sample_gemm(dA, lda, rows, inner, trans, dX, ldx, r, dY, ldy, alpha, beta, nsplit, partial, g_sample_df,
+                     nullptr, nullptr, st);
   count_launches(nsplit > 1 ? 2 : 1);
+  cudaError_t e = cudaGetLastError();
+  if (partial) {
+    cudaError_t f = cudaFreeAsync(partial, st);
+    if (e == cudaSuccess) e = f;
+  }
+  if (e != cudaSuccess) return set_cuda_error(e, "sample product");
+  return HSS_OK;
+}
+
+int hss_rc_sample(hss_rc R, const double* dA, int64_t lda, int32_t trans, const double* dX, int64_t ldx, int64_t r,
+                  double* dY, int64_t ldy, void* stream) {
+  if (!R) return set_error(HSS_ERR_INVALID, "null handle");
+  if (!g_sample_df) return hss_sample(dA, lda, R->m, R->n, trans, dX, ldx, r, dY, ldy, 1.0, 0.0, stream);
+  const int64_t m = R->m, n = R->n;
+  if (r < 0 || (trans != 0 && trans != 1)) return set_error(HSS_ERR_BAD_DIMS, "bad sizes");
+  const int64_t rows = trans ? n : m, inner = trans ? m : n;
+  if (lda < m || ldx < inner || ldy < rows) return set_error(HSS_ERR_BAD_DIMS, "leading dimension too small");
+  if (r == 0) return HSS_OK;
+  if (!dA || !dX || !dY) return set_error(HSS_ERR_INVALID, "null pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  RC_TRY(cudaSetDevice(R->device));
+  const int32_t* lr = R->d_leafof.p;        // rows of A
+  const int32_t* lc = R->d_leafof.p + m;    // columns of A
+  const int nsplit = sample_ksplit(rows, inner, r, sm_count(R->device));
+  double* partial = nullptr;
+  if (nsplit > 1) RC_TRY(cudaMallocAsync((void**)&partial, (size_t)nsplit * rows * r * sizeof(double), st));
+  // off-diagonal part in double-float, then + D * X of the leaves in FP64
+  launch_sample_gemm(dA, lda, rows, inner, trans, dX, ldx, r, dY, ldy, 1.0, 0.0, nsplit, partial, true,
+                     trans ? lc : lr, trans ? lr : lc, st);
+  count_launches(nsplit > 1 ? 2 : 1);
+  const int64_t nl = (int64_t)R->leaves.size();
+  const int64_t* dims = R->d_leafdims.p;
+  for (int64_t b = 0; b < nl; b += 65535) {
+    const int32_t cnt = (int32_t)std::min<int64_t>(65535, nl - b);
+    launch_blockdiag_gemm(cnt, trans ? R->leaf_nmax : R->leaf_mmax, dA, lda, dims + b, dims + nl + b,
+                          dims + 2 * nl + b, dims + 3 * nl + b, trans, dX, ldx, r, dY, ldy, 1.0, 1.0, st);
+    count_launches(1);
+  }
   cudaError_t e = cudaGetLastError();
   if (partial) {
     cudaError_t f = cudaFreeAsync(partial, st);

@@ -3,6 +3,8 @@
 //  * sample products S = A * Omega, S = A^T * Omega of the dense matrix
 //    (:290-291, :326-327, :336-337): FP64 tiles, split over K when the tile
 //    grid alone would not fill the GPU (partials reduced in a fixed order);
+//    or the same tiles in double-float arithmetic on the FP32 pipe
+//    (HSS_OPT_SAMPLE_DF), the mixed-precision form of the sampling;
 //  * leaf corrections S_i -= D_i * Omega_i, S_i -= D_i^T * Omega_i (:360-361),
 //    D_i addressed in place inside A (hss_blkdiag, :447-475, needs no copy);
 //  * the tree pass of `_randcompress!` (:358-430), one launch per tree level,
@@ -26,6 +28,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "hss_df.cuh"
 #include "hss_device.cuh"
 #include "hss_sample.h"
 
@@ -134,6 +137,109 @@ __global__ void sample_reduce_kernel(const double* __restrict__ P, int nsplit, i
     const int64_t i = e % m, j = e / m;
     double* y = Y + i + j * ldy;
     *y = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *y);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// double-float sample product
+// ---------------------------------------------------------------------------
+
+// (hi, lo) floats with hi + lo = x to ~2^-47 relative, from x's bits by
+// integer operations (GB300 runs FP64 instructions, conversions included, far
+// below its FP32 and integer rates): hi = x truncated to 24 significant bits,
+// lo = the remaining 29 bits rounded to 24 (nearest, ties to even).  Doubles
+// whose pieces leave float's normal range (zero, |x| < 2^-74, |x| >= 2^128,
+// inf, nan) take the conversion path.
+__device__ __forceinline__ float2 split_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  if (e < -74 || e > 127) return split_d(x);
+  const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+  const float h = __uint_as_float(sgn | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+  const unsigned low = (unsigned)b & 0x1fffffffu;   // value low * 2^(e - 52)
+  if (low == 0u) return make_float2(h, 0.f);
+  const int lz = __clz(low) - 3;                    // low < 2^29
+  const unsigned m = low << lz;                     // bit 28 set: value 1.f * 2^(e - 24 - lz)
+  unsigned mant = m >> 5;
+  const unsigned rem = m & 31u;
+  if (rem > 16u || (rem == 16u && (mant & 1u))) ++mant;
+  int el = e - 24 - lz;
+  if (mant >> 24) {
+    mant >>= 1;
+    ++el;
+  }
+  return make_float2(h, __uint_as_float(sgn | ((unsigned)(el + 127) << 23) | (mant & 0x7fffffu)));
+}
+
+// The tiles of sample_gemm_kernel with A and X split into float pairs as
+// they are staged and every product accumulated by df_fma (exact FMA product
+// error, TwoSum accumulation): ~2^-47 per operation instead of FP64's 2^-53.
+// Partials and the alpha/beta epilogue are FP64 (hi + lo is exact there).
+// With lrow/lin (leaf index of every row / inner index of op(A)), entries
+// whose row and inner index lie in the same leaf are skipped: the product of
+// A minus its diagonal leaf blocks, whose FP64 part is added separately.
+__global__ void __launch_bounds__(GT) dfsample_gemm_kernel(GemmProblem p, int trans, double alpha, double beta,
+                                                           int64_t kchunk, double* P, const int32_t* lrow,
+                                                           const int32_t* lin) {
+  __shared__ float2 As[TK][TM + 1];
+  __shared__ float2 Xs[TK][TN + 1];
+  const int64_t row0 = (int64_t)blockIdx.x * TM, col0 = (int64_t)blockIdx.y * TN;
+  const int64_t k0 = (int64_t)blockIdx.z * kchunk, k1 = min(p.k, k0 + kchunk);
+  const int tid = threadIdx.x;
+  const int tr = tid & 31, tc = tid >> 5;
+  const bool active = col0 + tc * 4 < p.r;
+  float ah[2][4], al[2][4];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) ah[a][b] = al[a][b] = 0.f;
+  for (int64_t kb = k0; kb < k1; kb += TK) {
+    for (int e = tid; e < TK * TM; e += GT) {
+      int i, kk;
+      if (!trans) { i = e % TM; kk = e / TM; }
+      else { kk = e % TK; i = e / TK; }
+      const int64_t gi = row0 + i, gk = kb + kk;
+      double v = 0.0;
+      if (gi < p.m && gk < k1 && !(lrow && __ldg(lrow + gi) == __ldg(lin + gk)))
+        v = trans ? p.A[gk + gi * p.lda] : p.A[gi + gk * p.lda];
+      As[kk][i] = split_bits(v);
+    }
+    for (int e = tid; e < TK * TN; e += GT) {
+      const int kk = e % TK, j = e / TK;
+      const int64_t gk = kb + kk, gj = col0 + j;
+      Xs[kk][j] = split_bits((gk < k1 && gj < p.r) ? p.X[gk + gj * p.ldx] : 0.0);
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int kk = 0; kk < TK; ++kk) {
+        const float2 a0 = As[kk][tr], a1 = As[kk][tr + 32];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const float2 x = Xs[kk][tc * 4 + b];
+          df_fma(ah[0][b], al[0][b], a0, x);
+          df_fma(ah[1][b], al[1][b], a1, x);
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    const int64_t gi = row0 + tr + 32 * a;
+    if (gi >= p.m) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int64_t gj = col0 + tc * 4 + b;
+      if (gj >= p.r) continue;
+      const double acc = (double)ah[a][b] + (double)al[a][b];
+      if (P) {
+        P[(int64_t)blockIdx.z * p.m * p.r + gi + gj * p.m] = acc;
+      } else {
+        double* y = p.Y + gi + gj * p.ldy;
+        *y = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *y);
+      }
+    }
   }
 }
 
@@ -453,13 +559,16 @@ int64_t sample_kchunk(int64_t k, int nsplit) {
 
 void launch_sample_gemm(const double* A, int64_t lda, int64_t m, int64_t k, int trans, const double* X,
                         int64_t ldx, int64_t r, double* Y, int64_t ldy, double alpha, double beta, int nsplit,
-                        double* partial, cudaStream_t st) {
+                        double* partial, bool df, const int32_t* lrow, const int32_t* lin, cudaStream_t st) {
   if (m <= 0 || r <= 0) return;
   GemmProblem p{A, lda, X, ldx, Y, ldy, m, k, r};
   const int64_t kchunk = sample_kchunk(std::max<int64_t>(k, 1), nsplit);
   nsplit = (int)((std::max<int64_t>(k, 1) + kchunk - 1) / kchunk);
   const dim3 grid((unsigned)((m + TM - 1) / TM), (unsigned)((r + TN - 1) / TN), (unsigned)nsplit);
-  sample_gemm_kernel<<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, nsplit > 1 ? partial : nullptr);
+  if (df)
+    dfsample_gemm_kernel<<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, nsplit > 1 ? partial : nullptr, lrow,
+                                              lin);
+  else sample_gemm_kernel<<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, nsplit > 1 ? partial : nullptr);
   if (nsplit > 1) {
     const int64_t tot = m * r;
     const unsigned blocks = (unsigned)std::min<int64_t>((tot + 255) / 256, 4096);

@@ -50,10 +50,16 @@ struct CopyTask {
 // Number of K splits of an m x r sample product over k for `sms` SMs.
 int sample_ksplit(int64_t m, int64_t k, int64_t r, int sms);
 // Y = alpha * op(A) * X + beta * Y with op(A) (m x k); trans = 1 reads A as
-// k x m.  With nsplit > 1, `partial` holds nsplit * m * r doubles.
+// k x m.  With nsplit > 1, `partial` holds nsplit * m * r doubles.  df: the
+// products in double-float arithmetic on the FP32 pipe (~2^-47 per operation;
+// entries of A and X within float's exponent range); with lrow (m leaf
+// indices of op(A)'s rows) and lin (k, of its inner index) the entries of the
+// diagonal leaf blocks are left out (df only).
 void launch_sample_gemm(const double* A, int64_t lda, int64_t m, int64_t k, int trans, const double* X,
                         int64_t ldx, int64_t r, double* Y, int64_t ldy, double alpha, double beta, int nsplit,
-                        double* partial, cudaStream_t st);
+                        double* partial, bool df, const int32_t* lrow, const int32_t* lin, cudaStream_t st);
+// HSS_OPT_SAMPLE_DF: hss_sample computes in double-float (default: FP64).
+extern bool g_sample_df;
 // Diagonal-block products of the leaves (see hss_sample.cu).
 void launch_blockdiag_gemm(int32_t count, int64_t max_dim, const double* A, int64_t lda, const int64_t* row0,
                            const int64_t* rows, const int64_t* col0, const int64_t* cols, int trans,

@@ -226,8 +226,19 @@ int64_t hss_launch_counter(void);
  * HSS_OPT_GRAPHS = 1 replays the per-level launch sequences of factorizations
  * and solve passes issued on a non-default stream as CUDA graphs: the second
  * call with unchanged task lists, buffers and sizes is captured, later ones
- * replay the graph (no capture on the legacy default stream). */
-enum { HSS_OPT_GENERIC_FACTOR = 1, HSS_OPT_RESIDUAL_FP64 = 2, HSS_OPT_LEVEL_PRODUCT = 3, HSS_OPT_GRAPHS = 4 };
+ * replay the graph (no capture on the legacy default stream).
+ * HSS_OPT_SAMPLE_DF = 1 computes hss_sample's products in double-float
+ * arithmetic on the FP32 pipe (~2^-47 relative per operation instead of
+ * FP64's 2^-53, several times faster on GB300; entries of A and X must lie
+ * within float's exponent range): the mixed-precision form of the sampling
+ * in randcompress.  0 (default): FP64. */
+enum {
+  HSS_OPT_GENERIC_FACTOR = 1,
+  HSS_OPT_RESIDUAL_FP64 = 2,
+  HSS_OPT_LEVEL_PRODUCT = 3,
+  HSS_OPT_GRAPHS = 4,
+  HSS_OPT_SAMPLE_DF = 5
+};
 int hss_set_option(int32_t option, int64_t value);
 
 const char* hss_last_error(void);
@@ -276,6 +287,17 @@ int hss_rc_compress(hss_rc rc, const double* dA, int64_t lda, const double* dSco
 /* Ranks of the last hss_rc_compress: 2 per cluster node (column side = U/R
  * rank, row side = V/W rank); 0 for the root. */
 int hss_rc_ranks(hss_rc rc, int32_t* ranks);
+
+/* S = op(A) * X for the m x n matrix of rc's clusters (new; the sample
+ * products of src/compression.jl:290-291, :336-337 for the mixed-precision
+ * form).  With HSS_OPT_SAMPLE_DF set, the part of A outside the diagonal leaf
+ * blocks is multiplied in double-float arithmetic and the leaf blocks' part
+ * D * X is added in FP64, so that the corrected sample S - D * X that
+ * hss_rc_compress forms keeps double-float accuracy relative to itself (the
+ * near-diagonal entries of kernel matrices dominate S).  Without the option:
+ * hss_sample in FP64. */
+int hss_rc_sample(hss_rc rc, const double* dA, int64_t lda, int32_t trans, const double* dX, int64_t ldx, int64_t r,
+                  double* dY, int64_t ldy, void* stream);
 
 /* Node table (nnodes x HSS_NODE_FIELDS, the hss_create format) and packed
  * generators of a single-tree handle, e.g. to rebuild the host HssMatrix. */

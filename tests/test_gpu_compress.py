@@ -57,6 +57,91 @@ def test_sample_product(pkg, m, n, s):
     assert abs(comp.sumsq(out) - np.sum(_host(out) ** 2)) <= 1e-12 * np.sum(_host(out) ** 2)
 
 
+@pytest.mark.parametrize("m,n,s", [(1000, 777, 13), (300, 20000, 37), (20000, 100, 5), (1, 1, 1)])
+def test_sample_product_double_float(pkg, m, n, s):
+    """The mixed-precision sampling (HSS_OPT_SAMPLE_DF): double-float products,
+    ~2^-47 relative per operation.  Tolerance: normwise 5e-12 on N(0,1) data
+    (the random-walk error sqrt(K) 2^-47 is ~1e-12 at K = 20000), and the
+    dot-product bound 1e-11 |A| |X| entrywise on entries spread over 40
+    decades with zeros."""
+    comp = pkg.compression
+    rng = np.random.default_rng(7 + m + n + s)
+    A = rng.standard_normal((m, n))
+    A.flat[3::7] = 0.0
+    Ad = comp.DenseDevice(A)
+    X = rng.standard_normal((n, s))
+    Y = rng.standard_normal((m, s))
+    with comp._SamplePrecision(Ad, "df") as sp:
+        assert sp.df
+        assert rel(_host(comp.sample(Ad, comp._cols_to_device(X))), A @ X) <= 5e-12
+        assert rel(_host(comp.sample(Ad, comp._cols_to_device(Y), trans=True)), A.T @ Y) <= 5e-12
+        C0 = rng.standard_normal((m, s))
+        out = comp._cols_to_device(C0)
+        comp.sample(Ad, comp._cols_to_device(X), out=out, alpha=2.0, beta=-0.5)
+        assert rel(_host(out), 2.0 * (A @ X) - 0.5 * C0) <= 5e-12
+        # magnitudes from 1e-20 to 1e20 (all within float's exponent range)
+        W = A * 10.0 ** rng.uniform(-20, 20, size=A.shape)
+        Wd = comp.DenseDevice(W)
+        got = _host(comp.sample(Wd, comp._cols_to_device(X)))
+        assert np.all(np.abs(got - W @ X) <= 1e-11 * (np.abs(W) @ np.abs(X)) + 1e-300)
+    # the option is off again: FP64 products
+    assert rel(_host(comp.sample(Ad, comp._cols_to_device(X))), A @ X) <= 1e-13
+
+
+@pytest.mark.parametrize("trans", [False, True])
+def test_cluster_sample_keeps_offdiagonal_accuracy(pkg, orc, trans):
+    """hss_rc_sample with double-float sampling: the leaf blocks' part in FP64,
+    the rest in double-float, so the corrected sample S - D X (what the tree
+    pass uses) has double-float accuracy relative to itself although the
+    near-diagonal entries of the kernel matrix dominate S.  Tolerance 5e-12
+    relative to the corrected sample; with FP64 sampling the same call is the
+    plain product (1e-13)."""
+    comp = pkg.compression
+    n = 3000
+    A = orc.cauchy_matrix(n)
+    cl = pkg.bisection_cluster(n, 64)
+    c = comp.Compressor(cl, cl)
+    Ad = comp.DenseDevice(A)
+    X = np.random.default_rng(11).standard_normal((n, 20))
+    mask = np.zeros((n, n), dtype=bool)
+    for row in c.table:
+        if row[0] < 0:
+            mask[row[2]:row[3], row[4]:row[5]] = True
+    Aop = A.T if trans else A
+    D = np.where(mask.T if trans else mask, Aop, 0.0)
+    off = (Aop - D) @ X
+    with comp._SamplePrecision(Ad, "df"):
+        S = _host(c.sample(Ad, comp._cols_to_device(X), trans=trans))
+    assert rel(S - D @ X, off) <= 5e-12
+    S64 = _host(c.sample(Ad, comp._cols_to_device(X), trans=trans))
+    assert rel(S64, Aop @ X) <= 1e-13
+
+
+def test_sample_precision_falls_back_outside_float_range(pkg):
+    comp = pkg.compression
+    A = np.full((40, 30), 1e200)
+    assert not comp._SamplePrecision(comp.DenseDevice(A), "df").df
+    with pytest.raises(ValueError):
+        comp._SamplePrecision(comp.DenseDevice(A), "fp16")
+
+
+def test_randcompress_adaptive_double_float_sampling(pkg, orc):
+    """The reference suite's compression (runtests.jl:36-40) with double-float
+    sample products: same test rounds and sample count as the oracle on the
+    same draws, error within c * tol."""
+    A = orc.runtests_matrix(2001)
+    tol = 1e-6
+    st_g, st_o = {}, {}
+    rcl = pkg.bisection_cluster(2001, 50)
+    h = pkg.randcompress_adaptive(A, rcl, rcl, kest=10, atol=tol, rtol=tol, noversampling=5, stepsize=10,
+                                  rng=np.random.default_rng(1), stats=st_g, sample_precision="df")
+    ocl = orc.bisection_cluster(2001, 50)
+    orc.randcompress_adaptive(A, ocl, ocl, 10, tol, tol, 5, 10, rng=np.random.default_rng(1), stats=st_o)
+    assert st_g["rounds"] == st_o["rounds"] and st_g["k"] == st_o["k"]
+    err = np.linalg.norm(A - orc.full(h))
+    assert err / np.linalg.norm(A) <= C_SAFETY * tol or err <= C_SAFETY * tol
+
+
 def test_sample_rejects_bad_shapes(pkg):
     comp = pkg.compression
     Ad = comp.DenseDevice(np.ones((10, 7)))
