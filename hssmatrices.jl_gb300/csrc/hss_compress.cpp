@@ -265,7 +265,7 @@ int hss_sample(const double* dA, int64_t lda, int64_t m, int64_t n, int32_t tran
   cudaStream_t st = (cudaStream_t)stream;
   int dev = 0;
   RC_TRY(cudaGetDevice(&dev));
-  const int nsplit = sample_ksplit(rows, inner, r, sm_count(dev));
+  const int nsplit = sample_ksplit(rows, inner, r, sm_count(dev), g_sample_df);
   // split-K partial sums: stream-ordered scratch, so calls on different streams do not share it
   double* partial = nullptr;
   if (nsplit > 1) RC_TRY(cudaMallocAsync((void**)&partial, (size_t)nsplit * rows * r * sizeof(double), st));
@@ -295,7 +295,7 @@ int hss_rc_sample(hss_rc R, const double* dA, int64_t lda, int32_t trans, const 
   RC_TRY(cudaSetDevice(R->device));
   const int32_t* lr = R->d_leafof.p;        // rows of A
   const int32_t* lc = R->d_leafof.p + m;    // columns of A
-  const int nsplit = sample_ksplit(rows, inner, r, sm_count(R->device));
+  const int nsplit = sample_ksplit(rows, inner, r, sm_count(R->device), true);
   double* partial = nullptr;
   if (nsplit > 1) RC_TRY(cudaMallocAsync((void**)&partial, (size_t)nsplit * rows * r * sizeof(double), st));
   // off-diagonal part in double-float, then + D * X of the leaves in FP64

@@ -171,76 +171,77 @@ __device__ __forceinline__ float2 split_bits(double x) {
   return make_float2(h, __uint_as_float(sgn | ((unsigned)(el + 127) << 23) | (mant & 0x7fffffu)));
 }
 
-// The tiles of sample_gemm_kernel with A and X split into float pairs as
-// they are staged and every product accumulated by df_fma (exact FMA product
-// error, TwoSum accumulation): ~2^-47 per operation instead of FP64's 2^-53.
+// Double-float sample product: A and X split into float pairs as they are
+// staged, every product accumulated by df_fma (exact FMA product error,
+// TwoSum accumulation): ~2^-47 per operation instead of FP64's 2^-53.
 // Partials and the alpha/beta epilogue are FP64 (hi + lo is exact there).
-// With lrow/lin (leaf index of every row / inner index of op(A)), entries
-// whose row and inner index lie in the same leaf are skipped: the product of
-// A minus its diagonal leaf blocks, whose FP64 part is added separately.
-__global__ void __launch_bounds__(GT) dfsample_gemm_kernel(GemmProblem p, int trans, double alpha, double beta,
+// Row-per-thread tiles for the narrow samples of randcompress (s = kest +
+// noversampling, stepsize: 20 columns by default): a block covers DR rows x
+// NC columns, each thread one row and all NC columns, so no warp idles when s
+// is not a multiple of 32.  K panels of TK as above.  With lrow/lin (leaf
+// index of every row / inner index of op(A)), entries whose row and inner
+// index lie in the same leaf are skipped: the product of A minus its diagonal
+// leaf blocks, whose FP64 part is added separately.
+constexpr int DR = 256;
+
+template <int NC>
+__global__ void __launch_bounds__(GT) dfsample_rows_kernel(GemmProblem p, int trans, double alpha, double beta,
                                                            int64_t kchunk, double* P, const int32_t* lrow,
                                                            const int32_t* lin) {
-  __shared__ float2 As[TK][TM + 1];
-  __shared__ float2 Xs[TK][TN + 1];
-  const int64_t row0 = (int64_t)blockIdx.x * TM, col0 = (int64_t)blockIdx.y * TN;
+  __shared__ float2 As[TK][DR];
+  __shared__ float2 Xs[TK][NC];
+  const int64_t row0 = (int64_t)blockIdx.x * DR, col0 = (int64_t)blockIdx.y * NC;
   const int64_t k0 = (int64_t)blockIdx.z * kchunk, k1 = min(p.k, k0 + kchunk);
   const int tid = threadIdx.x;
-  const int tr = tid & 31, tc = tid >> 5;
-  const bool active = col0 + tc * 4 < p.r;
-  float ah[2][4], al[2][4];
+  float ah[NC], al[NC];
 #pragma unroll
-  for (int a = 0; a < 2; ++a)
-#pragma unroll
-    for (int b = 0; b < 4; ++b) ah[a][b] = al[a][b] = 0.f;
+  for (int c = 0; c < NC; ++c) ah[c] = al[c] = 0.f;
   for (int64_t kb = k0; kb < k1; kb += TK) {
-    for (int e = tid; e < TK * TM; e += GT) {
+#pragma unroll 4
+    for (int e = tid; e < TK * DR; e += GT) {
       int i, kk;
-      if (!trans) { i = e % TM; kk = e / TM; }
-      else { kk = e % TK; i = e / TK; }
+      if (!trans) { i = e % DR; kk = e / DR; }   // consecutive threads walk A's rows
+      else { kk = e % TK; i = e / TK; }          // consecutive threads walk A's columns
       const int64_t gi = row0 + i, gk = kb + kk;
       double v = 0.0;
       if (gi < p.m && gk < k1 && !(lrow && __ldg(lrow + gi) == __ldg(lin + gk)))
         v = trans ? p.A[gk + gi * p.lda] : p.A[gi + gk * p.lda];
       As[kk][i] = split_bits(v);
     }
-    for (int e = tid; e < TK * TN; e += GT) {
+    for (int e = tid; e < TK * NC; e += GT) {
       const int kk = e % TK, j = e / TK;
       const int64_t gk = kb + kk, gj = col0 + j;
       Xs[kk][j] = split_bits((gk < k1 && gj < p.r) ? p.X[gk + gj * p.ldx] : 0.0);
     }
     __syncthreads();
-    if (active) {
+#pragma unroll 2
+    for (int kk = 0; kk < TK; ++kk) {
+      const float2 a = As[kk][tid];
 #pragma unroll
-      for (int kk = 0; kk < TK; ++kk) {
-        const float2 a0 = As[kk][tr], a1 = As[kk][tr + 32];
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const float2 x = Xs[kk][tc * 4 + b];
-          df_fma(ah[0][b], al[0][b], a0, x);
-          df_fma(ah[1][b], al[1][b], a1, x);
-        }
-      }
+      for (int c = 0; c < NC; ++c) df_fma(ah[c], al[c], a, Xs[kk][c]);
     }
     __syncthreads();
   }
+  const int64_t gi = row0 + tid;
+  if (gi >= p.m) return;
 #pragma unroll
-  for (int a = 0; a < 2; ++a) {
-    const int64_t gi = row0 + tr + 32 * a;
-    if (gi >= p.m) continue;
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const int64_t gj = col0 + tc * 4 + b;
-      if (gj >= p.r) continue;
-      const double acc = (double)ah[a][b] + (double)al[a][b];
-      if (P) {
-        P[(int64_t)blockIdx.z * p.m * p.r + gi + gj * p.m] = acc;
-      } else {
-        double* y = p.Y + gi + gj * p.ldy;
-        *y = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *y);
-      }
+  for (int c = 0; c < NC; ++c) {
+    const int64_t gj = col0 + c;
+    if (gj >= p.r) continue;
+    const double acc = (double)ah[c] + (double)al[c];
+    if (P) {
+      P[(int64_t)blockIdx.z * p.m * p.r + gi + gj * p.m] = acc;
+    } else {
+      double* y = p.Y + gi + gj * p.ldy;
+      *y = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *y);
     }
   }
+}
+
+template <int NC>
+void launch_dfrows(dim3 grid, cudaStream_t st, const GemmProblem& p, int trans, double alpha, double beta,
+                   int64_t kchunk, double* P, const int32_t* lrow, const int32_t* lin) {
+  dfsample_rows_kernel<NC><<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, P, lrow, lin);
 }
 
 // Block-diagonal product: problem z is the rows[z] x cols[z] block of A at
@@ -544,8 +545,8 @@ __global__ void copy_blocks_kernel(const CopyTask* __restrict__ t) {
 
 }  // namespace
 
-int sample_ksplit(int64_t m, int64_t k, int64_t r, int sms) {
-  const int64_t tiles = ((m + TM - 1) / TM) * ((r + TN - 1) / TN);
+int sample_ksplit(int64_t m, int64_t k, int64_t r, int sms, bool df) {
+  const int64_t tiles = df ? ((m + DR - 1) / DR) * ((r + 31) / 32) : ((m + TM - 1) / TM) * ((r + TN - 1) / TN);
   const int64_t want = 8LL * sms;   // several resident blocks per SM
   int64_t z = (want + tiles - 1) / tiles;
   z = std::min<int64_t>(z, std::max<int64_t>(1, k / (4 * TK)));   // at least 64 K per split
@@ -562,13 +563,34 @@ void launch_sample_gemm(const double* A, int64_t lda, int64_t m, int64_t k, int 
                         double* partial, bool df, const int32_t* lrow, const int32_t* lin, cudaStream_t st) {
   if (m <= 0 || r <= 0) return;
   GemmProblem p{A, lda, X, ldx, Y, ldy, m, k, r};
+  if (df) {
+    // row-per-thread tiles: NC = r rounded up to 4 (at most 32 per column tile)
+    const int nc = (int)std::min<int64_t>(32, (r + 3) / 4 * 4);
+    const int64_t kchunk = sample_kchunk(std::max<int64_t>(k, 1), nsplit);
+    nsplit = (int)((std::max<int64_t>(k, 1) + kchunk - 1) / kchunk);
+    const dim3 grid((unsigned)((m + DR - 1) / DR), (unsigned)((r + nc - 1) / nc), (unsigned)nsplit);
+    double* P = nsplit > 1 ? partial : nullptr;
+    switch (nc) {
+      case 4: launch_dfrows<4>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+      case 8: launch_dfrows<8>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+      case 12: launch_dfrows<12>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+      case 16: launch_dfrows<16>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+      case 20: launch_dfrows<20>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+      case 24: launch_dfrows<24>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+      case 28: launch_dfrows<28>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+      default: launch_dfrows<32>(grid, st, p, trans, alpha, beta, kchunk, P, lrow, lin); break;
+    }
+    if (nsplit > 1) {
+      const int64_t tot = m * r;
+      const unsigned blocks = (unsigned)std::min<int64_t>((tot + 255) / 256, 4096);
+      sample_reduce_kernel<<<blocks, 256, 0, st>>>(partial, nsplit, m, r, Y, ldy, alpha, beta);
+    }
+    return;
+  }
   const int64_t kchunk = sample_kchunk(std::max<int64_t>(k, 1), nsplit);
   nsplit = (int)((std::max<int64_t>(k, 1) + kchunk - 1) / kchunk);
   const dim3 grid((unsigned)((m + TM - 1) / TM), (unsigned)((r + TN - 1) / TN), (unsigned)nsplit);
-  if (df)
-    dfsample_gemm_kernel<<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, nsplit > 1 ? partial : nullptr, lrow,
-                                              lin);
-  else sample_gemm_kernel<<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, nsplit > 1 ? partial : nullptr);
+  sample_gemm_kernel<<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, nsplit > 1 ? partial : nullptr);
   if (nsplit > 1) {
     const int64_t tot = m * r;
     const unsigned blocks = (unsigned)std::min<int64_t>((tot + 255) / 256, 4096);

@@ -47,8 +47,9 @@ struct CopyTask {
   int64_t rows, cols;
 };
 
-// Number of K splits of an m x r sample product over k for `sms` SMs.
-int sample_ksplit(int64_t m, int64_t k, int64_t r, int sms);
+// Number of K splits of an m x r sample product over k for `sms` SMs (df:
+// the double-float kernel's tiles).
+int sample_ksplit(int64_t m, int64_t k, int64_t r, int sms, bool df);
 // Y = alpha * op(A) * X + beta * Y with op(A) (m x k); trans = 1 reads A as
 // k x m.  With nsplit > 1, `partial` holds nsplit * m * r doubles.  df: the
 // products in double-float arithmetic on the FP32 pipe (~2^-47 per operation;

@@ -289,8 +289,11 @@ def synthetic_requests(n_requests=10000, seed=3, rate=2000.0, factor_frac=0.2, n
     one of the `recent` most recently factored matrices.  Matrices come from a
     seeded pool of `pool_size` synthetic trees (each factor request gets a new
     matrix id and uploads its pool entry); right-hand sides are N(0,1) on the device.
-    The first request is a factor request."""
+    The first request is a factor request.  Each pool matrix is packed into the
+    upload layout here, when the request is made (a client sends a matrix in
+    that layout), not inside the serving loop."""
     import torch
+    from .packing import pack_cached
     from .synthetic import synthetic_hss
     rng = np.random.default_rng(seed)
     pool = []
@@ -298,6 +301,7 @@ def synthetic_requests(n_requests=10000, seed=3, rate=2000.0, factor_frac=0.2, n
         n = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
         k = int(rng.integers(k_range[0], k_range[1] + 1))
         pool.append(synthetic_hss(n, leafsize, k, rng))
+        pack_cached(pool[-1])
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
     t = 0.0
