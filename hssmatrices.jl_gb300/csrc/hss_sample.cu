@@ -148,10 +148,11 @@ __global__ void sample_reduce_kernel(const double* __restrict__ P, int nsplit, i
 // integer operations (GB300 runs FP64 instructions, conversions included, far
 // below its FP32 and integer rates): hi = x truncated to 24 significant bits,
 // lo = the remaining 29 bits rounded to 24 (nearest, ties to even).  Doubles
-// whose pieces leave float's normal range (zero, |x| < 2^-74, |x| >= 2^128,
-// inf, nan) take the conversion path.
+// whose pieces leave float's normal range (|x| < 2^-74 but not zero,
+// |x| >= 2^128, inf, nan) take the conversion path.
 __device__ __forceinline__ float2 split_bits(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  if ((b << 1) == 0ull) return make_float2(x, 0.f);   // +-0 (masked and padding entries)
   const int e = (int)((b >> 52) & 0x7ffu) - 1023;
   if (e < -74 || e > 127) return split_d(x);
   const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
@@ -184,45 +185,81 @@ __device__ __forceinline__ float2 split_bits(double x) {
 // leaf blocks, whose FP64 part is added separately.
 constexpr int DR = 256;
 
+// 8-byte asynchronous copy global -> shared; src_bytes = 0 zero-fills (src
+// must still be a valid address).
+__device__ __forceinline__ void cp8z(void* s, const void* g, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"((unsigned)__cvta_generic_to_shared(s)),
+               "l"(g), "r"(src_bytes)
+               : "memory");
+}
+
+// Shared memory: two raw FP64 panels of op(A) (TK x DR) and of X (TK x NC),
+// the split X panel, the leaf indices of the panel's inner index.
+template <int NC>
+constexpr size_t dfrows_smem() {
+  return (size_t)2 * TK * DR * 8 + (size_t)2 * TK * NC * 8 + (size_t)TK * NC * 8 + (size_t)2 * TK * 4;
+}
+
+// The next panel's copies are in flight while the current one is used; A is
+// split into its float pair where it is used (each element by one thread),
+// X once per panel (every thread uses every element).
 template <int NC>
 __global__ void __launch_bounds__(GT) dfsample_rows_kernel(GemmProblem p, int trans, double alpha, double beta,
                                                            int64_t kchunk, double* P, const int32_t* lrow,
                                                            const int32_t* lin) {
-  __shared__ float2 As[TK][DR];
-  __shared__ float2 Xs[TK][NC];
+  extern __shared__ __align__(16) unsigned char dfr_smem[];
+  double (*Araw)[TK][DR] = (double (*)[TK][DR])dfr_smem;                      // [2][TK][DR]
+  double (*Xraw)[TK][NC] = (double (*)[TK][NC])(dfr_smem + 2 * TK * DR * 8);  // [2][TK][NC]
+  float2 (*Xs)[NC] = (float2 (*)[NC])(dfr_smem + 2 * TK * DR * 8 + 2 * TK * NC * 8);
+  int32_t (*Ls)[TK] = (int32_t (*)[TK])(dfr_smem + 2 * TK * DR * 8 + 3 * TK * NC * 8);
   const int64_t row0 = (int64_t)blockIdx.x * DR, col0 = (int64_t)blockIdx.y * NC;
   const int64_t k0 = (int64_t)blockIdx.z * kchunk, k1 = min(p.k, k0 + kchunk);
   const int tid = threadIdx.x;
-  float ah[NC], al[NC];
-#pragma unroll
-  for (int c = 0; c < NC; ++c) ah[c] = al[c] = 0.f;
-  for (int64_t kb = k0; kb < k1; kb += TK) {
-#pragma unroll 4
+  const int64_t gi = row0 + tid;
+  const int32_t myleaf = (lrow && gi < p.m) ? __ldg(lrow + gi) : -1;
+  auto issue = [&](int64_t kb, int buf) {
     for (int e = tid; e < TK * DR; e += GT) {
       int i, kk;
       if (!trans) { i = e % DR; kk = e / DR; }   // consecutive threads walk A's rows
       else { kk = e % TK; i = e / TK; }          // consecutive threads walk A's columns
-      const int64_t gi = row0 + i, gk = kb + kk;
-      double v = 0.0;
-      if (gi < p.m && gk < k1 && !(lrow && __ldg(lrow + gi) == __ldg(lin + gk)))
-        v = trans ? p.A[gk + gi * p.lda] : p.A[gi + gk * p.lda];
-      As[kk][i] = split_bits(v);
+      const int64_t ri = row0 + i, gk = kb + kk;
+      const bool ok = ri < p.m && gk < k1;
+      const double* src = ok ? (trans ? p.A + gk + ri * p.lda : p.A + ri + gk * p.lda) : p.A;
+      cp8z(&Araw[buf][kk][i], src, ok ? 8 : 0);
     }
     for (int e = tid; e < TK * NC; e += GT) {
       const int kk = e % TK, j = e / TK;
       const int64_t gk = kb + kk, gj = col0 + j;
-      Xs[kk][j] = split_bits((gk < k1 && gj < p.r) ? p.X[gk + gj * p.ldx] : 0.0);
+      const bool ok = gk < k1 && gj < p.r;
+      cp8z(&Xraw[buf][kk][j], ok ? p.X + gk + gj * p.ldx : p.X, ok ? 8 : 0);
     }
+    if (tid < TK) Ls[buf][tid] = (lin && kb + tid < k1) ? __ldg(lin + kb + tid) : -2;
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  float ah[NC], al[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) ah[c] = al[c] = 0.f;
+  int buf = 0;
+  if (k0 < k1) issue(k0, 0);
+  for (int64_t kb = k0; kb < k1; kb += TK, buf ^= 1) {
+    if (kb + TK < k1) {
+      issue(kb + TK, buf ^ 1);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();   // panel kb is in place; the previous panel's Xs is no longer read
+    for (int e = tid; e < TK * NC; e += GT) Xs[e / NC][e % NC] = split_bits(Xraw[buf][e / NC][e % NC]);
     __syncthreads();
-#pragma unroll 2
+#pragma unroll(NC > 24 ? 1 : 2)
     for (int kk = 0; kk < TK; ++kk) {
-      const float2 a = As[kk][tid];
+      const double v = Araw[buf][kk][tid];
+      const float2 a = split_bits(myleaf >= 0 && Ls[buf][kk] == myleaf ? 0.0 : v);
 #pragma unroll
       for (int c = 0; c < NC; ++c) df_fma(ah[c], al[c], a, Xs[kk][c]);
     }
-    __syncthreads();
+    __syncthreads();   // every thread is done with buffer buf before it is refilled
   }
-  const int64_t gi = row0 + tid;
   if (gi >= p.m) return;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
@@ -241,7 +278,13 @@ __global__ void __launch_bounds__(GT) dfsample_rows_kernel(GemmProblem p, int tr
 template <int NC>
 void launch_dfrows(dim3 grid, cudaStream_t st, const GemmProblem& p, int trans, double alpha, double beta,
                    int64_t kchunk, double* P, const int32_t* lrow, const int32_t* lin) {
-  dfsample_rows_kernel<NC><<<grid, GT, 0, st>>>(p, trans, alpha, beta, kchunk, P, lrow, lin);
+  constexpr size_t smem = dfrows_smem<NC>();
+  static bool attr = false;   // set once per instantiation (the size is a compile-time constant)
+  if (!attr) {
+    cudaFuncSetAttribute(dfsample_rows_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  dfsample_rows_kernel<NC><<<grid, GT, smem, st>>>(p, trans, alpha, beta, kchunk, P, lrow, lin);
 }
 
 // Block-diagonal product: problem z is the rows[z] x cols[z] block of A at
