@@ -233,52 +233,70 @@ __device__ void blk_gram(int nb, int len, const float* Yt, float* G) {
   __syncthreads();
 }
 
-// T = S^{-1} explicitly (S = diag(1/tau) + strictly upper G), one column per
-// thread of warp 0: T(b,b) = tau_b, T(a,b) = -tau_a sum_{a<l<=b} G(a,l) T(l,b).
+// T = S^{-1} explicitly (S = diag(1/tau) + strictly upper G) by warp 0, one
+// row of T per lane in registers, columns in order (the recurrence of xLARFT):
+// T(i,i) = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i).  G's column i is
+// read as broadcasts; every step is 32 lanes' independent dot products.
 // Tm is row-major (ld GP), zero outside the upper triangle; also written to Tg
 // (32 x 32, column-major) for the solve.  Ends with a barrier.
 __device__ void blk_tmat(int nb, const float* G, const float* tau, float* Tm, float* Tg) {
   if (threadIdx.x < 32) {
-    const int b = threadIdx.x;
-    for (int a = b + 1; a < BP; ++a) Tm[a * GP + b] = 0.f;
-    if (b < nb) {
-      Tm[b * GP + b] = tau[b];
-      for (int a = b - 1; a >= 0; --a) {
+    const int l = threadIdx.x;
+    float tr[BP];
+#pragma unroll
+    for (int q = 0; q < BP; ++q) tr[q] = 0.f;
+#pragma unroll
+    for (int i = 0; i < BP; ++i) {
+      if (i < nb) {   // warp-uniform
         float s0 = 0.f, s1 = 0.f;
-        int l = a + 1;
-        for (; l + 1 <= b; l += 2) {
-          s0 = fmaf(G[a * GP + l], Tm[l * GP + b], s0);
-          s1 = fmaf(G[a * GP + l + 1], Tm[(l + 1) * GP + b], s1);
+#pragma unroll
+        for (int q = 0; q < i; ++q) {
+          if (q & 1) s1 = fmaf(tr[q], G[q * GP + i], s1);
+          else s0 = fmaf(tr[q], G[q * GP + i], s0);
         }
-        if (l <= b) s0 = fmaf(G[a * GP + l], Tm[l * GP + b], s0);
-        Tm[a * GP + b] = -tau[a] * (s0 + s1);
+        const float ti = tau[i];
+        tr[i] = l < i ? -ti * (s0 + s1) : (l == i ? ti : 0.f);
       }
-    } else {
-      for (int a = 0; a <= b; ++a) Tm[a * GP + b] = 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < BP; ++q) {
+      Tm[l * GP + q] = tr[q];
+      Tg[l + q * BP] = tr[q];
     }
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < BP * BP; e += FT) Tg[e] = Tm[(e % BP) * GP + e / BP];
 }
 
 // Inverses of the 32 x 32 diagonal blocks of L1 = lower part of D[0:mk, 0:mk]
-// (ld LDD), block p by warp p, column b by lane b (forward substitution),
-// written column-major to Lg + 1024 p.  `scr` holds 4 x 32 x 33 floats.
+// (ld LDD), block p by warp p: lane b holds column b of the inverse in
+// registers, rows in order (forward substitution, L(a, 0:a) read as
+// broadcasts); written column-major to Lg + 1024 p through `scr`
+// (4 x 32 x 33 floats) so that the global stores are coalesced.
 __device__ void blk_linv(int mk, const float* sD, int LDD, float* scr, float* Lg) {
   const int w = threadIdx.x >> 5, b = threadIdx.x & 31;
   const int i0 = w * BP;
   if (i0 < mk && w < 4) {
     const int nb = min(BP, mk - i0);
-    float* x = scr + w * BP * GP;   // row-major a*GP + b
-    for (int a = 0; a < BP; ++a) x[a * GP + b] = 0.f;
-    if (b < nb) {
-      x[b * GP + b] = __frcp_rn(sD[(i0 + b) + (i0 + b) * LDD]);
-      for (int a = b + 1; a < nb; ++a) {
-        float s = 0.f;
-        for (int l = b; l < a; ++l) s = fmaf(sD[(i0 + a) + (i0 + l) * LDD], x[l * GP + b], s);
-        x[a * GP + b] = -s * __frcp_rn(sD[(i0 + a) + (i0 + a) * LDD]);
+    float xc[BP];
+#pragma unroll
+    for (int a = 0; a < BP; ++a) xc[a] = 0.f;
+#pragma unroll
+    for (int a = 0; a < BP; ++a) {
+      if (a < nb) {   // warp-uniform
+        const float* La = sD + (i0 + a) + (int64_t)i0 * LDD;   // L(a, q) = La[q * LDD]
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int q = 0; q < a; ++q) {
+          if (q & 1) s1 = fmaf(La[q * LDD], xc[q], s1);
+          else s0 = fmaf(La[q * LDD], xc[q], s0);
+        }
+        const float r = __frcp_rn(La[a * LDD]);
+        xc[a] = a == b ? r : (a > b ? -(s0 + s1) * r : 0.f);
       }
     }
+    float* x = scr + w * BP * GP;   // row-major a*GP + b
+#pragma unroll
+    for (int a = 0; a < BP; ++a) x[a * GP + b] = xc[a];
     __syncwarp();
     for (int e = b; e < BP * BP; e += 32) Lg[w * 1024 + e] = x[(e % BP) * GP + e / BP];
   }
