@@ -21,6 +21,7 @@ L2 is flushed (a 512 MB write) before every timed step.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -761,6 +762,24 @@ def run_matvec_workload(args):
         out[r] = dict(res, algorithmic_bytes=alg, paths_rel_diff=diff / max(1e-300, float(torch.linalg.norm(dC))))
     clk = clocks.stop()
     g1 = out[1]["persistent"]["gbs"]
+    # full(hssA) on the device (src/hssmatrix.jl:270-305) for an n = 16384 tree
+    # of the same construction: 2.1 GB written, 2 n^2 k FLOP of off-diagonal blocks
+    nf = 16384
+    hf = pkg.synthetic_hss(nf, args.leafsize, args.rank, np.random.default_rng(5)).device()
+    Fo = torch.empty((nf, nf), dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        pkg._lib.check(lib.hss_full(hf.handle, ctypes.c_void_p(Fo.data_ptr()), nf, None))
+    torch.cuda.synchronize()
+    tf = []
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        pkg._lib.check(lib.hss_full(hf.handle, ctypes.c_void_p(Fo.data_ptr()), nf, None))
+        b.record()
+        torch.cuda.synchronize()
+        tf.append(a.elapsed_time(b))
+    full_ms = statistics.median(tf)
+    del Fo
     line = {
         "metric": "HSS matvec GB/s (FP64 hss_matmul, r=1)", "value": g1, "unit": "GB/s", "n_gpus": 1,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": out[1]["persistent"]["us_median"] / 1000.0,
@@ -771,6 +790,8 @@ def run_matvec_workload(args):
         "roofline": {"kernel": "pmv_kernel<PF64>", "bound": "hbm", "achieved": g1, "peak": peak, "unit": "GB/s",
                      "frac": g1 / peak, "peak_source": peak_src},
         "by_rhs": {str(r): v for r, v in out.items()}, "clocks": clk,
+        "full_n16384": {"ms": full_ms, "written_gbs": nf * nf * 8 / (full_ms * 1e-3) / 1e9,
+                        "fp64_tflops": 2.0 * nf * nf * args.rank / (full_ms * 1e-3) / 1e12},
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -1680,6 +1680,149 @@ int hss_trace_end(double* total_ms, int64_t* launches) {
   return HSS_OK;
 }
 
+// ---- getindex / full (src/hssmatrix.jl:102-153, 270-305) ---------------------
+
+int hss_getindex(hss_handle h, const int64_t* rows, int64_t nr, const int64_t* cols, int64_t nc, double* dOut,
+                 int64_t ldo, void* stream) {
+  if (!h) return fail(HSS_ERR_INVALID, "null handle");
+  if (h->ntrees != 1) return fail(HSS_ERR_INVALID, "getindex takes a single-tree handle");
+  if (nr < 0 || nc < 0 || ldo < std::max<int64_t>(1, nr)) return fail(HSS_ERR_BAD_DIMS, "bad sizes");
+  if (nr == 0 || nc == 0) return HSS_OK;
+  if (!rows || !cols || !dOut) return fail(HSS_ERR_INVALID, "null pointer");
+  const int64_t m = h->tree_m[0], n = h->tree_n[0];
+  for (int64_t i = 0; i < nr; ++i)
+    if (rows[i] < 0 || rows[i] >= m) return fail(HSS_ERR_BAD_DIMS, "row index out of range");
+  for (int64_t j = 0; j < nc; ++j)
+    if (cols[j] < 0 || cols[j] >= n) return fail(HSS_ERR_BAD_DIMS, "column index out of range");
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaSetDevice(h->device));
+  // sorted indices and their output positions (the sortperm of :110)
+  auto sorted = [](const int64_t* v, int64_t len, std::vector<int64_t>& val, std::vector<int64_t>& pos) {
+    pos.resize(len);
+    for (int64_t i = 0; i < len; ++i) pos[i] = i;
+    std::stable_sort(pos.begin(), pos.end(), [&](int64_t a, int64_t b) { return v[a] < v[b]; });
+    val.resize(len);
+    for (int64_t i = 0; i < len; ++i) val[i] = v[pos[i]];
+  };
+  std::vector<int64_t> R, pr, C, pc;
+  sorted(rows, nr, R, pr);
+  sorted(cols, nc, C, pc);
+  // the restricted tree (_getidx, :117-128): each node's part of the lists
+  const int64_t nn = (int64_t)h->nodes.size();
+  std::vector<GiRange> rg(nn);
+  int64_t ws = 0;
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& x = h->nodes[i];
+    GiRange& g = rg[i];
+    g.rlo = std::lower_bound(R.begin(), R.end(), x.row0) - R.begin();
+    g.rcnt = (std::lower_bound(R.begin(), R.end(), x.row0 + x.gm) - R.begin()) - g.rlo;
+    g.clo = std::lower_bound(C.begin(), C.end(), x.col0) - C.begin();
+    g.ccnt = (std::lower_bound(C.begin(), C.end(), x.col0 + x.gn) - C.begin()) - g.clo;
+  }
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& x = h->nodes[i];
+    GiRange& g = rg[i];
+    g.ub = ws; ws += x.root ? 0 : g.rcnt * x.ku;
+    g.vb = ws; ws += x.root ? 0 : g.ccnt * x.kv;
+    g.t12 = g.t21 = ws;
+    if (!x.leaf) {
+      const Node& c1 = h->nodes[x.left];
+      const Node& c2 = h->nodes[x.right];
+      g.t12 = ws; ws += rg[x.left].rcnt * c2.kv;
+      g.t21 = ws; ws += rg[x.right].rcnt * c1.kv;
+    }
+  }
+  // node lists by height (children before parents), leaves, tiles of every off-diagonal block
+  int max_h = 0;
+  for (const Node& x : h->nodes) max_h = std::max(max_h, (int)x.height);
+  std::vector<int32_t> lists, leaves;
+  std::vector<int64_t> loff;
+  for (int hh = 0; hh <= max_h; ++hh) {
+    loff.push_back((int64_t)lists.size());
+    for (int64_t i = 0; i < nn; ++i)
+      if (h->nodes[i].height == hh) lists.push_back((int32_t)i);
+  }
+  loff.push_back((int64_t)lists.size());
+  for (int64_t i = 0; i < nn; ++i)
+    if (h->nodes[i].leaf) leaves.push_back((int32_t)i);
+  std::vector<GiTile> tiles;
+  const int TTR = gi_tile_rows();
+  auto add_block = [&](int64_t T, int64_t ldt, int64_t V, int64_t ldv, int64_t rs, int64_t nrows, int64_t cs,
+                       int64_t ncols, int k) {
+    for (int64_t r0 = 0; r0 < nrows; r0 += TTR)
+      for (int64_t c0 = 0; c0 < ncols; c0 += TTR) {
+        GiTile t{};
+        t.T = T; t.V = V; t.ldt = std::max<int64_t>(ldt, 1); t.ldv = std::max<int64_t>(ldv, 1);
+        t.rs = rs; t.cs = cs;
+        t.r0 = (int32_t)r0; t.c0 = (int32_t)c0;
+        t.rows = (int32_t)std::min<int64_t>(TTR, nrows - r0);
+        t.cols = (int32_t)std::min<int64_t>(TTR, ncols - c0);
+        t.k = k;
+        tiles.push_back(t);
+      }
+  };
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& x = h->nodes[i];
+    if (x.leaf) continue;
+    const GiRange &g = rg[i], &g1 = rg[x.left], &g2 = rg[x.right];
+    const Node &c1 = h->nodes[x.left], &c2 = h->nodes[x.right];
+    if (g1.rcnt > (int64_t)INT32_MAX || g2.rcnt > (int64_t)INT32_MAX) return fail(HSS_ERR_BAD_DIMS, "too many indices");
+    add_block(g.t12, g1.rcnt, g2.vb, g2.ccnt, g1.rlo, g1.rcnt, g2.clo, g2.ccnt, c2.kv);   // A12 block
+    add_block(g.t21, g2.rcnt, g1.vb, g1.ccnt, g2.rlo, g2.rcnt, g1.clo, g1.ccnt, c1.kv);   // A21 block
+  }
+  // device copies (stream-ordered scratch)
+  int64_t *dR = nullptr, *dC = nullptr, *dpr = nullptr, *dpc = nullptr;
+  GiRange* drg = nullptr;
+  GiTile* dtl = nullptr;
+  int32_t *dlists = nullptr, *dleaves = nullptr;
+  double* dws = nullptr;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](auto** p, size_t count) {
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)p, std::max<size_t>(count, 1) * sizeof(**p), st);
+  };
+  auto put = [&](auto* d, const auto& v) {
+    if (e == cudaSuccess && !v.empty())
+      e = cudaMemcpyAsync(d, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, st);
+  };
+  alloc(&dR, nr); alloc(&dC, nc); alloc(&dpr, nr); alloc(&dpc, nc);
+  alloc(&drg, nn); alloc(&dtl, tiles.size()); alloc(&dlists, lists.size()); alloc(&dleaves, leaves.size());
+  alloc(&dws, (size_t)ws);
+  put(dR, R); put(dC, C); put(dpr, pr); put(dpc, pc); put(drg, rg); put(dtl, tiles); put(dlists, lists);
+  put(dleaves, leaves);
+  if (e == cudaSuccess) {
+    for (int hh = 0; hh <= max_h; ++hh) {
+      const int64_t cnt = loff[hh + 1] - loff[hh];
+      if (cnt > 0) {
+        launch_gi_basis(h->d_nodes, drg, dlists + loff[hh], cnt, dR, dC, dws, st);
+        count_launches(1);
+      }
+    }
+    if (!tiles.empty()) {
+      launch_gi_blocks(dtl, (int64_t)tiles.size(), dws, dpr, dpc, dOut, ldo, st);
+      count_launches(1);
+    }
+    launch_gi_leaves(h->d_nodes, drg, dleaves, (int64_t)leaves.size(), dR, dC, dpr, dpc, dOut, ldo, st);
+    count_launches(1);
+    e = cudaGetLastError();
+  }
+  // pageable sources: the copies were staged before the calls returned
+  for (void* p : {(void*)dR, (void*)dC, (void*)dpr, (void*)dpc, (void*)drg, (void*)dtl, (void*)dlists,
+                  (void*)dleaves, (void*)dws})
+    if (p) cudaFreeAsync(p, st);
+  if (e != cudaSuccess) return cuda_fail(e, "getindex");
+  return HSS_OK;
+}
+
+int hss_full(hss_handle h, double* dOut, int64_t ldo, void* stream) {
+  if (!h) return fail(HSS_ERR_INVALID, "null handle");
+  if (h->ntrees != 1) return fail(HSS_ERR_INVALID, "full takes a single-tree handle");
+  const int64_t m = h->tree_m[0], n = h->tree_n[0];
+  std::vector<int64_t> rows(m), cols(n);
+  for (int64_t i = 0; i < m; ++i) rows[i] = i;
+  for (int64_t j = 0; j < n; ++j) cols[j] = j;
+  return hss_getindex(h, rows.data(), m, cols.data(), n, dOut, ldo, stream);
+}
+
 int64_t hss_launch_counter(void) { return g_launches; }
 
 int hss_set_option(int32_t option, int64_t value) {

@@ -80,6 +80,24 @@ struct Slot {
   int32_t* sync;
 };
 
+// Entry extraction (hss_getindex.cu): per node, the node's part of the sorted
+// requested rows [rlo, rlo + rcnt) and columns [clo, clo + ccnt), and the
+// workspace offsets of its restricted bases Ub (rcnt x ku), Vb (ccnt x kv) and,
+// at a branch, of T12 = Ub1 B12 (rcnt1 x kv2) and T21 = Ub2 B21 (rcnt2 x kv1).
+struct GiRange {
+  int64_t rlo, rcnt, clo, ccnt;
+  int64_t ub, vb, t12, t21;
+};
+
+// One 64 x 64 output tile of an off-diagonal block: out rows
+// [rs + r0, rs + r0 + rows) of the sorted row list, columns [cs + c0, ...),
+// value sum_q ws[T + (r0 + i) + q ldt] ws[V + (c0 + j) + q ldv], q < k.
+struct GiTile {
+  int64_t T, V, ldt, ldv;
+  int64_t rs, cs;
+  int32_t r0, c0, rows, cols, k, pad;
+};
+
 // device status codes written into Slot::err
 enum { DEV_OK = 0, DEV_SINGULAR = 1, DEV_BAD = 2, DEV_TIMEOUT = 3 };
 

@@ -56,6 +56,18 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
                        int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
                        const void* prefetch, int64_t prefetch_bytes, int device, cudaStream_t st);
 
+// Entry extraction (hss_getindex.cu): basis pass for one list of nodes (one
+// tree height), the off-diagonal tiles, the diagonal leaf blocks.  R / C are
+// the sorted requested rows / columns, prow / pcol their output positions.
+void launch_gi_basis(const Node* nodes, const GiRange* rg, const int32_t* list, int64_t count, const int64_t* R,
+                     const int64_t* C, double* ws, cudaStream_t st);
+void launch_gi_blocks(const GiTile* tiles, int64_t count, const double* ws, const int64_t* prow, const int64_t* pcol,
+                      double* out, int64_t ldo, cudaStream_t st);
+void launch_gi_leaves(const Node* nodes, const GiRange* rg, const int32_t* leaves, int64_t count, const int64_t* R,
+                      const int64_t* C, const int64_t* prow, const int64_t* pcol, double* out, int64_t ldo,
+                      cudaStream_t st);
+int gi_tile_rows();
+
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,

@@ -237,6 +237,13 @@ class HssMatrix:
 
     __matmul__ = __mul__
 
+    def __getitem__(self, key):
+        """``hssA[i, j]`` (src/hssmatrix.jl:102-114), 0-based, on the device."""
+        from .linalg import getindex
+        if not isinstance(key, tuple) or len(key) != 2:
+            raise IndexError("HssMatrix takes two indices")
+        return getindex(self, key[0], key[1])
+
     def solve(self, b, **kw):
         """``hssA \\ b`` (src/hssmatrix.jl:234)."""
         from .linalg import ldiv

@@ -132,6 +132,34 @@ class DeviceHss:
         check(self.lib.hss_ulv_cols(self.handle, node, iptr(out), out.size, C.byref(ln)))
         return out[:ln.value]
 
+    # -- entries ------------------------------------------------------------
+    def getindex_device(self, rows, cols, out=None, stream=None):
+        """A[rows, cols] (0-based, any order, repeats allowed) into a device tensor
+        of shape (len(cols), len(rows)) (column-major), ``hss_getindex``."""
+        import torch
+        rows = np.ascontiguousarray(rows, dtype=np.int64).ravel()
+        cols = np.ascontiguousarray(cols, dtype=np.int64).ravel()
+        if out is None:
+            out = torch.empty((cols.size, rows.size), dtype=torch.float64, device="cuda")
+        check(self.lib.hss_getindex(self.handle, iptr(rows), rows.size, iptr(cols), cols.size, _ptr(out),
+                                    max(rows.size, 1), _stream(stream)))
+        return out
+
+    def getindex(self, rows, cols):
+        """A[rows, cols] as a host array (rows x cols)."""
+        import torch
+        out = self.getindex_device(rows, cols)
+        torch.cuda.synchronize()
+        return out.cpu().numpy().T
+
+    def full(self):
+        """``full(hssA)`` (src/hssmatrix.jl:270-305) as a host array, ``hss_full``."""
+        import torch
+        out = torch.empty((self.n, self.m), dtype=torch.float64, device="cuda")
+        check(self.lib.hss_full(self.handle, _ptr(out), max(self.m, 1), _stream(None)))
+        torch.cuda.synchronize()
+        return out.cpu().numpy().T
+
     # -- products -----------------------------------------------------------
     def matmul_host(self, B, alpha=1.0, beta=0.0, C_=None):
         B, vec = _as_cols(B, self.n)
@@ -292,6 +320,45 @@ def ulvfactor(hssA, precision="fp64"):
 def ulvfactsolve(hssA, b):
     """``ulvfactsolve(hssA, b)`` (src/ulvfactor.jl:10): FP64 factor + solve."""
     return ldiv(hssA, b, precision="fp64")
+
+
+def _index_list(k, size):
+    """One index of ``getindex`` (src/hssmatrix.jl:102-107): an int, a slice
+    (range or colon) or a sequence, 0-based; returns (array, scalar?)."""
+    if isinstance(k, (int, np.integer)):
+        if not -size <= k < size:
+            raise IndexError(f"index {k} out of range for size {size}")
+        return np.array([k % size], dtype=np.int64), True
+    if isinstance(k, slice):
+        return np.arange(size, dtype=np.int64)[k], False
+    a = np.asarray(k, dtype=np.int64).ravel()
+    if a.size and (a.min() < 0 or a.max() >= size):
+        raise IndexError("index out of range")
+    return a, False
+
+
+def getindex(hssA, i, j):
+    """``hssA[i, j]`` (src/hssmatrix.jl:102-114) on the device: ints, slices and
+    index sequences (0-based); a scalar for two ints, a vector when one index
+    is an int, else a matrix."""
+    m, n = hssA.size()
+    ri, si = _index_list(i, m)
+    cj, sj = _index_list(j, n)
+    dev = hssA.device() if hasattr(hssA, "device") else hssA
+    out = dev.getindex(ri, cj) if ri.size and cj.size else np.zeros((ri.size, cj.size))
+    if si and sj:
+        return float(out[0, 0])
+    if si:
+        return out[0, :]
+    if sj:
+        return out[:, 0]
+    return out
+
+
+def full(hssA):
+    """``full(hssA)`` / ``Matrix(hssA)`` (src/hssmatrix.jl:268-305) on the device."""
+    dev = hssA.device() if hasattr(hssA, "device") else hssA
+    return dev.full()
 
 
 def ldiv(hssA, b, precision="fp64", tol=None, maxit=10, stats=None):

@@ -211,6 +211,16 @@ enum {
 int hss_trace_begin(int32_t kind);
 int hss_trace_end(double* total_ms, int64_t* launches);
 
+/* Entries of a single-tree handle: out(i, j) = A(rows[i], cols[j]) into the
+ * nr x nc device matrix dOut (column-major, ld ldo >= nr), 0-based indices in
+ * any order, repeats allowed: `getindex(hssA, i::Vector, j::Vector)`
+ * (src/hssmatrix.jl:108-128).  The restricted bases of every node are formed
+ * level by level and the off-diagonal blocks in 64 x 64 FP64 tiles.
+ * hss_full is `full(hssA)` (:270-305) = all rows and columns. */
+int hss_getindex(hss_handle h, const int64_t* rows, int64_t nr, const int64_t* cols, int64_t nc, double* dOut,
+                 int64_t ldo, void* stream);
+int hss_full(hss_handle h, double* dOut, int64_t ldo, void* stream);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t hss_launch_counter(void);
 

@@ -292,6 +292,36 @@ def _full(h, A, U, V, ro, co, rootnode):
         V[co + n1:co + n1 + n2, :v2.shape[1]] = v2
 
 
+def getindex(h: HssMatrix, i, j):
+    """``getindex(hssA, i::Vector, j::Vector)`` (src/hssmatrix.jl:108-114):
+    sort both index lists, restrict the tree to them (``_getidx``, :117-128),
+    expand with ``full`` and undo the sorting.  0-based indices here."""
+    i = np.asarray(i, dtype=np.int64).ravel()
+    j = np.asarray(j, dtype=np.int64).ravel()
+    if i.size == 0 or j.size == 0:
+        return np.zeros((i.size, j.size))
+    ip = np.argsort(i, kind="stable")
+    jp = np.argsort(j, kind="stable")
+    sub = full(_getidx(h, i[ip], j[jp]))
+    out = np.empty_like(sub)
+    out[np.ix_(ip, jp)] = sub      # sub[invperm(ip), invperm(jp)]
+    return out
+
+
+def _getidx(h: HssMatrix, i, j):
+    """``_getidx(hssA, i::Vector, j::Vector)`` (src/hssmatrix.jl:117-128): the
+    HSS matrix of the selected (sorted) rows and columns."""
+    if h.leafnode:
+        x = HssMatrix.leaf(h.D[np.ix_(i, j)], h.U[i, :], h.V[j, :], rootnode=h.rootnode)
+        return x
+    m1, n1 = h.sz1
+    i1, j1 = i[i < m1], j[j < n1]
+    i2, j2 = i[i >= m1] - m1, j[j >= n1] - n1
+    A11 = _getidx(h.A11, i1, j1)
+    A22 = _getidx(h.A22, i2, j2)
+    return HssMatrix.branch(A11, A22, h.B12, h.B21, h.R1, h.W1, h.R2, h.W2, rootnode=h.rootnode)
+
+
 def adjoint(h: HssMatrix):
     """``adjoint`` (src/hssmatrix.jl:165-171) for real matrices."""
     if h.leafnode:
