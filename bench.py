@@ -70,6 +70,7 @@ def config(args, n_gpus):
         "n": args.n, "leafsize": args.leafsize, "k": args.rank, "rhs": args.rhs, "tol": args.tol,
         "seed": args.seed, "l2": "flushed before every timed step (512 MB write)",
         "parallelism": "replicas" if n_gpus > 1 else "single",
+        "launch": "dedicated stream; per-level launch sequences replayed as CUDA graphs (both FP32 and FP64 forms)",
     }
 
 
@@ -229,7 +230,12 @@ def run_ours(args, rank, world, local_rank):
     n, r = args.n, args.rhs
     A = pkg.synthetic_hss(n, args.leafsize, args.rank, np.random.default_rng(args.seed))
     dev = A.device()
-    stream = torch.cuda.current_stream()
+    # a dedicated stream, so that the library replays each step's per-level
+    # launch sequences as CUDA graphs (HSS_OPT_GRAPHS; no capture on the
+    # legacy default stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert dev.lib.hss_set_option(4, 1) == 0
     rng = np.random.default_rng(1)
     Bh = rng.standard_normal((n, r))
     # an n x r column-major matrix is an r x n row-major tensor

@@ -27,6 +27,19 @@ namespace {
 constexpr int ST = 256;
 constexpr int LDS = 257;   // odd leading dimension of the shared staging block
 
+// Asynchronous element copy global -> shared (cp.async, 4 or 8 bytes): the
+// staging copies of a block are all in flight at once; cpa_wait() waits for
+// this thread's copies, a barrier then publishes everyone's.  The sources
+// (factor blocks, the previous level's workspace) do not change during the
+// launch.
+template <typename T>
+__device__ __forceinline__ void cpa(T* s, const T* g) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  if constexpr (sizeof(T) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(g) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 template <int TPC, typename T>
 __device__ __forceinline__ T gsum(T v) {
 #pragma unroll
@@ -131,32 +144,45 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
   if (staged) {
     T* p = sx;
     if (nd.root) {
-      for (int e = tid; e < m * m; e += ST) p[e] = Lp[e];
+      for (int e = tid; e < m * m; e += ST) cpa(p + e, Lp + e);
       Lp = p; ldL = m; p += m * m;
     } else if (mk > 0) {
       T* q = p;
-      for (int e = tid; e < m * k; e += ST) q[e] = Up[e];
+      for (int e = tid; e < m * k; e += ST) cpa(q + e, Up + e);
       Up = q; ldU = m; q += m * k;
-      for (int e = tid; e < mk * mk; e += ST) q[e] = Lp[(e % mk) + (int64_t)(e / mk) * m];
+      for (int e = tid; e < mk * mk; e += ST) cpa(q + e, Lp + (e % mk) + (int64_t)(e / mk) * m);
       Lp = q; ldL = mk; q += mk * mk;
-      for (int e = tid; e < k * nk; e += ST) q[e] = L2p[(e % k) + (int64_t)(e / k) * m];
+      for (int e = tid; e < k * nk; e += ST) cpa(q + e, L2p + (e % k) + (int64_t)(e / k) * m);
       L2p = q; ldL2 = k; q += k * nk;
       // V[0:nk, :] transposed (element (l, c) at c + l*kv): consecutive threads read consecutive c
-      for (int e = tid; e < nk * kv; e += ST) q[(e / nk) + (e % nk) * kv] = Vap[(e % nk) + (int64_t)(e / nk) * n];
+      for (int e = tid; e < nk * kv; e += ST) cpa(q + (e / nk) + (e % nk) * kv, Vap + (e % nk) + (int64_t)(e / nk) * n);
       Vap = q; ldVa = -1; q += nk * kv;
       p = q;
     }
     if (!nd.leaf) {
-      for (int e = tid; e < mr1 * kv2; e += ST) p[e] = T12p[e];
+      for (int e = tid; e < mr1 * kv2; e += ST) cpa(p + e, T12p + e);
       T12p = p; p += mr1 * kv2;
-      for (int e = tid; e < mr2 * kv1; e += ST) p[e] = T21p[e];
+      for (int e = tid; e < mr2 * kv1; e += ST) cpa(p + e, T21p + e);
       T21p = p; p += mr2 * kv1;
       if (!nd.root) {
         sW1 = p; p += kv1 * kv;
         sW2 = p; p += kv2 * kv;
         // W1, W2 transposed (element (l, c) at c + l*kv)
-        for (int e = tid; e < kv1 * kv; e += ST) sW1[(e / kv1) + (e % kv1) * kv] = (T)nd.W1[e];
-        for (int e = tid; e < kv2 * kv; e += ST) sW2[(e / kv2) + (e % kv2) * kv] = (T)nd.W2[e];
+        // (converted from the FP64 generators: register loads, four in flight per thread)
+        auto stage_w = [&](T* dst, const double* src, int kc) {
+          for (int e0 = tid; e0 < kc * kv; e0 += 4 * ST) {
+            double w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) w[q] = e0 + q * ST < kc * kv ? __ldg(src + e0 + q * ST) : 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int e = e0 + q * ST;
+              if (e < kc * kv) dst[(e / kc) + (e % kc) * kv] = (T)w[q];
+            }
+          }
+        };
+        stage_w(sW1, nd.W1, kv1);
+        stage_w(sW2, nd.W2, kv2);
       }
       su1 = p; p += kv1 * CPB;
       su2 = p; p += kv2 * CPB;
@@ -183,10 +209,11 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
       const T* u1p = u1g;  int64_t ldu1 = ld;
       const T* u2p = u2g;  int64_t ldu2 = ld;
       if (staged) {
-        for (int e = tid; e < kv1 * ncol; e += ST) su1[e] = u1g[(e % kv1) + (int64_t)(e / kv1) * ld];
-        for (int e = tid; e < kv2 * ncol; e += ST) su2[e] = u2g[(e % kv2) + (int64_t)(e / kv2) * ld];
+        for (int e = tid; e < kv1 * ncol; e += ST) cpa(su1 + e, u1g + (e % kv1) + (int64_t)(e / kv1) * ld);
+        for (int e = tid; e < kv2 * ncol; e += ST) cpa(su2 + e, u2g + (e % kv2) + (int64_t)(e / kv2) * ld);
         u1p = su1; ldu1 = kv1;
         u2p = su2; ldu2 = kv2;
+        cpa_wait();
         __syncthreads();
       }
       for (int e = tid; e < m * CPB; e += ST) {
@@ -239,6 +266,7 @@ __global__ void __launch_bounds__(ST) ulv_solve_up_reg(const Task* __restrict__ 
         }
       }
     }
+    cpa_wait();   // leaves: the staged factor blocks
     __syncthreads();
     const int j = j0 + g;
     if (nd.root) {
@@ -369,8 +397,9 @@ __global__ void __launch_bounds__(ST) ulv_solve_down_reg(const Task* __restrict_
   const T* x = ws + nd.wx;
   const T* Qt = fb + nd.fQt;
   if (!nd.root && nd.mk > 0 && n * nd.mk <= stage_cap) {
-    for (int e = tid; e < n * nd.mk; e += ST) sQ[e] = Qt[e];
+    for (int e = tid; e < n * nd.mk; e += ST) cpa(sQ + e, Qt + e);
     Qt = sQ;
+    cpa_wait();
     __syncthreads();
   }
   for (int j0 = jchunk; j0 < jchunk + CPB && j0 < r; j0 += CPB) {
@@ -500,5 +529,16 @@ template void launch_ulv_solve_up_reg<double>(const Task*, int64_t, const Slot*,
 template void launch_ulv_solve_up_reg<float>(const Task*, int64_t, const Slot*, int, int64_t, int, cudaStream_t);
 template void launch_ulv_solve_down_reg<double>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
 template void launch_ulv_solve_down_reg<float>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
+
+void carveout_solve() {
+  const void* k[] = {(const void*)ulv_solve_up_reg<float, 32, 64>, (const void*)ulv_solve_up_reg<float, 32, 128>,
+                     (const void*)ulv_solve_up_reg<float, 32, 256>, (const void*)ulv_solve_up_reg<double, 32, 64>,
+                     (const void*)ulv_solve_up_reg<double, 32, 128>, (const void*)ulv_solve_up_reg<double, 32, 256>,
+                     (const void*)ulv_solve_down_reg<float, 32, 64>, (const void*)ulv_solve_down_reg<float, 32, 128>,
+                     (const void*)ulv_solve_down_reg<float, 32, 256>, (const void*)ulv_solve_down_reg<double, 32, 64>,
+                     (const void*)ulv_solve_down_reg<double, 32, 128>,
+                     (const void*)ulv_solve_down_reg<double, 32, 256>};
+  for (const void* f : k) cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+}
 
 }  // namespace hss
