@@ -399,9 +399,4 @@ void launch_bsolve_down(const Task* t, int64_t nt, const Slot* s, int mmax, int 
   bsolve_down<<<(unsigned)(nt * nchunk), BT, smem, st>>>(t, s, nchunk, ly);
 }
 
-void carveout_bsolve() {
-  cudaFuncSetAttribute((const void*)bsolve_up, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-  cudaFuncSetAttribute((const void*)bsolve_down, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-}
-
 }  // namespace hss

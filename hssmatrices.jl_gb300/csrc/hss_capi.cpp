@@ -7,7 +7,6 @@
 
 #include <algorithm>
 #include <atomic>
-#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -521,20 +520,10 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
 // so caches keyed on plans use these instead of pointers.
 std::atomic<uint64_t> g_plan_serial{0};
 
-std::once_flag g_carveout_once;
-
 // device_fill: the generator buffer is left for the caller to write on the device.
 int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill = false) {
   P->serial = ++g_plan_serial;
-  std::call_once(g_carveout_once, [] {
-    carveout_kernels();
-    carveout_factor_fast();
-    carveout_solve();
-    carveout_bsolve();
-    carveout_pmv();
-    carveout_matvec_df();
-    cudaGetLastError();   // an attribute the device does not take is only a hint
-  });
+
   for (auto& t : trees)
     if (t.npacked > 0 && t.packed == nullptr && !device_fill) return fail(HSS_ERR_INVALID, "null packed buffer");
   std::vector<GenOffsets> go;

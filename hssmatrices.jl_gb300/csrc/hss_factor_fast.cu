@@ -1076,9 +1076,4 @@ template void launch_ulv_factor_fast<double>(const Task*, int64_t, const Slot*, 
 template void launch_ulv_factor_fast<float>(const Task*, int64_t, const Slot*, int, int, int, int, size_t,
                                             cudaStream_t);
 
-void carveout_factor_fast() {
-  cudaFuncSetAttribute((const void*)ulv_factor_fast_kernel<float>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-  cudaFuncSetAttribute((const void*)ulv_factor_fast_kernel<double>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-}
-
 }  // namespace hss

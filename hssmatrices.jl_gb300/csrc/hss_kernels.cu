@@ -953,14 +953,4 @@ void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st) 
   sqrt_scale_kernel<<<(unsigned)((r + 255) / 256), 256, 0, st>>>(n2, s, r);
 }
 
-void carveout_kernels() {
-  const void* k[] = {(const void*)mv_leaf_kernel, (const void*)mv_leaf_final_kernel, (const void*)mv_up_kernel,
-                     (const void*)mv_down_kernel, (const void*)mv_up_staged_kernel, (const void*)mv_down_staged_kernel,
-                     (const void*)ulv_factor_kernel<float>, (const void*)ulv_factor_kernel<double>,
-                     (const void*)ulv_solve_up_kernel<float>, (const void*)ulv_solve_up_kernel<double>,
-                     (const void*)ulv_solve_down_kernel<float>, (const void*)ulv_solve_down_kernel<double>,
-                     (const void*)colnorm2_kernel, (const void*)sqrt_scale_kernel};
-  for (const void* f : k) cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-}
-
 }  // namespace hss

@@ -56,17 +56,6 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
                        int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
                        const void* prefetch, int64_t prefetch_bytes, int device, cudaStream_t st);
 
-// Every kernel on the product / factor / solve paths asks for the largest
-// shared-memory carveout, so that consecutive launches of different kernels
-// keep one L1 / shared-memory split (a change of split between two kernels
-// waits for the SM to drain).  Called once per process before the first launch.
-void carveout_kernels();
-void carveout_factor_fast();
-void carveout_solve();
-void carveout_bsolve();
-void carveout_pmv();
-void carveout_matvec_df();
-
 // Entry extraction (hss_getindex.cu): basis pass for one list of nodes (one
 // tree height), the off-diagonal tiles, the diagonal leaf blocks.  R / C are
 // the sorted requested rows / columns, prow / pcol their output positions.

@@ -275,10 +275,4 @@ void launch_dfmv_final(const Task* t, int64_t nt, const Slot* s, int rmax, cudaS
   if (nt > 0 && rmax > 0) dfmv_final_kernel<<<(unsigned)(nt * nchunks(rmax)), DT, 0, st>>>(t, s, nchunks(rmax));
 }
 
-void carveout_matvec_df() {
-  const void* k[] = {(const void*)df_split_kernel, (const void*)df_split_cols_kernel, (const void*)dfmv_leaf_kernel,
-                     (const void*)dfmv_up_kernel, (const void*)dfmv_down_kernel, (const void*)dfmv_final_kernel};
-  for (const void* f : k) cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-}
-
 }  // namespace hss

@@ -862,9 +862,4 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
                : cudaLaunchCooperativeKernel((void*)pmv_kernel<PF64>, grid, PT, args, smem, st);
 }
 
-void carveout_pmv() {
-  cudaFuncSetAttribute((const void*)pmv_kernel<PF64>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-  cudaFuncSetAttribute((const void*)pmv_kernel<PDF>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-}
-
 }  // namespace hss

@@ -530,15 +530,4 @@ template void launch_ulv_solve_up_reg<float>(const Task*, int64_t, const Slot*, 
 template void launch_ulv_solve_down_reg<double>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
 template void launch_ulv_solve_down_reg<float>(const Task*, int64_t, const Slot*, int, int, int, cudaStream_t);
 
-void carveout_solve() {
-  const void* k[] = {(const void*)ulv_solve_up_reg<float, 32, 64>, (const void*)ulv_solve_up_reg<float, 32, 128>,
-                     (const void*)ulv_solve_up_reg<float, 32, 256>, (const void*)ulv_solve_up_reg<double, 32, 64>,
-                     (const void*)ulv_solve_up_reg<double, 32, 128>, (const void*)ulv_solve_up_reg<double, 32, 256>,
-                     (const void*)ulv_solve_down_reg<float, 32, 64>, (const void*)ulv_solve_down_reg<float, 32, 128>,
-                     (const void*)ulv_solve_down_reg<float, 32, 256>, (const void*)ulv_solve_down_reg<double, 32, 64>,
-                     (const void*)ulv_solve_down_reg<double, 32, 128>,
-                     (const void*)ulv_solve_down_reg<double, 32, 256>};
-  for (const void* f : k) cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-}
-
 }  // namespace hss
