@@ -523,7 +523,6 @@ std::atomic<uint64_t> g_plan_serial{0};
 // device_fill: the generator buffer is left for the caller to write on the device.
 int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill = false) {
   P->serial = ++g_plan_serial;
-
   for (auto& t : trees)
     if (t.npacked > 0 && t.packed == nullptr && !device_fill) return fail(HSS_ERR_INVALID, "null packed buffer");
   std::vector<GenOffsets> go;
