@@ -173,3 +173,38 @@ def test_unpack_inverts_pack(pkg, orc):
     h2 = pkg.unpack(table, packed)
     t2, p2 = pkg.pack(h2)
     assert np.array_equal(table, t2) and np.array_equal(packed, p2)
+
+
+def test_getindex_index_forms(pkg):
+    """hssA[i, j] index normalisation (src/hssmatrix.jl:102-107): ints (also
+    negative), ranges, colons and sequences, 0-based; out of range raises."""
+    from hssmatrices_gb300.linalg import _index_list
+    a, scalar = _index_list(3, 10)
+    assert scalar and a.tolist() == [3]
+    a, scalar = _index_list(-1, 10)
+    assert scalar and a.tolist() == [9]
+    a, scalar = _index_list(slice(2, 8, 3), 10)
+    assert not scalar and a.tolist() == [2, 5]
+    a, _ = _index_list(slice(None), 4)
+    assert a.tolist() == [0, 1, 2, 3]
+    a, _ = _index_list([7, 1, 7], 10)
+    assert a.tolist() == [7, 1, 7]
+    for bad in (10, -11, [0, 10], [-1]):
+        with pytest.raises(IndexError):
+            _index_list(bad, 10)
+
+
+def test_sample_precision_switch(pkg, lib):
+    """The mixed-precision sampling switch: double-float only for matrices
+    within float's exponent range, the option reset after the compression."""
+    torch = pytest.importorskip("torch")
+    comp = pkg.compression
+    A = comp.DenseDevice(np.ones((5, 4)), device="cpu")
+    with comp._SamplePrecision(A, "df") as sp:
+        assert sp.df
+    assert not comp._SamplePrecision(A, "fp64").df
+    assert not comp._SamplePrecision(comp.DenseDevice(np.full((3, 3), 1e35), device="cpu"), "df").df
+    assert not comp._SamplePrecision(comp.DenseDevice(np.zeros((3, 3)), device="cpu"), "df").df
+    with pytest.raises(ValueError):
+        comp._SamplePrecision(A, "fp32")
+    assert lib.hss_set_option(5, 0) == 0

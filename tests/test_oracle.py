@@ -102,3 +102,18 @@ def test_oracle_cond_estimate(orc):
     A = orc.full(h)
     est = orc.cond_estimate(h, iters=40)
     assert abs(est - np.linalg.cond(A)) / np.linalg.cond(A) < 0.1
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_oracle_getindex_is_full_restricted(orc, name):
+    """getindex (src/hssmatrix.jl:108-128: sort, restrict the tree, full,
+    unsort) equals full()[i, j] for unsorted index lists with repeats."""
+    g = load_golden(name)
+    h = unpack_tree(g["table"], g["packed"], orc)
+    m, n = h.size()
+    rng = np.random.default_rng(m + n)
+    i = rng.integers(0, m, 40)
+    j = rng.integers(0, n, 33)
+    Af = orc.full(h)
+    assert np.allclose(orc.getindex(h, i, j), Af[np.ix_(i, j)], rtol=1e-13, atol=1e-13 * np.abs(Af).max())
+    assert orc.getindex(h, [], j).shape == (0, j.size)
