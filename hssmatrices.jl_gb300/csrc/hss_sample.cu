@@ -150,12 +150,16 @@ __global__ void sample_reduce_kernel(const double* __restrict__ P, int nsplit, i
 // lo = the remaining 29 bits rounded to 24 (nearest, ties to even).  Doubles
 // whose pieces leave float's normal range (|x| < 2^-74 but not zero,
 // |x| >= 2^128, inf, nan) take the conversion path.
+// the rare conversion path out of line, so that its FP64 instructions are not
+// if-converted into every call
+__device__ __noinline__ float2 split_far(double x) { return split_d(x); }
+
 __device__ __forceinline__ float2 split_bits(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  if ((b << 1) == 0ull) return make_float2(x, 0.f);   // +-0 (masked and padding entries)
-  const int e = (int)((b >> 52) & 0x7ffu) - 1023;
-  if (e < -74 || e > 127) return split_d(x);
   const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+  if ((b << 1) == 0ull) return make_float2(__uint_as_float(sgn), 0.f);   // +-0 (masked and padding entries)
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  if (e < -74 || e > 127) return split_far(x);
   const float h = __uint_as_float(sgn | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
   const unsigned low = (unsigned)b & 0x1fffffffu;   // value low * 2^(e - 52)
   if (low == 0u) return make_float2(h, 0.f);
