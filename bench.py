@@ -786,6 +786,18 @@ def run_matvec_workload(args):
         tf.append(a.elapsed_time(b))
     full_ms = statistics.median(tf)
     del Fo
+    # HSS x HSS product (src/matmul.jl:65-117) of two n = 65536, k = 32 trees
+    hb = pkg.synthetic_hss(n, args.leafsize, args.rank, np.random.default_rng(6)).device()
+    hp = ctypes.c_void_p()
+    th = []
+    for it in range(4):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pkg._lib.check(lib.hss_hssmul(dev.handle, hb.handle, ctypes.byref(hp), None))
+        th.append(time.perf_counter() - t0)
+        lib.hss_destroy(hp)
+    hssmul_ms = 1000.0 * statistics.median(th[1:])
+    leaf_flop = 2.0 * n * args.leafsize * args.leafsize * 2   # D_A D_B and the rank terms, leading order
     line = {
         "metric": "HSS matvec GB/s (FP64 hss_matmul, r=1)", "value": g1, "unit": "GB/s", "n_gpus": 1,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": out[1]["persistent"]["us_median"] / 1000.0,
@@ -798,6 +810,8 @@ def run_matvec_workload(args):
         "by_rhs": {str(r): v for r, v in out.items()}, "clocks": clk,
         "full_n16384": {"ms": full_ms, "written_gbs": nf * nf * 8 / (full_ms * 1e-3) / 1e9,
                         "fp64_tflops": 2.0 * nf * nf * args.rank / (full_ms * 1e-3) / 1e12},
+        "hssmul_n65536": {"ms": hssmul_ms, "leaf_fp64_tflops": leaf_flop / (hssmul_ms * 1e-3) / 1e12,
+                          "note": "host call to result handle (includes plan creation and the final synchronise)"},
     }
     print(json.dumps(line), flush=True)
     return 0

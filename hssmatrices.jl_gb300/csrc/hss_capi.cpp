@@ -1813,6 +1813,267 @@ int hss_getindex(hss_handle h, const int64_t* rows, int64_t nr, const int64_t* c
   return HSS_OK;
 }
 
+// ---- HSS x HSS product (src/matmul.jl:65-117) --------------------------------
+
+int hss_hssmul(hss_handle hA, hss_handle hB, hss_handle* out, void* stream) {
+  if (!hA || !hB || !out) return fail(HSS_ERR_INVALID, "null handle");
+  *out = nullptr;
+  if (hA->ntrees != 1 || hB->ntrees != 1) return fail(HSS_ERR_INVALID, "hssmul takes single-tree handles");
+  const std::vector<Node>& NA = hA->nodes;
+  const std::vector<Node>& NB = hB->nodes;
+  const int64_t nn = (int64_t)NA.size();
+  bool match = (int64_t)NB.size() == nn;
+  for (int64_t i = 0; match && i < nn; ++i)
+    match = NA[i].leaf == NB[i].leaf && NA[i].left == NB[i].left && NA[i].right == NB[i].right &&
+            NA[i].gn == NB[i].gm;
+  if (!match) return fail(HSS_ERR_BAD_DIMS, "Clusters don't seem to match");
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaSetDevice(hA->device));
+  // the product's node table: the same tree, ranks adding up
+  std::vector<int32_t> kuC(nn), kvC(nn);
+  for (int64_t i = 0; i < nn; ++i) {
+    kuC[i] = NA[i].ku + NB[i].ku;
+    kvC[i] = NA[i].kv + NB[i].kv;
+  }
+  std::vector<int64_t> table(nn * HSS_NODE_FIELDS, -1);
+  int64_t npk = 0;
+  auto blk = [&](int64_t rows, int64_t cols) -> int64_t {
+    if (rows * cols == 0) return -1;
+    const int64_t o = npk;
+    npk += rows * cols;
+    return o;
+  };
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& a = NA[i];
+    const Node& b = NB[i];
+    int64_t* f = &table[i * HSS_NODE_FIELDS];
+    f[0] = a.leaf ? -1 : a.left;
+    f[1] = a.leaf ? -1 : a.right;
+    f[2] = a.leaf ? a.gm : 0;
+    f[3] = a.leaf ? b.gn : 0;
+    f[4] = kuC[i];
+    f[5] = kvC[i];
+    f[15] = 0;
+    if (a.leaf) {
+      f[6] = blk(a.gm, b.gn);
+      f[7] = blk(a.gm, kuC[i]);
+      f[8] = blk(b.gn, kvC[i]);
+    } else {
+      f[9] = blk(kuC[a.left], kvC[a.right]);
+      f[10] = blk(kuC[a.right], kvC[a.left]);
+      f[11] = blk(kuC[a.left], kuC[i]);
+      f[12] = blk(kuC[a.right], kuC[i]);
+      f[13] = blk(kvC[a.left], kvC[i]);
+      f[14] = blk(kvC[a.right], kvC[i]);
+    }
+  }
+  hss_plan_s* PC = nullptr;
+  double* dgen = nullptr;
+  int rc = plan_create_device(nn, table.data(), npk, &PC, &dgen);
+  if (rc) return rc;
+  const std::vector<Node>& NC = PC->nodes;
+  // workspace: Z, F per non-root node; T1, T2, G1, G2, H1, H2 per branch; H per leaf
+  struct Ws { int64_t Z = -1, F = -1, T1 = -1, T2 = -1, G1 = -1, G2 = -1, H1 = -1, H2 = -1, H = -1; };
+  std::vector<Ws> w(nn);
+  int64_t wtot = 0;
+  auto wal = [&](int64_t rows, int64_t cols) { const int64_t o = wtot; wtot += std::max<int64_t>(rows * cols, 0); return o; };
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& a = NA[i];
+    const Node& b = NB[i];
+    if (!a.root) {
+      w[i].Z = wal(a.kv, b.ku);
+      w[i].F = wal(a.ku, b.kv);
+    }
+    if (a.leaf) {
+      if (!a.root) w[i].H = wal(a.ku, b.gn);
+    } else {
+      const Node &a1 = NA[a.left], &a2 = NA[a.right], &b1 = NB[b.left], &b2 = NB[b.right];
+      w[i].T1 = wal(a1.kv, b.ku);
+      w[i].T2 = wal(a2.kv, b.ku);
+      w[i].G1 = wal(a2.kv, b1.kv);
+      w[i].G2 = wal(a1.kv, b2.kv);
+      w[i].H1 = wal(a.ku, b1.kv);
+      w[i].H2 = wal(a.ku, b2.kv);
+    }
+  }
+  double* ws = nullptr;
+  MmTask* dtasks = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&ws, std::max<int64_t>(wtot, 1) * sizeof(double), st);
+  if (e != cudaSuccess) {
+    delete PC;
+    return cuda_fail(e, "hssmul workspace");
+  }
+  auto W = [&](int64_t o) { return ws + o; };
+  // task builders: C (m x n) = a1 op(A1) op(B1) [+ op(A2) op(B2)]; copies; zero fills
+  std::vector<std::vector<MmTask>> stages;
+  auto stage = [&]() { stages.emplace_back(); };
+  auto ld1 = [](int64_t v) { return (int32_t)std::max<int64_t>(v, 1); };
+  auto mm = [&](double* C, int64_t ldc, int64_t m, int64_t n, const double* A1, int64_t lda1, int ta1, const double* B1,
+                int64_t ldb1, int tb1, int64_t k1, const double* A2 = nullptr, int64_t lda2 = 1, int ta2 = 0,
+                const double* B2 = nullptr, int64_t ldb2 = 1, int tb2 = 0, int64_t k2 = 0) {
+    if (m * n == 0) return;
+    MmTask t{};
+    t.A1 = k1 > 0 ? A1 : nullptr; t.B1 = B1; t.A2 = k2 > 0 ? A2 : nullptr; t.B2 = B2; t.C = C;
+    t.lda1 = ld1(lda1); t.ldb1 = ld1(ldb1); t.lda2 = ld1(lda2); t.ldb2 = ld1(ldb2); t.ldc = ld1(ldc);
+    t.m = (int32_t)m; t.n = (int32_t)n; t.k1 = (int32_t)std::max<int64_t>(k1, 0); t.k2 = (int32_t)std::max<int64_t>(k2, 0);
+    t.ta1 = ta1; t.tb1 = tb1; t.ta2 = ta2; t.tb2 = tb2;
+    t.a1 = 1.0; t.a2 = 1.0; t.beta = 0.0;
+    stages.back().push_back(t);
+  };
+  auto cp = [&](double* C, int64_t ldc, int64_t m, int64_t n, const double* A, int64_t lda) {
+    if (m * n == 0) return;
+    MmTask t{};
+    t.A1 = A; t.C = C; t.lda1 = ld1(lda); t.ldc = ld1(ldc); t.m = (int32_t)m; t.n = (int32_t)n; t.k1 = -1;
+    stages.back().push_back(t);
+  };
+  int max_h = 0, max_d = 0;
+  for (const Node& a : NA) { max_h = std::max(max_h, (int)a.height); max_d = std::max(max_d, (int)a.depth); }
+  // upsweep (matmul.jl:86-94): Z = V_A^T U_B; Z = W1_A^T (Z1 R1_B) + W2_A^T (Z2 R2_B)
+  for (int h = 0; h <= max_h; ++h) {
+    stage();
+    for (int64_t i = 0; i < nn; ++i) {
+      const Node& a = NA[i];
+      const Node& b = NB[i];
+      if (a.height != h || a.leaf || a.root) continue;
+      const Node &a1 = NA[a.left], &a2 = NA[a.right], &b1 = NB[b.left], &b2 = NB[b.right];
+      mm(W(w[i].T1), a1.kv, a1.kv, b.ku, W(w[a.left].Z), a1.kv, 0, b.R1, b1.ku, 0, b1.ku);
+      mm(W(w[i].T2), a2.kv, a2.kv, b.ku, W(w[a.right].Z), a2.kv, 0, b.R2, b2.ku, 0, b2.ku);
+    }
+    stage();
+    for (int64_t i = 0; i < nn; ++i) {
+      const Node& a = NA[i];
+      const Node& b = NB[i];
+      if (a.height != h || a.root) continue;
+      if (a.leaf) {
+        mm(W(w[i].Z), a.kv, a.kv, b.ku, a.V, a.gn, 1, b.U, b.gm, 0, a.gn);
+      } else {
+        const Node &a1 = NA[a.left], &a2 = NA[a.right];
+        mm(W(w[i].Z), a.kv, a.kv, b.ku, a.W1, a1.kv, 1, W(w[i].T1), a1.kv, 0, a1.kv, a.W2, a2.kv, 1, W(w[i].T2),
+           a2.kv, 0, a2.kv);
+      }
+    }
+  }
+  // downsweep (:72-73, :104-105): F1 = B12_A (Z2 B21_B) + R1_A (F W1_B^T), F2 = B21_A (Z1 B12_B) + R2_A (F W2_B^T)
+  for (int d = 0; d <= max_d; ++d) {
+    stage();
+    for (int64_t i = 0; i < nn; ++i) {
+      const Node& a = NA[i];
+      const Node& b = NB[i];
+      if (a.depth != d || a.leaf) continue;
+      const Node &a1 = NA[a.left], &a2 = NA[a.right], &b1 = NB[b.left], &b2 = NB[b.right];
+      mm(W(w[i].G1), a2.kv, a2.kv, b1.kv, W(w[a.right].Z), a2.kv, 0, b.B21, b2.ku, 0, b2.ku);
+      mm(W(w[i].G2), a1.kv, a1.kv, b2.kv, W(w[a.left].Z), a1.kv, 0, b.B12, b1.ku, 0, b1.ku);
+      if (!a.root) {
+        mm(W(w[i].H1), a.ku, a.ku, b1.kv, W(w[i].F), a.ku, 0, b.W1, b1.kv, 1, b.kv);
+        mm(W(w[i].H2), a.ku, a.ku, b2.kv, W(w[i].F), a.ku, 0, b.W2, b2.kv, 1, b.kv);
+      }
+    }
+    stage();
+    for (int64_t i = 0; i < nn; ++i) {
+      const Node& a = NA[i];
+      const Node& b = NB[i];
+      if (a.depth != d || a.leaf) continue;
+      const Node &a1 = NA[a.left], &a2 = NA[a.right], &b1 = NB[b.left], &b2 = NB[b.right];
+      const int64_t kp = a.root ? 0 : a.ku;
+      mm(W(w[a.left].F), a1.ku, a1.ku, b1.kv, a.B12, a1.ku, 0, W(w[i].G1), a2.kv, 0, a2.kv, a.R1, a1.ku, 0,
+         W(w[i].H1), a.ku, 0, kp);
+      mm(W(w[a.right].F), a2.ku, a2.ku, b2.kv, a.B21, a2.ku, 0, W(w[i].G2), a1.kv, 0, a1.kv, a.R2, a2.ku, 0,
+         W(w[i].H2), a.ku, 0, kp);
+    }
+  }
+  // assembly (:98-101, :106-111)
+  stage();
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& a = NA[i];
+    const Node& b = NB[i];
+    if (a.leaf && !a.root) mm(W(w[i].H), a.ku, a.ku, b.gn, W(w[i].F), a.ku, 0, b.V, b.gn, 1, b.kv);
+  }
+  stage();
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& a = NA[i];
+    const Node& b = NB[i];
+    const Node& c = NC[i];
+    if (a.leaf) {
+      const int64_t m = a.gm, n = b.gn, p = a.gn;
+      const int64_t ku = a.root ? 0 : a.ku;
+      mm((double*)c.D, m, m, n, a.D, m, 0, b.D, p, 0, p, a.U, m, 0, W(w[i].H), std::max<int64_t>(a.ku, 1), 0, ku);
+      if (!a.root) {
+        cp((double*)c.U, m, m, a.ku, a.U, m);
+        mm((double*)c.U + m * a.ku, m, m, b.ku, a.D, m, 0, b.U, p, 0, p);
+        mm((double*)c.V, n, n, a.kv, b.D, p, 1, a.V, p, 0, p);
+        cp((double*)c.V + n * a.kv, n, n, b.kv, b.V, n);
+      }
+      continue;
+    }
+    const Node &a1 = NA[a.left], &a2 = NA[a.right], &b1 = NB[b.left], &b2 = NB[b.right];
+    const int64_t kp = a.root ? 0 : a.ku;
+    const int64_t u1 = kuC[a.left], u2 = kuC[a.right], v1 = kvC[a.left], v2 = kvC[a.right];
+    // B12 = [B12_A, R1_A F W2_B^T; 0, B12_B], B21 likewise
+    double* B12 = (double*)c.B12;
+    cp(B12, u1, a1.ku, a2.kv, a.B12, a1.ku);
+    mm(B12 + u1 * a2.kv, u1, a1.ku, b2.kv, a.R1, a1.ku, 0, W(w[i].H2), a.ku, 0, kp);
+    cp(B12 + a1.ku, u1, b1.ku, a2.kv, nullptr, 1);
+    cp(B12 + a1.ku + u1 * a2.kv, u1, b1.ku, b2.kv, b.B12, b1.ku);
+    double* B21 = (double*)c.B21;
+    cp(B21, u2, a2.ku, a1.kv, a.B21, a2.ku);
+    mm(B21 + u2 * a1.kv, u2, a2.ku, b1.kv, a.R2, a2.ku, 0, W(w[i].H1), a.ku, 0, kp);
+    cp(B21 + a2.ku, u2, b2.ku, a1.kv, nullptr, 1);
+    cp(B21 + a2.ku + u2 * a1.kv, u2, b2.ku, b1.kv, b.B21, b2.ku);
+    if (a.root) continue;
+    const int64_t up = kuC[i], vp = kvC[i];
+    // R1 = [R1_A, B12_A Z2 R2_B; 0, R1_B], R2 = [R2_A, B21_A Z1 R1_B; 0, R2_B]
+    double* R1 = (double*)c.R1;
+    cp(R1, u1, a1.ku, a.ku, a.R1, a1.ku);
+    mm(R1 + u1 * a.ku, u1, a1.ku, b.ku, a.B12, a1.ku, 0, W(w[i].T2), a2.kv, 0, a2.kv);
+    cp(R1 + a1.ku, u1, b1.ku, a.ku, nullptr, 1);
+    cp(R1 + a1.ku + u1 * a.ku, u1, b1.ku, b.ku, b.R1, b1.ku);
+    double* R2 = (double*)c.R2;
+    cp(R2, u2, a2.ku, a.ku, a.R2, a2.ku);
+    mm(R2 + u2 * a.ku, u2, a2.ku, b.ku, a.B21, a2.ku, 0, W(w[i].T1), a1.kv, 0, a1.kv);
+    cp(R2 + a2.ku, u2, b2.ku, a.ku, nullptr, 1);
+    cp(R2 + a2.ku + u2 * a.ku, u2, b2.ku, b.ku, b.R2, b2.ku);
+    // W1 = [W1_A, 0; (Z2 B21_B)^T W2_A, W1_B], W2 = [W2_A, 0; (Z1 B12_B)^T W1_A, W2_B]
+    double* W1 = (double*)c.W1;
+    cp(W1, v1, a1.kv, a.kv, a.W1, a1.kv);
+    cp(W1 + v1 * a.kv, v1, a1.kv, b.kv, nullptr, 1);
+    mm(W1 + a1.kv, v1, b1.kv, a.kv, W(w[i].G1), a2.kv, 1, a.W2, a2.kv, 0, a2.kv);
+    cp(W1 + a1.kv + v1 * a.kv, v1, b1.kv, b.kv, b.W1, b1.kv);
+    double* W2 = (double*)c.W2;
+    cp(W2, v2, a2.kv, a.kv, a.W2, a2.kv);
+    cp(W2 + v2 * a.kv, v2, a2.kv, b.kv, nullptr, 1);
+    mm(W2 + a2.kv, v2, b2.kv, a.kv, W(w[i].G2), a1.kv, 1, a.W1, a1.kv, 0, a1.kv);
+    cp(W2 + a2.kv + v2 * a.kv, v2, b2.kv, b.kv, b.W2, b2.kv);
+    (void)up; (void)vp;
+  }
+  // one upload, one launch per non-empty stage
+  std::vector<MmTask> all;
+  std::vector<std::pair<int64_t, int64_t>> ranges;
+  for (auto& sg : stages) {
+    if (sg.empty()) continue;
+    ranges.emplace_back((int64_t)all.size(), (int64_t)sg.size());
+    all.insert(all.end(), sg.begin(), sg.end());
+  }
+  if (!all.empty()) {
+    e = cudaMallocAsync((void**)&dtasks, all.size() * sizeof(MmTask), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtasks, all.data(), all.size() * sizeof(MmTask), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+      for (auto& r : ranges) launch_mm_list(dtasks + r.first, r.second, st);
+      count_launches((int64_t)ranges.size());
+      e = cudaGetLastError();
+    }
+    // the pageable task copy was staged before cudaMemcpyAsync returned
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  if (dtasks) cudaFreeAsync(dtasks, st);
+  cudaFreeAsync(ws, st);
+  if (e != cudaSuccess) {
+    delete PC;
+    return cuda_fail(e, "hssmul");
+  }
+  *out = PC;
+  return HSS_OK;
+}
+
 int hss_full(hss_handle h, double* dOut, int64_t ldo, void* stream) {
   if (!h) return fail(HSS_ERR_INVALID, "null handle");
   if (h->ntrees != 1) return fail(HSS_ERR_INVALID, "full takes a single-tree handle");

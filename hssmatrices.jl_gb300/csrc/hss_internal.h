@@ -98,6 +98,19 @@ struct GiTile {
   int32_t r0, c0, rows, cols, k, pad;
 };
 
+// One task of the HSS x HSS product (hss_hssmul.cu):
+// C (m x n, ld ldc) = a1 op(A1) op(B1) + a2 op(A2) op(B2) + beta C, op = transpose
+// when ta / tb is set; K = k1 (k2) columns of op(A); A2 may be null.  k1 = -1:
+// C = op(A1) (a block copy; A1 null: zeros).
+struct MmTask {
+  const double *A1, *B1, *A2, *B2;
+  double* C;
+  int32_t lda1, ldb1, lda2, ldb2, ldc;
+  int32_t m, n, k1, k2;
+  int32_t ta1, tb1, ta2, tb2;
+  double a1, a2, beta;
+};
+
 // device status codes written into Slot::err
 enum { DEV_OK = 0, DEV_SINGULAR = 1, DEV_BAD = 2, DEV_TIMEOUT = 3 };
 

@@ -68,6 +68,10 @@ void launch_gi_leaves(const Node* nodes, const GiRange* rg, const int32_t* leave
                       cudaStream_t st);
 int gi_tile_rows();
 
+// HSS x HSS product (hss_hssmul.cu): one launch runs a list of independent
+// small-product / copy tasks, one block per task.
+void launch_mm_list(const MmTask* tasks, int64_t count, cudaStream_t st);
+
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,

@@ -232,7 +232,10 @@ class HssMatrix:
 
     # -- operators mirroring src/matmul.jl:13-15, src/hssmatrix.jl:234 ------
     def __mul__(self, B):
-        from .linalg import matmul
+        """``hssA * B``: dense B (src/matmul.jl:13) or an HssMatrix (:65)."""
+        from .linalg import hssmul, matmul
+        if isinstance(B, HssMatrix):
+            return hssmul(self, B)
         return matmul(self, B)
 
     __matmul__ = __mul__

@@ -355,6 +355,18 @@ def getindex(hssA, i, j):
     return out
 
 
+def hssmul(hssA, hssB, device=False):
+    """``hssA * hssB`` for two HSS matrices (src/matmul.jl:65-117) on the
+    device: the product on the same cluster tree, ranks adding up.  Returns an
+    ``HssMatrix`` (or the ``DeviceHss`` handle with ``device=True``)."""
+    a = hssA.device() if hasattr(hssA, "device") else hssA
+    b = hssB.device() if hasattr(hssB, "device") else hssB
+    h = C.c_void_p()
+    check(a.lib.hss_hssmul(a.handle, b.handle, C.byref(h), _stream(None)))
+    dev = DeviceHss(_handle=h)
+    return dev if device else dev.to_host()
+
+
 def full(hssA):
     """``full(hssA)`` / ``Matrix(hssA)`` (src/hssmatrix.jl:268-305) on the device."""
     dev = hssA.device() if hasattr(hssA, "device") else hssA

@@ -221,6 +221,14 @@ int hss_getindex(hss_handle h, const int64_t* rows, int64_t nr, const int64_t* c
                  int64_t ldo, void* stream);
 int hss_full(hss_handle h, double* dOut, int64_t ldo, void* stream);
 
+/* C = A * B for two single-tree handles on matching cluster trees (A's column
+ * clusters = B's row clusters): `*(hssA::HssMatrix, hssB::HssMatrix)`
+ * (src/matmul.jl:65-117), a new handle whose ranks are the sums of the
+ * operands' (no recompression).  Upsweep, downsweep and generator assembly
+ * run as lists of small FP64 products on the device; the call synchronises
+ * `stream`. */
+int hss_hssmul(hss_handle a, hss_handle b, hss_handle* out, void* stream);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t hss_launch_counter(void);
 

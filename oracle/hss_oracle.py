@@ -292,6 +292,67 @@ def _full(h, A, U, V, ro, co, rootnode):
         V[co + n1:co + n1 + n2, :v2.shape[1]] = v2
 
 
+def hssmul(A: HssMatrix, B: HssMatrix):
+    """``*(hssA::HssMatrix, hssB::HssMatrix)`` (src/matmul.jl:65-84): the HSS
+    product of two matrices on matching cluster trees, ranks adding up
+    (no recompression).  The reference tests ``isleaf(hssA)`` twice (:66, :68);
+    on matching trees that is the same as testing both."""
+    if A.leafnode and B.leafnode:
+        return HssMatrix.leaf(A.D @ B.D, A.U, B.V, rootnode=True)
+    if A.leafnode or B.leafnode:
+        raise ValueError("Clusters don't seem to match")
+    A, B = rooted(A), rooted(B)
+    Z = _hmm_up(A, B)
+    F1 = A.B12 @ Z[2][0] @ B.B21
+    F2 = A.B21 @ Z[1][0] @ B.B12
+    B12 = _blkdiag(A.B12, B.B12)
+    B21 = _blkdiag(A.B21, B.B21)
+    C11 = _hmm_down(A.A11, B.A11, Z[1], F1)
+    C22 = _hmm_down(A.A22, B.A22, Z[2], F2)
+    return HssMatrix.branch(C11, C22, B12, B21, rootnode=True)
+
+
+def _blkdiag(X, Y):
+    out = np.zeros((X.shape[0] + Y.shape[0], X.shape[1] + Y.shape[1]))
+    out[:X.shape[0], :X.shape[1]] = X
+    out[X.shape[0]:, X.shape[1]:] = Y
+    return out
+
+
+def _hmm_up(A, B):
+    """``_matmatup(hssA, hssB)`` (src/matmul.jl:86-94): (Z, left, right) tree."""
+    if A.leafnode and B.leafnode:
+        return (A.V.T @ B.U, None, None)
+    if A.leafnode or B.leafnode:
+        raise ValueError("Clusters don't seem to match")
+    Z1 = _hmm_up(A.A11, B.A11)
+    Z2 = _hmm_up(A.A22, B.A22)
+    return (A.W1.T @ Z1[0] @ B.R1 + A.W2.T @ Z2[0] @ B.R2, Z1, Z2)
+
+
+def _hmm_down(A, B, Z, F):
+    """``_matmatdown!(hssA, hssB, Z, F)`` (src/matmul.jl:96-117)."""
+    if A.leafnode and B.leafnode:
+        D = A.D @ B.D + A.U @ F @ B.V.T
+        U = np.hstack([A.U, A.D @ B.U])
+        V = np.hstack([B.D.T @ A.V, B.V])
+        return HssMatrix.leaf(D, U, V, rootnode=False)
+    if A.leafnode or B.leafnode:
+        raise ValueError("Clusters don't seem to match")
+    Zl, Zr = Z[1][0], Z[2][0]
+    F1 = A.B12 @ Zr @ B.B21 + A.R1 @ F @ B.W1.T
+    F2 = A.B21 @ Zl @ B.B12 + A.R2 @ F @ B.W2.T
+    B12 = np.block([[A.B12, A.R1 @ F @ B.W2.T], [np.zeros((B.B12.shape[0], A.B12.shape[1])), B.B12]])
+    B21 = np.block([[A.B21, A.R2 @ F @ B.W1.T], [np.zeros((B.B21.shape[0], A.B21.shape[1])), B.B21]])
+    R1 = np.block([[A.R1, A.B12 @ Zr @ B.R2], [np.zeros((B.R1.shape[0], A.R1.shape[1])), B.R1]])
+    W1 = np.block([[A.W1, np.zeros((A.W1.shape[0], B.W1.shape[1]))], [B.B21.T @ Zr.T @ A.W2, B.W1]])
+    R2 = np.block([[A.R2, A.B21 @ Zl @ B.R1], [np.zeros((B.R2.shape[0], A.R2.shape[1])), B.R2]])
+    W2 = np.block([[A.W2, np.zeros((A.W2.shape[0], B.W2.shape[1]))], [B.B12.T @ Zl.T @ A.W1, B.W2]])
+    C11 = _hmm_down(A.A11, B.A11, Z[1], F1)
+    C22 = _hmm_down(A.A22, B.A22, Z[2], F2)
+    return HssMatrix.branch(C11, C22, B12, B21, R1, W1, R2, W2, rootnode=False)
+
+
 def getindex(h: HssMatrix, i, j):
     """``getindex(hssA, i::Vector, j::Vector)`` (src/hssmatrix.jl:108-114):
     sort both index lists, restrict the tree to them (``_getidx``, :117-128),
