@@ -42,7 +42,7 @@ EXPORTS = [
     "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option", "hss_matmul_noalloc",
     "hss_batcher_create", "hss_batcher_destroy", "hss_batcher_factor", "hss_batcher_solve",
     "hss_sample", "hss_sumsq", "hss_rc_create", "hss_rc_destroy", "hss_rc_size", "hss_rc_compress",
-    "hss_rc_ranks", "hss_rc_sample", "hss_export_size", "hss_export", "hss_getindex", "hss_full", "hss_hssmul",
+    "hss_rc_ranks", "hss_rc_sample", "hss_export_size", "hss_export", "hss_getindex", "hss_full", "hss_hssmul", "hss_recompress", "hss_orthonormalize",
 ]
 
 
@@ -118,6 +118,8 @@ def _declare(lib):
         "hss_getindex": (C.c_int, [P, P, I64, P, I64, P, I64, P]),
         "hss_full": (C.c_int, [P, P, I64, P]),
         "hss_hssmul": (C.c_int, [P, P, C.POINTER(C.c_void_p), P]),
+        "hss_recompress": (C.c_int, [P, D, D, C.POINTER(C.c_void_p), P]),
+        "hss_orthonormalize": (C.c_int, [P, C.POINTER(C.c_void_p), P]),
         "hss_export_size": (C.c_int, [P, PI64, PI64]),
         "hss_export": (C.c_int, [P, PI64, PD]),
         "hss_last_error": (C.c_char_p, []),

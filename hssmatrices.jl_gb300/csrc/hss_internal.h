@@ -111,6 +111,22 @@ struct MmTask {
   double a1, a2, beta;
 };
 
+// One truncated column-pivoted QR (hss_recompress.cu): G (p x q, ld ldg) is
+// factored in place; the rank (leading |R_jj| > max(atol, rtol |R_11|)) goes to
+// *rank, Q's first rank columns to Q (ld ldq), R's first rank rows with the
+// pivoting undone to R (ld ldr).
+struct PqrTask {
+  double* G;
+  int64_t ldg;
+  int32_t p, q;
+  double* Q;
+  int64_t ldq;
+  double* R;
+  int64_t ldr;
+  double atol, rtol;
+  int32_t* rank;
+};
+
 // device status codes written into Slot::err
 enum { DEV_OK = 0, DEV_SINGULAR = 1, DEV_BAD = 2, DEV_TIMEOUT = 3 };
 

@@ -72,6 +72,10 @@ int gi_tile_rows();
 // small-product / copy tasks, one block per task.
 void launch_mm_list(const MmTask* tasks, int64_t count, cudaStream_t st);
 
+// Truncated pivoted QRs (hss_recompress.cu), one block per task; qmax / kmax
+// bound the tasks' q and min(p, q).
+void launch_pqr(const PqrTask* tasks, int64_t count, int qmax, int kmax, cudaStream_t st);
+
 // ULV factor / solve (reference src/ulvfactor.jl:22-107), T = double or float.
 template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,

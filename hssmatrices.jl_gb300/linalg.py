@@ -367,6 +367,32 @@ def hssmul(hssA, hssB, device=False):
     return dev if device else dev.to_host()
 
 
+def recompress(hssA, atol=None, rtol=None, device=False):
+    """``recompress!(hssA; atol, rtol)`` (src/compression.jl:148-260) on the
+    device: orthonormalized generators, couplings truncated top-down.  Returns
+    a new ``HssMatrix`` (the reference modifies hssA in place); tolerances
+    default to ``HssOptions``'."""
+    from .hssmatrix import HssOptions
+    opts = HssOptions.current()
+    atol = opts.atol if atol is None else atol
+    rtol = opts.rtol if rtol is None else rtol
+    a = hssA.device() if hasattr(hssA, "device") else hssA
+    h = C.c_void_p()
+    check(a.lib.hss_recompress(a.handle, float(atol), float(rtol), C.byref(h), _stream(None)))
+    dev = DeviceHss(_handle=h)
+    return dev if device else dev.to_host()
+
+
+def orthonormalize_generators(hssA, device=False):
+    """``orthonormalize_generators!(hssA)`` (src/generators.jl:64-114) on the
+    device; returns a new ``HssMatrix``."""
+    a = hssA.device() if hasattr(hssA, "device") else hssA
+    h = C.c_void_p()
+    check(a.lib.hss_orthonormalize(a.handle, C.byref(h), _stream(None)))
+    dev = DeviceHss(_handle=h)
+    return dev if device else dev.to_host()
+
+
 def full(hssA):
     """``full(hssA)`` / ``Matrix(hssA)`` (src/hssmatrix.jl:268-305) on the device."""
     dev = hssA.device() if hasattr(hssA, "device") else hssA

@@ -229,6 +229,15 @@ int hss_full(hss_handle h, double* dOut, int64_t ldo, void* stream);
  * `stream`. */
 int hss_hssmul(hss_handle a, hss_handle b, hss_handle* out, void* stream);
 
+/* `recompress!(hssA; atol, rtol)` (src/compression.jl:148-260) on the device:
+ * orthonormalize the generators (src/generators.jl:64-114), then truncate
+ * the couplings top-down, every rank decision a column-pivoted QR on the GPU
+ * with `_compress_block!`'s rule (keep |R_ii| > max(atol, rtol |R_11|)).  The
+ * result is a new handle; the input is not modified.  hss_orthonormalize is
+ * the first half alone.  Both synchronise `stream` once per tree level. */
+int hss_recompress(hss_handle h, double atol, double rtol, hss_handle* out, void* stream);
+int hss_orthonormalize(hss_handle h, hss_handle* out, void* stream);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t hss_launch_counter(void);
 

@@ -698,6 +698,109 @@ def _compress_block(A, atol, rtol):
     return Q[:, :rk].copy(), R[:rk, :][:, inv].copy()
 
 
+# LowRankApprox's default relative tolerance for pqrfact without options
+# (assumed: 5 eps; the package is not in the reference tree, so unpinned).
+PQR_DEFAULT_RTOL = 5 * np.finfo(float).eps
+
+
+def _pqr(A):
+    """``pqrfact!(A, sketch=:none)`` with default tolerances: (Q, R P^T)."""
+    return _compress_block(np.asarray(A, float), 0.0, PQR_DEFAULT_RTOL)
+
+
+def orthonormalize_generators(h: HssMatrix):
+    """``orthonormalize_generators!`` (src/generators.jl:64-114): every U and
+    every stacked [R1; R2] (V, [W1; W2] likewise) replaced by the Q of its
+    pivoted QR, the R factors moved into the parent's B, R and W.  In place."""
+    if h.leafnode:
+        return h
+    def side(c):
+        """(RU, RV) of child c after orthonormalizing it (R with columns unpermuted)."""
+        if c.leafnode:
+            QU, RU = _pqr(c.U)
+            QV, RV = _pqr(c.V)
+            c.U, c.V = QU, QV
+            return RU, RV
+        orthonormalize_generators(c)
+        rm1, rn1 = c.R1.shape[0], c.W1.shape[0]
+        QU, RU = _pqr(np.vstack([c.R1, c.R2]))
+        QV, RV = _pqr(np.vstack([c.W1, c.W2]))
+        c.R1, c.R2 = QU[:rm1, :], QU[rm1:, :]
+        c.W1, c.W2 = QV[:rn1, :], QV[rn1:, :]
+        return RU, RV
+    RU1, RV1 = side(h.A11)
+    RU2, RV2 = side(h.A22)
+    h.B12 = RU1 @ h.B12 @ RV2.T
+    h.B21 = RU2 @ h.B21 @ RV1.T
+    h.R1 = RU1 @ h.R1
+    h.R2 = RU2 @ h.R2
+    h.W1 = RV1 @ h.W1
+    h.W2 = RV2 @ h.W2
+    return h
+
+
+def _push(c, P, Q):
+    """Children's generators after a parent's truncation (src/compression.jl:176-195)."""
+    if c.leafnode:
+        c.U = c.U @ P
+        c.V = c.V @ Q
+    else:
+        c.R1, c.R2 = c.R1 @ P, c.R2 @ P
+        c.W1, c.W2 = c.W1 @ Q, c.W2 @ Q
+
+
+def recompress(h: HssMatrix, atol=1e-9, rtol=1e-9):
+    """``recompress!`` (src/compression.jl:148-203): orthonormalize, then
+    truncate the couplings top-down with ``_compress_block!``.  In place."""
+    if h.leafnode:
+        return h
+    orthonormalize_generators(h)
+    P1, S2 = _compress_block(h.B12, atol, rtol)
+    Q2, T1 = _compress_block(h.B12.T.copy(), atol, rtol)
+    P2, S1 = _compress_block(h.B21, atol, rtol)
+    Q1, T2 = _compress_block(h.B21.T.copy(), atol, rtol)
+    h.B12 = S2 @ Q2
+    h.B21 = S1 @ Q1
+    h.R1 = h.R1[:h.B12.shape[0], :]
+    h.W1 = h.W1[:h.B21.shape[1], :]
+    h.R2 = h.R2[:h.B21.shape[0], :]
+    h.W2 = h.W2[:h.B12.shape[1], :]
+    _push(h.A11, P1, Q1)
+    _push(h.A22, P2, Q2)
+    if not h.A11.leafnode:
+        _recompress(h.A11, h.B12, h.B21.T.copy(), atol, rtol)
+    if not h.A22.leafnode:
+        _recompress(h.A22, h.B21, h.B12.T.copy(), atol, rtol)
+    return h
+
+
+def _recompress(h, Brow, Bcol, atol, rtol):
+    """``_recompress!`` (src/compression.jl:205-260)."""
+    Brow1 = np.hstack([h.B12, h.R1 @ Brow])
+    Bcol2 = np.hstack([h.B12.T, h.W2 @ Bcol])
+    P1, S2 = _compress_block(Brow1, atol, rtol)
+    Q2, T1 = _compress_block(Bcol2, atol, rtol)
+    rm1, rn2 = h.B12.shape
+    h.B12 = S2[:, :rn2] @ Q2
+    h.R1 = P1.T @ h.R1
+    h.W2 = Q2.T @ h.W2
+    Brow2 = np.hstack([h.B21, h.R2 @ Brow])
+    Bcol1 = np.hstack([h.B21.T, h.W1 @ Bcol])
+    P2, S1 = _compress_block(Brow2, atol, rtol)
+    Q1, T2 = _compress_block(Bcol1, atol, rtol)
+    rm2, rn1 = h.B21.shape
+    h.B21 = S1[:, :rn1] @ Q1
+    h.R2 = P2.T @ h.R2
+    h.W1 = Q1.T @ h.W1
+    _push(h.A11, P1, Q1)
+    _push(h.A22, P2, Q2)
+    if not h.A11.leafnode:
+        _recompress(h.A11, np.hstack([h.B12, S2[:, rn2:]]), np.hstack([h.B21.T, T2[:, rm2:]]), atol, rtol)
+    if not h.A22.leafnode:
+        _recompress(h.A22, np.hstack([h.B21, S1[:, rn1:]]), np.hstack([h.B12.T, T1[:, rm1:]]), atol, rtol)
+    return h
+
+
 def compress(A, rcl: ClusterTree, ccl: ClusterTree, atol=1e-9, rtol=1e-9):
     """``compress(A, rcl, ccl; atol, rtol)`` (src/compression.jl:47-63)."""
     A = np.asarray(A, dtype=float)
