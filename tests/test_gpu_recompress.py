@@ -82,3 +82,18 @@ def test_recompress_after_product_lowers_ranks(pkg, orc):
     assert pkg.hssrank(Cr) < pkg.hssrank(C)
     ref = orc.full(h) @ orc.full(h)
     assert rel(orc.full(as_oracle(pkg, orc, Cr)), ref) <= 1e-6
+
+
+def test_recompress_single_leaf_and_forest(pkg, orc):
+    """A single leaf has nothing to recompress (compression.jl:152); forests
+    are rejected (the reference works on one tree)."""
+    h = orc.synthetic_hss(60, 64, 5, np.random.default_rng(8))
+    r = as_oracle(pkg, orc, pkg.recompress(pkg.HssMatrix.from_tree(h), atol=1e-6, rtol=1e-6))
+    assert rel(orc.full(r), orc.full(h)) <= 1e-15
+    rng = np.random.default_rng(9)
+    trees = [orc.synthetic_hss(300, 64, 8, rng), orc.synthetic_hss(200, 64, 8, rng)]
+    dev = pkg.DeviceHss.from_trees([pkg.HssMatrix.from_tree(t) for t in trees])
+    with pytest.raises(ValueError):
+        pkg.recompress(dev)
+    with pytest.raises(ValueError):
+        pkg.orthonormalize_generators(dev)
