@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 struct hss_plan_s;
 
@@ -69,5 +70,14 @@ void count_launches(int64_t n);
 // the device; *d_gen receives its address.
 int plan_create_device(int64_t nnodes, const int64_t* table, int64_t npacked, hss_plan_s** out, double** d_gen);
 void plan_destroy(hss_plan_s* p);
+// A plan's host copy of its node descriptors (device pointers inside), the
+// device copy, and its device, tree count and the first tree's size.
+struct Node;
+const std::vector<Node>& plan_nodes(const hss_plan_s* p);
+const Node* plan_device_nodes(const hss_plan_s* p);
+int plan_device(const hss_plan_s* p);
+int32_t plan_ntrees(const hss_plan_s* p);
+int64_t plan_rows(const hss_plan_s* p);
+int64_t plan_cols(const hss_plan_s* p);
 
 }  // namespace hss
