@@ -765,7 +765,8 @@ def run_matvec_workload(args):
             finally:
                 lib.hss_set_option(3, 0)
         diff = float(np.linalg.norm(res.pop("C") - res.pop("C_level")))
-        out[r] = dict(res, algorithmic_bytes=alg, paths_rel_diff=diff / max(1e-300, float(torch.linalg.norm(dC))))
+        out[r] = dict(res, algorithmic_bytes=alg, paths_rel_diff=diff / max(1e-300, float(torch.linalg.norm(dC))),
+                      kernel="pmv_flat_kernel" if r <= 4 else "pmv_kernel<PF64>")
     clk = clocks.stop()
     g1 = out[1]["persistent"]["gbs"]
     # full(hssA) on the device (src/hssmatrix.jl:270-305) for an n = 16384 tree
@@ -822,8 +823,11 @@ def run_matvec_workload(args):
         "config": {"workload": (f"matvec: synthetic HSS n={n}, perfect tree leafsize {args.leafsize}, k={args.rank}; "
                                 f"C = A B with r = 1 and r = {args.rhs}; algorithmic bytes = 8 x generator entries "
                                 f"({entries}) + 16 n r"), "l2": "flushed before every timed call (512 MB write)"},
-        "roofline": {"kernel": "pmv_kernel<PF64>", "bound": "hbm", "achieved": g1, "peak": peak, "unit": "GB/s",
-                     "frac": g1 / peak, "peak_source": peak_src},
+        "roofline": {"kernel": "pmv_flat_kernel", "bound": "hbm", "achieved": g1, "peak": peak, "unit": "GB/s",
+                     "frac": g1 / peak, "peak_source": peak_src,
+                     "traffic": profiled_traffic("pmv_flat_kernel_f64_matvec_n65536_r1"),
+                     "traffic_source": "profiles/pmv_flat_kernel_f64_matvec_n65536_r1.md (ncu, one launch)",
+                     "note": "FP64 products of <= 4 columns run the flat persistent kernel, wider ones pmv_kernel<PF64>"},
         "by_rhs": {str(r): v for r, v in out.items()}, "clocks": clk,
         "full_n16384": {"ms": full_ms, "written_gbs": nf * nf * 8 / (full_ms * 1e-3) / 1e9,
                         "fp64_tflops": 2.0 * nf * nf * args.rank / (full_ms * 1e-3) / 1e12},

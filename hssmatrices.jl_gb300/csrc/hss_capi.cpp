@@ -67,6 +67,15 @@ struct SlotTable {
   DBuf<uint32_t> pstate;             // launch counters: zero between launches
   DBuf<unsigned long long> pq;       // queue entries, tagged with the epoch of their launch
   uint32_t epoch = 0;                // tag of the last persistent launch on pq
+  DBuf<double> ctb;                  // the flat product's leaf contributions
+  DBuf<uint32_t> dcnt;               // its per-(leaf, chunk) counters: zero between launches
+  cudaError_t ensure_flat(int64_t ctb_elems, int64_t counters, cudaStream_t st) {
+    cudaError_t e = ctb.ensure((size_t)ctb_elems);
+    if (e != cudaSuccess || (dcnt.p && dcnt.cap >= (size_t)counters)) return e;
+    e = dcnt.ensure((size_t)counters);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dcnt.p, 0, dcnt.cap * sizeof(uint32_t), st);
+    return e;
+  }
   cudaError_t ensure_pmv(int64_t entries, cudaStream_t st) {
     const size_t words = (size_t)pmv_state_words(), ents = (size_t)std::max<int64_t>(entries, 1);
     if (pstate.p && pstate.cap >= words && pq.p && pq.cap >= ents && epoch < pmv_epoch_limit()) return cudaSuccess;
@@ -111,6 +120,8 @@ bool g_generic_factor = false;
 bool g_residual_fp64 = false;
 // Forces the level-by-level product kernels instead of the persistent one.
 bool g_level_product = false;
+// Lets FP64 products of few columns run the flat form of the persistent product.
+bool g_flat_product = true;
 // Replays factor and solve launch sequences as CUDA graphs (non-default streams).
 bool g_graphs = false;
 // Autotuner: forces every solve level to the register (0) or the blocked (1)
@@ -177,6 +188,12 @@ struct hss_plan_s {
   int pmv_nleaf = 0, pmv_mleaf = 0, pmv_kmax = 0;   // largest leaf columns / rows, largest rank
   int64_t pmv_ninner = 0;                           // branches that are not roots
   int64_t tr_lo = 0, tr_hi = 0;         // element range of d_gen holding every translator (B, R, W)
+  // flat product tables (flat_dep = 0: it does not apply): per-node links,
+  // per-leaf ancestor paths (flat_dep entries each), the non-root branches
+  FlatLink* d_links = nullptr;
+  int32_t* d_paths = nullptr;
+  int32_t flat_dep = 0;
+  Seg branches;
   std::vector<Task> h_tasks;            // host copy of the task lists (merged batches)
   std::vector<int64_t> h_table;         // node table of a single-tree plan (hss_export)
   int64_t h_npacked = 0;                // its packed generator length
@@ -220,6 +237,8 @@ hss_plan_s::~hss_plan_s() {
   if (d_tasks) cudaFree(d_tasks);
   if (d_err) cudaFree(d_err);
   if (d_sync) cudaFree(d_sync);
+  if (d_links) cudaFree(d_links);
+  if (d_paths) cudaFree(d_paths);
 }
 
 
@@ -521,6 +540,65 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
 // so caches keyed on plans use these instead of pointers.
 std::atomic<uint64_t> g_plan_serial{0};
 
+// Tables of the flat product: the edge of every non-root node to its parent,
+// and every leaf's ancestors by depth.  It applies when each subtree's leaves
+// are contiguous in the leaf list (pre-order node numbering gives that) and
+// the trees are not deeper than kFlatDep - 1.
+int build_flat_tables(hss_plan_s* P, const std::vector<Task>& tasks) {
+  const std::vector<Node>& N = P->nodes;
+  const int64_t nn = (int64_t)N.size();
+  std::vector<int32_t> lo(nn, INT32_MAX), hi(nn, -1), cnt(nn, 0);
+  int maxd = 0;
+  for (int64_t t = 0; t < P->leaves.cnt; ++t) {
+    const int32_t i = tasks[P->leaves.off + t].node;
+    maxd = std::max(maxd, N[i].depth);
+    for (int32_t y = i; y >= 0; y = N[y].parent) {
+      lo[y] = std::min<int32_t>(lo[y], (int32_t)t);
+      hi[y] = std::max<int32_t>(hi[y], (int32_t)t);
+      ++cnt[y];
+    }
+  }
+  for (int64_t i = 0; i < nn; ++i)
+    if (cnt[i] > 0 && hi[i] - lo[i] + 1 != cnt[i]) return HSS_OK;
+  const int dep = maxd + 1;
+  if (dep < 2 || dep > kFlatDep) return HSS_OK;
+  std::vector<FlatLink> links(nn);
+  std::memset(links.data(), 0, links.size() * sizeof(FlatLink));
+  for (int64_t i = 0; i < nn; ++i) {
+    const Node& x = N[i];
+    if (x.root) continue;
+    const Node& p = N[x.parent];
+    const bool left = p.left == (int32_t)i;
+    const Node& sib = N[left ? p.right : p.left];
+    FlatLink& L = links[i];
+    L.W = left ? p.W1 : p.W2;
+    L.R = left ? p.R1 : p.R2;
+    L.B = left ? p.B21 : p.B12;
+    L.wf = x.wf;
+    L.swf = sib.wf;
+    L.ku = x.ku;
+    L.kv = x.kv;
+    L.kpu = p.ku;
+    L.kpv = p.kv;
+    L.sku = sib.ku;
+    L.depth = x.depth;
+    L.lf0 = lo[i];
+    L.lfn = cnt[i];
+  }
+  std::vector<int32_t> paths((size_t)std::max<int64_t>(P->leaves.cnt, 1) * dep, 0);
+  for (int64_t t = 0; t < P->leaves.cnt; ++t)
+    for (int32_t y = tasks[P->leaves.off + t].node; !N[y].root; y = N[y].parent) paths[t * dep + N[y].depth] = y;
+  CUDA_TRY(cudaMalloc((void**)&P->d_links, std::max<size_t>(links.size(), 1) * sizeof(FlatLink)));
+  CUDA_TRY(cudaMemcpy(P->d_links, links.data(), links.size() * sizeof(FlatLink), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMalloc((void**)&P->d_paths, paths.size() * sizeof(int32_t)));
+  CUDA_TRY(cudaMemcpy(P->d_paths, paths.data(), paths.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  P->branches.off = P->mv_up.empty() ? 0 : P->mv_up.front().off;
+  P->branches.cnt = 0;
+  for (const Seg& g : P->mv_up) P->branches.cnt += g.cnt;
+  P->flat_dep = dep;
+  return HSS_OK;
+}
+
 // device_fill: the generator buffer is left for the caller to write on the device.
 int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill = false) {
   P->serial = ++g_plan_serial;
@@ -598,7 +676,7 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill
   P->h_tasks = tasks;
   CUDA_TRY(cudaMalloc((void**)&P->d_tasks, std::max<size_t>(tasks.size(), 1) * sizeof(Task)));
   CUDA_TRY(cudaMemcpy(P->d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice));
-  return HSS_OK;
+  return build_flat_tables(P, tasks);
 }
 
 // ---------------------------------------------------------------------------
@@ -620,6 +698,11 @@ struct Levels {
   int64_t nodes_max = 0, nslots = 0;   // largest node array of a slot's plan; slots
   int64_t ninner = 0;                  // non-root branches
   int device = 0;
+  // flat product tables (flat_dep = 0: not available)
+  const FlatLink* links = nullptr;
+  const int32_t* paths = nullptr;
+  int flat_dep = 0;
+  Seg branches;
   // translators to prefetch into L2 (FP64 and pair copies; null: none)
   const double* pf64 = nullptr;
   const float2* pfdf = nullptr;
@@ -642,6 +725,10 @@ Levels plan_levels(const hss_plan_s* P) {
   L.nslots = P->ntrees;
   L.ninner = P->pmv_ninner;
   L.device = P->device;
+  L.links = P->d_links;
+  L.paths = P->d_paths;
+  L.flat_dep = P->flat_dep;
+  L.branches = P->branches;
   if (P->tr_hi > P->tr_lo) {
     L.pf64 = P->d_gen + P->tr_lo;
     L.pfdf = P->d_gen_df ? P->d_gen_df + P->tr_lo : nullptr;
@@ -657,7 +744,28 @@ bool use_pmv(const Levels& L, const SlotTable* pm, bool pairs, int rmax) {
          pmv_chunks(pairs, rmax) > 0 && pmv_queue_fits(L.nodes_max, L.nslots);
 }
 
+// The flat product takes FP64 products of few columns on plans that have its tables.
+bool use_flat(const Levels& L, bool pairs, int rmax) {
+  return !pairs && g_flat_product && L.flat_dep > 0 && pmv_flat_fits(L.nleaf, L.kmax, L.flat_dep, rmax);
+}
+
 int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable& pm, cudaStream_t st) {
+  if (use_flat(L, pairs, rmax)) {
+    CUDA_TRY(pm.ensure_pmv(1, st));
+    CUDA_TRY(pm.ensure_flat(pmv_flat_ctb_elems(L.leaves.cnt, L.flat_dep, L.kmax, rmax),
+                            L.leaves.cnt * pmv_flat_chunks(rmax), st));
+    cudaError_t e = cudaSuccess;
+    traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st, [&] {
+      e = launch_pmv_flat(L.d_tasks + L.leaves.off, L.leaves.cnt, L.d_tasks + L.branches.off, L.branches.cnt,
+                          L.links, L.paths, L.flat_dep, slots, rmax, L.nleaf, L.mleaf, L.kmax, pm.pstate.p,
+                          pm.ctb.p, pm.dcnt.p, L.device, st);
+    });
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "flat product launch");
+    }
+    return HSS_OK;
+  }
   CUDA_TRY(pm.ensure_pmv(pmv_queue_entries(L.ntasks, L.ninner, pmv_chunks(pairs, rmax)), st));
   ++pm.epoch;
   cudaError_t e = cudaSuccess;
@@ -1709,6 +1817,10 @@ int hss_set_option(int32_t option, int64_t value) {
   }
   if (option == HSS_OPT_SAMPLE_DF) {
     g_sample_df = value != 0;
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_FLAT_PRODUCT) {
+    g_flat_product = value != 0;
     return HSS_OK;
   }
   return fail(HSS_ERR_INVALID, "unknown option");

@@ -48,6 +48,19 @@ struct Node {
 };
 static_assert(sizeof(Node) % 8 == 0, "Node is copied as 8-byte words");
 
+// The edge from a non-root node x to its parent p, as the flat product reads
+// it (one chain of small products per leaf): the translators of p that act on
+// x, the F slots of x and of its sibling, the ranks involved and x's leaves.
+struct FlatLink {
+  const double* W;      // W1 or W2 of p (kv x kpv, ld kv): Z_p += W^T Z_x
+  const double* R;      // R1 or R2 of p (ku x kpu, ld ku): F_x = G_x + R F_p
+  const double* B;      // B21 (x left) or B12 (x right) of p (sku x kv, ld sku): G_sibling = B Z_x
+  int64_t wf, swf;      // product workspace rows of F_x and of F_sibling
+  int32_t ku, kv, kpu, kpv, sku, depth;
+  int32_t lf0, lfn;     // x's leaves: positions lf0 .. lf0 + lfn - 1 of the leaf list
+};
+static_assert(sizeof(FlatLink) % 8 == 0, "FlatLink is copied as 8-byte words");
+
 struct Task {
   const Node* nodes;   // node array the index refers to
   int32_t node;

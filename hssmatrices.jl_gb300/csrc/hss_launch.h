@@ -56,6 +56,25 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
                        int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
                        const void* prefetch, int64_t prefetch_bytes, int device, cudaStream_t st);
 
+// Flat persistent product (hss_pmv.cu), FP64 with few right-hand sides: every
+// leaf carries its own chain of small products up to the root and back, so
+// the launch has two grid barriers instead of the tree's dependency chain.
+// links: one per node of the plan (roots unused); paths: for leaf position t
+// of `leaves`, paths[t * dep + d] is its ancestor at depth d (1 <= d <= its
+// depth), dep > every leaf depth; branches: the non-root branches.  ctb holds
+// pmv_flat_ctb_elems doubles of contributions; dcnt one counter per (leaf,
+// chunk), zero before the first launch (the kernel leaves them zero).  The
+// state words are those of launch_pmv (zero between launches).
+constexpr int kFlatDep = 32;
+size_t pmv_flat_smem_elems(int nleaf, int kmax, int dep);
+bool pmv_flat_fits(int nleaf, int kmax, int dep, int rmax);
+int64_t pmv_flat_ctb_elems(int64_t nleaves, int dep, int kmax, int rmax);
+int64_t pmv_flat_chunks(int rmax);
+cudaError_t launch_pmv_flat(const Task* leaves, int64_t nleaves, const Task* branches, int64_t nbranch,
+                            const FlatLink* links, const int32_t* paths, int dep, const Slot* slots, int rmax,
+                            int nleaf, int mleaf, int kmax, uint32_t* state, double* ctb, uint32_t* dcnt,
+                            int device, cudaStream_t st);
+
 // Entry extraction (hss_getindex.cu): basis pass for one list of nodes (one
 // tree height), the off-diagonal tiles, the diagonal leaf blocks.  R / C are
 // the sorted requested rows / columns, prow / pcol their output positions.

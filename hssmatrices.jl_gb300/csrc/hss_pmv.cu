@@ -56,8 +56,10 @@ constexpr int LCH = 64;                      // rows of V staged per pass (leaf 
 constexpr uint32_t kIdleLimit = 1u << 22;    // polls of an idle block before it gives up
 constexpr int PART_ELEMS = PT * 4;           // split-K partials (8-byte accumulators)
 
-// launch counters, one 128-byte line each
-enum { ST_HEAD = 0, ST_TAIL = 32, ST_BULK = 64, ST_DONE = 96, ST_WORDS = 128 };
+// launch counters, one 128-byte line each (the flat product uses the same
+// words for its own counters and four more lines)
+enum { ST_HEAD = 0, ST_TAIL = 32, ST_BULK = 64, ST_DONE = 96, ST_WORDS = 224 };
+enum { FL_A = 0, FL_B = 32, FL_C = 64, FL_DONE = 96, FL_AFIN = 128, FL_D = 160, FL_BFIN = 192 };
 
 // A queue entry is one 64-bit word, so that a consumer reads the task and its
 // tag in one load: epoch (21 bits) | kind (1) | slot (16) | node (20) | column
@@ -216,12 +218,13 @@ __device__ __forceinline__ int out_slots(int nout) {
   return op;
 }
 
-// out(o) = sum_{l < K} term(o, l) for o < nout with every thread taking part;
-// epi(o, sum) consumes each result.  `part` holds PT accumulators.
+// out(o) = sum_{l < K} term(o, l) for o < nout with every thread taking part
+// (at most gmax groups of terms per output); epi(o, sum) consumes each result.
+// `part` holds PT accumulators.
 template <class P, class Term, class Epi>
-__device__ void sdot(int nout, int K, typename P::Acc* part, Term term, Epi epi) {
+__device__ void sdot(int nout, int K, typename P::Acc* part, Term term, Epi epi, int gmax = PT) {
   using Acc = typename P::Acc;
-  const int op = out_slots(nout), G = PT / op;
+  const int op = max(out_slots(nout), PT / gmax), G = PT / op;
   const int slot = threadIdx.x % op, g = threadIdx.x / op;
   for (int o0 = 0; o0 < nout; o0 += op) {
     const int o = o0 + slot;
@@ -244,9 +247,11 @@ __device__ void sdot(int nout, int K, typename P::Acc* part, Term term, Epi epi)
 // Z = V^T B for one leaf (matmul.jl:34).  B is staged, V in passes of LCH rows
 // (ld LCH + 1) through two buffers, the next pass's copies in flight while one
 // is used; thread (output slot, group) keeps its partial sums over the passes.
+// zsm (nullable, at least kv x nc elements, may overlay the V buffers) also
+// receives Z (ld kv).
 template <class P>
 __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename P::Acc* part,
-                        typename P::E* sm) {
+                        typename P::E* sm, typename P::E* zsm = nullptr) {
   using E = typename P::E;
   using Acc = typename P::Acc;
   const int n = nd.gn, kv = nd.kv;
@@ -294,6 +299,7 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
       issue(ps + 2);
     }
   }
+  if (zsm != nullptr) __syncthreads();   // every thread is done with the V buffers
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     const int o = s * op + slot;
@@ -304,7 +310,11 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
       if (g == 0 && o < nout)
         for (int gg = 1; gg < G; ++gg) P::acc(acc[s], part[gg * op + slot]);
     }
-    if (g == 0 && o < nout) ws[nd.wz + (o % kv) + (int64_t)(j0 + o / kv) * sl.ldws] = P::fin(acc[s]);
+    if (g == 0 && o < nout) {
+      const E z = P::fin(acc[s]);
+      ws[nd.wz + (o % kv) + (int64_t)(j0 + o / kv) * sl.ldws] = z;
+      if (zsm != nullptr) zsm[o] = z;
+    }
   }
 }
 
@@ -797,6 +807,405 @@ int resident_blocks(size_t smem, int device) {
   return c.blocks;
 }
 
+// ---- flat product (FP64, few right-hand sides) ------------------------------
+//
+// The queued product above hands every tree node from block to block, so its
+// time is the tree's chain of hand-offs (two per level).  With few columns the
+// small products are cheap next to that chain, and the flat product trades
+// them for it: every leaf carries its own chain of translator products, and
+// the launch has three phases, each starting once every unit of the one
+// before it has finished (a count of finished units, not a grid barrier).
+//
+//   A. per leaf, Z = V^T B (matmul.jl:34), the B-term that Z feeds
+//      (G_sibling = B Z, :51/:55), and the leaf's contributions to its
+//      ancestors' Z, W_a^T ... W_x^T Z (the terms of :39 unrolled);
+//   B. per non-root branch p, Z_p = the sum of its leaves' contributions (in
+//      leaf order, so the result does not depend on the schedule), then the
+//      B-term it feeds;
+//   C. per leaf, F along the root-to-leaf path, F_c = G_c + R_c F_p (:50-56,
+//      F of the root's children = G), then C += alpha U F (:47).
+//
+// The leaf products C = alpha D B + beta Y (:46), per leaf and row piece, have
+// no tree dependency: they are filler work, taken from their own counter by
+// any block that waits for the next phase or finds its phase's list empty,
+// and by a phase-C unit whose leaf still has pieces outstanding (a per-leaf
+// counter of finished pieces orders the two writes of C).  The translators above a leaf
+// are multiplied once per leaf below them instead of once, which costs FP64
+// issue slots but no extra HBM traffic (they stay in L2).
+
+constexpr int kFlatRows = 32;   // rows of a leaf's D per leaf-product unit
+constexpr int kFlatCw = 4;      // columns per chunk
+
+struct FlatArgs {
+  const Task* leaves;      // leaf list (a subtree's leaves are contiguous)
+  const Task* branches;    // non-root branches by height, lowest first
+  const FlatLink* links;   // by node index
+  const int32_t* paths;    // leaf t's ancestor at depth d: paths[t * dep + d]
+  const Slot* slots;
+  uint32_t* state;
+  double* ctb;             // contributions: ((depth * nleaves + leaf) * nchunk + chunk) * kw + (c + q kv)
+  uint32_t* dcnt;          // finished leaf-product pieces per (leaf, chunk); zero between launches
+  int32_t nleaves, nbranch, nchunk, npiece, dep, kmax, kw;
+};
+
+using FA = PF64::Acc;
+
+// A finished unit of phase A or B: its writes published, then counted.
+__device__ void flat_finish(uint32_t* ctr) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+  }
+}
+
+// Next unit of a phase, or -1 (uniform over the block).
+__device__ int flat_claim(uint32_t* ctr, int n, int* s_u) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t u = (uint32_t)n;
+    if (ld_vol(ctr) < (uint32_t)n) u = atomicAdd(ctr, 1u);
+    *s_u = u < (uint32_t)n ? (int)u : -1;
+  }
+  __syncthreads();
+  return *s_u;
+}
+
+// Copies the links of leaf t's path (depths 1 .. D) into shared memory.
+__device__ void flat_path(const FlatArgs& a, int t, int D, FlatLink* lk) {
+  constexpr int W = (int)(sizeof(FlatLink) / 8);
+  for (int e = threadIdx.x; e < D * W; e += PT) {
+    const int d = 1 + e / W, w = e % W;
+    const int node = __ldg(a.paths + (int64_t)t * a.dep + d);
+    ((unsigned long long*)&lk[d])[w] = __ldg((const unsigned long long*)&a.links[node] + w);
+  }
+  __syncthreads();
+}
+
+// The B-term that Z_x feeds (zs: kv x nc, ld kv), into the sibling's F slot.
+__device__ void flat_bterm(const Slot& sl, const FlatLink& lk, const double* zs, int j0, int nc, FA* part) {
+  const int ks = lk.sku, kv = lk.kv;
+  const double* B = lk.B;
+  double* ws = (double*)sl.ws;
+  const int64_t ld = sl.ldws, off = lk.swf;
+  sdot<PF64>(ks * nc, kv, part,
+             [&](int o, int l, FA& s) { PF64::fma(s, __ldg(B + (o % ks) + (int64_t)l * ks), zs[l + (o / ks) * kv]); },
+             [&](int o, const FA& s) { ws[off + (o % ks) + (int64_t)(j0 + o / ks) * ld] = s.s; }, 4);
+}
+
+// Phase A, upsweep unit of leaf t: Z, the B-term it feeds, and the chain of
+// contributions t_{d-1} = W_d^T t_d up to depth 1, W staged one step ahead.
+__device__ void flat_up(const FlatArgs& a, int t, int ch, FA* part, double* sm, FlatLink* lk) {
+  const Task tk = a.leaves[t];
+  const Slot& sl = a.slots[tk.slot];
+  const Node& x = tk.nodes[tk.node];
+  const int j0 = ch * kFlatCw, nc = min(kFlatCw, sl.r - j0);
+  if (x.root || nc <= 0) return;
+  const int D = x.depth;
+  flat_path(a, t, D, lk);
+  const int km = a.kmax, kk = km * kFlatCw;
+  double* cur = sm + x.gn * RC;   // over leaf_up's V buffers
+  double* nxt = cur + kk;
+  double* const Wb = nxt + kk;   // two buffers of (km | 1) x km
+  const int wstride = (km | 1) * km;
+  leaf_up<PF64>(sl, x, j0, nc, part, sm, cur);
+  auto stage_w = [&](int d, int b) {
+    const FlatLink& L = lk[d];
+    stage_gen(Wb + b * wstride, L.kv | 1, L.W, L.kv, L.kv, L.kpv);
+    cp_commit();
+  };
+  __syncthreads();
+  if (D >= 2) stage_w(D, 0);
+  flat_bterm(sl, lk[D], cur, j0, nc, part);
+  int buf = 0;
+  for (int d = D; d >= 2; --d) {
+    if (d > 2) {
+      stage_w(d - 1, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    const FlatLink& L = lk[d];
+    const int ky = L.kv, kq = L.kpv, ldw = ky | 1;
+    const double* Ws = Wb + buf * wstride;
+    double* dst = a.ctb + ((int64_t)((d - 1) * a.nleaves + t) * a.nchunk + ch) * a.kw;
+    sdot<PF64>(kq * nc, ky, part,
+               [&](int o, int l, FA& s) { PF64::fma(s, Ws[l + (o % kq) * ldw], cur[l + (o / kq) * ky]); },
+               [&](int o, const FA& s) {
+                 nxt[o] = s.s;
+                 dst[o] = s.s;
+               },
+               4);
+    __syncthreads();
+    double* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+    buf ^= 1;
+  }
+}
+
+// Phase A, leaf product unit: rows pc * kFlatRows .. of C = alpha D B + beta Y
+// (a single-leaf tree: the whole product, column norms included).
+__device__ void flat_dpiece(const FlatArgs& a, int t, int pc, int ch, FA* part, double* Xs) {
+  const Task tk = a.leaves[t];
+  const Slot& sl = a.slots[tk.slot];
+  const Node& nd = tk.nodes[tk.node];
+  const int j0 = ch * kFlatCw, m = nd.gm, n = nd.gn, r0 = pc * kFlatRows;
+  if (j0 >= sl.r || r0 >= m) return;
+  const int nc = min(kFlatCw, sl.r - j0), mr = min(kFlatRows, m - r0);
+  __syncthreads();
+  const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
+  for (int e = threadIdx.x; e < n * nc; e += PT) {
+    const int l = e % n, q = e / n;
+    Xs[l + q * n] = __ldg(X + l + (int64_t)q * sl.ldb);
+  }
+  __syncthreads();
+  double* C = sl.C + nd.row0 + r0 + (int64_t)j0 * sl.ldc;
+  const double* Y = sl.Y ? sl.Y + nd.row0 + r0 + (int64_t)j0 * sl.ldy : nullptr;
+  const bool yterm = sl.beta != 0.0 && Y != nullptr;
+  double* cn = (nd.root && sl.colnorm2) ? sl.colnorm2 + j0 : nullptr;
+  rows_cols_n<PF64>(nd.D + r0, mr, n, m, Xs, n, nc, part, cn, [&](int i, int q, const FA& s) {
+    double v = sl.alpha * s.s;
+    if (yterm) v += sl.beta * __ldcg(Y + i + (int64_t)q * sl.ldy);
+    C[i + (int64_t)q * sl.ldc] = v;
+    return v;
+  });
+}
+
+// Leaf-product unit u (leaf, piece, chunk), then its (leaf, chunk) counter.
+__device__ void flat_dunit(const FlatArgs& a, int u, FA* part, double* sm) {
+  const int per = a.npiece * a.nchunk, t = u / per, ch = u % a.nchunk;
+  flat_dpiece(a, t, (u % per) / a.nchunk, ch, part, sm);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(&a.dcnt[t * a.nchunk + ch], 1u);
+  }
+}
+
+// Runs leaf-product units until `done` holds (thread 0 evaluates it; the
+// caller's acquire follows) or, with done = nullptr, until none are left.
+// The wait for `done` is bounded: DEV_TIMEOUT, then the block goes on.
+template <class Done>
+__device__ void flat_fill(const FlatArgs& a, Done done, bool drain, FA* part, double* sm, int* s_u) {
+  const int nd = a.nleaves * a.npiece * a.nchunk;
+  uint32_t polls = 0;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int cmd = -1;   // -2: finished, >= 0: a unit, -1: nothing to do yet
+      if (!drain && done()) {
+        cmd = -2;
+      } else if (ld_vol(&a.state[FL_D]) < (uint32_t)nd) {
+        const uint32_t u = atomicAdd(&a.state[FL_D], 1u);
+        if (u < (uint32_t)nd) cmd = (int)u;
+      }
+      if (cmd == -1) {
+        if (drain) {
+          cmd = -2;
+        } else if (++polls > kIdleLimit) {
+          set_err(a.slots[0], DEV_TIMEOUT);
+          cmd = -2;
+        } else {
+          __nanosleep(64);
+        }
+      }
+      *s_u = cmd;
+    }
+    __syncthreads();
+    const int cmd = *s_u;
+    if (cmd == -2) break;
+    if (cmd >= 0) flat_dunit(a, cmd, part, sm);
+  }
+  if (threadIdx.x == 0) __threadfence();   // acquire
+  __syncthreads();
+}
+
+// Phase B unit: Z of branch bi from its leaves' contributions, then its B-term.
+__device__ void flat_z(const FlatArgs& a, int bi, int ch, FA* part, double* sm) {
+  const Task tk = a.branches[bi];
+  const Slot& sl = a.slots[tk.slot];
+  const FlatLink lk = a.links[tk.node];
+  const int j0 = ch * kFlatCw, nc = min(kFlatCw, sl.r - j0);
+  if (nc <= 0) return;
+  double* zs = sm;
+  // the leaves' contributions are consecutive blocks of kw (ld nchunk kw); the
+  // block sums them with eight loads in flight per thread
+  const int64_t lstride = (int64_t)a.nchunk * a.kw;
+  const double* src = a.ctb + ((int64_t)(lk.depth * a.nleaves + lk.lf0) * a.nchunk + ch) * a.kw;
+  const int nout = lk.kv * nc, op = out_slots(nout), G = PT / op;
+  const int slot = threadIdx.x % op, g = threadIdx.x / op;
+  for (int o0 = 0; o0 < nout; o0 += op) {
+    const int o = o0 + slot;
+    double acc = 0.0;
+    if (o < nout) {
+      for (int l0 = g; l0 < lk.lfn; l0 += 8 * G) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int l = l0 + u * G;
+          v[u] = l < lk.lfn ? __ldcg(src + (int64_t)l * lstride + o) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc += v[u];
+      }
+    }
+    if (G > 1) {
+      __syncthreads();
+      part[threadIdx.x].s = acc;
+      __syncthreads();
+      if (g == 0 && o < nout)
+        for (int gg = 1; gg < G; ++gg) acc += part[gg * op + slot].s;
+    }
+    if (g == 0 && o < nout) zs[o] = acc;
+  }
+  __syncthreads();
+  flat_bterm(sl, lk, zs, j0, nc, part);
+}
+
+// Phase C unit of leaf t: the G of every node on its path in one round of
+// loads, F down the path with R staged one step ahead, then C += alpha U F.
+__device__ void flat_down(const FlatArgs& a, int t, int ch, FA* part, double* sm, FlatLink* lk, int* s_u) {
+  const Task tk = a.leaves[t];
+  const Slot& sl = a.slots[tk.slot];
+  const Node& x = tk.nodes[tk.node];
+  const int j0 = ch * kFlatCw, nc = min(kFlatCw, sl.r - j0);
+  if (x.root || nc <= 0) return;
+  const int D = x.depth;
+  flat_path(a, t, D, lk);
+  const int km = a.kmax, kk = km * kFlatCw;   // every F / G block below has ld km
+  double* Gs = sm;                            // depth d at Gs + d kk (d = 1 .. D)
+  double* const Fb = Gs + (D + 1) * kk;   // two F buffers (kk each)
+  double* const Rb = Gs + (D + 3) * kk;   // two R buffers (km x km each)
+  auto stage_r = [&](int d, int b) {
+    const FlatLink& L = lk[d];
+    stage_gen(Rb + b * km * km, L.ku, L.R, L.ku, L.ku, L.kpu);
+    cp_commit();
+  };
+  if (D >= 2) stage_r(2, 0);
+  const double* ws = (const double*)sl.ws;
+  const int64_t ld = sl.ldws;
+  for (int e0 = threadIdx.x; e0 < D * kk; e0 += 4 * PT) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * PT;
+      v[u] = 0.0;
+      if (e < D * kk) {
+        const FlatLink& L = lk[1 + e / kk];
+        const int i = (e % kk) % km, q = (e % kk) / km;
+        if (i < L.ku && q < nc) v[u] = __ldcg(ws + L.wf + i + (int64_t)(j0 + q) * ld);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (e0 + u * PT < D * kk) Gs[kk + e0 + u * PT] = v[u];
+  }
+  __syncthreads();
+  const double* f = Gs + kk;   // F at depth 1 = G
+  int buf = 0;
+  for (int d = 2; d <= D; ++d) {
+    if (d < D) {
+      stage_r(d + 1, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    const FlatLink& L = lk[d];
+    const int kc = L.ku, kp = L.kpu;
+    const double* Rs = Rb + buf * km * km;
+    const double* G = Gs + d * kk;
+    double* out = Fb + buf * kk;
+    sdot<PF64>(kc * nc, kp, part,
+               [&](int o, int l, FA& s) { PF64::fma(s, Rs[(o % kc) + l * kc], f[l + (o / kc) * km]); },
+               [&](int o, const FA& s) {
+                 const int i = o % kc, q = o / kc;
+                 out[i + q * km] = s.s + G[i + q * km];
+               },
+               4);
+    __syncthreads();
+    f = out;
+    buf ^= 1;
+  }
+  // C holds alpha D B + beta Y once the leaf's pieces are done; help with them
+  const uint32_t* cnt = a.dcnt + t * a.nchunk + ch;
+  flat_fill(a, [&] { return ld_vol(cnt) >= (uint32_t)a.npiece; }, false, part, Rb, s_u);   // R buffers are free
+  double* C = sl.C + x.row0 + (int64_t)j0 * sl.ldc;
+  double* cn = sl.colnorm2 ? sl.colnorm2 + j0 : nullptr;
+  rows_cols_n<PF64>(x.U, x.gm, x.ku, x.gm, f, km, nc, part, cn, [&](int i, int q, const FA& s) {
+    const double v = __ldcg(C + i + (int64_t)q * sl.ldc) + sl.alpha * s.s;
+    C[i + (int64_t)q * sl.ldc] = v;
+    return v;
+  });
+}
+
+__global__ void __launch_bounds__(PT, 4) pmv_flat_kernel(FlatArgs a) {
+  extern __shared__ __align__(16) unsigned char pmv_smem[];
+  FA* part = (FA*)pmv_smem;
+  double* sm = (double*)pmv_smem + PART_ELEMS;
+  __shared__ FlatLink s_lk[kFlatDep];
+  __shared__ int s_u;
+  const int nup = a.nleaves * a.nchunk, nb = a.nbranch * a.nchunk;
+  for (;;) {   // A
+    const int u = flat_claim(&a.state[FL_A], nup, &s_u);
+    if (u < 0) break;
+    flat_up(a, u / a.nchunk, u % a.nchunk, part, sm, s_lk);
+    flat_finish(&a.state[FL_AFIN]);
+  }
+  // B starts once every A unit is done (not every block: blocks busy with a
+  // leaf product join late)
+  flat_fill(a, [&] { return ld_vol(&a.state[FL_AFIN]) >= (uint32_t)nup; }, false, part, sm, &s_u);
+  for (;;) {   // B: branches, highest first (the longest sums)
+    const int u = flat_claim(&a.state[FL_B], nb, &s_u);
+    if (u < 0) break;
+    flat_z(a, a.nbranch - 1 - u / a.nchunk, u % a.nchunk, part, sm);
+    flat_finish(&a.state[FL_BFIN]);
+  }
+  flat_fill(a, [&] { return ld_vol(&a.state[FL_BFIN]) >= (uint32_t)nb; }, false, part, sm, &s_u);
+  for (;;) {   // C
+    const int u = flat_claim(&a.state[FL_C], nup, &s_u);
+    if (u < 0) break;
+    flat_down(a, u / a.nchunk, u % a.nchunk, part, sm, s_lk, &s_u);
+  }
+  flat_fill(a, [] { return true; }, true, part, sm, &s_u);   // the leaf products left
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_u = atomicAdd(&a.state[FL_DONE], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_u) {   // the last block out resets the counters
+    for (int i = threadIdx.x; i < a.nleaves * a.nchunk; i += PT) a.dcnt[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      a.state[FL_A] = 0;
+      a.state[FL_B] = 0;
+      a.state[FL_C] = 0;
+      a.state[FL_D] = 0;
+      a.state[FL_AFIN] = 0;
+      a.state[FL_BFIN] = 0;
+      __threadfence();
+      a.state[FL_DONE] = 0;
+    }
+  }
+}
+
+int flat_resident_blocks(size_t smem, int device) {
+  static Occ<PF64> cache[8];
+  if (device < 0 || device >= 8) device = 0;
+  Occ<PF64>& c = cache[device];
+  if (c.smem == smem && c.blocks > 0) return c.blocks;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(pmv_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pmv_flat_kernel, PT, smem) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  c.smem = smem;
+  c.blocks = per_sm * sms;
+  return c.blocks;
+}
+
 }  // namespace
 
 // Shared memory (elements of 8 bytes) the persistent product needs for leaves
@@ -860,6 +1269,59 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
   const unsigned grid = (unsigned)std::min<int64_t>(cap, std::max<int64_t>(1, 2 * (int64_t)a.nbulk));
   return pairs ? cudaLaunchCooperativeKernel((void*)pmv_kernel<PDF>, grid, PT, args, smem, st)
                : cudaLaunchCooperativeKernel((void*)pmv_kernel<PF64>, grid, PT, args, smem, st);
+}
+
+
+size_t pmv_flat_smem_elems(int nleaf, int kmax, int dep) {
+  const size_t k = kmax > 0 ? kmax : 1, kk = k * kFlatCw;
+  const size_t up = std::max((size_t)nleaf * RC + 2 * (size_t)(LCH + 1) * k,   // leaf_up
+                             (size_t)nleaf * RC + 2 * kk + 2 * (k | 1) * k);   // the W chain
+  const size_t down = (size_t)(dep + 2) * kk + std::max(2 * k * k, (size_t)nleaf * RC);   // G's, F, R buffers
+                                                                                      // (or a leaf product)
+  return PART_ELEMS + std::max(std::max(up, down), std::max((size_t)nleaf * RC, kk));
+}
+
+bool pmv_flat_fits(int nleaf, int kmax, int dep, int rmax) {
+  return rmax >= 1 && rmax <= kFlatCw && dep >= 2 && dep <= kFlatDep && nleaf <= 512 && kmax <= 64 &&
+         pmv_flat_smem_elems(nleaf, kmax, dep) * 8 <= 160 * 1024;
+}
+
+int64_t pmv_flat_chunks(int rmax) { return (std::max(rmax, 1) + kFlatCw - 1) / kFlatCw; }
+
+int64_t pmv_flat_ctb_elems(int64_t nleaves, int dep, int kmax, int rmax) {
+  const int64_t nchunk = (std::max(rmax, 1) + kFlatCw - 1) / kFlatCw;
+  return std::max<int64_t>(1, nleaves * dep * nchunk * (int64_t)std::max(kmax, 1) * kFlatCw);
+}
+
+cudaError_t launch_pmv_flat(const Task* leaves, int64_t nleaves, const Task* branches, int64_t nbranch,
+                            const FlatLink* links, const int32_t* paths, int dep, const Slot* slots, int rmax,
+                            int nleaf, int mleaf, int kmax, uint32_t* state, double* ctb, uint32_t* dcnt,
+                            int device, cudaStream_t st) {
+  if (nleaves <= 0) return cudaSuccess;
+  if (!pmv_flat_fits(nleaf, kmax, dep, rmax)) return cudaErrorInvalidValue;
+  const size_t smem = pmv_flat_smem_elems(nleaf, kmax, dep) * 8;
+  FlatArgs a;
+  a.leaves = leaves;
+  a.branches = branches;
+  a.links = links;
+  a.paths = paths;
+  a.slots = slots;
+  a.state = state;
+  a.ctb = ctb;
+  a.dcnt = dcnt;
+  a.nleaves = (int32_t)nleaves;
+  a.nbranch = (int32_t)nbranch;
+  a.nchunk = (rmax + kFlatCw - 1) / kFlatCw;
+  a.npiece = (std::max(mleaf, 1) + kFlatRows - 1) / kFlatRows;
+  a.dep = dep;
+  a.kmax = std::max(kmax, 1);
+  a.kw = a.kmax * kFlatCw;
+  const int cap = flat_resident_blocks(smem, device);
+  if (cap <= 0) return cudaErrorLaunchOutOfResources;
+  const int64_t units = nleaves * a.nchunk * (1 + a.npiece);
+  const unsigned grid = (unsigned)std::min<int64_t>(cap, std::max<int64_t>(1, units));
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel((void*)pmv_flat_kernel, grid, PT, args, smem, st);
 }
 
 }  // namespace hss

@@ -258,13 +258,19 @@ int64_t hss_launch_counter(void);
  * arithmetic on the FP32 pipe (~2^-47 relative per operation instead of
  * FP64's 2^-53, several times faster on GB300; entries of A and X must lie
  * within float's exponent range): the mixed-precision form of the sampling
- * in randcompress.  0 (default): FP64. */
+ * in randcompress.  0 (default): FP64.
+ * HSS_OPT_FLAT_PRODUCT = 0 turns off the flat form of the persistent FP64
+ * product (1, default: FP64 products of at most 4 columns run it, with every
+ * leaf carrying its own chain of translator products and two grid barriers
+ * in place of the tree's dependency chain); used to test the two forms
+ * against each other. */
 enum {
   HSS_OPT_GENERIC_FACTOR = 1,
   HSS_OPT_RESIDUAL_FP64 = 2,
   HSS_OPT_LEVEL_PRODUCT = 3,
   HSS_OPT_GRAPHS = 4,
-  HSS_OPT_SAMPLE_DF = 5
+  HSS_OPT_SAMPLE_DF = 5,
+  HSS_OPT_FLAT_PRODUCT = 6
 };
 int hss_set_option(int32_t option, int64_t value);
 

@@ -208,3 +208,12 @@ def test_sample_precision_switch(pkg, lib):
     with pytest.raises(ValueError):
         comp._SamplePrecision(A, "fp32")
     assert lib.hss_set_option(5, 0) == 0
+
+
+def test_process_options_known(lib):
+    """Every process-wide switch of hssgpu.h is accepted (and left at its
+    default); an unknown one is rejected."""
+    defaults = {1: 0, 2: 0, 3: 0, 4: 0, 5: 0, 6: 1}
+    for opt, val in defaults.items():
+        assert lib.hss_set_option(opt, val) == 0
+    assert lib.hss_set_option(99, 1) != 0
