@@ -248,9 +248,16 @@ class HssMatrix:
         return getindex(self, key[0], key[1])
 
     def solve(self, b, **kw):
-        """``hssA \\ b`` (src/hssmatrix.jl:234)."""
+        """``hssA \\ b`` (src/hssmatrix.jl:234; an HssMatrix b: :235)."""
         from .linalg import ldiv
         return ldiv(self, b, **kw)
+
+    def __truediv__(self, other):
+        """``hssB / hssA`` for an HssMatrix hssA (src/hssmatrix.jl:237)."""
+        from .linalg import rdiv
+        if not isinstance(other, HssMatrix):
+            return NotImplemented
+        return rdiv(self, other)
 
 
 def gensize(h):

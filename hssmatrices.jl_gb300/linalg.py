@@ -399,9 +399,13 @@ def full(hssA):
     return dev.full()
 
 
-def ldiv(hssA, b, precision="fp64", tol=None, maxit=10, stats=None):
+def ldiv(hssA, b, precision="fp64", tol=None, maxit=10, stats=None, **kw):
     """``hssA \\ b`` (src/hssmatrix.jl:234).  ``precision='fp32'`` factors in FP32 and
-    refines with FP64 HSS products to ``tol`` (default 1e-10 relative residual)."""
+    refines with FP64 HSS products to ``tol`` (default 1e-10 relative residual).
+    An HssMatrix ``b`` gives ``hssA \\ hssB`` (``hss_ldiv``)."""
+    from .hssmatrix import HssMatrix
+    if isinstance(b, HssMatrix):
+        return hss_ldiv(hssA, b, stats=stats, **kw)
     dev = hssA.device()
     prec = PREC[precision]
     tol = (1e-10 if prec == _lib.HSS_PREC_FP32 else 0.0) if tol is None else tol
@@ -414,3 +418,116 @@ def ldiv(hssA, b, precision="fp64", tol=None, maxit=10, stats=None):
     if stats is not None:
         stats.update(iterations=st.iterations, converged=bool(st.converged), residual=st.residual)
     return x.reshape(-1) if vec else x
+
+
+# ---------------------------------------------------------------------------
+# HSS-valued division (src/ulvdivide.jl:13-17, src/hssmatrix.jl:235-237)
+# ---------------------------------------------------------------------------
+
+
+def transpose(hssA):
+    """``hssA'`` for real generators (the adjoint of src/hssmatrix.jl): every
+    leaf's D transposed with U and V swapped, every branch's B12 and B21
+    exchanged and transposed, R and W swapped."""
+    from .hssmatrix import HssMatrix
+    if hssA.isleaf():
+        cp = lambda x: None if x is None else np.array(x, dtype=np.float64)
+        return HssMatrix.leaf(np.asarray(hssA.D).T.copy(), cp(hssA.V), cp(hssA.U), rootnode=hssA.rootnode)
+    return HssMatrix.branch(transpose(hssA.A11), transpose(hssA.A22), hssA.B21.T.copy(), hssA.B12.T.copy(),
+                            R1=hssA.W1.copy(), W1=hssA.R1.copy(), R2=hssA.W2.copy(), W2=hssA.R2.copy(),
+                            rootnode=hssA.rootnode)
+
+
+def cluster_trees(hssA, r0=1, c0=1):
+    """The row and column cluster trees of ``hssA`` (1-based ranges, as
+    ``bisection_cluster`` makes them)."""
+    from .hssmatrix import ClusterTree
+    m, n = hssA.size()
+    rc, cc = ClusterTree(r0, r0 + m - 1), ClusterTree(c0, c0 + n - 1)
+    if hssA.isbranch():
+        m1, n1 = hssA.A11.size()
+        rc.left, cc.left = cluster_trees(hssA.A11, r0, c0)
+        rc.right, cc.right = cluster_trees(hssA.A22, r0 + m1, c0 + n1)
+    return rc, cc
+
+
+def _solve_columns(F, Bt, n, chunk):
+    """X = A^-1 B for a column-major B held as a (columns, n) tensor, in
+    chunks of columns through the FP64 ULV solve."""
+    import torch
+    Xt = torch.empty_like(Bt)
+    for c0 in range(0, Bt.shape[0], chunk):
+        c1 = min(Bt.shape[0], c0 + chunk)
+        F.solve_device(Bt[c0:c1], n, c1 - c0, Xt[c0:c1], n, tol=0.0)
+    return Xt
+
+
+def _compress_dense(Xt, rcl, ccl, opts, stats, kw):
+    """randcompress_adaptive of a column-major device matrix (tensor of
+    shape (columns, rows))."""
+    from .compression import DenseDevice, randcompress_adaptive
+    st = {}
+    out = randcompress_adaptive(DenseDevice(Xt.t()), rcl, ccl, opts=opts, stats=st, **kw)
+    if stats is not None:
+        stats.update(st)
+    return out
+
+
+def hss_ldiv(hssA, hssB, opts=None, stats=None, chunk=512, **kw):
+    """``hssA \\ hssB`` / ``ldiv!(hssA, hssB)`` (src/hssmatrix.jl:235,
+    src/ulvdivide.jl:13) on the device: an HssMatrix X with ``full(X)``
+    approximating A^-1 full(B) to the compression tolerances (``HssOptions``
+    or ``opts`` / keywords), on A's column and B's column cluster trees.
+
+    The reference eliminates leaf by leaf on the generators (_ldiv!,
+    src/ulvdivide.jl:22-52, recompressing as it recurses).  Here B is expanded
+    on the device (``hss_full``), solved with A's FP64 ULV factorization in
+    chunks of columns, and the dense result recompressed by the adaptive
+    randomized compression (``randcompress_adaptive``): O(n^2) device memory
+    and O(n^2 k) work, every step a GPU kernel.  The generators (and ranks)
+    can differ from the reference's; the operator agrees to the tolerance, as
+    the reference's own test checks (test/runtests.jl:73)."""
+    import torch
+    a = hssA.device()
+    b = hssB.device()
+    if a.m != a.n:
+        raise ValueError("hssA must be square")
+    if b.m != a.m:
+        raise ValueError("DimensionMismatch: rows of hssB must match hssA")
+    Bt = torch.empty((b.n, b.m), dtype=torch.float64, device="cuda")
+    check(b.lib.hss_full(b.handle, Bt.data_ptr(), max(b.m, 1), None))
+    F = a.ulvfactor("fp64")
+    Xt = _solve_columns(F, Bt, a.n, chunk)
+    del Bt
+    rcl = cluster_trees(hssA)[1]
+    ccl = cluster_trees(hssB)[1]
+    return _compress_dense(Xt, rcl, ccl, opts, stats, kw)
+
+
+def rdiv(hssB, hssA, opts=None, stats=None, chunk=512, **kw):
+    """``hssB / hssA`` / ``rdiv!(hssB, hssA)`` (src/hssmatrix.jl:237,
+    src/ulvdivide.jl:15-17): X with ``full(X)`` approximating full(B) A^-1, on
+    B's row and A's row cluster trees; the reference forms it as
+    (A' \\ B')', and so does this function, with A' factored on the device."""
+    import torch
+    a = hssA.device()
+    b = hssB.device()
+    if a.m != a.n:
+        raise ValueError("hssA must be square")
+    if b.n != a.m:
+        raise ValueError("DimensionMismatch: columns of hssB must match hssA")
+    Bt = torch.empty((b.n, b.m), dtype=torch.float64, device="cuda")   # column-major B
+    check(b.lib.hss_full(b.handle, Bt.data_ptr(), max(b.m, 1), None))
+    Btt = Bt.t().contiguous()                                        # column-major B'
+    del Bt
+    F = transpose(hssA).device().ulvfactor("fp64")
+    Yt = _solve_columns(F, Btt, a.n, chunk)                           # column-major A'^-1 B'
+    del Btt
+    rcl = cluster_trees(hssB)[0]
+    ccl = cluster_trees(hssA)[0]
+    from .compression import DenseDevice, randcompress_adaptive
+    st = {}
+    out = randcompress_adaptive(DenseDevice(Yt), rcl, ccl, opts=opts, stats=st, **kw)   # (A'^-1 B')' = B A^-1
+    if stats is not None:
+        stats.update(st)
+    return out

@@ -217,3 +217,22 @@ def test_process_options_known(lib):
     for opt, val in defaults.items():
         assert lib.hss_set_option(opt, val) == 0
     assert lib.hss_set_option(99, 1) != 0
+
+
+def test_transpose_and_cluster_trees(pkg, orc):
+    """transpose (the adjoint of real generators) and the cluster trees read
+    back from a generator tree: host only."""
+    rng = np.random.default_rng(11)
+    for n, ls, k in [(700, 64, 8), (50, 64, 8), (129, 64, 4)]:
+        h = orc.synthetic_hss(n, ls, k, rng)
+        A = pkg.HssMatrix.from_tree(h)
+        At = pkg.transpose(A)
+        assert np.abs(orc.full(At) - orc.full(h).T).max() <= 1e-13
+        rc, cc = pkg.cluster_trees(A)
+        ref = pkg.bisection_cluster(n, ls)
+
+        def same(a, b):
+            return (a.lo, a.hi) == (b.lo, b.hi) and a.isleaf() == b.isleaf() and (
+                a.isleaf() or (same(a.left, b.left) and same(a.right, b.right)))
+
+        assert same(rc, ref) and same(cc, ref)
