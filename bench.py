@@ -815,6 +815,20 @@ def run_matvec_workload(args):
     rec_rank = int(info[6])
     lib.hss_destroy(hr)
     lib.hss_destroy(hp)
+    # hssA \ hssB (src/ulvdivide.jl:13) for two n = 16384 trees: expansion of B,
+    # FP64 ULV solve of its 16384 columns, adaptive recompression to 1e-9
+    hA = pkg.synthetic_hss(nf, args.leafsize, args.rank, np.random.default_rng(7))
+    hB = pkg.synthetic_hss(nf, args.leafsize, args.rank, np.random.default_rng(8))
+    hA.device(), hB.device()
+    td = []
+    for it in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = {}
+        X = pkg.hss_ldiv(hA, hB, atol=1e-9, rtol=1e-9, stats=st)
+        td.append(time.perf_counter() - t0)
+    ldiv_rank = pkg.hssrank(X)
+    del X
     leaf_flop = 2.0 * n * args.leafsize * args.leafsize * 2   # D_A D_B and the rank terms, leading order
     line = {
         "metric": "HSS matvec GB/s (FP64 hss_matmul, r=1)", "value": g1, "unit": "GB/s", "n_gpus": 1,
@@ -835,6 +849,9 @@ def run_matvec_workload(args):
                           "note": "host call to result handle (includes plan creation and the final synchronise)"},
         "recompress_product_n65536": {"ms": recompress_ms, "rank_in": 2 * args.rank, "rank_out_node1": rec_rank,
                                       "tol": 1e-9},
+        "hss_ldiv_n16384": {"ms": 1000.0 * td[-1], "rank_out": ldiv_rank, "rounds": st.get("rounds"),
+                            "tol": 1e-9, "note": "host call to result tree (expansion, chunked FP64 solve, "
+                                                 "adaptive recompression, copy to host)"},
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -41,7 +41,7 @@ __global__ void df_split_cols_kernel(const double* __restrict__ X, int64_t ldx, 
   const int64_t tot = n * r;
   for (int64_t e = blockIdx.x * (int64_t)DT + threadIdx.x; e < tot; e += (int64_t)gridDim.x * DT) {
     const int64_t i = e % n, j = e / n;
-    Xs[e] = split_d(X[i + j * ldx]);
+    Xs[e] = split_bits(X[i + j * ldx]);
   }
 }
 

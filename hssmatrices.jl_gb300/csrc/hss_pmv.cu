@@ -107,7 +107,7 @@ struct PDF {
   __device__ static __forceinline__ double dbl(const Acc& a) { return (double)a.h + (double)a.l; }
   __device__ static __forceinline__ const E* gen(const Slot& s, const double* p) { return s.gdf + (p - s.gbase); }
   __device__ static __forceinline__ E* ws(const Slot& s) { return s.ws2; }
-  __device__ static __forceinline__ E xin(double x) { return split_d(x); }
+  __device__ static __forceinline__ E xin(double x) { return split_bits(x); }
 };
 
 // ---- device-side scheduling -------------------------------------------------
