@@ -833,7 +833,6 @@ int resident_blocks(size_t smem, int device) {
 // are multiplied once per leaf below them instead of once, which costs FP64
 // issue slots but no extra HBM traffic (they stay in L2).
 
-constexpr int kFlatRows = 32;   // rows of a leaf's D per leaf-product unit
 constexpr int kFlatCw = 4;      // columns per chunk
 
 struct FlatArgs {
@@ -846,6 +845,7 @@ struct FlatArgs {
   double* ctb;             // contributions: ((depth * nleaves + leaf) * nchunk + chunk) * kw + (c + q kv)
   uint32_t* dcnt;          // finished leaf-product pieces per (leaf, chunk); zero between launches
   int32_t nleaves, nbranch, nchunk, npiece, dep, kmax, kw;
+  int32_t rows;            // rows of a leaf's D per leaf-product unit
 };
 
 using FA = PF64::Acc;
@@ -945,15 +945,15 @@ __device__ void flat_up(const FlatArgs& a, int t, int ch, FA* part, double* sm, 
   }
 }
 
-// Phase A, leaf product unit: rows pc * kFlatRows .. of C = alpha D B + beta Y
+// Leaf-product unit: rows pc * a.rows .. of C = alpha D B + beta Y
 // (a single-leaf tree: the whole product, column norms included).
 __device__ void flat_dpiece(const FlatArgs& a, int t, int pc, int ch, FA* part, double* Xs) {
   const Task tk = a.leaves[t];
   const Slot& sl = a.slots[tk.slot];
   const Node& nd = tk.nodes[tk.node];
-  const int j0 = ch * kFlatCw, m = nd.gm, n = nd.gn, r0 = pc * kFlatRows;
+  const int j0 = ch * kFlatCw, m = nd.gm, n = nd.gn, r0 = pc * a.rows;
   if (j0 >= sl.r || r0 >= m) return;
-  const int nc = min(kFlatCw, sl.r - j0), mr = min(kFlatRows, m - r0);
+  const int nc = min(kFlatCw, sl.r - j0), mr = min(a.rows, m - r0);
   __syncthreads();
   const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
   for (int e = threadIdx.x; e < n * nc; e += PT) {
@@ -1312,7 +1312,10 @@ cudaError_t launch_pmv_flat(const Task* leaves, int64_t nleaves, const Task* bra
   a.nleaves = (int32_t)nleaves;
   a.nbranch = (int32_t)nbranch;
   a.nchunk = (rmax + kFlatCw - 1) / kFlatCw;
-  a.npiece = (std::max(mleaf, 1) + kFlatRows - 1) / kFlatRows;
+  // pieces of 64 rows for one or two columns (fewer, longer units: 6 % faster
+  // at r = 1 on n = 65536), 32 rows for three or four (better balance)
+  a.rows = rmax <= 2 ? 64 : 32;
+  a.npiece = (std::max(mleaf, 1) + a.rows - 1) / a.rows;
   a.dep = dep;
   a.kmax = std::max(kmax, 1);
   a.kw = a.kmax * kFlatCw;
