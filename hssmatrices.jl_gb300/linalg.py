@@ -488,12 +488,13 @@ def hss_ldiv(hssA, hssB, opts=None, stats=None, chunk=512, **kw):
     can differ from the reference's; the operator agrees to the tolerance, as
     the reference's own test checks (test/runtests.jl:73)."""
     import torch
+    (am, an), (bm, _bn) = hssA.size(), hssB.size()
+    if am != an:
+        raise ValueError("hssA must be square")
+    if bm != am:
+        raise ValueError("DimensionMismatch: rows of hssB must match hssA")
     a = hssA.device()
     b = hssB.device()
-    if a.m != a.n:
-        raise ValueError("hssA must be square")
-    if b.m != a.m:
-        raise ValueError("DimensionMismatch: rows of hssB must match hssA")
     Bt = torch.empty((b.n, b.m), dtype=torch.float64, device="cuda")
     check(b.lib.hss_full(b.handle, Bt.data_ptr(), max(b.m, 1), None))
     F = a.ulvfactor("fp64")
@@ -510,12 +511,13 @@ def rdiv(hssB, hssA, opts=None, stats=None, chunk=512, **kw):
     B's row and A's row cluster trees; the reference forms it as
     (A' \\ B')', and so does this function, with A' factored on the device."""
     import torch
+    (am, an), (_bm, bn) = hssA.size(), hssB.size()
+    if am != an:
+        raise ValueError("hssA must be square")
+    if bn != am:
+        raise ValueError("DimensionMismatch: columns of hssB must match hssA")
     a = hssA.device()
     b = hssB.device()
-    if a.m != a.n:
-        raise ValueError("hssA must be square")
-    if b.n != a.m:
-        raise ValueError("DimensionMismatch: columns of hssB must match hssA")
     Bt = torch.empty((b.n, b.m), dtype=torch.float64, device="cuda")   # column-major B
     check(b.lib.hss_full(b.handle, Bt.data_ptr(), max(b.m, 1), None))
     Btt = Bt.t().contiguous()                                        # column-major B'

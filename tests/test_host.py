@@ -236,3 +236,15 @@ def test_transpose_and_cluster_trees(pkg, orc):
                 a.isleaf() or (same(a.left, b.left) and same(a.right, b.right)))
 
         assert same(rc, ref) and same(cc, ref)
+
+
+def test_hss_division_shape_checks(pkg, orc):
+    """hssA \\ hssB and hssB / hssA reject mismatched sizes before any device
+    work (host only)."""
+    rng = np.random.default_rng(2)
+    A = pkg.HssMatrix.from_tree(orc.synthetic_hss(512, 64, 8, rng))
+    B = pkg.HssMatrix.from_tree(orc.synthetic_hss(640, 64, 8, rng))
+    with pytest.raises(ValueError):
+        pkg.hss_ldiv(A, B)
+    with pytest.raises(ValueError):
+        pkg.rdiv(B, A)
