@@ -177,16 +177,13 @@ class Clocks:
 # ---------------------------------------------------------------------------
 
 
-def profiled_traffic(name):
-    """DRAM bytes per launch (read + write) recorded from an ncu capture in
-    profiles/<name>.md ("traffic_bytes_per_launch: N"), or None."""
-    try:
-        for ln in open(os.path.join(ROOT, "profiles", name + ".md")):
-            if ln.startswith("traffic_bytes_per_launch:"):
-                return int(ln.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+# DRAM bytes (read + write) of one leaf-level launch of ulv_factor_fast_kernel<float>
+# on the default workload (n = 65536, leafsize 128, k = 32), from one ncu capture
+# of that launch (dram__bytes_read.sum + dram__bytes_write.sum).  It belongs to
+# that kernel and size only; re-capture it when the kernel changes.
+FACTOR_LEAF_TRAFFIC = {(65536, 128, 32): 143171584}
+# the same for one r = 1 launch of pmv_flat_kernel (FP64 product) on that tree
+MATVEC_R1_TRAFFIC = {(65536, 128, 32): 133241344}
 
 
 def factor_leaf_bytes(A, factor_itemsize):
@@ -354,10 +351,11 @@ def run_ours(args, rank, world, local_rank):
         peak, peak_src = 6800.0, "fallback"
     alg_bytes = factor_leaf_bytes(A, 4) if args.roofline_kernel == "factor_leaf" else None
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9 if alg_bytes and per_launch_ms > 0 else None
-    traffic = profiled_traffic("ulv_factor_fast_leaf_f32_n65536") if args.roofline_kernel == "factor_leaf" else None
+    traffic = (FACTOR_LEAF_TRAFFIC.get((n, args.leafsize, args.rank)) if args.roofline_kernel == "factor_leaf"
+               else None)
     roof = {"kernel": args.roofline_kernel, "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-            "traffic_source": "profiles/ulv_factor_fast_leaf_f32_n65536.md (ncu, one launch)" if traffic else None,
+            "traffic_source": "ncu capture of one leaf-level launch at this size" if traffic else None,
             "peak_source": peak_src, "launch_ms": per_launch_ms, "launches": k_cnt,
             "algorithmic_bytes": alg_bytes}
     cpu = None
@@ -427,14 +425,20 @@ def run_serve(args):
     flat = [1000.0 * (r.done - r.arrival) for r in done if r.kind == "factor"]
     nsolve = sum(1 for r in done if r.kind == "solve")
     nrhs = sum(r.rhs.shape[0] for r in done if r.kind == "solve")
-    # accuracy: true residuals of a sample of served solves (FP64 product on the GPU)
-    worst = 0.0
-    for r in [q for q in done if q.kind == "solve"][:64]:
-        A = srv.matrices[r.matrix]
-        b = r.rhs.cpu().numpy().T
-        x = r.out.cpu().numpy().T
-        res = np.linalg.norm(b - pkg.matmul(pkg.HssMatrix.from_tree(A), x), axis=0) / np.linalg.norm(b, axis=0)
-        worst = max(worst, float(res.max()))
+    # accuracy: the true residual of every served solve (FP64 product on the GPU)
+    worst, checked = 0.0, 0
+    by_matrix = {}
+    for q in done:
+        if q.kind == "solve":
+            by_matrix.setdefault(q.matrix, []).append(q)
+    for mi, lst in by_matrix.items():
+        dv = pkg.linalg.DeviceHss(pkg.HssMatrix.from_tree(srv.matrices[mi]))
+        for q in lst:
+            R = q.rhs.clone()
+            dv.matmul_device(q.out, dv.n, q.rhs.shape[0], R, dv.m, alpha=-1.0, beta=1.0)
+            worst = max(worst, float((torch.linalg.norm(R, dim=1) / torch.linalg.norm(q.rhs, dim=1)).max()))
+            checked += 1
+        del dv
     # the served stream's device memory goes back before the FP64 comparison:
     # resident factorizations and every request's right-hand side and result
     srv.resident.clear()
@@ -477,7 +481,7 @@ def run_serve(args):
         "solve_p50_ms": _pct(slat, 0.5), "solve_p99_ms": _pct(slat, 0.99),
         "factor_p50_ms": _pct(flat, 0.5), "factor_p99_ms": _pct(flat, 0.99),
         "rhs_per_s": nrhs / makespan, "batches": srv.batches, "evictions": srv.evictions,
-        "reloads": srv.reloads, "max_residual_sampled": worst, "clocks": clk,
+        "reloads": srv.reloads, "max_residual": worst, "residuals_checked": checked, "clocks": clk,
         "fp64_one_at_a_time": {"solves_per_s": nsolve / makespan64, "p50_ms": _pct(lat64, 0.5),
                                "p99_ms": _pct(lat64, 0.99), "makespan_s": makespan64},
         "makespan_s": makespan,
@@ -529,8 +533,16 @@ def run_batch(args):
             F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=tol, maxit=20, stream=stream)
             stream.synchronize()
             times.append(time.perf_counter() - t0)
-        out[prec] = {"ms_per_step": 1000.0 * statistics.mean(times), "p50_ms": 1000.0 * statistics.median(times)}
-        del F
+        # true residual of every matrix: R = B - A X with the FP64 product of the forest
+        with torch.cuda.stream(stream):
+            Rs = [b.clone() for b in Bs]
+            forest.matmul_batch_device(Xs, ns, rs, Rs, ns, alpha=-1.0, beta=1.0, stream=stream)
+            res = max(float((torch.linalg.norm(R, dim=1) / torch.linalg.norm(b, dim=1)).max())
+                      for R, b in zip(Rs, Bs))
+        stream.synchronize()
+        out[prec] = {"ms_per_step": 1000.0 * statistics.mean(times), "p50_ms": 1000.0 * statistics.median(times),
+                     "max_residual": res}
+        del F, Rs
     lib.hss_set_option(4, 0)
     # looping plain FP64 per matrix (separate plans, one matrix at a time)
     devs = [pkg.linalg.DeviceHss(t) for t in trees]
@@ -557,7 +569,9 @@ def run_batch(args):
                                 f"level across all matrices, factor/solve sequences replayed as CUDA graphs, "
                                 f"solve kernels autotuned per level")},
         "autotune": tuning,
-        "fp64_batched_ms": out["fp64"]["ms_per_step"], "fp64_loop_ms": loop_ms,
+        "max_residual_all_matrices": out["fp32"]["max_residual"],
+        "fp64_batched_ms": out["fp64"]["ms_per_step"], "fp64_batched_max_residual": out["fp64"]["max_residual"],
+        "fp64_loop_ms": loop_ms,
         "speedup_vs_fp64_loop": loop_ms / m32, "total_rhs": sum(rs),
     }
     print(json.dumps(line), flush=True)
@@ -839,8 +853,8 @@ def run_matvec_workload(args):
                                 f"({entries}) + 16 n r"), "l2": "flushed before every timed call (512 MB write)"},
         "roofline": {"kernel": "pmv_flat_kernel", "bound": "hbm", "achieved": g1, "peak": peak, "unit": "GB/s",
                      "frac": g1 / peak, "peak_source": peak_src,
-                     "traffic": profiled_traffic("pmv_flat_kernel_f64_matvec_n65536_r1"),
-                     "traffic_source": "profiles/pmv_flat_kernel_f64_matvec_n65536_r1.md (ncu, one launch)",
+                     "traffic": MATVEC_R1_TRAFFIC.get((n, args.leafsize, args.rank)),
+                     "traffic_source": "ncu capture of one r = 1 launch at this size",
                      "note": "FP64 products of <= 4 columns run the flat persistent kernel, wider ones pmv_kernel<PF64>"},
         "by_rhs": {str(r): v for r, v in out.items()}, "clocks": clk,
         "full_n16384": {"ms": full_ms, "written_gbs": nf * nf * 8 / (full_ms * 1e-3) / 1e9,

@@ -29,6 +29,16 @@ TRACE = {"mv_leaf": 0, "mv_up": 1, "mv_down": 2, "mv_final": 3, "factor_leaf": 4
 HSS_PREC_FP64 = 0
 HSS_PREC_FP32 = 1
 
+# hss_set_option switches
+HSS_OPT_GENERIC_FACTOR = 1
+HSS_OPT_RESIDUAL_FP64 = 2
+HSS_OPT_LEVEL_PRODUCT = 3
+HSS_OPT_GRAPHS = 4
+HSS_OPT_SAMPLE_DF = 5
+HSS_OPT_FLAT_PRODUCT = 6
+HSS_OPT_POLL_LIMIT = 7
+HSS_OPT_FAIL_ALLOC = 8
+
 NODE_FIELDS = 16
 CLUSTER_FIELDS = 6
 INFO_FIELDS = 13
@@ -56,6 +66,10 @@ class HssError(RuntimeError):
 
 class NoConvergence(HssError):
     pass
+
+
+class HssTimeout(HssError, TimeoutError):
+    """A bounded device-side wait ran out (HSS_ERR_TIMEOUT); the plan stays usable."""
 
 
 class SolveStats(C.Structure):
@@ -163,6 +177,8 @@ def check(rc):
         raise NoConvergence(rc, msg)
     if rc == HSS_ERR_OOM:
         raise MemoryError(msg)
+    if rc == HSS_ERR_TIMEOUT:
+        raise HssTimeout(rc, msg)
     raise HssError(rc, msg)
 
 

@@ -444,7 +444,7 @@ struct Arena {
     if (bytes > left) {
       const size_t sz = std::max<size_t>(bytes, size_t(64) << 20);
       void* q = nullptr;
-      const cudaError_t e = cudaMalloc(&q, sz);
+      const cudaError_t e = dev_alloc(&q, sz);
       if (e != cudaSuccess) { err = e; return nullptr; }
       chunks.push_back(q);
       cur = (char*)q;

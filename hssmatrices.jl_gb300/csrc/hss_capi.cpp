@@ -588,9 +588,9 @@ int build_flat_tables(hss_plan_s* P, const std::vector<Task>& tasks) {
   std::vector<int32_t> paths((size_t)std::max<int64_t>(P->leaves.cnt, 1) * dep, 0);
   for (int64_t t = 0; t < P->leaves.cnt; ++t)
     for (int32_t y = tasks[P->leaves.off + t].node; !N[y].root; y = N[y].parent) paths[t * dep + N[y].depth] = y;
-  CUDA_TRY(cudaMalloc((void**)&P->d_links, std::max<size_t>(links.size(), 1) * sizeof(FlatLink)));
+  CUDA_TRY(dev_alloc((void**)&P->d_links, std::max<size_t>(links.size(), 1) * sizeof(FlatLink)));
   CUDA_TRY(cudaMemcpy(P->d_links, links.data(), links.size() * sizeof(FlatLink), cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMalloc((void**)&P->d_paths, paths.size() * sizeof(int32_t)));
+  CUDA_TRY(dev_alloc((void**)&P->d_paths, paths.size() * sizeof(int32_t)));
   CUDA_TRY(cudaMemcpy(P->d_paths, paths.data(), paths.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   P->branches.off = P->mv_up.empty() ? 0 : P->mv_up.front().off;
   P->branches.cnt = 0;
@@ -613,11 +613,11 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill
   CUDA_TRY(cudaGetDevice(&P->device));
   const int64_t total_gen = gbases.back();
   P->gen_len = total_gen;
-  CUDA_TRY(cudaMalloc((void**)&P->d_gen, std::max<int64_t>(total_gen, 1) * sizeof(double)));
-  CUDA_TRY(cudaMalloc((void**)&P->d_err, sizeof(int32_t)));
+  CUDA_TRY(dev_alloc((void**)&P->d_gen, std::max<int64_t>(total_gen, 1) * sizeof(double)));
+  CUDA_TRY(dev_alloc((void**)&P->d_err, sizeof(int32_t)));
   CUDA_TRY(cudaMemset(P->d_err, 0, sizeof(int32_t)));
   const size_t nsync = std::max<size_t>(P->nodes.size(), 1) * pmv_sync_chunks();
-  CUDA_TRY(cudaMalloc((void**)&P->d_sync, nsync * sizeof(int32_t)));
+  CUDA_TRY(dev_alloc((void**)&P->d_sync, nsync * sizeof(int32_t)));
   CUDA_TRY(cudaMemset(P->d_sync, 0, nsync * sizeof(int32_t)));
   for (const Node& x : P->nodes) {
     if (x.leaf) {
@@ -670,11 +670,11 @@ int build_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, bool device_fill
     x.R1 = gp(o.R1); x.R2 = gp(o.R2); x.W1 = gp(o.W1); x.W2 = gp(o.W2);
   }
   const int64_t total_nodes = (int64_t)P->nodes.size();
-  CUDA_TRY(cudaMalloc((void**)&P->d_nodes, total_nodes * sizeof(Node)));
+  CUDA_TRY(dev_alloc((void**)&P->d_nodes, total_nodes * sizeof(Node)));
   CUDA_TRY(cudaMemcpy(P->d_nodes, P->nodes.data(), total_nodes * sizeof(Node), cudaMemcpyHostToDevice));
   for (auto& t : tasks) t.nodes = P->d_nodes;
   P->h_tasks = tasks;
-  CUDA_TRY(cudaMalloc((void**)&P->d_tasks, std::max<size_t>(tasks.size(), 1) * sizeof(Task)));
+  CUDA_TRY(dev_alloc((void**)&P->d_tasks, std::max<size_t>(tasks.size(), 1) * sizeof(Task)));
   CUDA_TRY(cudaMemcpy(P->d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice));
   return build_flat_tables(P, tasks);
 }
@@ -830,7 +830,7 @@ int run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st,
 
 int ensure_df(hss_plan_s* P, cudaStream_t st) {
   if (P->d_gen_df) return HSS_OK;
-  CUDA_TRY(cudaMalloc((void**)&P->d_gen_df, std::max<int64_t>(P->gen_len, 1) * sizeof(float2)));
+  CUDA_TRY(dev_alloc((void**)&P->d_gen_df, std::max<int64_t>(P->gen_len, 1) * sizeof(float2)));
   launch_df_split(P->d_gen, P->d_gen_df, P->gen_len, st);
   ++g_launches;
   CUDA_TRY(cudaGetLastError());
@@ -1520,6 +1520,24 @@ int set_error(int code, const std::string& msg) { return fail(code, msg); }
 int set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
 void count_launches(int64_t n) { g_launches += n; }
 
+// Armed allocation failure (HSS_OPT_FAIL_ALLOC): 0 = none, k > 0 = the k-th
+// allocation from now fails.
+std::atomic<int64_t> g_fail_alloc{0};
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  int64_t k = g_fail_alloc.load();
+  while (k > 0) {
+    if (g_fail_alloc.compare_exchange_weak(k, k - 1)) {
+      if (k == 1) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
+
 int plan_create_device(int64_t nnodes, const int64_t* table, int64_t npacked, hss_plan_s** out, double** d_gen) {
   *out = nullptr;
   *d_gen = nullptr;
@@ -1683,12 +1701,12 @@ int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, d
     return fail(HSS_ERR_BAD_DIMS, "allocation-free product: workspace of " + std::to_string(h->ws_mv) + " rows x " +
                                       std::to_string(r) + " right-hand sides exceeds the fixed scratch of " +
                                       std::to_string(noalloc_ws_capacity()) + " doubles");
-  int dev = 0;
-  CUDA_TRY(cudaGetDevice(&dev));
+  // the plan's node tables live on its device: run there, with that device's scratch
+  CUDA_TRY(cudaSetDevice(h->device));
   double* ws = nullptr;
   Slot* dslot = nullptr;
   std::string err;
-  rc = noalloc_scratch(dev, &ws, &dslot, &err);
+  rc = noalloc_scratch(h->device, &ws, &dslot, &err);
   if (rc) return fail(rc, err);
   Slot x;
   std::memset(&x, 0, sizeof(Slot));
@@ -1700,9 +1718,10 @@ int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, d
   x.r = (int32_t)r;
   x.err = h->d_err;
   cudaStream_t st = (cudaStream_t)stream;
-  // pageable source: staged by the driver before the call returns
-  CUDA_TRY(cudaMemcpyAsync(dslot, &x, sizeof(Slot), cudaMemcpyHostToDevice, st));
-  run_matvec(h, dslot, (int)r, st);   // level kernels: the persistent product's state would be allocated
+  CUDA_TRY(noalloc_write_slot(dslot, x, st));
+  ++g_launches;
+  // level kernels: the persistent product's state would be allocated
+  if ((rc = run_matvec(h, dslot, (int)r, st))) return rc;
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -1734,7 +1753,7 @@ int hss_matmul_host(hss_handle h, const double* B, int64_t ldb, int64_t r, doubl
   if ((rc = matmul_impl(h, dio, alpha, beta, st, nullptr, nullptr, nullptr, h->mv_slots))) return rc;
   if ((rc = copy_out(C, ldc, h->hC.p, m, r, st))) return rc;
   CUDA_TRY(cudaStreamSynchronize(st));
-  return HSS_OK;
+  return read_dev_err(h, st);   // a persistent product that gave up (HSS_ERR_TIMEOUT)
 }
 
 int hss_ulvfactor(hss_handle h, int32_t precision, hss_factor* out, void* stream) {
@@ -1747,10 +1766,10 @@ int hss_ulvfactor(hss_handle h, int32_t precision, hss_factor* out, void* stream
   f->prec = precision;
   const size_t es = precision == HSS_PREC_FP32 ? sizeof(float) : sizeof(double);
   f->fac_bytes = (size_t)h->fac_elems * es;
-  cudaError_t e = cudaMalloc(&f->d_fac, f->fac_bytes);
+  cudaError_t e = dev_alloc(&f->d_fac, f->fac_bytes);
   if (e != cudaSuccess) {
     delete f;
-    return cuda_fail(e, "cudaMalloc(factor)");
+    return cuda_fail(e, "device allocation (factor)");
   }
   int rc = precision == HSS_PREC_FP32 ? ensure_df(h, (cudaStream_t)stream) : HSS_OK;
   if (!rc)
@@ -1821,6 +1840,16 @@ int hss_set_option(int32_t option, int64_t value) {
   }
   if (option == HSS_OPT_FLAT_PRODUCT) {
     g_flat_product = value != 0;
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_FAIL_ALLOC) {
+    if (value < 0) return fail(HSS_ERR_INVALID, "allocation-failure countdown must be >= 0");
+    g_fail_alloc.store(value);
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_POLL_LIMIT) {
+    if (value < 0 || value > 0xffffffffll) return fail(HSS_ERR_INVALID, "poll limit must be in [0, 2^32)");
+    pmv_set_poll_limit((uint32_t)value);
     return HSS_OK;
   }
   return fail(HSS_ERR_INVALID, "unknown option");
@@ -1931,8 +1960,8 @@ int hss_batcher_factor(hss_batcher b, int32_t count, const hss_handle* hs, int32
     f->plan = plans[i];
     f->prec = precision;
     f->fac_bytes = (size_t)plans[i]->fac_elems * es;
-    cudaError_t e = cudaMalloc(&f->d_fac, f->fac_bytes);
-    if (e != cudaSuccess) { delete f; rc = cuda_fail(e, "cudaMalloc(factor)"); break; }
+    cudaError_t e = dev_alloc(&f->d_fac, f->fac_bytes);
+    if (e != cudaSuccess) { delete f; rc = cuda_fail(e, "device allocation (factor)"); break; }
     fs[i] = f;
     if (precision == HSS_PREC_FP32) rc = ensure_df(plans[i], st);
   }

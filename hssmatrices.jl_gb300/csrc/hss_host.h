@@ -13,6 +13,11 @@ struct hss_plan_s;
 
 namespace hss {
 
+// Every device allocation of the library goes through here: cudaMalloc, or,
+// while a failure is armed (hss_set_option(HSS_OPT_FAIL_ALLOC, k)), the k-th
+// call from then on returns cudaErrorMemoryAllocation without reaching the driver.
+cudaError_t dev_alloc(void** p, size_t bytes);
+
 // Grow-only device buffer.
 template <typename T>
 struct DBuf {
@@ -31,7 +36,7 @@ struct DBuf {
     if (n <= cap && p) return cudaSuccess;
     release();
     size_t want = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+    cudaError_t e = dev_alloc((void**)&p, want * sizeof(T));
     if (e == cudaSuccess) cap = want;
     else p = nullptr;
     return e;

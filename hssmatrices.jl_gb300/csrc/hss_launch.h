@@ -48,6 +48,9 @@ uint32_t pmv_epoch_limit();
 bool pmv_queue_fits(int64_t nodes, int64_t slots);
 // Per-node counters: a plan holds nodes * pmv_sync_chunks() of them, zeroed.
 int pmv_sync_chunks();
+// Polls of an idle or waiting block of the persistent products before it
+// records DEV_TIMEOUT and gives up (0: the default, 2^22); taken by later launches.
+void pmv_set_poll_limit(uint32_t polls);
 // ntasks = non-root nodes of all trees, ninner = non-root branches; the slots' nodes/sync must be set and
 // every sync counter even (zeroed at allocation); epoch must differ from every earlier launch on state.
 // [prefetch, prefetch + prefetch_bytes) (nullable) is brought into L2 first.
@@ -138,5 +141,8 @@ void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st);
 // addresses of the file-scope arrays on `device`, resolved once per device.
 int noalloc_scratch(int device, double** ws, Slot** slot, std::string* err);
 int64_t noalloc_ws_capacity();
+// Writes `x` into the device slot `dslot` on `st` with a one-thread kernel
+// that takes the slot by value (no host staging buffer, no allocation).
+cudaError_t noalloc_write_slot(Slot* dslot, const Slot& x, cudaStream_t st);
 
 }  // namespace hss

@@ -17,6 +17,8 @@
 //     different streams) race on them; calls on one stream are ordered;
 //   * nothing in the scratch needs clearing: every workspace entry is written
 //     before it is read within a call;
+//   * the argument slot is written on the caller's stream by a one-thread
+//     kernel that takes it by value, so nothing is staged in host memory;
 //   * the first call on a device looks up the arrays' device addresses
 //     (cudaGetSymbolAddress); make that first call before capturing a stream.
 #include <cuda_runtime.h>
@@ -80,5 +82,16 @@ int noalloc_scratch(int device, double** ws, Slot** slot, std::string* err) {
 }
 
 int64_t noalloc_ws_capacity() { return kNoAllocWsDoubles; }
+
+namespace {
+// The argument slot travels as a kernel parameter, which the launch copies;
+// the host object may go out of scope as soon as the launch returns.
+__global__ void noalloc_slot_kernel(Slot* dst, Slot x) { *dst = x; }
+}  // namespace
+
+cudaError_t noalloc_write_slot(Slot* dslot, const Slot& x, cudaStream_t st) {
+  noalloc_slot_kernel<<<1, 1, 0, st>>>(dslot, x);
+  return cudaGetLastError();
+}
 
 }  // namespace hss

@@ -53,7 +53,8 @@ constexpr int PT = 256;                      // threads per block
 constexpr int RC = 8;                        // widest column chunk
 constexpr int kSyncChunks = 64;              // column chunks per node in the counter array
 constexpr int LCH = 64;                      // rows of V staged per pass (leaf upsweep)
-constexpr uint32_t kIdleLimit = 1u << 22;    // polls of an idle block before it gives up
+constexpr uint32_t kIdleLimit = 1u << 22;    // default polls of an idle block before it gives up
+uint32_t g_idle_limit = kIdleLimit;          // host copy, passed to every launch (hss_set_option)
 constexpr int PART_ELEMS = PT * 4;           // split-K partials (8-byte accumulators)
 
 // launch counters, one 128-byte line each (the flat product uses the same
@@ -78,6 +79,7 @@ struct PmvArgs {
   int32_t nleaves, ntasks, nchunk, nbulk;
   int32_t cw;            // columns per chunk (<= RC)
   uint32_t epoch;
+  uint32_t idle_limit;   // polls of an idle block before DEV_TIMEOUT
 };
 
 // ---- arithmetic policies ----------------------------------------------------
@@ -716,7 +718,7 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
         }
       }
       if (cmd == 0) {
-        if (++idle > kIdleLimit) {
+        if (++idle > a.idle_limit) {
           set_err(a.slots[0], DEV_TIMEOUT);
           cmd = 3;
         } else {
@@ -846,6 +848,7 @@ struct FlatArgs {
   uint32_t* dcnt;          // finished leaf-product pieces per (leaf, chunk); zero between launches
   int32_t nleaves, nbranch, nchunk, npiece, dep, kmax, kw;
   int32_t rows;            // rows of a leaf's D per leaf-product unit
+  uint32_t idle_limit;     // polls of a waiting block before DEV_TIMEOUT
 };
 
 using FA = PF64::Acc;
@@ -1004,7 +1007,7 @@ __device__ void flat_fill(const FlatArgs& a, Done done, bool drain, FA* part, do
       if (cmd == -1) {
         if (drain) {
           cmd = -2;
-        } else if (++polls > kIdleLimit) {
+        } else if (++polls > a.idle_limit) {
           set_err(a.slots[0], DEV_TIMEOUT);
           cmd = -2;
         } else {
@@ -1240,6 +1243,7 @@ bool pmv_queue_fits(int64_t nodes, int64_t slots) {
   return nodes <= (int64_t(1) << (QE_SLOT - QE_NODE)) && slots <= (int64_t(1) << (QE_EPOCH - QE_SLOT));
 }
 int pmv_sync_chunks() { return kSyncChunks; }
+void pmv_set_poll_limit(uint32_t polls) { g_idle_limit = polls == 0 ? kIdleLimit : polls; }
 
 cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks,
                        int64_t ninner, int rmax,
@@ -1262,6 +1266,7 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
   a.epoch = epoch;
   a.pf = (const char*)prefetch;
   a.pf_bytes = prefetch ? prefetch_bytes : 0;
+  a.idle_limit = g_idle_limit;
   void* args[] = {&a};
   const int cap = pairs ? resident_blocks<PDF>(smem, device) : resident_blocks<PF64>(smem, device);
   if (cap <= 0) return cudaErrorLaunchOutOfResources;
@@ -1319,6 +1324,7 @@ cudaError_t launch_pmv_flat(const Task* leaves, int64_t nleaves, const Task* bra
   a.dep = dep;
   a.kmax = std::max(kmax, 1);
   a.kw = a.kmax * kFlatCw;
+  a.idle_limit = g_idle_limit;
   const int cap = flat_resident_blocks(smem, device);
   if (cap <= 0) return cudaErrorLaunchOutOfResources;
   const int64_t units = nleaves * a.nchunk * (1 + a.npiece);

@@ -111,9 +111,10 @@ int hss_matmul_host(hss_handle h, const double* B, int64_t ldb, int64_t r, doubl
  * loads the library until the process exits): at most 2^20 doubles of workspace (workspace rows
  * x r; e.g. n = 65536 at rank 32 allows r <= 16), larger calls return
  * HSS_ERR_BAD_DIMS.  The arrays are shared by all calls on a device: calls
- * that overlap on the GPU race; calls on one stream are ordered.  The first
- * call on a device resolves the arrays' addresses (make it before any stream
- * capture).  Same arguments and result as hss_matmul. */
+ * that overlap on the GPU race; calls on one stream are ordered.  The call
+ * makes the handle's device current; the first call on a device resolves the
+ * arrays' addresses there (make it before any stream capture).  Same
+ * arguments and result as hss_matmul. */
 int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC,
                        int64_t ldc, double alpha, double beta, void* stream);
 
@@ -263,14 +264,29 @@ int64_t hss_launch_counter(void);
  * product (1, default: FP64 products of at most 4 columns run it, with every
  * leaf carrying its own chain of translator products and two grid barriers
  * in place of the tree's dependency chain); used to test the two forms
- * against each other. */
+ * against each other.
+ * HSS_OPT_POLL_LIMIT = p sets how many times a block of the persistent
+ * products polls for ready work before it gives up, records a device status
+ * and exits (0: the default, 2^22 polls, i.e. seconds).  The next
+ * synchronising call on the plan (hss_matmul_host, hss_ulvsolve* with
+ * refinement) returns HSS_ERR_TIMEOUT and clears the plan's counters; the
+ * product's result is then undefined, the plan stays usable.  A small value
+ * makes the waits run out on purpose (failure-detection tests).  Launch
+ * sequences already captured as CUDA graphs keep the limit they were
+ * captured with.
+ * HSS_OPT_FAIL_ALLOC = k > 0 makes the k-th device allocation of this library
+ * from now on fail as out of memory, on the host, before the CUDA driver is
+ * called (0 disarms): fault injection for the HSS_ERR_OOM paths.  The call
+ * that hits it returns HSS_ERR_OOM and leaves no partial object behind. */
 enum {
   HSS_OPT_GENERIC_FACTOR = 1,
   HSS_OPT_RESIDUAL_FP64 = 2,
   HSS_OPT_LEVEL_PRODUCT = 3,
   HSS_OPT_GRAPHS = 4,
   HSS_OPT_SAMPLE_DF = 5,
-  HSS_OPT_FLAT_PRODUCT = 6
+  HSS_OPT_FLAT_PRODUCT = 6,
+  HSS_OPT_POLL_LIMIT = 7,
+  HSS_OPT_FAIL_ALLOC = 8
 };
 int hss_set_option(int32_t option, int64_t value);
 

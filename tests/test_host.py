@@ -248,3 +248,14 @@ def test_hss_division_shape_checks(pkg, orc):
         pkg.hss_ldiv(A, B)
     with pytest.raises(ValueError):
         pkg.rdiv(B, A)
+
+
+def test_failure_options_validate_arguments(lib, pkg):
+    """The fault-injection switches check their values on the host (no GPU needed)."""
+    L = pkg._lib
+    assert lib.hss_set_option(L.HSS_OPT_POLL_LIMIT, -1) == L.HSS_ERR_INVALID
+    assert lib.hss_set_option(L.HSS_OPT_POLL_LIMIT, 1 << 33) == L.HSS_ERR_INVALID
+    assert lib.hss_set_option(L.HSS_OPT_FAIL_ALLOC, -1) == L.HSS_ERR_INVALID
+    assert lib.hss_set_option(L.HSS_OPT_POLL_LIMIT, 0) == L.HSS_OK
+    assert lib.hss_set_option(L.HSS_OPT_FAIL_ALLOC, 0) == L.HSS_OK
+    assert lib.hss_set_option(99, 1) == L.HSS_ERR_INVALID

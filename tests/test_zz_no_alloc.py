@@ -25,22 +25,28 @@ def test_noalloc_product_matches_regular(pkg, lib, orc):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(17)
     h = orc.synthetic_hss(2001, 64, 16, rng)
-    A = pkg.HssMatrix.from_tree(h)
-    dev = A.device()
     n, r = 2001, 5
     X = rng.standard_normal((n, r))
     Y0 = rng.standard_normal((n, r))
     # column-major n x r matrices are r x n row-major tensors
     dX = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
     ref = torch.from_numpy(np.ascontiguousarray(Y0.T)).cuda()
-    assert _call(lib.hss_matmul, dev, dX, n, r, ref, n, 0.5, -1.5) == 0, lib.hss_last_error()
+    # the regular product on a handle of its own: it grows that handle's
+    # workspace, which the allocation-free product must not touch
+    reg = pkg.HssMatrix.from_tree(h).device()
+    assert _call(lib.hss_matmul, reg, dX, n, r, ref, n, 0.5, -1.5) == 0, lib.hss_last_error()
     torch.cuda.synchronize()
     ref_h = ref.cpu().numpy().T
     assert np.linalg.norm(ref_h - orc.matmul(h, X, 0.5, -1.5, Y0)) <= MV_TOL * np.linalg.norm(ref_h)
-    for _ in range(2):   # two calls in a row share the fixed scratch
-        out = torch.from_numpy(np.ascontiguousarray(Y0.T)).cuda()
+    dev = pkg.HssMatrix.from_tree(h).device()   # fresh handle: never ran a product
+    outs = [torch.from_numpy(np.ascontiguousarray(Y0.T)).cuda() for _ in range(2)]
+    torch.cuda.synchronize()
+    for i, out in enumerate(outs):   # two calls in a row share the fixed scratch
+        free0 = torch.cuda.mem_get_info()[0]
         assert _call(lib.hss_matmul_noalloc, dev, dX, n, r, out, n, 0.5, -1.5) == 0, lib.hss_last_error()
         torch.cuda.synchronize()
+        if i > 0:   # the first call on a device may load the library's module there
+            assert torch.cuda.mem_get_info()[0] == free0, "the allocation-free product allocated device memory"
         got = out.cpu().numpy().T
         assert np.linalg.norm(got - ref_h) <= MV_TOL * np.linalg.norm(ref_h)
 
