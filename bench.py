@@ -56,6 +56,7 @@ def parse():
     p.add_argument("--compress-n", type=int, default=16384)
     p.add_argument("--requests", type=int, default=10000)
     p.add_argument("--rate", type=float, default=1000.0)
+    p.add_argument("--rates", default="1000,2000,4000,8000", help="offered loads of the serving sweep (requests/s)")
     p.add_argument("--pool", type=int, default=32)
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--matrices", type=int, default=256)
@@ -395,96 +396,92 @@ def _pct(v, q):
     return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))]
 
 
-def run_serve(args):
-    """Serving: Poisson stream of factor (20%) and solve (80%) requests; the
-    continuous-batching FP32+refinement server vs plain FP64 one at a time."""
-    import numpy as np
+def _serve_once(pkg, serve, args, rate, precision, overlap=True, check=True):
+    """One replay of the request stream at `rate` requests/s; returns its summary."""
     import torch
-    import __graft_entry__ as g
-    pkg = g.load_package()
-    from hssmatrices_gb300 import serve
-    reqs, pool = serve.synthetic_requests(n_requests=args.requests, seed=3, rate=args.rate,
-                                          pool_size=args.pool)
-    budget = int(args.budget_gb * 1e9)
-    # warm-up: factor and solve one pool matrix with both paths
-    w = serve.HssServer(budget_bytes=budget, precision="fp32", tol=args.tol)
-    serve.run_stream(w, [serve.Request(0, "factor", 0.0, 0, hss=pool[0]),
-                         serve.Request(1, "solve", 0.0, 0, rhs=torch.randn((4, pool[0].size()[0]),
-                                                                            dtype=torch.float64, device="cuda"))])
-    del w
+    reqs, _pool = serve.synthetic_requests(n_requests=args.requests, seed=3, rate=rate, pool_size=args.pool)
     torch.cuda.synchronize()
-    srv = serve.HssServer(budget_bytes=budget, precision="fp32", tol=args.tol)
-    clocks = Clocks(0)
-    clocks.start()
+    srv = serve.HssServer(budget_bytes=int(args.budget_gb * 1e9), precision=precision, tol=args.tol,
+                          overlap=overlap)
     t0 = time.perf_counter()
     done = serve.run_stream(srv, reqs)
     makespan = time.perf_counter() - t0
-    clk = clocks.stop()
     lat = [1000.0 * (r.done - r.arrival) for r in done]
     slat = [1000.0 * (r.done - r.arrival) for r in done if r.kind == "solve"]
     flat = [1000.0 * (r.done - r.arrival) for r in done if r.kind == "factor"]
     nsolve = sum(1 for r in done if r.kind == "solve")
     nrhs = sum(r.rhs.shape[0] for r in done if r.kind == "solve")
-    # accuracy: the true residual of every served solve (FP64 product on the GPU)
-    worst, checked = 0.0, 0
-    by_matrix = {}
-    for q in done:
-        if q.kind == "solve":
-            by_matrix.setdefault(q.matrix, []).append(q)
-    for mi, lst in by_matrix.items():
-        dv = pkg.linalg.DeviceHss(pkg.HssMatrix.from_tree(srv.matrices[mi]))
-        for q in lst:
-            R = q.rhs.clone()
-            dv.matmul_device(q.out, dv.n, q.rhs.shape[0], R, dv.m, alpha=-1.0, beta=1.0)
-            worst = max(worst, float((torch.linalg.norm(R, dim=1) / torch.linalg.norm(q.rhs, dim=1)).max()))
-            checked += 1
-        del dv
-    # the served stream's device memory goes back before the FP64 comparison:
-    # resident factorizations and every request's right-hand side and result
+    out = {"offered_per_s": rate, "precision": precision, "overlap": overlap,
+           "solves_per_s": nsolve / makespan, "requests_per_s": len(done) / makespan, "rhs_per_s": nrhs / makespan,
+           "p50_ms": _pct(lat, 0.5), "p99_ms": _pct(lat, 0.99), "solve_p50_ms": _pct(slat, 0.5),
+           "solve_p99_ms": _pct(slat, 0.99), "factor_p50_ms": _pct(flat, 0.5), "factor_p99_ms": _pct(flat, 0.99),
+           "makespan_s": makespan, "arrival_span_s": reqs[-1].arrival, "factor_batches": srv.factor_batches,
+           "solve_batches": srv.solve_batches, "overlapped_factor_batches": srv.overlapped,
+           "evictions": srv.evictions, "reloads": srv.reloads}
+    if check:
+        # the true residual of every served solve (FP64 product on the GPU)
+        worst, checked = 0.0, 0
+        by_matrix = {}
+        for q in done:
+            if q.kind == "solve":
+                by_matrix.setdefault(q.matrix, []).append(q)
+        for mi, lst in by_matrix.items():
+            dv = pkg.linalg.DeviceHss(pkg.HssMatrix.from_tree(srv.matrices[mi]))
+            for q in lst:
+                R = q.rhs.clone()
+                dv.matmul_device(q.out, dv.n, q.rhs.shape[0], R, dv.m, alpha=-1.0, beta=1.0)
+                worst = max(worst, float((torch.linalg.norm(R, dim=1) / torch.linalg.norm(q.rhs, dim=1)).max()))
+                checked += 1
+            del dv
+        out["max_residual"] = worst
+        out["residuals_checked"] = checked
     srv.resident.clear()
-    srv.batcher = None
-    for r in done:
-        r.out = None
+    del srv, done, reqs
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
-    # plain FP64, one request at a time in arrival order (same arrival clock)
-    t0 = time.perf_counter()
-    res64 = {}
-    lat64 = []
-    for r in reqs:
-        now = time.perf_counter() - t0
-        if r.arrival > now:
-            time.sleep(r.arrival - now)
-        if r.kind == "factor":
-            dev = pkg.linalg.DeviceHss(r.hss)
-            res64[r.matrix] = (dev, dev.ulvfactor("fp64"))
-            torch.cuda.synchronize()
-        else:
-            dev, F = res64[r.matrix]
-            X = torch.empty_like(r.rhs)
-            F.solve_device(r.rhs, dev.n, r.rhs.shape[0], X, dev.n, tol=0.0)
-            torch.cuda.synchronize()
-        lat64.append(1000.0 * (time.perf_counter() - t0 - r.arrival))
-        if len(res64) > 32:   # solves go to the 16 most recently factored matrices
-            res64.pop(next(iter(res64)))
-    makespan64 = time.perf_counter() - t0
+    return out
+
+
+def run_serve(args):
+    """Serving: Poisson streams of factor (20%) and solve (80%) requests at rising
+    offered loads; the continuous-batching server (factor and solve batches on two
+    streams, overlapping) in FP32 + refinement and in plain FP64 through the same
+    batcher, plus the FP32 server without overlap at the highest load."""
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    from hssmatrices_gb300 import serve
+    rates = [float(x) for x in args.rates.split(",")]
+    # warm-up: both precisions, a short stream
+    for prec in ("fp32", "fp64"):
+        w = serve.HssServer(budget_bytes=int(args.budget_gb * 1e9), precision=prec, tol=args.tol)
+        reqs, _ = serve.synthetic_requests(n_requests=40, seed=9, rate=4000.0, pool_size=4, n_range=(2048, 8192))
+        serve.run_stream(w, reqs)
+        del w, reqs
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    sweep32 = [_serve_once(pkg, serve, args, rate, "fp32") for rate in rates]
+    clk = clocks.stop()
+    sweep64 = [_serve_once(pkg, serve, args, rate, "fp64", check=False) for rate in rates]
+    no_overlap = _serve_once(pkg, serve, args, rates[-1], "fp32", overlap=False, check=False)
+    best = max(sweep32, key=lambda x: x["solves_per_s"])
+    head = sweep32[rates.index(args.rate)] if args.rate in rates else best
     line = {
-        "metric": METRIC, "value": nsolve / makespan, "unit": UNIT, "n_gpus": 1, "steps": len(reqs),
-        "warmup": 1, "ms_per_step": 1000.0 * makespan / len(reqs), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
-        "config": {"workload": (f"serving: {len(reqs)} Poisson requests at {args.rate:g}/s (seed 3), 20% factor "
-                                f"(n log-uniform 2048..65536, k 16..48, leafsize 128, pool of {args.pool} "
-                                f"matrices), 80% solve (r 1..32) against resident factorizations; "
-                                f"{args.budget_gb:g} GB HBM budget"),
+        "metric": METRIC, "value": best["solves_per_s"], "unit": UNIT, "n_gpus": 1, "steps": args.requests,
+        "warmup": 1, "ms_per_step": 1000.0 * best["makespan_s"] / args.requests, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+        "config": {"workload": (f"serving: {args.requests} Poisson requests per run (seed 3) at offered loads "
+                                f"{rates} per s, 20% factor (n log-uniform 2048..65536, k 16..48, leafsize 128, "
+                                f"pool of {args.pool} matrices), 80% solve (r 1..32) against resident "
+                                f"factorizations; {args.budget_gb:g} GB HBM budget; value = the highest "
+                                f"served solves/s over the loads (FP32 + refinement)"),
                    "tol": args.tol},
-        "p50_ms": _pct(lat, 0.5), "p99_ms": _pct(lat, 0.99),
-        "solve_p50_ms": _pct(slat, 0.5), "solve_p99_ms": _pct(slat, 0.99),
-        "factor_p50_ms": _pct(flat, 0.5), "factor_p99_ms": _pct(flat, 0.99),
-        "rhs_per_s": nrhs / makespan, "batches": srv.batches, "evictions": srv.evictions,
-        "reloads": srv.reloads, "max_residual": worst, "residuals_checked": checked, "clocks": clk,
-        "fp64_one_at_a_time": {"solves_per_s": nsolve / makespan64, "p50_ms": _pct(lat64, 0.5),
-                               "p99_ms": _pct(lat64, 0.99), "makespan_s": makespan64},
-        "makespan_s": makespan,
+        "p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"], "at_offered_per_s": head["offered_per_s"],
+        "max_residual": max(x["max_residual"] for x in sweep32),
+        "residuals_checked": sum(x["residuals_checked"] for x in sweep32),
+        "sweep_fp32": sweep32, "sweep_fp64_same_batcher": sweep64, "fp32_without_overlap": no_overlap,
+        "clocks": clk,
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -1,5 +1,5 @@
 // Blocked FP32 ULV solve sweeps (reference src/ulvfactor.jl:10-107) over a
-// factorization made by the blocked FP32 reduction (hss_factor_fast.cu), which
+// factorization made by the blocked reduction (hss_factor_blk.cu), which
 // also stores, per node, the compact-WY T of every panel of 32 QL and LQ
 // reflectors and the inverses of L1's 32 x 32 diagonal blocks.
 //

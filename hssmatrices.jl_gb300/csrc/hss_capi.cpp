@@ -113,7 +113,15 @@ struct Seg {
 inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
 
 // Launch accounting and optional CUDA-event bracketing of one kernel kind.
-int64_t g_launches = 0;
+// Kernel launches of the process (host calls may come from several threads).
+// Launches issued while a thread captures a graph are counted into that
+// thread's capture counter and added each time the graph is replayed.
+std::atomic<int64_t> g_launches{0};
+thread_local int64_t* t_capture = nullptr;
+inline void add_launches(int64_t n) {
+  if (t_capture) *t_capture += n;
+  else g_launches += n;
+}
 // Forces the global-memory factor kernel for every level (parity tests of the two kernels).
 bool g_generic_factor = false;
 // Forces the native FP64 product for the refinement residual.
@@ -153,7 +161,7 @@ void traced(int kind, int64_t cnt, cudaStream_t st, F&& launch) {
     if (a) cudaEventRecord(a, st);
   }
   launch();
-  ++g_launches;
+  add_launches(1);
   if (on) {
     cudaEvent_t b = trace_event();
     if (b) cudaEventRecord(b, st);
@@ -832,7 +840,7 @@ int ensure_df(hss_plan_s* P, cudaStream_t st) {
   if (P->d_gen_df) return HSS_OK;
   CUDA_TRY(dev_alloc((void**)&P->d_gen_df, std::max<int64_t>(P->gen_len, 1) * sizeof(float2)));
   launch_df_split(P->d_gen, P->d_gen_df, P->gen_len, st);
-  ++g_launches;
+  add_launches(1);
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -850,8 +858,8 @@ bool run_factor(const Levels& L, const Slot* slots, cudaStream_t st) {
                            (size_t)(g.c1v + g.c2v) * g.kvmax + (size_t)g.c1mr * g.c1u + (size_t)g.c2mr * g.c2u +
                            (size_t)g.c1nr * g.c1v + (size_t)g.c2nr * g.c2v + (size_t)g.c1mr * g.c2v +
                            (size_t)g.c2mr * g.c1v;
-      if (!g_generic_factor && factor_fast_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra)) {
-        launch_ulv_factor_fast<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, g.kvmax, extra, st);
+      if (!g_generic_factor && factor_blk_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra)) {
+        launch_ulv_factor_blk<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, g.kvmax, extra, st);
       } else {
         launch_ulv_factor<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
         all_fast = false;
@@ -1105,8 +1113,10 @@ int graphed(GraphCache& gc, uint64_t key, cudaStream_t st, bool& flag, F&& launc
     gc.reset();
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    const int64_t l0 = g_launches;
+    int64_t captured = 0;
+    t_capture = &captured;
     const bool fl = launch();
+    t_capture = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
     const cudaError_t ie = cudaGraphInstantiate(&gc.exec, g, 0);
@@ -1116,12 +1126,11 @@ int graphed(GraphCache& gc, uint64_t key, cudaStream_t st, bool& flag, F&& launc
       return cuda_fail(ie, "cudaGraphInstantiate");
     }
     gc.key = key;
-    gc.launches = g_launches - l0;
+    gc.launches = captured;
     gc.flag = fl;
-    g_launches = l0;
   }
   CUDA_TRY(cudaGraphLaunch(gc.exec, st));
-  g_launches += gc.launches;
+  add_launches(gc.launches);
   flag = gc.flag;
   return HSS_OK;
 }
@@ -1260,11 +1269,11 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     for (size_t i = 0; i < ni; ++i) {
       const Item& it = items[i];
       launch_colnorm2(it.io.B, it.io.ldb, it.f->plan->tree_m[it.tree], it.io.r, B.bn2.p + off[i], st);
-      ++g_launches;
+      add_launches(1);
     }
     if (fp32) {
       launch_sqrt_scale(B.bn2.p, B.scale.p, rtot, st);
-      ++g_launches;
+      add_launches(1);
       scale = B.scale.p;
     }
     CUDA_TRY(cudaMemcpyAsync(B.h_bn2.p, B.bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1322,7 +1331,7 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
       for (size_t i = 0; i < ni; ++i) {
         const Item& it = items[i];
         launch_df_split_cols(it.io.C, it.io.ldc, it.f->plan->tree_n[it.tree], it.io.r, B.xs.p + xoff[i], st);
-        ++g_launches;
+        add_launches(1);
       }
     CUDA_TRY(B.mv.upload(ms, st));
     rc = dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, pm) : run_matvec(L, B.mv.dev.p, (int)rmax, st, pm);
@@ -1348,7 +1357,7 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     }
     if (iter >= maxit || std::isnan(res)) break;
     launch_sqrt_scale(B.rn2.p, B.scale.p, rtot, st);
-    ++g_launches;
+    add_launches(1);
     rc = fp32 ? solve_pass<float>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st, tf)
               : solve_pass<double>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st, tf);
     if (rc) return rc;
@@ -1518,7 +1527,7 @@ namespace hss {
 
 int set_error(int code, const std::string& msg) { return fail(code, msg); }
 int set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
-void count_launches(int64_t n) { g_launches += n; }
+void count_launches(int64_t n) { add_launches(n); }
 
 // Armed allocation failure (HSS_OPT_FAIL_ALLOC): 0 = none, k > 0 = the k-th
 // allocation from now fails.
@@ -1719,7 +1728,7 @@ int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, d
   x.err = h->d_err;
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(noalloc_write_slot(dslot, x, st));
-  ++g_launches;
+  add_launches(1);
   // level kernels: the persistent product's state would be allocated
   if ((rc = run_matvec(h, dslot, (int)r, st))) return rc;
   CUDA_TRY(cudaGetLastError());
@@ -1815,7 +1824,7 @@ int hss_trace_end(double* total_ms, int64_t* launches) {
   return HSS_OK;
 }
 
-int64_t hss_launch_counter(void) { return g_launches; }
+int64_t hss_launch_counter(void) { return g_launches.load(); }
 
 int hss_set_option(int32_t option, int64_t value) {
   if (option == HSS_OPT_GENERIC_FACTOR) {

@@ -102,12 +102,15 @@ void launch_pqr(const PqrTask* tasks, int64_t count, int qmax, int kmax, cudaStr
 template <typename T>
 void launch_ulv_factor(const Task* t, int64_t ntasks, const Slot* s, int max_m, int max_n,
                        cudaStream_t st);
-// On-chip factor kernel (hss_factor_fast.cu); `extra` = merge staging elements.
+// Blocked on-chip factor kernel (hss_factor_blk.cu), FP32 (two blocks per SM)
+// or FP64; `extra` = merge staging elements.
 template <typename T>
-bool factor_fast_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra);
+bool factor_blk_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra);
 template <typename T>
-void launch_ulv_factor_fast(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax, int kvmax,
-                            size_t extra, cudaStream_t st);
+size_t factor_blk_smem(int mmax, int nmax, int kumax, int kvmax, size_t extra);
+template <typename T>
+void launch_ulv_factor_blk(const Task* t, int64_t ntasks, const Slot* s, int mmax, int nmax, int kumax, int kvmax,
+                           size_t extra, cudaStream_t st);
 // Blocked FP32 solve sweeps (hss_bsolve.cu) over factors of the blocked FP32
 // reduction: sizes are the level's largest node and children's ranks.
 bool bsolve_fits(int mmax, int nmax, int kmax, int kvmax);

@@ -2,17 +2,23 @@
 
 Requests are either *factor* requests (a new HSS matrix: upload its generators,
 factorize, keep the factorization resident) or *solve* requests (right-hand
-sides against a resident factorization).  ``HssServer.step()`` takes every
-request that has arrived, admits factor requests while the HBM budget allows
-(evicting least-recently-used factorizations that no queued request needs),
-factorizes all admitted matrices in one batched launch sequence
-(``hss_batcher_factor``), joins the right-hand sides of all solve requests per
-matrix and solves every matrix of the batch in one launch sequence per tree
-level with FP64-accurate refinement (``hss_batcher_solve``).  Requests that
-arrive while a batch runs join the next one.  Results of a request are the
-same alone and in any mix: every matrix of a batch is an independent slot of
-the same kernels (the refinement of a batch stops when all its columns meet
-the tolerance, so a column may get an extra correction).
+sides against a resident factorization).
+
+``HssServer`` keeps two CUDA streams busy at once.  The caller's thread admits
+factor requests while the HBM budget allows (evicting least-recently-used
+factorizations that no queued or running request needs) and launches each
+admitted group as one batched factorization (``hss_batcher_factor``) on the
+factor stream, without waiting for it.  A solve worker thread takes every solve
+request whose matrix is resident (its factorization may still be running: the
+solve stream waits for it on the device), joins the right-hand sides per matrix
+and solves all of them in one launch sequence per tree level with
+FP64-accurate refinement (``hss_batcher_solve``) on the solve stream.  Requests
+that arrive while a batch runs are admitted by the next pass of either loop, so
+factorizations of new matrices overlap solves against resident ones on the
+device.  A request's result is the same alone and in any mix: every matrix of a
+batch is an independent slot of the same kernels (the refinement of a batch
+stops when all its columns meet the tolerance, so a column may get an extra
+correction).
 
 There is no CPU path: every step runs the CUDA library.
 """
@@ -20,6 +26,7 @@ from __future__ import annotations
 
 import collections
 import ctypes as C
+import threading
 import time
 from dataclasses import dataclass, field
 from typing import Optional
@@ -105,6 +112,7 @@ class Request:
     out: object = None
     batch: int = -1
     nbytes: int = 0
+    ready: object = None           # solve: event after which rhs is valid (recorded at submit)
 
 
 @dataclass
@@ -114,13 +122,18 @@ class Resident:
     nbytes: int
     n: int
     last_use: float = 0.0
+    ready: object = None           # event recorded after the factorization on the factor stream
 
 
 class HssServer:
-    """Continuous-batching HSS factor/solve server on one GPU."""
+    """Continuous-batching HSS factor/solve server on one GPU (two streams, a solve worker).
+
+    ``overlap=False`` runs the same batches one after the other on the caller's
+    thread (factor batch, then solve batch, each waited for): the form without
+    overlap, kept for comparison."""
 
     def __init__(self, budget_bytes=150 * 10**9, precision="fp32", tol=1e-10, maxit=20,
-                 max_factor_batch=32, stream=None):
+                 max_factor_batch=32, overlap=True):
         import torch
         self.torch = torch
         self.budget = int(budget_bytes)
@@ -128,16 +141,30 @@ class HssServer:
         self.tol = tol
         self.maxit = maxit
         self.max_factor_batch = max_factor_batch
-        self.stream = stream if stream is not None else torch.cuda.current_stream()
-        self.batcher = Batcher()
+        self.overlap = overlap
+        self.fstream = torch.cuda.Stream()
+        self.sstream = torch.cuda.Stream()
+        self.fbatcher = Batcher()
+        self.sbatcher = Batcher()
+        self.cv = threading.Condition()
         self.resident: "collections.OrderedDict[int, Resident]" = collections.OrderedDict()
         self.pending_factor: "collections.deque[Request]" = collections.deque()
         self.pending_solve: "list[Request]" = []
+        self.inflight = collections.deque()    # (event, factor requests) on the factor stream
+        self.busy = set()                      # matrices of the running solve batch
+        self.completed = []
         self.used = 0
         self.batches = 0
+        self.factor_batches = 0
+        self.solve_batches = 0
         self.evictions = 0
         self.reloads = 0
+        self.overlapped = 0            # factor batches launched while a solve batch ran
         self.matrices = {}             # matrix id -> host HssMatrix (re-admission after eviction)
+        self.now_fn = time.perf_counter
+        self.error = None
+        self._stop = False
+        self._worker = None
 
     # -- accounting --------------------------------------------------------
     @staticmethod
@@ -168,87 +195,205 @@ class HssServer:
 
     # -- request intake ------------------------------------------------------
     def submit(self, req: Request):
-        if req.kind == "factor":
-            self.matrices[req.matrix] = req.hss
-            self.pending_factor.append(req)
-        else:
-            self.pending_solve.append(req)
+        if req.kind == "solve" and req.rhs is not None:
+            req.ready = self.torch.cuda.Event()
+            req.ready.record()   # the caller's stream: rhs is valid after this point
+        with self.cv:
+            if req.kind == "factor":
+                self.matrices[req.matrix] = req.hss
+                self.pending_factor.append(req)
+            else:
+                self.pending_solve.append(req)
+            self.cv.notify_all()
 
-    # -- one batch -----------------------------------------------------------
-    def step(self, now_fn):
-        """Run one batch of factor and solve work; returns the completed requests."""
-        torch = self.torch
-        completed = []
-        keep = {r.matrix for r in self.pending_solve}
-        # a matrix evicted while solves for it were still to come is loaded again
-        queued = {r.matrix for r in self.pending_factor}
-        for mid in keep:
-            if mid not in self.resident and mid not in queued and mid in self.matrices:
-                self.pending_factor.appendleft(Request(-1, "factor", now_fn(), mid, hss=self.matrices[mid]))
-                queued.add(mid)
-                self.reloads += 1
-        admitted = []
-        while self.pending_factor and len(admitted) < self.max_factor_batch:
-            req = self.pending_factor[0]
-            need = self.estimate_bytes(req.hss, self.precision)
-            if need > self.budget:
-                raise MemoryError(f"matrix {req.matrix} needs {need} bytes, above the budget {self.budget}")
-            if not self._evict_for(need, keep | {r.matrix for r in admitted}):
-                break
-            self.pending_factor.popleft()
-            self.used += need
-            req.nbytes = need
-            admitted.append(req)
-        if admitted:
-            devs = [DeviceHss(r.hss) for r in admitted]
-            factors = self.batcher.factor(devs, self.precision, stream=self.stream)
+    # -- factor side (the caller's thread) -------------------------------------
+    def _admit_and_factor(self):
+        """Admit queued factor requests within the budget and launch them as one
+        batch on the factor stream; does not wait for the device."""
+        with self.cv:
+            keep = {r.matrix for r in self.pending_solve} | self.busy
+            for _ev, reqs in self.inflight:
+                keep |= {r.matrix for r in reqs}
+            # a matrix evicted while solves for it were still to come is loaded again
+            queued = {r.matrix for r in self.pending_factor}
+            for mid in {r.matrix for r in self.pending_solve}:
+                if mid not in self.resident and mid not in queued and mid in self.matrices:
+                    self.pending_factor.appendleft(Request(-1, "factor", self.now_fn(), mid,
+                                                           hss=self.matrices[mid]))
+                    queued.add(mid)
+                    self.reloads += 1
+            admitted = []
+            while self.pending_factor and len(admitted) < self.max_factor_batch:
+                req = self.pending_factor[0]
+                need = self.estimate_bytes(req.hss, self.precision)
+                if need > self.budget:
+                    raise MemoryError(f"matrix {req.matrix} needs {need} bytes, above the budget {self.budget}")
+                if not self._evict_for(need, keep | {r.matrix for r in admitted}):
+                    break
+                self.pending_factor.popleft()
+                self.used += need
+                req.nbytes = need
+                admitted.append(req)
+        if not admitted:
+            return False
+        devs = [DeviceHss(r.hss) for r in admitted]
+        with self.cv:
+            if self.busy:
+                self.overlapped += 1   # launched while a solve batch is on the device
+        factors = self.fbatcher.factor(devs, self.precision, stream=self.fstream)
+        ev = self.torch.cuda.Event()
+        ev.record(self.fstream)
+        with self.cv:
             for r, d, f in zip(admitted, devs, factors):
-                self.resident[r.matrix] = Resident(d, f, r.nbytes, d.n, now_fn())
+                self.resident[r.matrix] = Resident(d, f, r.nbytes, d.n, self.now_fn(), ev)
                 self.resident.move_to_end(r.matrix)
-        # solves: every request whose matrix is resident, joined per matrix
+            self.inflight.append((ev, admitted))
+            self.factor_batches += 1
+            self.batches += 1
+            self.cv.notify_all()
+        return True
+
+    def _reap_factors(self, wait=False):
+        """Completes the factor requests of finished factor batches."""
+        with self.cv:
+            while self.inflight:
+                ev, reqs = self.inflight[0]
+                if wait:
+                    ev.synchronize()
+                elif not ev.query():
+                    break
+                self.inflight.popleft()
+                t = self.now_fn()
+                for r in reqs:
+                    if r.rid < 0:
+                        continue   # internal re-admission
+                    r.done = t
+                    r.batch = self.factor_batches
+                    self.completed.append(r)
+
+    # -- solve side (the worker thread, or the caller's without overlap) ---------
+    def _take_solves(self):
+        """Every queued solve whose matrix is resident, grouped per matrix (lock held)."""
         ready = [r for r in self.pending_solve if r.matrix in self.resident]
-        if ready:
-            self.pending_solve = [r for r in self.pending_solve if r.matrix not in self.resident]
-            groups = collections.OrderedDict()
-            for r in ready:
-                groups.setdefault(r.matrix, []).append(r)
-            facs, dBs, dXs, rows, rs = [], [], [], [], []
-            for mid, reqs in groups.items():
-                res = self.resident[mid]
-                res.last_use = now_fn()
-                self.resident.move_to_end(mid)
+        if not ready:
+            return None
+        self.pending_solve = [r for r in self.pending_solve if r.matrix not in self.resident]
+        groups = collections.OrderedDict()
+        for r in ready:
+            groups.setdefault(r.matrix, []).append(r)
+        batch = []
+        for mid, reqs in groups.items():
+            res = self.resident[mid]
+            res.last_use = self.now_fn()
+            self.resident.move_to_end(mid)
+            batch.append((mid, res, reqs))
+        self.busy = set(groups)
+        return batch
+
+    def _run_solves(self, batch):
+        torch = self.torch
+        st = self.sstream
+        facs, dBs, dXs, rows, rs = [], [], [], [], []
+        for _mid, res, reqs in batch:
+            st.wait_event(res.ready)             # the factorization, on the device
+            for q in reqs:
+                if q.ready is not None:
+                    st.wait_event(q.ready)       # the right-hand sides
+        with torch.cuda.stream(st):
+            for _mid, res, reqs in batch:
                 B = torch.cat([q.rhs for q in reqs], dim=0) if len(reqs) > 1 else reqs[0].rhs
-                X = torch.empty_like(B)
                 facs.append(res.factor)
                 dBs.append(B)
-                dXs.append(X)
+                dXs.append(torch.empty_like(B))
                 rows.append(res.n)
                 rs.append(B.shape[0])
-            self.batcher.solve(facs, dBs, dXs, rows, rs, tol=self.tol, maxit=self.maxit, stream=self.stream)
-            self.stream.synchronize()
-            t = now_fn()
-            for (mid, reqs), X in zip(groups.items(), dXs):
+        self.sbatcher.solve(facs, dBs, dXs, rows, rs, tol=self.tol, maxit=self.maxit, stream=st)
+        st.synchronize()
+        t = self.now_fn()
+        with self.cv:
+            self.solve_batches += 1
+            self.batches += 1
+            for (_mid, _res, reqs), X in zip(batch, dXs):
                 c0 = 0
                 for q in reqs:
                     q.out = X[c0:c0 + q.rhs.shape[0]]
                     c0 += q.rhs.shape[0]
                     q.done = t
-                    q.batch = self.batches
-                    completed.append(q)
-        if admitted:
-            self.stream.synchronize()
-            t = now_fn()
-            for r in admitted:
-                if r.rid < 0:
-                    continue   # internal re-admission
-                r.done = t
-                r.batch = self.batches
-                completed.append(r)
-        self.batches += 1
-        return completed
+                    q.batch = self.solve_batches
+                    self.completed.append(q)
+            self.busy = set()
+            self.cv.notify_all()
+
+    def _solve_loop(self):
+        try:
+            while True:
+                with self.cv:
+                    batch = None
+                    while not self._stop:
+                        batch = self._take_solves()
+                        if batch is not None:
+                            break
+                        self.cv.wait(0.01)
+                    if batch is None:
+                        return
+                self._run_solves(batch)
+        except BaseException as e:   # surfaced on the caller's thread by pump()
+            with self.cv:
+                self.error = e
+                self.busy = set()
+                self.cv.notify_all()
+
+    # -- driving -----------------------------------------------------------------
+    def start(self, now_fn=None):
+        if now_fn is not None:
+            self.now_fn = now_fn
+        if self.overlap and self._worker is None:
+            self._stop = False
+            self._worker = threading.Thread(target=self._solve_loop, name="hss-solve", daemon=True)
+            self._worker.start()
+
+    def stop(self):
+        if self._worker is not None:
+            with self.cv:
+                self._stop = True
+                self.cv.notify_all()
+            self._worker.join()
+            self._worker = None
+        self._reap_factors(wait=True)
+
+    def pump(self):
+        """One pass of the caller's loop: launch admitted factorizations, complete
+        finished ones (and, without overlap, run the solve batch); returns the
+        requests completed since the last call."""
+        if self.error is not None:
+            raise self.error
+        launched = self._admit_and_factor()
+        if not self.overlap:
+            if launched:
+                self._reap_factors(wait=True)
+            with self.cv:
+                batch = self._take_solves()
+            if batch is not None:
+                self._run_solves(batch)
+        self._reap_factors()
+        with self.cv:
+            done, self.completed = self.completed, []
+        return done
+
+    def step(self, now_fn):
+        """Runs the queued work to completion without overlap (one factor batch,
+        then one solve batch); returns the completed requests."""
+        self.now_fn = now_fn
+        overlap, self.overlap = self.overlap, False
+        try:
+            return self.pump()
+        finally:
+            self.overlap = overlap
 
     def idle(self):
-        return not self.pending_factor and not self.pending_solve
+        with self.cv:
+            return (not self.pending_factor and not self.pending_solve and not self.inflight
+                    and not self.busy and not self.completed)
 
 
 def run_stream(server, requests, time_scale=1.0, poll=0.0):
@@ -259,24 +404,30 @@ def run_stream(server, requests, time_scale=1.0, poll=0.0):
     def now():
         return (time.perf_counter() - t0) / time_scale
 
+    server.start(now)
     i = 0
     out = []
     n = len(requests)
-    while len(out) < n:
-        t = now()
-        while i < n and requests[i].arrival <= t:
-            server.submit(requests[i])
-            i += 1
-        if server.idle():
-            if i < n:
+    try:
+        while len(out) < n:
+            t = now()
+            while i < n and requests[i].arrival <= t:
+                server.submit(requests[i])
+                i += 1
+            out.extend(server.pump())
+            if len(out) >= n:
+                break
+            if server.idle() and i < n:
                 wait = (requests[i].arrival - now()) * time_scale
                 if wait > 0:
                     time.sleep(min(wait, 0.001))
-            continue
-        done = server.step(now)
-        out.extend(done)
-        if poll:
-            time.sleep(poll)
+            elif poll:
+                time.sleep(poll)
+            else:
+                time.sleep(0.0002)   # leave the interpreter to the solve worker
+    finally:
+        server.stop()
+    out.extend(server.pump())
     return out
 
 

@@ -5,18 +5,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_served_results_equal_alone(pkg, orc):
-    torch = pytest.importorskip("torch")
-    from hssmatrices_gb300 import serve
-    reqs, pool = serve.synthetic_requests(n_requests=80, seed=5, rate=4000.0, factor_frac=0.25,
-                                          n_range=(300, 1500), k_range=(8, 16), leafsize=64, r_range=(1, 6),
-                                          pool_size=4, recent=4)
-    # a budget of about two matrices forces evictions and reloads
-    need = max(serve.HssServer.estimate_bytes(h, "fp32") for h in pool)
-    srv = serve.HssServer(budget_bytes=2 * need + 1, precision="fp32", tol=1e-10)
-    done = serve.run_stream(srv, reqs, time_scale=1.0)
-    assert len(done) == len(reqs)
-    assert srv.evictions > 0 and srv.batches > 1
+def _check_against_alone(pkg, orc, reqs):
     factored = {}
     for r in reqs:
         if r.kind == "factor":
@@ -36,6 +25,38 @@ def test_served_results_equal_alone(pkg, orc):
         res = np.linalg.norm(b - A @ x_mix, axis=0) / np.linalg.norm(b, axis=0)
         assert res.max() <= 2e-10
         assert r.done >= r.arrival
+
+
+@pytest.mark.parametrize("overlap", [True, False])
+def test_served_results_equal_alone(pkg, orc, overlap):
+    torch = pytest.importorskip("torch")
+    from hssmatrices_gb300 import serve
+    reqs, pool = serve.synthetic_requests(n_requests=80, seed=5, rate=4000.0, factor_frac=0.25,
+                                          n_range=(300, 1500), k_range=(8, 16), leafsize=64, r_range=(1, 6),
+                                          pool_size=4, recent=4)
+    # a budget of about two matrices forces evictions and reloads
+    need = max(serve.HssServer.estimate_bytes(h, "fp32") for h in pool)
+    srv = serve.HssServer(budget_bytes=2 * need + 1, precision="fp32", tol=1e-10, overlap=overlap)
+    done = serve.run_stream(srv, reqs, time_scale=1.0)
+    assert len(done) == len(reqs) and len({id(r) for r in done}) == len(reqs)
+    assert srv.evictions > 0 and srv.batches > 1
+    _check_against_alone(pkg, orc, reqs)
+
+
+def test_requests_arriving_during_a_batch_overlap_it(pkg, orc):
+    """Factor requests that arrive while a solve batch runs are factored on the
+    factor stream during that batch; every result still equals the solo solve."""
+    torch = pytest.importorskip("torch")
+    from hssmatrices_gb300 import serve
+    reqs, pool = serve.synthetic_requests(n_requests=400, seed=6, rate=1500.0, factor_frac=0.3,
+                                          n_range=(2000, 8000), k_range=(8, 24), leafsize=64, r_range=(1, 8),
+                                          pool_size=6, recent=4)
+    srv = serve.HssServer(budget_bytes=10**11, precision="fp32", tol=1e-10, overlap=True)
+    done = serve.run_stream(srv, reqs, time_scale=1.0)
+    assert len(done) == len(reqs)
+    assert srv.overlapped > 0, "no factor batch was launched while a solve batch ran"
+    assert srv.solve_batches > 1 and srv.factor_batches > 1
+    _check_against_alone(pkg, orc, reqs)
 
 
 def test_batcher_rejects_repeated_factor(pkg, orc):
