@@ -308,6 +308,12 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     t64 = [a.elapsed_time(b) for a, b in ev64]
     ms64 = sum(t64) / args.steps
+    breakdown64 = {}
+    for kind in ("factor_leaf", "factor_merge", "solve_up", "solve_down"):
+        L.trace_begin(kind)
+        step64(dX64)
+        kms, _kn = L.trace_end()
+        breakdown64[kind] = kms
     X64 = dX64.cpu().numpy().T
     res64 = float(np.max(np.linalg.norm(Bh - pkg.matmul(A, X64), axis=0) / np.linalg.norm(Bh, axis=0)))
     # end to end through the host-buffer C entry point, pinned memory
@@ -374,7 +380,7 @@ def run_ours(args, rank, world, local_rank):
         "p99_ms": st_sorted[min(len(st_sorted) - 1, int(math.ceil(0.99 * len(st_sorted))) - 1)],
         "rhs_per_s": value * r, "refine_iters": iters, "residual": res32,
         "fp64": {"solves_per_s": world * 1000.0 / ms64, "ms_per_step": ms64, "residual": res64,
-                 "p50_ms": statistics.median(t64)},
+                 "p50_ms": statistics.median(t64), "breakdown_ms_per_step": breakdown64},
         "speedup_vs_fp64": ms64 / ms,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n * r,
                 "d2h_bytes_per_step": 8 * n * r, "ms_per_step": 1000.0 * e2e_total / args.steps},

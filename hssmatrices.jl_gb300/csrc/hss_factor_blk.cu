@@ -48,7 +48,6 @@ constexpr int BMAX = 128;           // largest m, n
 constexpr int BKMAX = 64;           // largest ku, kv
 constexpr int BP = 32;              // panel width (reflectors per panel)
 constexpr int PL = 8;               // lanes per panel column (QL) or row (LQ)
-constexpr int PE = BMAX / PL;       // entries per lane of a panel column / row
 constexpr int XC = 64;              // columns (QL) or rows (LQ) of C per GEMM chunk
 constexpr int XP = XC + 4;          // ld of the GEMM intermediate (>= kv, multiple of 4)
 constexpr int GP = BP + 1;          // ld of the Gram matrix and of T
@@ -57,9 +56,10 @@ constexpr size_t kBlkSmemCap = 226 * 1024;
 static_assert(NT == 8 * BP, "the panel mapping puts 8 lanes on each of 32 columns (rows)");
 static_assert(XP >= BKMAX, "X holds Y V (32 x kv) in the V update");
 
-__host__ __device__ constexpr int al4(int x) { return (x + 3) & ~3; }
 __host__ __device__ constexpr size_t sz4(size_t e) { return (e + 3) & ~size_t(3); }
 __host__ __device__ constexpr size_t zmax(size_t a, size_t b) { return a > b ? a : b; }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 
 // shared-memory layout (elements of T), the same on host and device:
 //   D (m x n, ld LDD) | W: U (ld LDU) in the QL phase, the LQ panel (ld YP) in
@@ -70,14 +70,15 @@ __host__ __device__ constexpr size_t zmax(size_t a, size_t b) { return a > b ? a
 struct BlkLayout {
   int LDD, LDU, YP, LDV;
   size_t oW, oV, oX, oG, oSV, oT, oTau, total;
-  __host__ __device__ BlkLayout(int mmax, int nmax, int kumax, int kvmax, size_t extra) {
-    LDD = mmax | 1;                      // odd: conflict-free column walks
-    LDU = al4(mmax) + 4;                 // 16-byte aligned column segments
-    YP = al4(nmax) + 4;                  // LQ panel, reflector-major
-    LDV = nmax | 1;
+  // S: the level's node-size bucket (largest m and n rounded up to 32)
+  __host__ __device__ BlkLayout(int S, int kumax, int kvmax, size_t extra) {
+    LDD = S + 1;                         // odd: conflict-free column walks
+    LDU = S + 4;                         // 16-byte aligned column segments
+    YP = S + 4;                          // LQ panel, reflector-major
+    LDV = S + 1;
     const int ku = kumax > 0 ? kumax : 1, kvv = kvmax > 0 ? kvmax : 1;
     const size_t w = zmax(zmax((size_t)LDU * ku, (size_t)BP * YP), (size_t)4 * BP * GP);
-    oW = sz4((size_t)LDD * (nmax > 0 ? nmax : 1));
+    oW = sz4((size_t)LDD * S);
     oV = oW + sz4(w);
     oX = oV + sz4((size_t)LDV * kvv);
     oG = oX;
@@ -88,6 +89,9 @@ struct BlkLayout {
     total = oX + zmax(tail, sz4(extra));
   }
 };
+__host__ __device__ constexpr int size_bucket(int mmax, int nmax) {
+  return (((mmax > nmax ? mmax : nmax) + 31) / 32) * 32;
+}
 static_assert(BP * GP + 4 + 2 * SVP <= BP * XP, "the Gram matrix and the broadcast reflectors fit in X");
 
 // dst(i, j) = (T) src[i + j * sld] for i < rows <= 128, j < cols (dst ld `ld`):
@@ -124,36 +128,51 @@ struct CopyJob {
   int dst;   // element offset of the destination in shared memory
 };
 
-// Runs up to 8 copy jobs as one flat list, 16 loads in flight per thread.
+// One warp copies one job: lane = row (32 at a time), 16 columns per round, so
+// that every lane has 16 loads in flight.
 template <typename T, typename S>
-__device__ void stage_jobs(T* sm, const CopyJob<S>* jobs, int njobs) {
-  int total = 0;
-  for (int k = 0; k < njobs; ++k) total += jobs[k].rows * jobs[k].cols;
-  constexpr int UNR = 16;
-  for (int e0 = threadIdx.x; e0 < total; e0 += NT * UNR) {
-    S v[UNR];
-    int dst[UNR];
+__device__ __forceinline__ void stage_warp(T* sm, const CopyJob<S>& J) {
+  const int lane = threadIdx.x & 31;
+  for (int r0 = 0; r0 < J.rows; r0 += 32) {
+    const int i = r0 + lane;
+    for (int j0 = 0; j0 < J.cols; j0 += 16) {
+      S v[16];
 #pragma unroll
-    for (int u = 0; u < UNR; ++u) {
-      int e = e0 + u * NT;
-      dst[u] = -1;
-      v[u] = S(0);
-      if (e < total) {
-        int k = 0;
-        while (e >= jobs[k].rows * jobs[k].cols) {
-          e -= jobs[k].rows * jobs[k].cols;
-          ++k;
-        }
-        const CopyJob<S>& J = jobs[k];
-        const int i = e % J.rows, j = e / J.rows;
-        if (!(J.tril && j > i)) v[u] = __ldg(J.src + i + (int64_t)j * J.sld);
-        dst[u] = J.dst + i + j * J.dld;
+      for (int q = 0; q < 16; ++q) {
+        const int j = j0 + q;
+        v[q] = (i < J.rows && j < J.cols && !(J.tril && j > i)) ? __ldg(J.src + i + (int64_t)j * J.sld) : S(0);
+      }
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int j = j0 + q;
+        if (i < J.rows && j < J.cols) sm[J.dst + i + j * J.dld] = (T)v[q];
       }
     }
-#pragma unroll
-    for (int u = 0; u < UNR; ++u)
-      if (dst[u] >= 0) sm[dst[u]] = (T)v[u];
   }
+}
+
+// Y(i, j) = sum_l A[i + l lda] * B[j bj + l bl] for i < rows, j < cols (B or
+// B^T by the strides), thread (row i, columns j = jb, jb + NT / RMAX, ...); also
+// written to Yg (column-major, ld rows) when it is not null.
+template <int RMAX, typename T>
+__device__ __forceinline__ void small_mm_r(T* Y, int ldy, T* Yg, const T* A, int lda, const T* B, int bj, int bl,
+                                           int rows, int cols, int K) {
+  const int i = threadIdx.x % RMAX, jb = threadIdx.x / RMAX;
+  if (i >= rows) return;
+  for (int j = jb; j < cols; j += NT / RMAX) {
+    T s = T(0);
+    for (int l = 0; l < K; ++l) s = fma_t(A[i + l * lda], B[j * bj + l * bl], s);
+    Y[i + j * ldy] = s;
+    if (Yg) Yg[i + j * rows] = s;
+  }
+}
+// the same with the row span matched to `rows` (<= 128), so that every thread works
+template <typename T>
+__device__ __forceinline__ void small_mm(T* Y, int ldy, T* Yg, const T* A, int lda, const T* B, int bj, int bl,
+                                         int rows, int cols, int K) {
+  if (rows <= 32) small_mm_r<32>(Y, ldy, Yg, A, lda, B, bj, bl, rows, cols, K);
+  else if (rows <= 64) small_mm_r<64>(Y, ldy, Yg, A, lda, B, bj, bl, rows, cols, K);
+  else small_mm_r<128>(Y, ldy, Yg, A, lda, B, bj, bl, rows, cols, K);
 }
 
 template <typename T>
@@ -164,9 +183,9 @@ __device__ __forceinline__ T gsum8(T v, unsigned gm) {   // sum over the 8 lanes
   return v;
 }
 
-// xLARFG from alpha and the squared tail norm.  FP32: the norm as
-// sqrt(alpha^2 + ss) (hypot only when that overflows) and correctly rounded
-// reciprocals; FP64: LAPACK's form (hypot, divisions).
+// xLARFG from alpha and the squared tail norm: the norm as sqrt(alpha^2 + ss)
+// (hypot only near overflow or underflow); FP32 with correctly rounded
+// reciprocals, FP64 with divisions.
 __device__ __forceinline__ void larfg_t(float alpha, float ss, float& beta, float& tau, float& scal) {
   if (ss == 0.f) {
     tau = 0.f;
@@ -181,11 +200,21 @@ __device__ __forceinline__ void larfg_t(float alpha, float ss, float& beta, floa
   scal = __frcp_rn(alpha - beta);
 }
 __device__ __forceinline__ void larfg_t(double alpha, double ss, double& beta, double& tau, double& scal) {
-  larfg_ss(alpha, ss, beta, tau, scal);
+  // FP64 runs at 1/64 of the FP32 rate here: the norm as sqrt(alpha^2 + ss)
+  // (hypot only outside [1e-290, 1e290]), the two divisions independent
+  if (ss == 0.0) {
+    tau = 0.0;
+    beta = alpha;
+    scal = 1.0;
+    return;
+  }
+  const double t = fma(alpha, alpha, ss);
+  const double nrm = (t > 1e-290 && t < 1e290) ? sqrt(t) : hypot(alpha, sqrt(ss));
+  beta = -copysign(nrm, alpha);
+  tau = (beta - alpha) / beta;
+  scal = 1.0 / (alpha - beta);
 }
 
-__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
-__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 
 // four consecutive elements, 16-byte aligned (FP32) or 32-byte aligned (FP64)
 __device__ __forceinline__ void ld4(float (&v)[4], const float* p) {
@@ -304,7 +333,7 @@ __device__ void blk_tmat(int nb, const T* G, const T* tau, T* Tm, T* Tg) {
 // order (forward substitution); written column-major to Lg + 1024 w through
 // `scr` (4 x 32 x GP) so that the global stores are coalesced.
 template <typename T>
-__device__ void blk_linv(int mk, const T* sD, int LDD, T* scr, T* Lg) {
+__device__ __forceinline__ void blk_linv(int mk, const T* sD, int LDD, T* scr, T* Lg) {
   const int w = threadIdx.x >> 5, b = threadIdx.x & 31;
   const int i0 = w * BP;
   if (w < 4 && i0 < mk) {
@@ -341,7 +370,7 @@ __device__ void blk_linv(int mk, const T* sD, int LDD, T* scr, T* Lg) {
 // Strictly upper Gram matrix of a QL panel, G(a, b) = Y(:, a)^T Y(:, b) for
 // a < b < nb, Y read from U (column c0 + a, pivot row mk + c0 + a).
 template <typename T>
-__device__ void ql_gram(const T* sU, int LDU, int c0, int nb, int mk, T* G) {
+__device__ __forceinline__ void ql_gram(const T* sU, int LDU, int c0, int nb, int mk, T* G) {
   const int a = threadIdx.x & 31, bq = threadIdx.x >> 5;   // G(a, 4 bq .. 4 bq + 3)
   const int pa = mk + c0 + a;
   T acc[4] = {T(0), T(0), T(0), T(0)};
@@ -373,7 +402,7 @@ __device__ void ql_gram(const T* sU, int LDU, int c0, int nb, int mk, T* G) {
 // (columns c0 .. c0 + nb - 1 of U), in chunks of XC columns.  Rows from
 // mk + c0 + nb on are not touched (Y is zero there).
 template <typename T>
-__device__ void ql_apply(T* C, int ldc, int ncols, int m, const T* sU, int LDU, int c0, int nb, int mk,
+__device__ __forceinline__ void ql_apply(T* C, int ldc, int ncols, int m, const T* sU, int LDU, int c0, int nb, int mk,
                          const T* Tm, T* X) {
   const int tid = threadIdx.x, jj = tid & (XC - 1), grp = tid / XC;   // grp: 0..3
   const int rlim = min(m, mk + c0 + nb);
@@ -482,7 +511,7 @@ __device__ void ql_apply(T* C, int ldc, int ncols, int m, const T* sU, int LDU, 
 
 // Strictly upper Gram matrix of an LQ panel held reflector-major in Yc.
 template <typename T>
-__device__ void lq_gram(const T* Yc, int YP, int n, int nb, T* G) {
+__device__ __forceinline__ void lq_gram(const T* Yc, int YP, int n, int nb, T* G) {
   const int a = threadIdx.x & 31, bq = threadIdx.x >> 5;
   T acc[4] = {T(0), T(0), T(0), T(0)};
   if (a < nb) {
@@ -507,7 +536,7 @@ __device__ void lq_gram(const T* Yc, int YP, int n, int nb, T* G) {
 // Rows r0 .. m-1 of C (n columns, ld ldc) <- C - (C Y^T) T Y, Y = Yc (nb x n,
 // reflector-major, zero-padded to a multiple of 4 columns), chunks of XC rows.
 template <typename T>
-__device__ void lq_apply_right(T* C, int ldc, int r0, int m, int n, const T* Yc, int YP, int nb, const T* Tm,
+__device__ __forceinline__ void lq_apply_right(T* C, int ldc, int r0, int m, int n, const T* Yc, int YP, int nb, const T* Tm,
                                T* X) {
   const int tid = threadIdx.x, rr = tid & (XC - 1), grp = tid / XC;
   for (int R0 = r0; R0 < m; R0 += XC) {
@@ -591,7 +620,7 @@ __device__ void lq_apply_right(T* C, int ldc, int r0, int m, int n, const T* Yc,
 
 // V (n x kv, ld LDV) <- V - Y^T (T^T (Y V)) for one LQ panel, Y = Yc (nb x n).
 template <typename T>
-__device__ void lq_apply_v(T* V, int LDV, int n, int kv, const T* Yc, int YP, int nb, const T* Tm, T* X) {
+__device__ __forceinline__ void lq_apply_v(T* V, int LDV, int n, int kv, const T* Yc, int YP, int nb, const T* Tm, T* X) {
   const int tid = threadIdx.x, c = tid & 31, ab = tid >> 5;   // ab: reflectors 4 ab .. 4 ab + 3
   // Z = Y V (nb x kv) into X
   for (int cc = c; cc < kv; cc += 32) {
@@ -660,22 +689,23 @@ __device__ void lq_apply_v(T* V, int LDV, int n, int kv, const T* Yc, int YP, in
   __syncthreads();
 }
 
-template <typename T>
+template <typename T, int S>
 __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
-    ulv_factor_blk_kernel(const Task* __restrict__ tasks, const Slot* __restrict__ slots, int mmax, int nmax,
-                          int kumax, int kvmax, int extra) {
+    ulv_factor_blk_kernel(const Task* __restrict__ tasks, const Slot* __restrict__ slots, int kumax, int kvmax,
+                          int extra) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ T bvals[NW];
   __shared__ int bidx[NW];
   __shared__ int prow;
-  const BlkLayout Lo(mmax, nmax, kumax, kvmax, (size_t)extra);
+  const BlkLayout Lo(S, kumax, kvmax, (size_t)extra);
   const Task tk = tasks[blockIdx.x];
   const Node* nodes = tk.nodes;
   const Node& nd = nodes[tk.node];
   const Slot& sl = slots[tk.slot];
   T* fb = (T*)sl.fbase;
   const int m = nd.m, n = nd.n, ku = nd.ku, kv = nd.kv;
-  const int LDD = Lo.LDD, LDU = Lo.LDU, YP = Lo.YP, LDV = Lo.LDV;
+  constexpr int LDD = S + 1, LDU = S + 4, YP = S + 4, LDV = S + 1;   // as in BlkLayout
+  constexpr int PE = S / PL;                                        // panel entries per lane
   T* sm = (T*)smraw;
   T* sD = sm;                 // m x n, ld LDD
   T* sW = sm + Lo.oW;         // U (ld LDU) / LQ panel (ld YP) / L1-inverse scratch
@@ -720,26 +750,32 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
     const int o12 = oV2 + nr2 * v2;   // T12 = U1 B12, mr1 x v2
     const int o21 = o12 + mr1 * v2;   // T21 = U2 B21, mr2 x v1
     {
-      // the copy lists live in shared memory (uniform reads, no local memory)
-      __shared__ CopyJob<double> g64[6];
-      __shared__ CopyJob<T> gch[6];
-      if (tid == 0) {
-        g64[0] = {nd.B12, u1, u1, v2, u1, 0, oB12};
-        g64[1] = {nd.B21, u2, u2, v1, u2, 0, oB21};
-        g64[2] = {nd.R1, u1, u1, kuo, u1, 0, oR1};
-        g64[3] = {nd.R2, u2, u2, kuo, u2, 0, oR2};
-        g64[4] = {nd.W1, v1, v1, kvo, v1, 0, oW1};
-        g64[5] = {nd.W2, v2, v2, kvo, v2, 0, oW2};
-        gch[0] = {fb + c1.fU + c1.mk, c1.m, mr1, u1, mr1, c1.lower_u, oU1};
-        gch[1] = {fb + c2.fU + c2.mk, c2.m, mr2, u2, mr2, c2.lower_u, oU2};
-        gch[2] = {fb + c1.fV + c1.nk, c1.n, nr1, v1, nr1, 0, oV1};
-        gch[3] = {fb + c2.fV + c2.nk, c2.n, nr2, v2, nr2, 0, oV2};
-        gch[4] = {fb + c1.fD + c1.mk + (int64_t)c1.nk * c1.m, c1.m, mr1, nr1, LDD, 0, 0};
-        gch[5] = {fb + c2.fD + c2.mk + (int64_t)c2.nk * c2.m, c2.m, mr2, nr2, LDD, 0, mr1 + nr1 * LDD};
+      // one job per warp: the FP64 generator blocks (converted to T), and the
+      // children's reduced blocks (factor storage, already T)
+      const int w = tid >> 5;
+      CopyJob<double> G64{nullptr, 0, 0, 0, 0, 0, 0};
+      switch (w) {
+        case 0: G64 = {nd.B12, u1, u1, v2, u1, 0, oB12}; break;
+        case 1: G64 = {nd.B21, u2, u2, v1, u2, 0, oB21}; break;
+        case 2: G64 = {nd.R1, u1, u1, kuo, u1, 0, oR1}; break;
+        case 3: G64 = {nd.R2, u2, u2, kuo, u2, 0, oR2}; break;
+        case 4: G64 = {nd.W1, v1, v1, kvo, v1, 0, oW1}; break;
+        case 5: G64 = {nd.W2, v2, v2, kvo, v2, 0, oW2}; break;
+        default: break;
       }
-      __syncthreads();
-      stage_jobs(sm, g64, 6);
-      stage_jobs(sm, gch, 6);
+      if (w < 6) stage_warp(sm, G64);
+      CopyJob<T> J{nullptr, 0, 0, 0, 0, 0, 0};
+      const int wc = (w + 6) % NW;   // warps 6 and 7 take the first of these, the others follow
+      switch (wc) {
+        case 0: J = {fb + c1.fU + c1.mk, c1.m, mr1, u1, mr1, c1.lower_u, oU1}; break;
+        case 1: J = {fb + c2.fU + c2.mk, c2.m, mr2, u2, mr2, c2.lower_u, oU2}; break;
+        case 2: J = {fb + c1.fV + c1.nk, c1.n, nr1, v1, nr1, 0, oV1}; break;
+        case 3: J = {fb + c2.fV + c2.nk, c2.n, nr2, v2, nr2, 0, oV2}; break;
+        case 4: J = {fb + c1.fD + c1.mk + (int64_t)c1.nk * c1.m, c1.m, mr1, nr1, LDD, 0, 0}; break;
+        case 5: J = {fb + c2.fD + c2.mk + (int64_t)c2.nk * c2.m, c2.m, mr2, nr2, LDD, 0, mr1 + nr1 * LDD}; break;
+        default: break;
+      }
+      if (wc < 6) stage_warp(sm, J);
     }
     __syncthreads();
     const T* gB12 = sm + oB12;
@@ -754,61 +790,20 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
     const T* cV2 = sm + oV2;
     T* sT12 = sm + o12;
     T* sT21 = sm + o21;
-    T* T12 = fb + nd.fT12;
-    T* T21 = fb + nd.fT21;
-    for (int o = tid; o < mr1 * v2; o += NT) {
-      const int i = o % mr1, j = o / mr1;
-      T s = T(0);
-      for (int l = 0; l < u1; ++l) s = fma_t(cU1[i + l * mr1], gB12[l + j * u1], s);
-      sT12[o] = s;
-      T12[o] = s;
-    }
-    for (int o = tid; o < mr2 * v1; o += NT) {
-      const int i = o % mr2, j = o / mr2;
-      T s = T(0);
-      for (int l = 0; l < u2; ++l) s = fma_t(cU2[i + l * mr2], gB21[l + j * u2], s);
-      sT21[o] = s;
-      T21[o] = s;
-    }
+    // T12 = U1 B12, T21 = U2 B21 (also kept for the solve); U = [U1 R1; U2 R2],
+    // V = [V1 W1; V2 W2] (src/ulvfactor.jl:78-79)
+    small_mm(sT12, mr1, fb + nd.fT12, cU1, mr1, gB12, u1, 1, mr1, v2, u1);
+    small_mm(sT21, mr2, fb + nd.fT21, cU2, mr2, gB21, u2, 1, mr2, v1, u2);
     if (!nd.root) {
-      // U = [U1 R1; U2 R2], V = [V1 W1; V2 W2] (src/ulvfactor.jl:78-79)
-      for (int o = tid; o < m * ku; o += NT) {
-        const int i = o % m, j = o / m;
-        T s = T(0);
-        if (i < mr1) {
-          for (int l = 0; l < u1; ++l) s = fma_t(cU1[i + l * mr1], gR1[l + j * u1], s);
-        } else {
-          const int i2 = i - mr1;
-          for (int l = 0; l < u2; ++l) s = fma_t(cU2[i2 + l * mr2], gR2[l + j * u2], s);
-        }
-        sW[i + j * LDU] = s;
-      }
-      for (int o = tid; o < n * kv; o += NT) {
-        const int i = o % n, j = o / n;
-        T s = T(0);
-        if (i < nr1) {
-          for (int l = 0; l < v1; ++l) s = fma_t(cV1[i + l * nr1], gW1[l + j * v1], s);
-        } else {
-          const int i2 = i - nr1;
-          for (int l = 0; l < v2; ++l) s = fma_t(cV2[i2 + l * nr2], gW2[l + j * v2], s);
-        }
-        sV[i + j * LDV] = s;
-      }
+      small_mm(sW, LDU, (T*)nullptr, cU1, mr1, gR1, u1, 1, mr1, ku, u1);
+      small_mm(sW + mr1, LDU, (T*)nullptr, cU2, mr2, gR2, u2, 1, mr2, ku, u2);
+      small_mm(sV, LDV, (T*)nullptr, cV1, nr1, gW1, v1, 1, nr1, kv, v1);
+      small_mm(sV + nr1, LDV, (T*)nullptr, cV2, nr2, gW2, v2, 1, nr2, kv, v2);
     }
     __syncthreads();
     // the off-diagonal blocks U1 B12 V2^T and U2 B21 V1^T (src/ulvfactor.jl:75)
-    for (int o = tid; o < mr1 * nr2; o += NT) {
-      const int i = o % mr1, j2 = o / mr1;
-      T s = T(0);
-      for (int l = 0; l < v2; ++l) s = fma_t(sT12[i + l * mr1], cV2[j2 + l * nr2], s);
-      sD[i + (nr1 + j2) * LDD] = s;
-    }
-    for (int o = tid; o < mr2 * nr1; o += NT) {
-      const int i2 = o % mr2, j = o / mr2;
-      T s = T(0);
-      for (int l = 0; l < v1; ++l) s = fma_t(sT21[i2 + l * mr2], cV1[j + l * nr1], s);
-      sD[mr1 + i2 + j * LDD] = s;
-    }
+    small_mm(sD + nr1 * LDD, LDD, (T*)nullptr, sT12, mr1, cV2, 1, nr2, mr1, nr2, v2);
+    small_mm(sD + mr1, LDD, (T*)nullptr, sT21, mr2, cV1, 1, nr1, mr2, nr1, v1);
   }
   __syncthreads();
 
@@ -843,17 +838,14 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
     }
     auto gen = [&](int c, int buf) {   // the 8 lanes of column c
       const int p = mk + c;
-      T s0 = T(0), s1 = T(0), mine = T(0);
+      T sq[4] = {T(0), T(0), T(0), T(0)}, mine = T(0);
 #pragma unroll
       for (int t = 0; t < PE; ++t) {
         const int row = l8 + PL * t;
-        if (row < p) {
-          if (t & 1) s1 += u[t] * u[t];
-          else s0 += u[t] * u[t];
-        }
+        if (row < p) sq[t & 3] = fma_t(u[t], u[t], sq[t & 3]);
         if (row == p) mine = u[t];
       }
-      const T ss = gsum8(s0 + s1, gm);
+      const T ss = gsum8((sq[0] + sq[1]) + (sq[2] + sq[3]), gm);
       const T alpha = __shfl_sync(gm, mine, (lane & 24) | (p & 7));
       T beta, tau, sc;
       larfg_t(alpha, ss, beta, tau, sc);
@@ -922,17 +914,14 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
       d[t] = (g < nb && col < n) ? sD[row + col * LDD] : T(0);
     }
     auto gen = [&](int i, int buf) {   // the 8 lanes of row i
-      T s0 = T(0), s1 = T(0), mine = T(0);
+      T sq[4] = {T(0), T(0), T(0), T(0)}, mine = T(0);
 #pragma unroll
       for (int t = 0; t < PE; ++t) {
         const int col = l8 + PL * t;
-        if (col > i) {
-          if (t & 1) s1 += d[t] * d[t];
-          else s0 += d[t] * d[t];
-        }
+        if (col > i) sq[t & 3] = fma_t(d[t], d[t], sq[t & 3]);
         if (col == i) mine = d[t];
       }
-      const T ss = gsum8(s0 + s1, gm);
+      const T ss = gsum8((sq[0] + sq[1]) + (sq[2] + sq[3]), gm);
       const T alpha = __shfl_sync(gm, mine, (lane & 24) | (i & 7));
       T beta, tau, sc;
       larfg_t(alpha, ss, beta, tau, sc);
@@ -1002,7 +991,7 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
 
 template <typename T>
 size_t factor_blk_smem(int mmax, int nmax, int kumax, int kvmax, size_t extra) {
-  return BlkLayout(mmax, nmax, kumax, kvmax, extra).total * sizeof(T);
+  return BlkLayout(size_bucket(mmax, nmax), kumax, kvmax, extra).total * sizeof(T);
 }
 
 template <typename T>
@@ -1011,17 +1000,30 @@ bool factor_blk_fits(int mmax, int nmax, int kumax, int kvmax, size_t extra) {
          factor_blk_smem<T>(mmax, nmax, kumax, kvmax, extra) <= kBlkSmemCap;
 }
 
+namespace {
+template <typename T, int S>
+void launch_blk_sized(const Task* t, int64_t nt, const Slot* s, int kumax, int kvmax, size_t extra, size_t smem,
+                      cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(ulv_factor_blk_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBlkSmemCap);
+    attr_set = true;
+  }
+  ulv_factor_blk_kernel<T, S><<<(unsigned)nt, NT, smem, st>>>(t, s, kumax, kvmax, (int)extra);
+}
+}  // namespace
+
 template <typename T>
 void launch_ulv_factor_blk(const Task* t, int64_t nt, const Slot* s, int mmax, int nmax, int kumax, int kvmax,
                            size_t extra, cudaStream_t st) {
   if (nt <= 0) return;
   const size_t smem = factor_blk_smem<T>(mmax, nmax, kumax, kvmax, extra);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(ulv_factor_blk_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBlkSmemCap);
-    attr_set = true;
+  switch (size_bucket(mmax, nmax)) {
+    case 32: launch_blk_sized<T, 32>(t, nt, s, kumax, kvmax, extra, smem, st); break;
+    case 64: launch_blk_sized<T, 64>(t, nt, s, kumax, kvmax, extra, smem, st); break;
+    case 96: launch_blk_sized<T, 96>(t, nt, s, kumax, kvmax, extra, smem, st); break;
+    default: launch_blk_sized<T, 128>(t, nt, s, kumax, kvmax, extra, smem, st); break;
   }
-  ulv_factor_blk_kernel<T><<<(unsigned)nt, NT, smem, st>>>(t, s, mmax, nmax, kumax, kvmax, (int)extra);
 }
 
 template bool factor_blk_fits<double>(int, int, int, int, size_t);
