@@ -278,7 +278,7 @@ def run_ours(args, rank, world, local_rank):
     # per kernel kind: device time per mixed step (CUDA events around each
     # launch of one kind at a time, a few extra steps per kind)
     breakdown = {}
-    for kind in ("factor_leaf", "factor_merge", "solve_up", "solve_down", "mv_leaf", "mv_up", "mv_down",
+    for kind in ("factor_leaf", "factor_merge", "solve_up", "solve_down", "mv_dx", "mv_leaf", "mv_up", "mv_down",
                  "mv_final"):
         L.trace_begin(kind)
         for _ in range(3):

@@ -24,7 +24,7 @@ HSS_ERR_CUDA = 6
 HSS_ERR_INVALID = 7
 
 TRACE = {"mv_leaf": 0, "mv_up": 1, "mv_down": 2, "mv_final": 3, "factor_leaf": 4, "factor_merge": 5,
-         "solve_up": 6, "solve_down": 7}
+         "solve_up": 6, "solve_down": 7, "mv_dx": 8}
 
 HSS_PREC_FP64 = 0
 HSS_PREC_FP32 = 1
@@ -38,6 +38,7 @@ HSS_OPT_SAMPLE_DF = 5
 HSS_OPT_FLAT_PRODUCT = 6
 HSS_OPT_POLL_LIMIT = 7
 HSS_OPT_FAIL_ALLOC = 8
+HSS_OPT_TENSOR_RESIDUAL = 9
 
 NODE_FIELDS = 16
 CLUSTER_FIELDS = 6

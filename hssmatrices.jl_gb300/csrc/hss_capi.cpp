@@ -130,6 +130,7 @@ bool g_residual_fp64 = false;
 bool g_level_product = false;
 // Lets FP64 products of few columns run the flat form of the persistent product.
 bool g_flat_product = true;
+bool g_tensor_dx = true;   // HSS_OPT_TENSOR_RESIDUAL
 // Replays factor and solve launch sequences as CUDA graphs (non-default streams).
 bool g_graphs = false;
 // Autotuner: forces every solve level to the register (0) or the blocked (1)
@@ -777,11 +778,21 @@ int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable&
   CUDA_TRY(pm.ensure_pmv(pmv_queue_entries(L.ntasks, L.ninner, pmv_chunks(pairs, rmax)), st));
   ++pm.epoch;
   cudaError_t e = cudaSuccess;
+  // double-float residual: the leaf products D X on the tensor cores first
+  const bool dx = pairs && g_tensor_dx && dx_tc_fits(L.mleaf, L.nleaf);
+  if (dx) {
+    traced(HSS_TRACE_MV_DX, L.leaves.cnt, st, [&] { e = launch_dx_tc(L.d_tasks + L.leaves.off, L.leaves.cnt,
+                                                                     slots, rmax, st); });
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "tensor-core leaf product launch");
+    }
+  }
   traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st, [&] {
     const void* pf = pairs ? (const void*)L.pfdf : (const void*)L.pf64;
     e = launch_pmv(pairs, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, L.ntasks, L.ninner, rmax, L.nleaf, L.kmax,
                    pm.pstate.p,
-                   pm.pq.p, pm.epoch, pf, pf ? L.pf_elems * 8 : 0, L.device, st);
+                   pm.pq.p, pm.epoch, pf, pf ? L.pf_elems * 8 : 0, L.device, st, dx);
   });
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -1849,6 +1860,10 @@ int hss_set_option(int32_t option, int64_t value) {
   }
   if (option == HSS_OPT_FLAT_PRODUCT) {
     g_flat_product = value != 0;
+    return HSS_OK;
+  }
+  if (option == HSS_OPT_TENSOR_RESIDUAL) {
+    g_tensor_dx = value != 0;
     return HSS_OK;
   }
   if (option == HSS_OPT_FAIL_ALLOC) {

@@ -57,7 +57,14 @@ void pmv_set_poll_limit(uint32_t polls);
 cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks,
                        int64_t ninner, int rmax,
                        int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
-                       const void* prefetch, int64_t prefetch_bytes, int device, cudaStream_t st);
+                       const void* prefetch, int64_t prefetch_bytes, int device, cudaStream_t st,
+                       bool dx_ready = false);
+// Tensor-core leaf products of the double-float residual (hss_dx_tc.cu): for
+// every non-root leaf task and chunk of 32 columns, D X at ~48-bit accuracy
+// into the slot's pair buffer (sl.tmp), X = the slot's B; leaves up to 128 x 128.
+// A persistent pair product launched after it with dx_ready skips those products.
+bool dx_tc_fits(int mleaf, int nleaf);
+cudaError_t launch_dx_tc(const Task* leaves, int64_t nleaves, const Slot* slots, int rmax, cudaStream_t st);
 
 // Flat persistent product (hss_pmv.cu), FP64 with few right-hand sides: every
 // leaf carries its own chain of small products up to the root and back, so

@@ -80,6 +80,7 @@ struct PmvArgs {
   int32_t cw;            // columns per chunk (<= RC)
   uint32_t epoch;
   uint32_t idle_limit;   // polls of an idle block before DEV_TIMEOUT
+  int32_t dx_ready;      // pairs: the non-root leaves' D B is already in the pair buffer (tensor cores)
 };
 
 // ---- arithmetic policies ----------------------------------------------------
@@ -582,7 +583,8 @@ __device__ void bulk_unit(const PmvArgs& a, int u, typename P::Acc* part, typena
     for (int64_t off = (int64_t)threadIdx.x * 128; off < bytes; off += PT * 128)
       asm volatile("prefetch.global.L2 [%0];" ::"l"(ub + off));
   }
-  if (j0 < sl.r) {
+  constexpr bool pairs_e = !std::is_same<E, double>::value;
+  if (j0 < sl.r && !(pairs_e && a.dx_ready && !nd.root)) {
     const int nc = min(a.cw, sl.r - j0), m = nd.gm, n = nd.gn;
     E* Xs = sm;
     __syncthreads();
@@ -1249,7 +1251,7 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
                        int64_t ninner, int rmax,
                        int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
                        const void* prefetch,
-                       int64_t prefetch_bytes, int device, cudaStream_t st) {
+                       int64_t prefetch_bytes, int device, cudaStream_t st, bool dx_ready) {
   if (nleaves <= 0) return cudaSuccess;
   const size_t smem = pmv_smem_elems(nleaf, kmax, nullptr) * 8;
   PmvArgs a;
@@ -1267,6 +1269,7 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
   a.pf = (const char*)prefetch;
   a.pf_bytes = prefetch ? prefetch_bytes : 0;
   a.idle_limit = g_idle_limit;
+  a.dx_ready = (pairs && dx_ready) ? 1 : 0;
   void* args[] = {&a};
   const int cap = pairs ? resident_blocks<PDF>(smem, device) : resident_blocks<PF64>(smem, device);
   if (cap <= 0) return cudaErrorLaunchOutOfResources;

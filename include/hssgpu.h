@@ -207,7 +207,8 @@ enum {
   HSS_TRACE_FACTOR_MERGE = 5, /* merge + reduction per level (src/ulvfactor.jl:74-89) */
   HSS_TRACE_SOLVE_UP = 6,     /* upward solve per level */
   HSS_TRACE_SOLVE_DOWN = 7,   /* Q^T back-application per level (src/ulvfactor.jl:98-107) */
-  HSS_TRACE_KINDS = 8
+  HSS_TRACE_MV_DX = 8,        /* tensor-core leaf products D X of the refinement residual (src/matmul.jl:46) */
+  HSS_TRACE_KINDS = 9
 };
 int hss_trace_begin(int32_t kind);
 int hss_trace_end(double* total_ms, int64_t* launches);
@@ -274,6 +275,11 @@ int64_t hss_launch_counter(void);
  * makes the waits run out on purpose (failure-detection tests).  Launch
  * sequences already captured as CUDA graphs keep the limit they were
  * captured with.
+ * HSS_OPT_TENSOR_RESIDUAL = 0 turns off the tensor-core leaf products of the
+ * double-float refinement residual (1, default: for leaves up to 128 x 128
+ * the products D X run as exact bf16 slice products on tcgen05, with FP32
+ * accumulation in tensor memory, about 48 significant bits like the rest of
+ * the residual; 0: on the FP32 pipe in double-float arithmetic).
  * HSS_OPT_FAIL_ALLOC = k > 0 makes the k-th device allocation of this library
  * from now on fail as out of memory, on the host, before the CUDA driver is
  * called (0 disarms): fault injection for the HSS_ERR_OOM paths.  The call
@@ -286,7 +292,8 @@ enum {
   HSS_OPT_SAMPLE_DF = 5,
   HSS_OPT_FLAT_PRODUCT = 6,
   HSS_OPT_POLL_LIMIT = 7,
-  HSS_OPT_FAIL_ALLOC = 8
+  HSS_OPT_FAIL_ALLOC = 8,
+  HSS_OPT_TENSOR_RESIDUAL = 9
 };
 int hss_set_option(int32_t option, int64_t value);
 

@@ -191,20 +191,54 @@ def test_factor_kernels_agree(pkg, lib, orc, name):
 @pytest.mark.parametrize("name", ["synthetic_perfect", "synthetic_uneven", "synthetic_earlyexit",
                                   "cauchy2001_compress"])
 def test_refinement_residual_paths(pkg, lib, orc, name):
-    """FP32 factorization refined with the double-float residual product (default) and with
-    the native FP64 product: both reach 1e-10 in true (oracle, FP64) residual."""
+    """FP32 factorization refined with the double-float residual product, its leaf
+    products D X on the tensor cores (default) or on the FP32 pipe, and with the
+    native FP64 product: all reach 1e-10 in true (oracle, FP64) residual, and the
+    residual each reports is the true one."""
+    L = pkg._lib
     g, h, A = _golden(pkg, orc, name)
     Af = orc.full(h)
     sols = []
-    for native in (0, 1):
-        assert lib.hss_set_option(2, native) == 0
+    for native, tensor in ((0, 1), (0, 0), (1, 1)):
+        assert lib.hss_set_option(L.HSS_OPT_RESIDUAL_FP64, native) == 0
+        assert lib.hss_set_option(L.HSS_OPT_TENSOR_RESIDUAL, tensor) == 0
         try:
             st = {}
             z = pkg.ldiv(A, g["b"], precision="fp32", tol=1e-10, maxit=30, stats=st)
         finally:
-            lib.hss_set_option(2, 0)
+            lib.hss_set_option(L.HSS_OPT_RESIDUAL_FP64, 0)
+            lib.hss_set_option(L.HSS_OPT_TENSOR_RESIDUAL, 1)
         assert st["converged"]
         res = np.linalg.norm(g["b"] - Af @ z, axis=0) / np.linalg.norm(g["b"], axis=0)
-        assert res.max() <= 2e-10, (native, res.max())
+        assert res.max() <= 2e-10, (native, tensor, res.max())
+        # the reported residual is computed before the last correction's effect
+        # is known only to the residual's own accuracy: ~1e-14 of |A| |x| / |b|
+        assert abs(st["residual"] - res.max()) <= 1e-12 + 1e-2 * res.max(), (native, tensor)
         sols.append(z)
-    assert rel(sols[0], sols[1]) <= 1e-6
+    assert rel(sols[0], sols[1]) <= 1e-6 and rel(sols[0], sols[2]) <= 1e-6
+
+
+@pytest.mark.parametrize("r", [1, 5, 32, 40])
+def test_tensor_residual_matches_fp64(pkg, lib, orc, r):
+    """One refinement step from the same FP32 solution with the residual formed by
+    the tensor-core leaf products and by the native FP64 product: the residual
+    norms agree to the residual's accuracy (1e-13 of |A||x|), on a tree with
+    uneven 62/63-row leaves and r below, at and above one 32-column chunk."""
+    L = pkg._lib
+    rng = np.random.default_rng(40 + r)
+    h = orc.synthetic_hss(2001, 64, 16, rng)
+    A = pkg.HssMatrix.from_tree(h)
+    b = rng.standard_normal((2001, r))
+    out = {}
+    F = pkg.ulvfactor(A, "fp32")
+    for native in (0, 1):
+        assert lib.hss_set_option(L.HSS_OPT_RESIDUAL_FP64, native) == 0
+        try:
+            with pytest.raises(pkg._lib.NoConvergence):   # one correction, then the residual again
+                F.solve(b, tol=1e-300, maxit=1)
+        finally:
+            lib.hss_set_option(L.HSS_OPT_RESIDUAL_FP64, 0)
+        out[native] = (F.stats.iterations, F.stats.residual)
+    assert out[0][0] == out[1][0] == 1
+    r0, r1 = out[0][1], out[1][1]
+    assert 0.0 < r1 < 1e-9 and abs(r0 - r1) <= 1e-12 + 1e-3 * r1, (r0, r1)
