@@ -193,6 +193,8 @@ struct hss_plan_s {
   hss_factor_s* fused[2] = {nullptr, nullptr};   // storage reused by hss_ulvfactsolve_host
   int64_t gen_len = 0;                  // elements of d_gen
   float2* d_gen_df = nullptr;           // generators as (hi, lo) float pairs, made on first use
+  unsigned char* d_dx = nullptr;        // slices of the leaf blocks D for the tensor-core residual (first use)
+  int64_t dx_bytes = 0;
   int32_t* d_sync = nullptr;            // per-node arrival counters of the persistent product
   int pmv_nleaf = 0, pmv_mleaf = 0, pmv_kmax = 0;   // largest leaf columns / rows, largest rank
   int64_t pmv_ninner = 0;                           // branches that are not roots
@@ -241,6 +243,7 @@ hss_plan_s::~hss_plan_s() {
   delete fused[0];
   delete fused[1];
   if (d_gen_df) cudaFree(d_gen_df);
+  if (d_dx) cudaFree(d_dx);
   if (d_gen) cudaFree(d_gen);
   if (d_nodes) cudaFree(d_nodes);
   if (d_tasks) cudaFree(d_tasks);
@@ -472,6 +475,11 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
         x.fT21 = fac; fac += align16((int64_t)c2.mr * c1.kv);
       }
       if (x.root) { x.fpiv = fac; fac += align16(x.m); }
+      x.fdx = -1;
+      if (x.leaf && !x.root && dx_tc_fits(x.m, x.n)) {
+        x.fdx = P->dx_bytes;
+        P->dx_bytes += (dx_leaf_bytes(x.n) + 255) & ~int64_t(255);
+      }
       if (!x.root && x.mk > 0) {
         x.fTq = fac; fac += align16((int64_t)((x.k + 31) / 32) * 1024);
         x.fTl = fac; fac += align16((int64_t)((x.mk + 31) / 32) * 1024);
@@ -758,7 +766,10 @@ bool use_flat(const Levels& L, bool pairs, int rmax) {
   return !pairs && g_flat_product && L.flat_dep > 0 && pmv_flat_fits(L.nleaf, L.kmax, L.flat_dep, rmax);
 }
 
-int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable& pm, cudaStream_t st) {
+// dx: the slots carry prepared slices of their leaf blocks (pairs only): the
+// leaf products D X run on the tensor cores before the persistent product.
+int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable& pm, cudaStream_t st,
+            bool dx_slices = false) {
   if (use_flat(L, pairs, rmax)) {
     CUDA_TRY(pm.ensure_pmv(1, st));
     CUDA_TRY(pm.ensure_flat(pmv_flat_ctb_elems(L.leaves.cnt, L.flat_dep, L.kmax, rmax),
@@ -779,7 +790,7 @@ int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable&
   ++pm.epoch;
   cudaError_t e = cudaSuccess;
   // double-float residual: the leaf products D X on the tensor cores first
-  const bool dx = pairs && g_tensor_dx && dx_tc_fits(L.mleaf, L.nleaf);
+  const bool dx = pairs && dx_slices && dx_tc_fits(L.mleaf, L.nleaf);
   if (dx) {
     traced(HSS_TRACE_MV_DX, L.leaves.cnt, st, [&] { e = launch_dx_tc(L.d_tasks + L.leaves.off, L.leaves.cnt,
                                                                      slots, rmax, st); });
@@ -831,8 +842,9 @@ int run_matvec(hss_plan_s* P, const Slot* slots, int rmax, cudaStream_t st, Slot
   return run_matvec(plan_levels(P), slots, rmax, st, pm);
 }
 
-int run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, SlotTable* pm = nullptr) {
-  if (use_pmv(L, pm, true, rmax)) return run_pmv(L, slots, rmax, true, *pm, st);
+int run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, SlotTable* pm = nullptr,
+                  bool dx_slices = false) {
+  if (use_pmv(L, pm, true, rmax)) return run_pmv(L, slots, rmax, true, *pm, st, dx_slices);
   const Task* T = L.d_tasks;
   traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st,
          [&] { launch_dfmv_leaf(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
@@ -845,6 +857,27 @@ int run_matvec_df(const Levels& L, const Slot* slots, int rmax, cudaStream_t st,
   traced(HSS_TRACE_MV_FINAL, L.leaves.cnt, st,
          [&] { launch_dfmv_final(T + L.leaves.off, L.leaves.cnt, slots, rmax, st); });
   return HSS_OK;
+}
+
+// The tensor-core residual's slices of every leaf block D, made once per plan
+// (the generators do not change); false when the plan has no such leaves or
+// the buffer cannot be allocated (the residual then runs without them).
+bool ensure_dx(hss_plan_s* P, cudaStream_t st) {
+  if (P->d_dx) return true;
+  if (P->dx_bytes <= 0 || P->leaves.cnt <= 0) return false;
+  if (dev_alloc((void**)&P->d_dx, (size_t)P->dx_bytes) != cudaSuccess) {
+    P->d_dx = nullptr;
+    cudaGetLastError();
+    return false;
+  }
+  if (launch_dx_prep(P->d_tasks + P->leaves.off, P->leaves.cnt, P->d_dx, st) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(P->d_dx);
+    P->d_dx = nullptr;
+    return false;
+  }
+  add_launches(1);
+  return true;
 }
 
 int ensure_df(hss_plan_s* P, cudaStream_t st) {
@@ -1302,6 +1335,7 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     CUDA_TRY(B.tmp.ensure(std::max<int64_t>(roff[ni], 1)));
   }
   std::vector<Slot> ms(ni);
+  bool dx_slices = dfres && g_tensor_dx;   // every item's plan has its leaf slices prepared
   for (size_t i = 0; i < ni; ++i) {
     const Item& it = items[i];
     hss_plan_s* P = it.f->plan;
@@ -1326,6 +1360,8 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
       x.ldws = P->ws_mv;
       x.gdf = P->d_gen_df;
       x.gbase = P->d_gen;
+      x.dxs = (g_tensor_dx && ensure_dx(P, st)) ? P->d_dx : nullptr;
+      dx_slices = dx_slices && x.dxs != nullptr;
     } else {
       CUDA_TRY(P->mv_ws.ensure((size_t)P->ws_mv * rmax));
       x.ws = P->mv_ws.p;
@@ -1345,7 +1381,8 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
         add_launches(1);
       }
     CUDA_TRY(B.mv.upload(ms, st));
-    rc = dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, pm) : run_matvec(L, B.mv.dev.p, (int)rmax, st, pm);
+    rc = dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, pm, dx_slices)
+               : run_matvec(L, B.mv.dev.p, (int)rmax, st, pm);
     if (rc) return rc;
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(B.h_rn2.p, B.rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));

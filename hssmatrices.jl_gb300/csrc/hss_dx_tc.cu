@@ -17,16 +17,21 @@
 // summed from d = 6 down in double-float arithmetic (TwoSum) and scaled by the
 // power of two: about 48 significant bits, as the rest of the residual.
 //
-// One block of 256 threads per (leaf, chunk of 32 right-hand sides), leaves
-// up to 128 x 128.  K is processed in two halves of 64: for each half the
-// threads write the 7 slices of D (128 x 64 bf16 each) and of X (32 x 64) to
-// shared memory in the no-swizzle K-major layout of 8 x 8 core matrices, and
-// one thread issues the 28 slice products (4 MMAs of K = 16 each, M = 128,
-// N = 32) into the 7 accumulators; a commit to an mbarrier tells the block
-// that the half's operands are consumed.  Four warps read the accumulators
-// back (tcgen05.ld, one row per thread) and write the pairs.  Waits are
-// bounded: a wait that runs out records DEV_TIMEOUT, waits (bounded) for the
-// tensor core once more and frees tensor memory before returning.
+// The slices of D depend only on the generators: dx_prep_kernel writes them
+// once per plan (with each row's exponent) to global memory, already in the
+// shared-memory layout of the MMA operands (no-swizzle K-major 8 x 8 core
+// matrices), by quarters of K = 32.  A residual call then runs one block of
+// 256 threads per (leaf, chunk of 32 right-hand sides), leaves up to
+// 128 x 128: per quarter of K, one thread starts bulk asynchronous copies
+// (cp.async.bulk, the TMA engine) of the 7 slices of D into shared memory
+// while the threads slice X (32 x 32) next to them, and one thread issues the
+// 28 slice products (2 MMAs of K = 16 each, M = 128, N = 32) into the 7
+// accumulators; mbarriers track the copies (transaction bytes) and the MMAs
+// (commit).  A block holds 70 KB of operands, so two blocks share an SM and
+// overlap each other's copies.  Four warps read the accumulators back
+// (tcgen05.ld, one row per thread) and write the pairs.  Waits are bounded: a
+// wait that runs out records DEV_TIMEOUT, waits (bounded) for the tensor core
+// once more and frees tensor memory before returning.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -43,12 +48,15 @@ constexpr int XT = 256;        // threads
 constexpr int NS = 7;          // slices per operand
 constexpr int XN = 32;         // right-hand sides per block (MMA N)
 constexpr int XM = 128;        // rows per block (MMA M)
-constexpr int XKH = 64;        // K per half
+constexpr int XKQ = 32;        // K per quarter
+constexpr int NQ = 4;          // quarters (K <= 128)
 constexpr uint32_t kTmemCols = 256;                   // 7 accumulators x 32 columns
-constexpr int A_SLICE = XM * XKH * 2;                 // bytes: 16 KB
-constexpr int B_SLICE = XN * XKH * 2;                 // bytes: 4 KB
-constexpr int SMEM_BYTES = NS * (A_SLICE + B_SLICE);  // 140 KB
+constexpr int AQ = XM * XKQ * 2;                      // bytes of one slice of D per quarter: 8 KB
+constexpr int BQ = XN * XKQ * 2;                      // of X: 2 KB
+constexpr int OPER_BYTES = NS * (AQ + BQ);            // 70 KB
+constexpr int SMEM_BYTES = 100 * 1024;                // requested: at most two blocks per SM (tensor memory)
 constexpr uint32_t kWaitLimit = 1u << 24;
+static_assert(OPER_BYTES <= SMEM_BYTES, "operands fit the requested shared memory");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -114,13 +122,78 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
 }
 
-__global__ void __launch_bounds__(XT, 1) dx_tc_kernel(const Task* __restrict__ leaves, int nchunk,
+// Largest biased exponent of row r of D over its n columns (0: the row is zero).
+__device__ __forceinline__ int row_emax(const double* D, int m, int n, int r, int c0, int cstep) {
+  int emax = 0;
+  if (r < m) {
+    int c = c0;
+    for (; c + 7 * cstep < n; c += 8 * cstep) {   // eight loads in flight
+      unsigned long long b[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) b[u] = (unsigned long long)__double_as_longlong(__ldg(D + r + (int64_t)(c + u * cstep) * m));
+#pragma unroll
+      for (int u = 0; u < 8; ++u) emax = max(emax, (int)((b[u] >> 52) & 0x7FF));
+    }
+    for (; c < n; c += cstep)
+      emax = max(emax, (int)(((unsigned long long)__double_as_longlong(__ldg(D + r + (int64_t)c * m)) >> 52) & 0x7FF));
+  }
+  return emax;
+}
+
+// Eight consecutive K entries of one row (column) into the seven slices, one
+// 16-byte store per slice at dst + p * stride.
+template <class Ld>
+__device__ __forceinline__ void slice_row8(unsigned char* dst, int stride, int emax, Ld ld) {
+  float sv[8][NS];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) slices7(ld(e), emax, sv[e]);
+#pragma unroll
+  for (int p = 0; p < NS; ++p) {
+    uint4 w;
+    w.x = pack_bf16(sv[0][p], sv[1][p]);
+    w.y = pack_bf16(sv[2][p], sv[3][p]);
+    w.z = pack_bf16(sv[4][p], sv[5][p]);
+    w.w = pack_bf16(sv[6][p], sv[7][p]);
+    *reinterpret_cast<uint4*>(dst + p * stride) = w;
+  }
+}
+
+// Once per plan: the slices of every non-root leaf's D and its row exponents.
+// Leaf region (at nd.fdx): quarter q, slice p at (q NS + p) AQ bytes, the
+// 128 row exponents (int) after the nq quarters.
+__global__ void __launch_bounds__(XT) dx_prep_kernel(const Task* __restrict__ leaves, unsigned char* __restrict__ base) {
+  __shared__ int s_emax[2][XM];
+  const Task tk = leaves[blockIdx.x];
+  const Node& nd = tk.nodes[tk.node];
+  if (nd.root || nd.fdx < 0) return;
+  const int m = nd.gm, n = nd.gn, tid = threadIdx.x;
+  const double* D = nd.D;
+  unsigned char* reg = base + nd.fdx;
+  const int nq = (n + XKQ - 1) / XKQ;
+  {
+    const int r = tid & (XM - 1), h = tid >> 7;
+    s_emax[h][r] = row_emax(D, m, n, r, h, 2);
+  }
+  __syncthreads();
+  const int r = tid & (XM - 1), kgh = tid >> 7;
+  const int emax = max(s_emax[0][r], s_emax[1][r]);
+  if (kgh == 0) reinterpret_cast<int*>(reg + (size_t)nq * NS * AQ)[r] = emax;
+  for (int q = 0; q < nq; ++q)
+    for (int kg = kgh; kg < XKQ / 8; kg += 2) {
+      const int off = (r >> 3) * 512 + kg * 128 + (r & 7) * 16;
+      slice_row8(reg + (size_t)q * NS * AQ + off, AQ, emax, [&](int e) {
+        const int c = XKQ * q + 8 * kg + e;
+        return (r < m && c < n) ? (unsigned long long)__double_as_longlong(__ldg(D + r + (int64_t)c * m)) : 0ull;
+      });
+    }
+}
+
+__global__ void __launch_bounds__(XT, 2) dx_tc_kernel(const Task* __restrict__ leaves, int nchunk,
                                                       const Slot* __restrict__ slots) {
   extern __shared__ __align__(1024) unsigned char xsm[];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bar;
-  __shared__ int s_emax[2][XM];   // per row of D: largest biased exponent, per half of the columns
-  __shared__ int s_gmax[XN];      // per column of X
+  __shared__ __align__(8) uint64_t s_bar[2];   // [0]: copies of D's slices, [1]: MMAs
+  __shared__ int s_gmax[XN];                   // per column of X
   __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5;
   const Task tk = leaves[blockIdx.x / nchunk];
@@ -128,12 +201,12 @@ __global__ void __launch_bounds__(XT, 1) dx_tc_kernel(const Task* __restrict__ l
   const Slot& sl = slots[tk.slot];
   const Node& nd = tk.nodes[tk.node];
   const int j0 = ch * XN;
-  if (nd.root || j0 >= sl.r) return;   // uniform over the block
-  const int m = nd.gm, n = nd.gn, nc = min(XN, sl.r - j0);
-  const double* D = nd.D;                                            // m x n, ld m
+  if (nd.root || nd.fdx < 0 || j0 >= sl.r) return;   // uniform over the block
+  const int m = nd.gm, n = nd.gn, nc = min(XN, sl.r - j0), nq = (n + XKQ - 1) / XKQ;
   const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;           // n x nc, ld ldb
-  unsigned char* Abuf = xsm;                                         // NS slices of A
-  unsigned char* Bbuf = xsm + NS * A_SLICE;                          // NS slices of B
+  const unsigned char* reg = sl.dxs + nd.fdx;                        // prepared slices of D
+  unsigned char* Abuf = xsm;                                         // NS slices of D, one quarter
+  unsigned char* Bbuf = xsm + NS * AQ;                               // NS slices of X, one quarter
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
@@ -141,22 +214,12 @@ __global__ void __launch_bounds__(XT, 1) dx_tc_kernel(const Task* __restrict__ l
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar[1])));
     asm volatile("fence.mbarrier_init.release.cluster;");
     s_fail = 0;
   }
-  // largest exponent of every row of D (thread: row r, every other column) ...
-  {
-    const int r = tid & (XM - 1), h = tid >> 7;
-    int emax = 0;
-    if (r < m)
-      for (int c = h; c < n; c += 2) {
-        const unsigned long long b = (unsigned long long)__double_as_longlong(__ldg(D + r + (int64_t)c * m));
-        emax = max(emax, (int)((b >> 52) & 0x7FF));
-      }
-    s_emax[h][r] = emax;
-  }
-  // ... and of every column of X (8 threads per column)
+  // largest exponent of every column of X (8 threads per column)
   {
     const int c = tid >> 3, t8 = tid & 7;
     int g = 0;
@@ -176,86 +239,62 @@ __global__ void __launch_bounds__(XT, 1) dx_tc_kernel(const Task* __restrict__ l
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = s_tmem;
 
-  const int nhalf = n > XKH ? 2 : 1;
   bool ok = true;
-  for (int h = 0; h < nhalf; ++h) {
-    // A slices: thread (row r, core-matrix column groups kg = cg, cg + 2, ...):
-    // eight consecutive columns per group, one 16-byte store per slice
-    {
-      const int r = tid & (XM - 1), cg = tid >> 7;
-      const int emax = max(s_emax[0][r], s_emax[1][r]);
-      for (int kg = cg; kg < XKH / 8; kg += 2) {
-        float sv[8][NS];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          const int c = XKH * h + 8 * kg + e;
-          unsigned long long b = 0ull;
-          if (r < m && c < n) b = (unsigned long long)__double_as_longlong(__ldg(D + r + (int64_t)c * m));
-          slices7(b, emax, sv[e]);
-        }
-        const int off = (r >> 3) * 1024 + kg * 128 + (r & 7) * 16;
-#pragma unroll
-        for (int p = 0; p < NS; ++p) {
-          uint4 w;
-          w.x = pack_bf16(sv[0][p], sv[1][p]);
-          w.y = pack_bf16(sv[2][p], sv[3][p]);
-          w.z = pack_bf16(sv[4][p], sv[5][p]);
-          w.w = pack_bf16(sv[6][p], sv[7][p]);
-          *reinterpret_cast<uint4*>(Abuf + p * A_SLICE + off) = w;
-        }
-      }
+  int qfail = 0;
+  for (int q = 0; q < nq; ++q) {
+    qfail = q;
+    // the quarter's slices of D: bulk copies, completion counted in bytes
+    if (tid == 0) {
+      const uint32_t bar = smem_u32(&s_bar[0]);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"((uint32_t)(NS * AQ)));
+      for (int p = 0; p < NS; ++p)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(Abuf + p * AQ)),
+                     "l"(reg + (size_t)(q * NS + p) * AQ), "r"((uint32_t)AQ), "r"(bar)
+                     : "memory");
     }
-    // B slices: thread (column c of X, core-matrix row group kg of K)
-    {
-      const int c = tid & (XN - 1), kg = tid >> 5;   // kg: 0..7
+    // the quarter's slices of X: thread (column c, core-matrix row group kg)
+    if (tid < XN * (XKQ / 8)) {
+      const int c = tid & (XN - 1), kg = tid >> 5;
       const int gmax = s_gmax[c];
-      float sv[8][NS];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int k = XKH * h + 8 * kg + e;
-        unsigned long long b = 0ull;
-        if (c < nc && k < n) b = (unsigned long long)__double_as_longlong(__ldg(X + k + (int64_t)c * sl.ldb));
-        slices7(b, gmax, sv[e]);
-      }
-      const int off = (c >> 3) * 1024 + kg * 128 + (c & 7) * 16;
-#pragma unroll
-      for (int p = 0; p < NS; ++p) {
-        uint4 w;
-        w.x = pack_bf16(sv[0][p], sv[1][p]);
-        w.y = pack_bf16(sv[2][p], sv[3][p]);
-        w.z = pack_bf16(sv[4][p], sv[5][p]);
-        w.w = pack_bf16(sv[6][p], sv[7][p]);
-        *reinterpret_cast<uint4*>(Bbuf + p * B_SLICE + off) = w;
-      }
+      slice_row8(Bbuf + (c >> 3) * 512 + kg * 128 + (c & 7) * 16, BQ, gmax, [&](int e) {
+        const int k = XKQ * q + 8 * kg + e;
+        return (c < nc && k < n) ? (unsigned long long)__double_as_longlong(__ldg(X + k + (int64_t)c * sl.ldb))
+                                 : 0ull;
+      });
     }
-    // the generic-proxy stores become visible to the tensor core
-    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("fence.proxy.async.shared::cta;");   // generic-proxy stores -> tensor core
     __syncthreads();
+    if (!mbar_wait(&s_bar[0], (uint32_t)(q & 1))) s_fail = 1;
+    __syncthreads();
+    if (s_fail) {
+      ok = false;
+      break;
+    }
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t a0 = smem_u32(Abuf), b0 = smem_u32(Bbuf);
       for (int d = 0; d < NS; ++d)
         for (int p = 0; p <= d; ++p) {
-          const int q = d - p;
+          const int qq = d - p;
 #pragma unroll
-          for (int kk = 0; kk < XKH / 16; ++kk) {
-            const uint64_t ad = sdesc(a0 + p * A_SLICE + kk * 256, 128, 1024);
-            const uint64_t bd = sdesc(b0 + q * B_SLICE + kk * 256, 128, 1024);
-            mma_bf16(tmem + (uint32_t)(XN * d), ad, bd, (h > 0 || p > 0 || kk > 0) ? 1u : 0u);
+          for (int kk = 0; kk < XKQ / 16; ++kk) {
+            const uint64_t ad = sdesc(a0 + p * AQ + kk * 256, 128, 512);
+            const uint64_t bd = sdesc(b0 + qq * BQ + kk * 256, 128, 512);
+            mma_bf16(tmem + (uint32_t)(XN * d), ad, bd, (q > 0 || p > 0 || kk > 0) ? 1u : 0u);
           }
         }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(&s_bar)));
+          smem_u32(&s_bar[1])));
     }
-    if (!mbar_wait(&s_bar, (uint32_t)h)) {
-      s_fail = 1;
-      ok = false;
-    }
+    if (!mbar_wait(&s_bar[1], (uint32_t)(q & 1))) s_fail = 1;
     asm volatile("tcgen05.fence::after_thread_sync;");
     __syncthreads();
-    if (s_fail) break;
+    if (s_fail) {
+      ok = false;
+      break;
+    }
   }
-  ok = ok && !s_fail;
 
   // read the accumulators back: warp w (< 4) has rows 32 w .. 32 w + 31
   if (ok && warp < 4) {
@@ -290,7 +329,7 @@ __global__ void __launch_bounds__(XT, 1) dx_tc_kernel(const Task* __restrict__ l
       }
     }
     if (r < m) {
-      const int er = max(s_emax[0][r], s_emax[1][r]);
+      const int er = reinterpret_cast<const int*>(reg + (size_t)nq * NS * AQ)[r];
       float2* T = (float2*)sl.tmp + nd.row0 + r + (int64_t)j0 * sl.ldt2;
 #pragma unroll
       for (int c = 0; c < XN; ++c) {
@@ -304,8 +343,9 @@ __global__ void __launch_bounds__(XT, 1) dx_tc_kernel(const Task* __restrict__ l
   }
   if (!ok && tid == 0) {
     if (sl.err) atomicCAS((int*)sl.err, DEV_OK, DEV_TIMEOUT);
-    // the tensor core may still be working on this block's operands
-    mbar_wait(&s_bar, (uint32_t)(nhalf - 1));
+    // a copy or the tensor core may still be working on this block's buffers
+    mbar_wait(&s_bar[0], (uint32_t)(qfail & 1));
+    mbar_wait(&s_bar[1], (uint32_t)(qfail & 1));
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -314,7 +354,17 @@ __global__ void __launch_bounds__(XT, 1) dx_tc_kernel(const Task* __restrict__ l
 
 }  // namespace
 
-bool dx_tc_fits(int mleaf, int nleaf) { return mleaf <= XM && nleaf <= 2 * XKH; }
+bool dx_tc_fits(int mleaf, int nleaf) { return mleaf <= XM && nleaf <= NQ * XKQ; }
+
+int64_t dx_leaf_bytes(int n) {
+  return (int64_t)((n + XKQ - 1) / XKQ) * NS * AQ + XM * (int64_t)sizeof(int);
+}
+
+cudaError_t launch_dx_prep(const Task* leaves, int64_t nleaves, unsigned char* base, cudaStream_t st) {
+  if (nleaves <= 0) return cudaSuccess;
+  dx_prep_kernel<<<(unsigned)nleaves, XT, 0, st>>>(leaves, base);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_dx_tc(const Task* leaves, int64_t nleaves, const Slot* slots, int rmax, cudaStream_t st) {
   if (nleaves <= 0 || rmax <= 0) return cudaSuccess;

@@ -41,6 +41,9 @@ struct Node {
   // column-major) of the QL (fTq, ceil(k/32) panels) and LQ (fTl, ceil(mk/32))
   // reflectors, and the inverses of L1's 32 x 32 diagonal blocks (fLi)
   int64_t fTq, fTl, fLi;
+  // tensor-core residual: byte offset of this leaf's prepared slices of D in
+  // the plan's slice buffer (-1: none)
+  int64_t fdx;
   // the children's ranks, leaf flags and product workspace offsets (left, right),
   // so that a product task reads one descriptor
   int32_t cku[2], ckv[2], cleaf[2];
@@ -91,6 +94,8 @@ struct Slot {
   // its per-node event counters (even between launches)
   const Node* nodes;
   int32_t* sync;
+  // tensor-core residual: the plan's prepared slices of the leaf blocks D
+  const unsigned char* dxs;
 };
 
 // Entry extraction (hss_getindex.cu): per node, the node's part of the sorted

@@ -64,6 +64,10 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
 // into the slot's pair buffer (sl.tmp), X = the slot's B; leaves up to 128 x 128.
 // A persistent pair product launched after it with dx_ready skips those products.
 bool dx_tc_fits(int mleaf, int nleaf);
+// Bytes of one leaf's prepared slices (n columns), and the once-per-plan
+// preparation over the plan's leaf tasks (regions at each leaf's fdx in base).
+int64_t dx_leaf_bytes(int n);
+cudaError_t launch_dx_prep(const Task* leaves, int64_t nleaves, unsigned char* base, cudaStream_t st);
 cudaError_t launch_dx_tc(const Task* leaves, int64_t nleaves, const Slot* slots, int rmax, cudaStream_t st);
 
 // Flat persistent product (hss_pmv.cu), FP64 with few right-hand sides: every

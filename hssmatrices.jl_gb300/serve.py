@@ -176,7 +176,9 @@ class HssServer:
         m = hss.size()[0]
         fac_elems = 2 * packed.size + 8 * m     # factor blocks, reflector copies, tau vectors
         item = 4 if precision == "fp32" else 8
-        extra = gen if precision == "fp32" else 0
+        # FP32 + refinement: the generators' pair copy, and the bf16 slices of the
+        # leaf blocks for the tensor-core residual (7 x 2 bytes per entry)
+        extra = 3 * gen if precision == "fp32" else 0
         return gen + extra + fac_elems * item + 64 * m * 8
 
     def _evict_for(self, need, keep):
