@@ -21,6 +21,7 @@ L2 is flushed (a 512 MB write) before every timed step.
 from __future__ import annotations
 
 import argparse
+import gc
 import ctypes
 import json
 import math
@@ -58,7 +59,7 @@ def parse():
     p.add_argument("--rate", type=float, default=1000.0)
     p.add_argument("--rates", default="1000,2000,4000,8000", help="offered loads of the serving sweep (requests/s)")
     p.add_argument("--pool", type=int, default=32)
-    p.add_argument("--budget-gb", type=float, default=150.0)
+    p.add_argument("--budget-gb", type=float, default=120.0)
     p.add_argument("--matrices", type=int, default=256)
     return p.parse_args()
 
@@ -178,11 +179,11 @@ class Clocks:
 # ---------------------------------------------------------------------------
 
 
-# DRAM bytes (read + write) of one leaf-level launch of ulv_factor_fast_kernel<float>
+# DRAM bytes (read + write) of one leaf-level launch of ulv_factor_blk_kernel<float, 128>
 # on the default workload (n = 65536, leafsize 128, k = 32), from one ncu capture
 # of that launch (dram__bytes_read.sum + dram__bytes_write.sum).  It belongs to
 # that kernel and size only; re-capture it when the kernel changes.
-FACTOR_LEAF_TRAFFIC = {(65536, 128, 32): 143171584}
+FACTOR_LEAF_TRAFFIC = {(65536, 128, 32): 143628288}
 # the same for one r = 1 launch of pmv_flat_kernel (FP64 product) on that tree
 MATVEC_R1_TRAFFIC = {(65536, 128, 32): 133241344}
 
@@ -346,6 +347,24 @@ def run_ours(args, rank, world, local_rank):
         td.all_reduce(t, op=td.ReduceOp.MAX)
         e2e_total = float(t.item())
     e2e_value = world * args.steps / e2e_total
+    # the HSS x dense product (FP64 hss_matmul, persistent kernel) on the same
+    # tree: r = 1 and r = rhs columns, L2 flushed before each call
+    matvec_us = {}
+    for rr in sorted({1, r}):
+        mB = torch.randn((rr, n), dtype=torch.float64, device="cuda")
+        mC = torch.empty_like(mB)
+        for _ in range(3):
+            dev.matmul_device(mB, n, rr, mC, n, stream=stream)
+        ev_m = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+        torch.cuda.synchronize()
+        for a, b in ev_m:
+            flush.zero_()
+            a.record(stream)
+            dev.matmul_device(mB, n, rr, mC, n, stream=stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        matvec_us[rr] = 1000.0 * statistics.median(a.elapsed_time(b) for a, b in ev_m)
+        del mB, mC
     if rank != 0:
         return 0
     # roofline of the dominant kernel (per launch)
@@ -388,6 +407,8 @@ def run_ours(args, rank, world, local_rank):
         "breakdown_ms_per_step": breakdown,
         "factor_bytes": {"fp32": F32.nbytes(), "fp64": F64.nbytes()},
     }
+    for rr, us in matvec_us.items():
+        line[f"matvec_r{rr}_us"] = us
     print(json.dumps(line), flush=True)
     return 0
 
@@ -441,8 +462,10 @@ def _serve_once(pkg, serve, args, rate, precision, overlap=True, check=True):
             del dv
         out["max_residual"] = worst
         out["residuals_checked"] = checked
+    out["resident_gb_at_end"] = srv.used / 1e9
     srv.resident.clear()
     del srv, done, reqs
+    gc.collect()
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     return out

@@ -1938,6 +1938,31 @@ int hss_factor_bytes(hss_factor f, int64_t* bytes) {
   return HSS_OK;
 }
 
+int hss_device_bytes(hss_handle h, hss_factor f, int64_t* bytes) {
+  if (!bytes || (!h && !f)) return fail(HSS_ERR_INVALID, "null handle and factor");
+  auto slots = [](const SlotTable& s) {
+    return (int64_t)(s.dev.cap * sizeof(Slot) + s.pstate.cap * 4 + s.pq.cap * 8 + s.ctb.cap * 8 + s.dcnt.cap * 4);
+  };
+  int64_t b = 0;
+  if (h) {
+    const int64_t nn = (int64_t)h->nodes.size();
+    b += h->gen_len * 8;
+    if (h->d_gen_df) b += h->gen_len * 8;
+    if (h->d_dx) b += h->dx_bytes;
+    // node descriptors, task lists, flat-product links, paths and counters
+    b += nn * (int64_t)(sizeof(Node) + 4 * sizeof(Task) + sizeof(FlatLink) + 4 * (h->flat_dep + 1));
+    b += (int64_t)(h->mv_ws.cap + h->hB.cap + h->hC.cap) * 8 + slots(h->mv_slots);
+  }
+  if (f) {
+    b += (int64_t)f->fac_bytes + (int64_t)f->sv_ws.cap + (int64_t)f->ws2.cap * 8 + slots(f->fac_slots);
+    const SolveBufs& q = f->bufs;
+    b += (int64_t)(q.R.cap + q.bn2.cap + q.rn2.cap + q.scale.cap + q.xs.cap + q.tmp.cap) * 8;
+    b += slots(q.sv0) + slots(q.sv1) + slots(q.mv) + (int64_t)(f->hB.cap + f->hX.cap) * 8;
+  }
+  *bytes = b;
+  return HSS_OK;
+}
+
 int hss_ulvsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double* dX, int64_t ldx,
                  double tol, int32_t maxit, hss_solve_stats* stats, void* stream) {
   if (!f) return fail(HSS_ERR_INVALID, "null factor");

@@ -181,6 +181,14 @@ class HssServer:
         extra = 3 * gen if precision == "fp32" else 0
         return gen + extra + fac_elems * item + 64 * m * 8
 
+    def _account(self, res):
+        """Replaces a resident matrix's share of the budget by the device memory its
+        handle and factorization hold now (lock held)."""
+        b = C.c_int64()
+        check(res.dev.lib.hss_device_bytes(res.dev.handle, res.factor.handle, C.byref(b)))
+        self.used += b.value - res.nbytes
+        res.nbytes = b.value
+
     def _evict_for(self, need, keep):
         while self.used + need > self.budget:
             victim = None
@@ -247,7 +255,9 @@ class HssServer:
         ev.record(self.fstream)
         with self.cv:
             for r, d, f in zip(admitted, devs, factors):
-                self.resident[r.matrix] = Resident(d, f, r.nbytes, d.n, self.now_fn(), ev)
+                res = Resident(d, f, r.nbytes, d.n, self.now_fn(), ev)
+                self._account(res)
+                self.resident[r.matrix] = res
                 self.resident.move_to_end(r.matrix)
             self.inflight.append((ev, admitted))
             self.factor_batches += 1
@@ -315,6 +325,8 @@ class HssServer:
         with self.cv:
             self.solve_batches += 1
             self.batches += 1
+            for _mid, res, _reqs in batch:
+                self._account(res)          # workspaces grown by the solve
             for (_mid, _res, reqs), X in zip(batch, dXs):
                 c0 = 0
                 for q in reqs:

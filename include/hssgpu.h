@@ -181,6 +181,10 @@ int hss_batcher_solve(hss_batcher b, int32_t count, const hss_factor* fs, const 
 
 /* Device memory held by a factorization (bytes). */
 int hss_factor_bytes(hss_factor f, int64_t* bytes);
+/* Device memory held now by a handle and / or a factorization (either may be
+ * null): generators and their derived copies, node and task tables, factor
+ * storage and the workspaces grown by earlier calls (bytes). */
+int hss_device_bytes(hss_handle h, hss_factor f, int64_t* bytes);
 
 /* Autotuner (new; the reference has no GPU kernels to choose between).  Times,
  * on scratch right-hand sides with r columns, the two solve kernels of every

@@ -1038,6 +1038,226 @@ def _randcompress(h, A, Scol, Srow, Ocol, Orow, ro, co, atol, rtol, rootnode=Fal
 # ---------------------------------------------------------------------------
 # fixtures: kernel matrices and synthetic generator trees
 # ---------------------------------------------------------------------------
+# HSS-valued division (src/ulvdivide.jl), HSS sums (src/hssmatrix.jl:218-231),
+# prune_leaves! and _hssleaf (src/hssmatrix.jl:325-348)
+# ---------------------------------------------------------------------------
+
+
+def _leaf_raw(D, U, V, rootnode):
+    """``HssMatrix(D, U, V, rootnode)``: a leaf keeping U and V even at the root."""
+    h = HssMatrix()
+    h.leafnode, h.rootnode = True, bool(rootnode)
+    h.D, h.U, h.V = np.asarray(D, float), np.asarray(U, float), np.asarray(V, float)
+    return h
+
+
+def _branch_raw(A11, A22, B12, B21, R1, W1, R2, W2, rootnode):
+    """``HssMatrix(A11, A22, B12, B21, R1, W1, R2, W2, rootnode)``."""
+    return HssMatrix.branch(A11, A22, B12, B21, R1, W1, R2, W2, rootnode=bool(rootnode))
+
+
+def hssleaf(h: HssMatrix):
+    """``_hssleaf`` (src/hssmatrix.jl:339-348): D, U, V of the whole subtree."""
+    if h.leafnode:
+        return h.D, h.U, h.V
+    D1, U1, V1 = hssleaf(h.A11)
+    D2, U2, V2 = hssleaf(h.A22)
+    D = np.block([[D1, U1 @ h.B12 @ V2.T], [U2 @ h.B21 @ V1.T, D2]])
+    return D, np.vstack([U1 @ h.R1, U2 @ h.R2]), np.vstack([V1 @ h.W1, V2 @ h.W2])
+
+
+def prune_leaves(h: HssMatrix):
+    """``prune_leaves!`` (src/hssmatrix.jl:325-336): every branch whose children
+    are both leaves becomes one leaf."""
+    if h.leafnode:
+        return h
+    if h.A11.leafnode and h.A22.leafnode:
+        return _leaf_raw(*hssleaf(h), h.rootnode)
+    h.A11 = prune_leaves(h.A11)
+    h.A22 = prune_leaves(h.A22)
+    h.sz1, h.sz2 = h.A11.size(), h.A22.size()
+    return h
+
+
+def hss_add(A: HssMatrix, B: HssMatrix, sign=1.0):
+    """``+`` / ``-`` of two HSS matrices (src/hssmatrix.jl:218-231): leaves add
+    (U, V side by side), branches stack the generators block-diagonally."""
+    if tuple(A.size()) != tuple(B.size()):
+        raise ValueError(f"A has dimensions {A.size()} but B has dimensions {B.size()}")
+    root = A.rootnode and B.rootnode
+    if A.leafnode and B.leafnode:
+        return _leaf_raw(A.D + sign * B.D, np.hstack([A.U, B.U]), np.hstack([A.V, B.V]), root)
+    if A.leafnode or B.leafnode:
+        raise ValueError("Cannot add leaves and branches.")
+    return _branch_raw(hss_add(A.A11, B.A11, sign), hss_add(A.A22, B.A22, sign), _blkdiag(A.B12, sign * B.B12),
+                       _blkdiag(A.B21, sign * B.B21), _blkdiag(A.R1, B.R1), _blkdiag(A.W1, B.W1),
+                       _blkdiag(A.R2, B.R2), _blkdiag(A.W2, B.W2), root)
+
+
+class _BN:
+    """``BinaryNode`` (src/binarytree.jl) holding per-node data of the division."""
+    __slots__ = ("data", "left", "right")
+
+    def __init__(self, data=None, left=None, right=None):
+        self.data, self.left, self.right = data, left, right
+
+
+def _ulvreduce_div(D, U, V):
+    """``_ulvreduce!(D, U, V)`` (src/ulvdivide.jl:58-85): the leaf reduction without
+    a right-hand side; returns L2 (k x n), tril U, Q V, L1, the QL and LQ
+    factorizations, m - k, nk and k.  k > m (more generator columns than rows) is
+    outside what the reference handles; it is treated like k = m here."""
+    m, n = D.shape
+    k = min(U.shape[1], m)
+    nk = max(0, min(m - k, n))
+    if k >= m:
+        return D, U, V, np.zeros((0, 0)), None, None, 0, 0, k
+    qlf = QLFact(U)
+    Ur = np.tril(qlf.L())
+    D = qlf.apply_qt(D)
+    lqf = LQFact(D[:m - k, :])
+    L1 = lqf.L()[:, :nk]
+    L2 = lqf.apply_right_qt(D[m - k:, :])
+    V = lqf.apply_left_q(V)
+    return L2, Ur, V, L1, qlf, lqf, m - k, nk, k
+
+
+def _ulvfactor_leaves(h: HssMatrix):
+    """``_ulvfactor_leaves!`` (src/ulvdivide.jl:88-112): reduces every leaf; returns
+    the reduced matrix and the trees of QL factorizations, L1 blocks, LQ
+    factorizations, nk and k."""
+    if h.leafnode:
+        D, U, V, L1, qlf, lqf, _mk, nk, k = _ulvreduce_div(h.D, h.U, h.V)
+        return _leaf_raw(D, U, V, h.rootnode), _BN(qlf), _BN(L1), _BN(lqf), _BN(nk), _BN(k)
+    A11, qu1, ql1, qv1, nk1, k1 = _ulvfactor_leaves(h.A11)
+    A22, qu2, ql2, qv2, nk2, k2 = _ulvfactor_leaves(h.A22)
+    out = _branch_raw(A11, A22, h.B12, h.B21, h.R1, h.W1, h.R2, h.W2, h.rootnode)
+    return (out, _BN(None, qu1, qu2), _BN(None, ql1, ql2), _BN(None, qv1, qv2), _BN(None, nk1, nk2),
+            _BN(None, k1, k2))
+
+
+def _map_leaves(h: HssMatrix, t: _BN, f):
+    """Applies f(leaf, node of t) at every leaf (the generated branch functions of
+    src/ulvdivide.jl:145-158 and :167-179); branches keep their generators."""
+    if h.leafnode:
+        return f(h, t)
+    return _branch_raw(_map_leaves(h.A11, t.left, f), _map_leaves(h.A22, t.right, f), h.B12, h.B21, h.R1, h.W1,
+                       h.R2, h.W2, h.rootnode)
+
+
+def _utransform_leaf(h, t):
+    """``_utransforms_kernel!`` (src/ulvdivide.jl:115-121): D, U <- Q^T D, Q^T U."""
+    if t.data is None:
+        return _leaf_raw(h.D.copy(), h.U.copy(), h.V, h.rootnode)
+    return _leaf_raw(t.data.apply_qt(h.D), t.data.apply_qt(h.U), h.V, h.rootnode)
+
+
+def _ltransform_leaf(h, t):
+    """``_ltransforms_kernel!`` (src/ulvdivide.jl:122-129): the first nk rows of D and
+    U solved with L1, the other rows zeroed."""
+    L1 = t.data
+    nk = L1.shape[0]
+    D = np.zeros_like(h.D)
+    U = np.zeros_like(h.U)
+    if nk:
+        D[:nk] = sla.solve_triangular(L1, h.D[:nk], lower=True)
+        U[:nk] = sla.solve_triangular(L1, h.U[:nk], lower=True)
+    return _leaf_raw(D, U, h.V, h.rootnode)
+
+
+def _vtransform_leaf(h, t):
+    """``_vtransforms_kernel!`` (src/ulvdivide.jl:130-136): D, U <- Q^T D, Q^T U with
+    the LQ factor's Q."""
+    if t.data is None:
+        return h
+    return _leaf_raw(t.data.apply_left_qt(h.D), t.data.apply_left_qt(h.U), h.V, h.rootnode)
+
+
+def _unpackadd_rows(A: HssMatrix, B: HssMatrix, kt: _BN):
+    """``_unpackadd_rows!`` (src/ulvdivide.jl:182-234): adds the solution B of the
+    reduced problem (one level shallower) into the bottom rows of A's leaves."""
+    if not A.leafnode:
+        if not B.leafnode:
+            A11 = _unpackadd_rows(A.A11, B.A11, kt.left)
+            A22 = _unpackadd_rows(A.A22, B.A22, kt.right)
+            return _branch_raw(A11, A22, _blkdiag(A.B12, B.B12), _blkdiag(A.B21, B.B21), _blkdiag(A.R1, B.R1),
+                               _blkdiag(A.W1, B.W1), _blkdiag(A.R2, B.R2), _blkdiag(A.W2, B.W2), A.rootnode)
+        k1, k2 = kt.left.data, kt.right.data
+        if k1 + k2 != B.D.shape[0]:
+            raise ValueError("first dimension of D does not match the expected k1+k2 rows")
+        n1 = A.sz1[1]
+        r, w = gensize(B)
+        eye = lambda q: np.eye(q)
+        B12 = _blkdiag(_blkdiag(A.B12, np.zeros((r, w))), eye(k1))
+        B21 = _blkdiag(_blkdiag(A.B21, np.zeros((r, w))), eye(k2))
+        R1 = np.vstack([_blkdiag(A.R1, eye(r)), np.zeros((k1, A.R1.shape[1] + r))])
+        W1 = np.vstack([_blkdiag(A.W1, eye(w)), np.zeros((k2, A.W1.shape[1] + w))])
+        R2 = np.vstack([_blkdiag(A.R2, eye(r)), np.zeros((k2, A.R2.shape[1] + r))])
+        W2 = np.vstack([_blkdiag(A.W2, eye(w)), np.zeros((k1, A.W2.shape[1] + w))])
+        A11 = _unpackadd_leaf(A.A11, B.D[:k1, :n1], B.U[:k1], B.V[:n1], B.D[k1:, :n1])
+        A22 = _unpackadd_leaf(A.A22, B.D[k1:, n1:], B.U[k1:], B.V[n1:], B.D[:k1, n1:])
+        return _branch_raw(A11, A22, B12, B21, R1, W1, R2, W2, A.rootnode)
+    if not B.leafnode:
+        raise ValueError("Something went wrong. Expected hssB to also be a leaf node")
+    k, rk = B.U.shape
+    m = A.D.shape[0]
+    if k > m:
+        raise ValueError("expected hssB to have less rows than hssA.")
+    U = np.hstack([A.U, np.zeros((m, rk))])
+    U[m - k:, U.shape[1] - rk:] = B.U
+    D = A.D.copy()
+    D[m - k:] += B.D
+    return _leaf_raw(D, U, np.hstack([A.V, B.V]), A.rootnode)
+
+
+def _unpackadd_leaf(A: HssMatrix, D, U, V, Brow):
+    """``_unpackadd_rows!(hssA, D, U, V, Brow)`` (src/ulvdivide.jl:236-252)."""
+    if not A.leafnode:
+        raise ValueError("Expected hssA to be a leaf node")
+    k = D.shape[0]
+    m = A.D.shape[0]
+    DA = A.D.copy()
+    DA[m - k:] += D
+    q = U.shape[1] + k
+    UA = np.hstack([A.U, np.zeros((m, q))])
+    UA[m - k:, UA.shape[1] - q:] = np.hstack([U, np.eye(k)])
+    return _leaf_raw(DA, UA, np.hstack([A.V, V, Brow.T]), A.rootnode)
+
+
+def ldiv_hss(A: HssMatrix, B: HssMatrix, atol=1e-9, rtol=1e-9):
+    """``hssA \\ hssB`` = ``_ldiv!(copy(hssA), copy(hssB))`` (src/hssmatrix.jl:235,
+    src/ulvdivide.jl:13, :22-54): the leaves of A reduced (QL of U, LQ of the
+    top rows of D), the same transforms applied to B's leaf rows, the reduced
+    part solved and the rest (B's remainder minus the coupling, recompressed
+    and pruned) solved recursively on the pruned reduced matrix, then unpacked
+    back into the leaves and recompressed."""
+    if A.leafnode:
+        D, U, V = hssleaf(B)
+        return _leaf_raw(np.linalg.solve(full(A), D), U, V, B.rootnode)
+    L, QU, QL, QV, nkt, kt = _ulvfactor_leaves(A)
+    B = _map_leaves(B, QU, _utransform_leaf)
+    QB = _map_leaves(B, nkt, lambda h, t: _leaf_raw(h.D[t.data:], h.U[t.data:], h.V, h.rootnode))
+    Y0 = _map_leaves(B, QL, _ltransform_leaf)
+    if QB.size()[0] == 0:
+        return _map_leaves(Y0, QV, _vtransform_leaf)
+    QB = hss_add(QB, hssmul(L, Y0), -1.0)
+    QB = recompress(QB, atol, rtol)
+    QB = prune_leaves(QB)
+    L = _map_leaves(L, nkt, lambda h, t: _leaf_raw(h.D[:, t.data:], h.U, h.V[t.data:], h.rootnode))
+    L = prune_leaves(L)
+    Y1 = ldiv_hss(L, QB, atol, rtol)
+    X = _unpackadd_rows(Y0, Y1, kt)
+    X = _map_leaves(X, QV, _vtransform_leaf)
+    return recompress(X, atol, rtol)
+
+
+def rdiv_hss(B: HssMatrix, A: HssMatrix, atol=1e-9, rtol=1e-9):
+    """``hssB / hssA`` = ``adjoint(_ldiv!(adjoint(hssA), adjoint(hssB)))``
+    (src/hssmatrix.jl:237, src/ulvdivide.jl:15-17)."""
+    return adjoint(ldiv_hss(adjoint(A), adjoint(B), atol, rtol))
+
+
+# ---------------------------------------------------------------------------
 
 
 def cauchy_matrix(n=2001, lo=-1.0, hi=1.0):

@@ -39,6 +39,46 @@ def test_runtests_compression_and_arithmetic(orc, leafsize):
     assert _ok(np.linalg.norm(x0 - xs) / np.linalg.norm(x0), np.linalg.norm(x0 - xs))
 
 
+@pytest.mark.parametrize("leafsize", [50, 64])
+def test_runtests_hss_division(orc, leafsize):
+    """test/runtests.jl:68-77 for T = Float64: hssA \\ hssI and hssI / hssA against
+    inv(A), then the same with A11 of both pruned (an unbalanced tree), through
+    the restatement of src/ulvdivide.jl."""
+    A = orc.runtests_matrix(2001)
+    ccl = orc.bisection_cluster(2001, leafsize)
+    h = orc.compress(A, ccl, ccl, TOL, TOL)
+    hI = orc.hss_blkdiag(np.eye(2001), ccl, ccl)
+    Ainv = np.linalg.inv(A)
+
+    def check(X):
+        E = Ainv - orc.full(X)
+        assert _ok(np.linalg.norm(E) / np.linalg.norm(Ainv), np.linalg.norm(E))
+
+    check(orc.ldiv_hss(h, hI, TOL, TOL))
+    check(orc.rdiv_hss(hI, h, TOL, TOL))
+    h.A11 = orc.prune_leaves(h.A11)
+    h.sz1 = h.A11.size()
+    hI.A11 = orc.prune_leaves(hI.A11)
+    hI.sz1 = hI.A11.size()
+    check(orc.ldiv_hss(h, hI, TOL, TOL))
+    check(orc.rdiv_hss(hI, h, TOL, TOL))
+
+
+def test_hss_division_is_exact_division(orc):
+    """At a tight tolerance the division equals full(hssA)^-1 full(hssB) to rounding
+    (a general B of rank 8 on the same tree)."""
+    rng = np.random.default_rng(4)
+    hA = orc.synthetic_hss(1000, 64, 10, rng)
+    hB = orc.synthetic_hss(1000, 64, 8, rng)
+    FA, FB = orc.full(hA), orc.full(hB)
+    X = orc.ldiv_hss(hA, hB, 1e-13, 1e-13)
+    ref = np.linalg.solve(FA, FB)
+    assert np.linalg.norm(ref - orc.full(X)) / np.linalg.norm(ref) < 1e-12
+    Y = orc.rdiv_hss(hB, hA, 1e-13, 1e-13)
+    ref = FB @ np.linalg.inv(FA)
+    assert np.linalg.norm(ref - orc.full(Y)) / np.linalg.norm(ref) < 1e-12
+
+
 def test_config1_cauchy(orc):
     """Cauchy-type kernel on -1:0.001:1 with leafsize 64 and compress at 1e-6."""
     A = orc.cauchy_matrix(2001)
