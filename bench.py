@@ -889,9 +889,9 @@ def run_matvec_workload(args):
                           "note": "host call to result handle (includes plan creation and the final synchronise)"},
         "recompress_product_n65536": {"ms": recompress_ms, "rank_in": 2 * args.rank, "rank_out_node1": rec_rank,
                                       "tol": 1e-9},
-        "hss_ldiv_n16384": {"ms": 1000.0 * td[-1], "rank_out": ldiv_rank, "rounds": st.get("rounds"),
-                            "tol": 1e-9, "note": "host call to result tree (expansion, chunked FP64 solve, "
-                                                 "adaptive recompression, copy to host)"},
+        "hss_ldiv_n16384": {"ms": 1000.0 * td[-1], "rank_out": ldiv_rank, "tol": 1e-9,
+                            "note": "host call to result tree (FP64 ULV factor of A, the level-by-level "
+                                    "recursion on the generators with recompression, copy to host)"},
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -19,7 +19,8 @@ LIB_PATH = os.path.join(LIB_DIR, "libhssgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["hss_kernels.cu", "hss_factor_blk.cu", "hss_solve.cu", "hss_matvec_df.cu", "hss_pmv.cu", "hss_bsolve.cu", "hss_getindex.cu", "hss_hssmul.cu", "hss_recompress.cu", "hss_noalloc.cu", "hss_dx_tc.cu",
-           "hss_sample.cu", "hss_capi.cpp", "hss_arith.cpp", "hss_compress.cpp"]
+           "hss_sample.cu", "hss_divide.cu", "hss_capi.cpp", "hss_arith.cpp", "hss_compress.cpp",
+           "hss_divide.cpp"]
 
 
 def _nvcc():

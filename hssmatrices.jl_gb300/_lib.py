@@ -54,7 +54,7 @@ EXPORTS = [
     "hss_batcher_create", "hss_batcher_destroy", "hss_batcher_factor", "hss_batcher_solve",
     "hss_sample", "hss_sumsq", "hss_rc_create", "hss_rc_destroy", "hss_rc_size", "hss_rc_compress",
     "hss_rc_ranks", "hss_rc_sample", "hss_export_size", "hss_export", "hss_getindex", "hss_full", "hss_hssmul", "hss_recompress", "hss_orthonormalize",
-    "hss_device_bytes",
+    "hss_device_bytes", "hss_transpose", "hss_matmul_t", "hss_ldiv", "hss_rdiv",
 ]
 
 
@@ -111,6 +111,10 @@ def _declare(lib):
         "hss_ulvfactsolve_host": (C.c_int, [P, I32, PD, I64, I64, PD, I64, D, I32, C.POINTER(SolveStats)]),
         "hss_factor_bytes": (C.c_int, [P, PI64]),
         "hss_device_bytes": (C.c_int, [P, P, PI64]),
+        "hss_transpose": (C.c_int, [P, C.POINTER(P), P]),
+        "hss_matmul_t": (C.c_int, [P, P, I64, I64, P, I64, D, D, P]),
+        "hss_ldiv": (C.c_int, [P, P, D, D, C.POINTER(P), P]),
+        "hss_rdiv": (C.c_int, [P, P, D, D, C.POINTER(P), P]),
         "hss_autotune": (C.c_int, [P, I64, P]),
         "hss_autotune_info": (C.c_int, [P, C.POINTER(C.c_int32), C.c_char_p, C.POINTER(C.c_int32), C.c_char_p,
                                         C.POINTER(C.c_int32)]),

@@ -18,6 +18,7 @@
 #include "hss_host.h"
 #include "hss_internal.h"
 #include "hss_launch.h"
+#include "hss_stages.h"
 
 using namespace hss;
 
@@ -424,130 +425,13 @@ int hss_hssmul(hss_handle hA, hss_handle hB, hss_handle* out, void* stream) {
 // ---- orthonormalize_generators! / recompress! (src/generators.jl:64-114,
 // src/compression.jl:148-260) ----------------------------------------------------
 
-namespace {
+}  // extern "C"
 
-// A column-major block on the device: data, leading dimension, shape.
-struct Blk {
-  double* p = nullptr;
-  int64_t ld = 1, rows = 0, cols = 0;
-  double* at(int64_t i, int64_t j) const { return p + i + j * ld; }
-};
-
-// Device memory for the intermediate blocks: chunks of at least 64 MB, freed together.
-struct Arena {
-  std::vector<void*> chunks;
-  char* cur = nullptr;
-  size_t left = 0;
-  cudaError_t err = cudaSuccess;
-  void* raw(size_t bytes) {
-    bytes = (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
-    if (bytes > left) {
-      const size_t sz = std::max<size_t>(bytes, size_t(64) << 20);
-      void* q = nullptr;
-      const cudaError_t e = dev_alloc(&q, sz);
-      if (e != cudaSuccess) { err = e; return nullptr; }
-      chunks.push_back(q);
-      cur = (char*)q;
-      left = sz;
-    }
-    void* r = cur;
-    cur += bytes;
-    left -= bytes;
-    return r;
-  }
-  Blk blk(int64_t rows, int64_t cols) {
-    Blk b;
-    b.rows = rows;
-    b.cols = cols;
-    b.ld = std::max<int64_t>(rows, 1);
-    b.p = (double*)raw((size_t)b.ld * std::max<int64_t>(cols, 1) * sizeof(double));
-    return b;
-  }
-  ~Arena() {
-    for (void* q : chunks) cudaFree(q);
-  }
-};
-
-// Task lists run stage by stage on one stream.
-struct Stages {
-  cudaStream_t st;
-  Arena& ar;
-  std::vector<MmTask> mm;
-  std::vector<PqrTask> qr;
-  int qmax = 1, kmax = 1;
-  // C = A1 op B1 (+ A2 op B2): shapes from the blocks, ta / tb transpose
-  void gemm(const Blk& C, const Blk& A1, int ta1, const Blk& B1, int tb1, const Blk* A2 = nullptr, int ta2 = 0,
-            const Blk* B2 = nullptr, int tb2 = 0) {
-    if (C.rows * C.cols == 0) return;
-    MmTask t{};
-    const int64_t k1 = ta1 ? A1.rows : A1.cols;
-    t.A1 = k1 > 0 ? A1.p : nullptr; t.B1 = B1.p; t.lda1 = (int32_t)A1.ld; t.ldb1 = (int32_t)B1.ld;
-    t.ta1 = ta1; t.tb1 = tb1; t.k1 = (int32_t)k1; t.a1 = 1.0;
-    if (A2) {
-      const int64_t k2 = ta2 ? A2->rows : A2->cols;
-      t.A2 = k2 > 0 ? A2->p : nullptr; t.B2 = B2->p; t.lda2 = (int32_t)A2->ld; t.ldb2 = (int32_t)B2->ld;
-      t.ta2 = ta2; t.tb2 = tb2; t.k2 = (int32_t)k2; t.a2 = 1.0;
-    } else {
-      t.lda2 = t.ldb2 = 1;
-    }
-    t.C = C.p; t.ldc = (int32_t)C.ld; t.m = (int32_t)C.rows; t.n = (int32_t)C.cols;
-    mm.push_back(t);
-  }
-  // C = A (or A^T)
-  void copy(const Blk& C, const Blk& A, int ta = 0) {
-    if (C.rows * C.cols == 0) return;
-    MmTask t{};
-    t.A1 = A.p; t.lda1 = (int32_t)A.ld; t.ta1 = ta; t.k1 = -1; t.ldb1 = t.lda2 = t.ldb2 = 1;
-    t.C = C.p; t.ldc = (int32_t)C.ld; t.m = (int32_t)C.rows; t.n = (int32_t)C.cols;
-    mm.push_back(t);
-  }
-  cudaError_t run_mm() {
-    if (mm.empty()) return cudaSuccess;
-    auto* d = (MmTask*)ar.raw(mm.size() * sizeof(MmTask));
-    if (!d) return ar.err;
-    cudaError_t e = cudaMemcpyAsync(d, mm.data(), mm.size() * sizeof(MmTask), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) launch_mm_list(d, (int64_t)mm.size(), st);
-    count_launches(1);
-    mm.clear();
-    return e == cudaSuccess ? cudaGetLastError() : e;
-  }
-  // pivoted QRs of the listed blocks (factored in place); returns their ranks
-  cudaError_t run_qr(std::vector<int32_t>& ranks) {
-    ranks.assign(qr.size(), 0);
-    if (qr.empty()) return cudaSuccess;
-    auto* dr = (int32_t*)ar.raw(qr.size() * sizeof(int32_t));
-    auto* d = (PqrTask*)ar.raw(qr.size() * sizeof(PqrTask));
-    if (!d || !dr) return ar.err;
-    for (size_t i = 0; i < qr.size(); ++i) qr[i].rank = dr + i;
-    cudaError_t e = cudaMemcpyAsync(d, qr.data(), qr.size() * sizeof(PqrTask), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) launch_pqr(d, (int64_t)qr.size(), qmax, kmax, st);
-    count_launches(1);
-    if (e == cudaSuccess) e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ranks.data(), dr, qr.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    qr.clear();
-    qmax = kmax = 1;
-    return e;
-  }
-  // queue the QR of a copy of G: returns (Q, R) blocks sized for the full rank
-  std::pair<Blk, Blk> pqr(const Blk& G, double atol, double rtol) {
-    const int64_t km = std::min(G.rows, G.cols);
-    Blk Q = ar.blk(G.rows, km), R = ar.blk(km, G.cols);
-    PqrTask t{};
-    t.G = G.p; t.ldg = G.ld; t.p = (int32_t)G.rows; t.q = (int32_t)G.cols;
-    t.Q = Q.p; t.ldq = Q.ld; t.R = R.p; t.ldr = R.ld; t.atol = atol; t.rtol = rtol;
-    if (G.rows * G.cols > 0) {
-      qr.push_back(t);
-      qmax = std::max<int>(qmax, (int)G.cols);
-      kmax = std::max<int>(kmax, (int)km);
-    }
-    return {Q, R};
-  }
-};
+namespace hss {
 
 // orthonormalize_generators! and, unless ortho_only, the truncation of
 // recompress!; the result is a new single-tree handle.
-int recompress_impl(hss_handle h, double atol, double rtol, bool ortho_only, hss_handle* out, cudaStream_t st) {
+int recompress_impl(hss_plan_s* h, double atol, double rtol, bool ortho_only, hss_plan_s** out, cudaStream_t st) {
   const std::vector<Node>& N = plan_nodes(h);
   const int64_t nn = (int64_t)N.size();
   Arena ar;
@@ -859,7 +743,9 @@ int recompress_impl(hss_handle h, double atol, double rtol, bool ortho_only, hss
   return HSS_OK;
 }
 
-}  // namespace
+}  // namespace hss
+
+extern "C" {
 
 int hss_recompress(hss_handle h, double atol, double rtol, hss_handle* out, void* stream) {
   if (!h || !out) return set_error(HSS_ERR_INVALID, "null handle");

@@ -208,6 +208,8 @@ struct hss_plan_s {
   std::vector<Task> h_tasks;            // host copy of the task lists (merged batches)
   std::vector<int64_t> h_table;         // node table of a single-tree plan (hss_export)
   int64_t h_npacked = 0;                // its packed generator length
+  hss_plan_s* tplan = nullptr;          // the adjoint's plan (hss_matmul_t), made on first use
+  std::string ulv_why;                  // why the ULV reduction cannot factor this plan (empty: it can)
   ~hss_plan_s();
 };
 
@@ -240,6 +242,7 @@ struct hss_factor_s {
 };
 
 hss_plan_s::~hss_plan_s() {
+  delete tplan;
   delete fused[0];
   delete fused[1];
   if (d_gen_df) cudaFree(d_gen_df);
@@ -404,16 +407,18 @@ int layout_plan(hss_plan_s* P, const std::vector<TreeIn>& trees, std::vector<Gen
         x.n = c1.nr + c2.nr;
       }
       max_h = std::max(max_h, x.height);
+      // a plan that the ULV reduction cannot factor (rectangular, or a block
+      // with m - k > n) is still a valid operand of the products; its
+      // factorization is refused when asked for
       if (root) {
-        if (x.m != x.n)
-          return fail(HSS_ERR_BAD_DIMS, "root block of the ULV reduction is not square");
+        if (x.m != x.n && P->ulv_why.empty()) P->ulv_why = "root block of the ULV reduction is not square";
         x.k = x.m; x.mk = 0; x.nk = 0; x.mr = x.m; x.nr = x.n; x.lower_u = 0;
       } else {
         x.k = std::min(x.ku, x.m);               // src/ulvfactor.jl:27
         x.mk = x.m - x.k;
         x.nk = std::min(x.mk, x.n);              // :28
-        if (x.mk > x.n)
-          return fail(HSS_ERR_BAD_DIMS, "m - k > n in the ULV reduction (trsm needs a square L1)");
+        if (x.mk > x.n && P->ulv_why.empty())
+          P->ulv_why = "m - k > n in the ULV reduction (trsm needs a square L1)";
         x.mr = x.m - x.mk;
         x.nr = x.n - x.nk;
         x.lower_u = x.mk > 0;
@@ -1614,6 +1619,12 @@ int plan_device(const hss_plan_s* p) { return p->device; }
 int32_t plan_ntrees(const hss_plan_s* p) { return p->ntrees; }
 int64_t plan_rows(const hss_plan_s* p) { return p->tree_m[0]; }
 int64_t plan_cols(const hss_plan_s* p) { return p->tree_n[0]; }
+const void* factor_storage(const hss_factor_s* f) { return f->d_fac; }
+size_t factor_storage_bytes(const hss_factor_s* f) { return f->fac_bytes; }
+const double* plan_gen(const hss_plan_s* p, int64_t* len) {
+  *len = p->gen_len;
+  return p->d_gen;
+}
 
 }  // namespace hss
 
@@ -1746,6 +1757,18 @@ int hss_matmul(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* d
   return matmul_impl(h, io, alpha, beta, (cudaStream_t)stream, nullptr, nullptr, nullptr, h->mv_slots);
 }
 
+int hss_matmul_t(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC, int64_t ldc, double alpha,
+                 double beta, void* stream) {
+  if (!h) return fail(HSS_ERR_INVALID, "null handle");
+  if (h->ntrees != 1) return fail(HSS_ERR_INVALID, "the product with the adjoint takes a single matrix");
+  if (!h->tplan) {
+    CUDA_TRY(cudaSetDevice(h->device));
+    int rc = plan_transpose(h, &h->tplan, (cudaStream_t)stream);
+    if (rc) return rc;
+  }
+  return hss_matmul(h->tplan, dB, ldb, r, dC, ldc, alpha, beta, stream);
+}
+
 int hss_matmul_noalloc(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC, int64_t ldc,
                        double alpha, double beta, void* stream) {
   if (!h) return fail(HSS_ERR_INVALID, "null handle");
@@ -1818,6 +1841,7 @@ int hss_ulvfactor(hss_handle h, int32_t precision, hss_factor* out, void* stream
   if (precision != HSS_PREC_FP64 && precision != HSS_PREC_FP32)
     return fail(HSS_ERR_INVALID, "precision must be HSS_PREC_FP64 or HSS_PREC_FP32");
   *out = nullptr;
+  if (!h->ulv_why.empty()) return fail(HSS_ERR_BAD_DIMS, h->ulv_why);
   auto* f = new hss_factor_s();
   f->plan = h;
   f->prec = precision;
@@ -2037,6 +2061,7 @@ int hss_batcher_factor(hss_batcher b, int32_t count, const hss_handle* hs, int32
   for (int32_t i = 0; i < count; ++i) {
     out[i] = nullptr;
     if (!hs[i] || hs[i]->ntrees != 1) return fail(HSS_ERR_INVALID, "batched factorization takes single-tree plans");
+    if (!hs[i]->ulv_why.empty()) return fail(HSS_ERR_BAD_DIMS, hs[i]->ulv_why);
     plans[i] = hs[i];
   }
   int rc = HSS_OK;

@@ -10,6 +10,7 @@
 #include <vector>
 
 struct hss_plan_s;
+struct hss_factor_s;
 
 namespace hss {
 
@@ -84,5 +85,13 @@ int plan_device(const hss_plan_s* p);
 int32_t plan_ntrees(const hss_plan_s* p);
 int64_t plan_rows(const hss_plan_s* p);
 int64_t plan_cols(const hss_plan_s* p);
+// The adjoint of a single-tree plan as a new plan (same node numbering);
+// synchronises st.
+int plan_transpose(const hss_plan_s* h, hss_plan_s** out, cudaStream_t st);
+// A factorization's device storage (elements of its precision) and its size in bytes.
+const void* factor_storage(const hss_factor_s* f);
+size_t factor_storage_bytes(const hss_factor_s* f);
+// A plan's generator buffer and its length (doubles).
+const double* plan_gen(const hss_plan_s* p, int64_t* len);
 
 }  // namespace hss

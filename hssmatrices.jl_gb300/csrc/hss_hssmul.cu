@@ -46,10 +46,14 @@ __global__ void __launch_bounds__(MT) mm_list_kernel(const MmTask* __restrict__ 
   __shared__ double Bs[TK][TI + 1];
   const MmTask t = tasks[blockIdx.x];
   const int tid = threadIdx.x;
-  if (t.k1 < 0) {   // copy (A1 != null) or zero fill
+  if (t.k1 < 0) {   // copy (A1 != null) or zero fill, by cmode
     for (int64_t e = tid; e < (int64_t)t.m * t.n; e += MT) {
       const int i = (int)(e % t.m), j = (int)(e / t.m);
-      t.C[i + (int64_t)j * t.ldc] = t.A1 ? opA(t.A1, t.lda1, t.ta1, i, j) : 0.0;
+      double* c = t.C + i + (int64_t)j * t.ldc;
+      double v = t.cmode == MM_EYE ? (i == j ? 1.0 : 0.0) : (t.A1 ? opA(t.A1, t.lda1, t.ta1, i, j) : 0.0);
+      if (t.cmode == MM_TRIL && j > i) v = 0.0;
+      if (t.cmode == MM_AXPY) v = t.beta != 0.0 ? fma(t.a1, v, t.beta * *c) : t.a1 * v;
+      *c = v;
     }
     return;
   }

@@ -119,14 +119,35 @@ struct GiTile {
 // One task of the HSS x HSS product (hss_hssmul.cu):
 // C (m x n, ld ldc) = a1 op(A1) op(B1) + a2 op(A2) op(B2) + beta C, op = transpose
 // when ta / tb is set; K = k1 (k2) columns of op(A); A2 may be null.  k1 = -1:
-// C = op(A1) (a block copy; A1 null: zeros).
+// a block copy by cmode: MM_COPY C = op(A1) (A1 null: zeros), MM_AXPY
+// C = a1 op(A1) + beta C, MM_TRIL C = the lower triangle of op(A1) (zeros above
+// the diagonal), MM_EYE C = the identity.
+enum { MM_COPY = 0, MM_AXPY = 1, MM_TRIL = 2, MM_EYE = 3 };
 struct MmTask {
   const double *A1, *B1, *A2, *B2;
   double* C;
   int32_t lda1, ldb1, lda2, ldb2, ldc;
   int32_t m, n, k1, k2;
   int32_t ta1, tb1, ta2, tb2;
+  int32_t cmode;
   double a1, a2, beta;
+};
+
+// One block of rows transformed with a factored node of an FP64 ULV
+// factorization (hss_divide.cu): columns [0, cols) of src (rows x cols, ld
+// lds).  DIV_QL: Q_ql^T, then the first mk rows solved with L1 and written to
+// top (rows x cols, the other rows zero), the last rows - mk rows written to
+// bot.  DIV_LQ: Q_lq^T, written to top.  DIV_ROOT: the root block's LU solve,
+// written to top.  top may alias src.
+enum { DIV_QL = 0, DIV_LQ = 1, DIV_ROOT = 2 };
+struct DivTask {
+  const Node* nd;       // the factored node (device descriptor)
+  const double* fb;     // the factorization's storage
+  const double* src;
+  double* top;
+  double* bot;
+  int64_t lds, ldt, ldb;
+  int32_t rows, cols, mode, pad;
 };
 
 // One truncated column-pivoted QR (hss_recompress.cu): G (p x q, ld ldg) is

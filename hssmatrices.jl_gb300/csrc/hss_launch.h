@@ -159,4 +159,9 @@ int64_t noalloc_ws_capacity();
 // that takes the slot by value (no host staging buffer, no allocation).
 cudaError_t noalloc_write_slot(Slot* dslot, const Slot& x, cudaStream_t st);
 
+// Row transforms of the HSS-valued division (hss_divide.cu): one launch over
+// the tasks, every task's columns in chunks of 32; rows <= div_rows_max().
+int div_rows_max();
+cudaError_t launch_div_rows(const DivTask* tasks, int64_t count, int maxrows, int maxcols, cudaStream_t st);
+
 }  // namespace hss

@@ -240,6 +240,21 @@ class HssMatrix:
 
     __matmul__ = __mul__
 
+    # numpy defers A @ hssB and A / hssB to the methods below
+    __array_ufunc__ = None
+
+    def __rmul__(self, A):
+        """``A * hssB`` for a dense A (src/matmul.jl:14): (hssB' * A')' on the device."""
+        from .linalg import rmatmul
+        return rmatmul(A, self)
+
+    __rmatmul__ = __rmul__
+
+    def __rtruediv__(self, B):
+        """``B / hssA`` for a dense B (src/hssmatrix.jl:236): (hssA' \\ B')'."""
+        from .linalg import rdiv
+        return rdiv(B, self)
+
     def __getitem__(self, key):
         """``hssA[i, j]`` (src/hssmatrix.jl:102-114), 0-based, on the device."""
         from .linalg import getindex

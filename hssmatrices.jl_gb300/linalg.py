@@ -173,9 +173,17 @@ class DeviceHss:
                                        out.shape[0], float(alpha), float(beta)))
         return out.reshape(-1) if vec else out
 
-    def matmul_device(self, dB, ldb, r, dC, ldc, alpha=1.0, beta=0.0, stream=None):
-        check(self.lib.hss_matmul(self.handle, _ptr(dB), ldb, r, _ptr(dC), ldc, float(alpha),
-                                  float(beta), _stream(stream)))
+    def matmul_device(self, dB, ldb, r, dC, ldc, alpha=1.0, beta=0.0, stream=None, trans=False):
+        """C = alpha op(A) B + beta C on device buffers; op(A) = A^T with trans
+        (``hss_matmul_t``: the adjoint's generators made on the device once)."""
+        f = self.lib.hss_matmul_t if trans else self.lib.hss_matmul
+        check(f(self.handle, _ptr(dB), ldb, r, _ptr(dC), ldc, float(alpha), float(beta), _stream(stream)))
+
+    def transpose(self):
+        """The adjoint as a new device handle (``hss_transpose``, src/hssmatrix.jl:165-178)."""
+        h = C.c_void_p()
+        check(self.lib.hss_transpose(self.handle, C.byref(h), _stream(None)))
+        return DeviceHss(_handle=h)
 
     def matmul_batch_device(self, dBs, ldbs, rs, dCs, ldcs, alpha=1.0, beta=0.0, stream=None):
         k = self.ntrees
@@ -451,85 +459,92 @@ def cluster_trees(hssA, r0=1, c0=1):
     return rc, cc
 
 
-def _solve_columns(F, Bt, n, chunk):
-    """X = A^-1 B for a column-major B held as a (columns, n) tensor, in
-    chunks of columns through the FP64 ULV solve."""
-    import torch
-    Xt = torch.empty_like(Bt)
-    for c0 in range(0, Bt.shape[0], chunk):
-        c1 = min(Bt.shape[0], c0 + chunk)
-        F.solve_device(Bt[c0:c1], n, c1 - c0, Xt[c0:c1], n, tol=0.0)
-    return Xt
+def _div_tols(opts, kw):
+    from .hssmatrix import HssOptions
+    o = (opts or HssOptions.current()).copy(**{k: v for k, v in kw.items() if k in ("atol", "rtol")})
+    return float(o.atol), float(o.rtol)
 
 
-def _compress_dense(Xt, rcl, ccl, opts, stats, kw):
-    """randcompress_adaptive of a column-major device matrix (tensor of
-    shape (columns, rows))."""
-    from .compression import DenseDevice, randcompress_adaptive
-    st = {}
-    out = randcompress_adaptive(DenseDevice(Xt.t()), rcl, ccl, opts=opts, stats=st, **kw)
-    if stats is not None:
-        stats.update(st)
-    return out
-
-
-def hss_ldiv(hssA, hssB, opts=None, stats=None, chunk=512, **kw):
+def hss_ldiv(hssA, hssB, opts=None, stats=None, device=False, **kw):
     """``hssA \\ hssB`` / ``ldiv!(hssA, hssB)`` (src/hssmatrix.jl:235,
-    src/ulvdivide.jl:13) on the device: an HssMatrix X with ``full(X)``
-    approximating A^-1 full(B) to the compression tolerances (``HssOptions``
-    or ``opts`` / keywords), on A's column and B's column cluster trees.
-
-    The reference eliminates leaf by leaf on the generators (_ldiv!,
-    src/ulvdivide.jl:22-52, recompressing as it recurses).  Here B is expanded
-    on the device (``hss_full``), solved with A's FP64 ULV factorization in
-    chunks of columns, and the dense result recompressed by the adaptive
-    randomized compression (``randcompress_adaptive``): O(n^2) device memory
-    and O(n^2 k) work, every step a GPU kernel.  The generators (and ranks)
-    can differ from the reference's; the operator agrees to the tolerance, as
-    the reference's own test checks (test/runtests.jl:73)."""
-    import torch
+    src/ulvdivide.jl:13-54) on the device (``hss_ldiv``): the reference's
+    recursion on the generators -- A's leaves reduced with its FP64 ULV
+    factorization, the same transforms applied to B's leaf rows, the remainder
+    recompressed to (atol, rtol) and pruned level by level, the root block
+    solved, the solution unpacked back up with recompression.  Memory is
+    O(n k) per level; no dense n x n block is formed.  Returns an HssMatrix on
+    B's column clusters (or the DeviceHss handle with ``device=True``)."""
     (am, an), (bm, _bn) = hssA.size(), hssB.size()
     if am != an:
         raise ValueError("hssA must be square")
     if bm != am:
         raise ValueError("DimensionMismatch: rows of hssB must match hssA")
-    a = hssA.device()
-    b = hssB.device()
-    Bt = torch.empty((b.n, b.m), dtype=torch.float64, device="cuda")
-    check(b.lib.hss_full(b.handle, Bt.data_ptr(), max(b.m, 1), None))
-    F = a.ulvfactor("fp64")
-    Xt = _solve_columns(F, Bt, a.n, chunk)
-    del Bt
-    rcl = cluster_trees(hssA)[1]
-    ccl = cluster_trees(hssB)[1]
-    return _compress_dense(Xt, rcl, ccl, opts, stats, kw)
+    atol, rtol = _div_tols(opts, kw)
+    a, b = hssA.device(), hssB.device()
+    h = C.c_void_p()
+    check(a.lib.hss_ldiv(a.handle, b.handle, atol, rtol, C.byref(h), _stream(None)))
+    dev = DeviceHss(_handle=h)
+    if stats is not None:
+        stats.update(hssrank=dev_rank(dev))
+    return dev if device else dev.to_host()
 
 
-def rdiv(hssB, hssA, opts=None, stats=None, chunk=512, **kw):
-    """``hssB / hssA`` / ``rdiv!(hssB, hssA)`` (src/hssmatrix.jl:237,
-    src/ulvdivide.jl:15-17): X with ``full(X)`` approximating full(B) A^-1, on
-    B's row and A's row cluster trees; the reference forms it as
-    (A' \\ B')', and so does this function, with A' factored on the device."""
-    import torch
-    (am, an), (_bm, bn) = hssA.size(), hssB.size()
+def rdiv(hssB, hssA, opts=None, stats=None, device=False, **kw):
+    """``hssB / hssA``: for an HssMatrix hssB, ``rdiv!`` = adjoint(hssA' \\ hssB')
+    (src/hssmatrix.jl:237, src/ulvdivide.jl:15-17) on the device
+    (``hss_rdiv``: the adjoints made on the device); for a dense B,
+    ``B / hssA`` = (hssA' \\ B')' (src/hssmatrix.jl:236) with the FP64 ULV
+    factorization of the device adjoint."""
+    from .hssmatrix import HssMatrix
+    (am, an) = hssA.size()
     if am != an:
         raise ValueError("hssA must be square")
+    if not isinstance(hssB, HssMatrix):
+        B = np.asarray(hssB, dtype=np.float64)
+        vec = B.ndim == 1
+        B2 = B.reshape(1, -1) if vec else B
+        if B2.shape[1] != an:
+            raise ValueError("DimensionMismatch: columns of B must match hssA")
+        a = hssA.device()
+        # B' as a column-major array is B's rows: a host layout change only
+        Bt = np.asfortranarray(B2.T)
+        at = a.transpose()
+        Xt = at.ulvfactor("fp64").solve(Bt)
+        X = np.asarray(Xt).T
+        return X.reshape(-1) if vec else X
+    (_bm, bn) = hssB.size()
     if bn != am:
         raise ValueError("DimensionMismatch: columns of hssB must match hssA")
-    a = hssA.device()
-    b = hssB.device()
-    Bt = torch.empty((b.n, b.m), dtype=torch.float64, device="cuda")   # column-major B
-    check(b.lib.hss_full(b.handle, Bt.data_ptr(), max(b.m, 1), None))
-    Btt = Bt.t().contiguous()                                        # column-major B'
-    del Bt
-    F = transpose(hssA).device().ulvfactor("fp64")
-    Yt = _solve_columns(F, Btt, a.n, chunk)                           # column-major A'^-1 B'
-    del Btt
-    rcl = cluster_trees(hssB)[0]
-    ccl = cluster_trees(hssA)[0]
-    from .compression import DenseDevice, randcompress_adaptive
-    st = {}
-    out = randcompress_adaptive(DenseDevice(Yt), rcl, ccl, opts=opts, stats=st, **kw)   # (A'^-1 B')' = B A^-1
+    atol, rtol = _div_tols(opts, kw)
+    a, b = hssA.device(), hssB.device()
+    h = C.c_void_p()
+    check(a.lib.hss_rdiv(b.handle, a.handle, atol, rtol, C.byref(h), _stream(None)))
+    dev = DeviceHss(_handle=h)
     if stats is not None:
-        stats.update(st)
-    return out
+        stats.update(hssrank=dev_rank(dev))
+    return dev if device else dev.to_host()
+
+
+def rmatmul(A, hssB):
+    """``A * hssB`` for a dense A (src/matmul.jl:14): (hssB' * A')' with the
+    product by the adjoint on the device (``hss_matmul_t``)."""
+    import torch
+    dev = hssB.device()
+    A = np.asarray(A, dtype=np.float64)
+    vec = A.ndim == 1
+    A2 = A.reshape(1, -1) if vec else A
+    if A2.shape[1] != dev.m:
+        raise ValueError("DimensionMismatch: columns of A must match rows of hssB")
+    p = A2.shape[0]
+    # A' (m x p, column-major) is A's rows, i.e. A row-major: a p x m tensor
+    dAt = torch.from_numpy(np.ascontiguousarray(A2)).cuda()
+    dCt = torch.empty((p, dev.n), dtype=torch.float64, device="cuda")
+    dev.matmul_device(dAt, dev.m, p, dCt, dev.n, trans=True, stream=torch.cuda.current_stream())
+    out = dCt.cpu().numpy()     # row-major p x n = C
+    return out.reshape(-1) if vec else out
+
+
+def dev_rank(dev):
+    """``hssrank`` of a device handle from its node table."""
+    table, _packed = dev.export()
+    return int(max(table[:, 4].max(initial=0), table[:, 5].max(initial=0)))

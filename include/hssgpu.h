@@ -244,6 +244,34 @@ int hss_hssmul(hss_handle a, hss_handle b, hss_handle* out, void* stream);
 int hss_recompress(hss_handle h, double atol, double rtol, hss_handle* out, void* stream);
 int hss_orthonormalize(hss_handle h, hss_handle* out, void* stream);
 
+/* `adjoint(hssA)` / `transpose(hssA)` for real generators (src/hssmatrix.jl:
+ * 165-178) on the device: D^T, U and V exchanged, B12 and B21 exchanged and
+ * transposed, R and W exchanged; a new handle with the same node numbering.
+ * Synchronises `stream`. */
+int hss_transpose(hss_handle h, hss_handle* out, void* stream);
+
+/* C = alpha A^T B + beta C (dense B, C on the device): the product with the
+ * adjoint, for `*(A::AbstractMatrix, hssB)` (src/matmul.jl:14, as
+ * (hssB' * A')') and `hssA' * B`.  The adjoint's generators are made on the
+ * device at the first call and kept with the handle (twice the generator
+ * memory from then on); otherwise as hss_matmul. */
+int hss_matmul_t(hss_handle h, const double* dB, int64_t ldb, int64_t r, double* dC, int64_t ldc, double alpha,
+                 double beta, void* stream);
+
+/* HSS-valued division (src/ulvdivide.jl:13-252): X = hssA \ hssB (hss_ldiv,
+ * `ldiv!`, src/hssmatrix.jl:235) and X = hssB / hssA (hss_rdiv, `rdiv!` =
+ * adjoint(hssA' \ hssB'), :237), new handles on B's column (ldiv) or row
+ * (rdiv) clusters.  The reference's recursion on the generators: A's leaves
+ * reduced by its FP64 ULV factorization, the same transforms applied to B's
+ * leaf rows, the remainder B - L Y0 recompressed (atol, rtol) and pruned one
+ * level per step, the root block solved, and the solution unpacked back up
+ * with recompression at every level.  Memory is O(n k) per level, no dense
+ * n x n block is formed.  hssA must be square on matching row and column
+ * clusters with square leaves of at most 512 rows; hssB on A's cluster tree.
+ * Synchronises `stream` several times per level. */
+int hss_ldiv(hss_handle hA, hss_handle hB, double atol, double rtol, hss_handle* out, void* stream);
+int hss_rdiv(hss_handle hB, hss_handle hA, double atol, double rtol, hss_handle* out, void* stream);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t hss_launch_counter(void);
 

@@ -88,13 +88,14 @@ def test_inspect_rejects_bad_trees(lib, pkg, orc):
     t[2, 1] = 2
     rc, _ = _inspect(lib, t, g["packed"].size)
     assert rc == pkg._lib.HSS_ERR_BAD_DIMS
-    # non-square leaf root
+    # a rectangular (3 x 4) leaf root is a valid operand of the products
+    # (src/matmul.jl); only its ULV factorization is refused
     one = np.full((1, 16), -1, dtype=np.int64)
     one[0, 2:6] = [3, 4, 0, 0]
     one[0, 6] = 0
     one[0, 15] = 0
     rc, _ = _inspect(lib, one, 12)
-    assert rc == pkg._lib.HSS_ERR_BAD_DIMS
+    assert rc == pkg._lib.HSS_OK
 
 
 def test_host_mirror_api(pkg, orc):
