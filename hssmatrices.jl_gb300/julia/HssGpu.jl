@@ -118,6 +118,35 @@ function LinearAlgebra.ldiv!(X::Matrix{Float64}, F::GpuUlv, B::Matrix{Float64}; 
     X
 end
 
+# a handle made on the device (division, adjoint), with its size
+function adopt(h::Ptr{Cvoid})
+    m, n = Ref{Int64}(), Ref{Int64}()
+    check(ccall((:hss_size, lib), Cint, (Ptr{Cvoid}, Int32, Ref{Int64}, Ref{Int64}), h, Int32(0), m, n))
+    g = GpuHss(h, m[], n[])
+    finalizer(x -> ccall((:hss_destroy, lib), Cint, (Ptr{Cvoid},), x.ptr), g)
+end
+
+# hssA \ hssB and hssB / hssA -- src/ulvdivide.jl:13-17, src/hssmatrix.jl:235-237
+function Base.:\(a::GpuHss, b::GpuHss; atol=1e-9, rtol=1e-9)
+    h = Ref{Ptr{Cvoid}}()
+    check(ccall((:hss_ldiv, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Float64, Ref{Ptr{Cvoid}}, Ptr{Cvoid}),
+                a.ptr, b.ptr, atol, rtol, h, C_NULL))
+    adopt(h[])
+end
+function Base.:/(b::GpuHss, a::GpuHss; atol=1e-9, rtol=1e-9)
+    h = Ref{Ptr{Cvoid}}()
+    check(ccall((:hss_rdiv, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Float64, Ref{Ptr{Cvoid}}, Ptr{Cvoid}),
+                b.ptr, a.ptr, atol, rtol, h, C_NULL))
+    adopt(h[])
+end
+
+# adjoint(hssA) -- src/hssmatrix.jl:165-171
+function Base.adjoint(a::GpuHss)
+    h = Ref{Ptr{Cvoid}}()
+    check(ccall((:hss_transpose, lib), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}, Ptr{Cvoid}), a.ptr, h, C_NULL))
+    adopt(h[])
+end
+
 # process-wide switches (HSS_OPT_* of the header)
 set_option(opt::Integer, value::Integer) =
     check(ccall((:hss_set_option, lib), Cint, (Int32, Int64), Int32(opt), Int64(value)))

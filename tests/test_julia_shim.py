@@ -25,6 +25,7 @@ JULIA_TO_C = {
     "Ptr{Float64}": {"double*", "const double*"},
     "Ptr{Int64}": {"int64_t*", "const int64_t*"},
     "Ref{Ptr{Cvoid}}": {"hss_handle*", "hss_factor*"},
+    "Ref{Int64}": {"int64_t*"},
     "Ref{SolveStats}": {"hss_solve_stats*"},
 }
 
@@ -85,7 +86,8 @@ def test_shim_is_present_and_parsed():
     calls = shim_calls()
     names = {c[0] for c in calls}
     for need in ("hss_create", "hss_destroy", "hss_matmul_host", "hss_ulvfactsolve_host", "hss_ulvfactor",
-                 "hss_ulvsolve_host", "hss_factor_destroy", "hss_last_error", "hss_set_option"):
+                 "hss_ulvsolve_host", "hss_factor_destroy", "hss_last_error", "hss_set_option", "hss_ldiv",
+                 "hss_rdiv", "hss_transpose", "hss_size"):
         assert need in names, need
 
 
