@@ -221,11 +221,44 @@ __device__ __forceinline__ int out_slots(int nout) {
   return op;
 }
 
-// out(o) = sum_{l < K} term(o, l) for o < nout with every thread taking part
-// (at most gmax groups of terms per output); epi(o, sum) consumes each result.
+// The terms of one output of a small product: at most two strided segments,
+// sum_{l < k1} a1[l sa1] b1[l sb1] + sum_{l < k2} a2[l sa2] b2[l sb2].  The
+// call sites form the segment pointers once per output, so the inner loops
+// hold no index arithmetic.
+template <class E>
+struct Terms {
+  const E* a1;
+  const E* b1;
+  int sa1, sb1, k1;
+  const E* a2;
+  const E* b2;
+  int sa2, sb2, k2;
+};
+
+template <class E>
+__device__ __forceinline__ Terms<E> terms1(const E* a, int sa, const E* b, int sb, int k) {
+  return Terms<E>{a, b, sa, sb, k, nullptr, nullptr, 0, 0, 0};
+}
+
+// acc[0..3] += the segment's terms l = g, g + G, ...: four independent chains
+template <class P>
+__device__ __forceinline__ void seg_acc(typename P::Acc (&acc)[4], const typename P::E* a, int sa,
+                                        const typename P::E* b, int sb, int k, int g, int G) {
+  int l = g;
+  for (; l + 3 * G < k; l += 4 * G) {
+    P::fma(acc[0], a[l * sa], b[l * sb]);
+    P::fma(acc[1], a[(l + G) * sa], b[(l + G) * sb]);
+    P::fma(acc[2], a[(l + 2 * G) * sa], b[(l + 2 * G) * sb]);
+    P::fma(acc[3], a[(l + 3 * G) * sa], b[(l + 3 * G) * sb]);
+  }
+  for (; l < k; l += G) P::fma(acc[0], a[l * sa], b[l * sb]);
+}
+
+// out(o) = the sum of terms(o) for o < nout with every thread taking part (at
+// most gmax groups of terms per output); epi(o, sum) consumes each result.
 // `part` holds PT accumulators.
-template <class P, class Term, class Epi>
-__device__ void sdot(int nout, int K, typename P::Acc* part, Term term, Epi epi, int gmax = PT) {
+template <class P, class Setup, class Epi>
+__device__ void sdot(int nout, typename P::Acc* part, Setup terms, Epi epi, int gmax = PT) {
   using Acc = typename P::Acc;
   const int op = max(out_slots(nout), PT / gmax), G = PT / op;
   const int slot = threadIdx.x % op, g = threadIdx.x / op;
@@ -233,8 +266,14 @@ __device__ void sdot(int nout, int K, typename P::Acc* part, Term term, Epi epi,
     const int o = o0 + slot;
     Acc acc = P::zero();
     if (o < nout) {
-#pragma unroll 4
-      for (int l = g; l < K; l += G) term(o, l, acc);
+      const Terms<typename P::E> t = terms(o);
+      Acc a4[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
+      if (t.k1 > 0) seg_acc<P>(a4, t.a1, t.sa1, t.b1, t.sb1, t.k1, g, G);
+      if (t.k2 > 0) seg_acc<P>(a4, t.a2, t.sa2, t.b2, t.sb2, t.k2, g, G);
+      P::acc(a4[0], a4[1]);
+      P::acc(a4[2], a4[3]);
+      P::acc(a4[0], a4[2]);
+      acc = a4[0];
     }
     if (G > 1) {
       __syncthreads();
@@ -345,11 +384,10 @@ __device__ void z_node(const Slot& sl, const Node& p, int j0, int nc, typename P
   stage_ws(Z2, v2, ws + p.cwz[1] + (int64_t)j0 * ld, ld, v2, nc);
   cp_wait<0>();
   __syncthreads();
-  sdot<P>(kv * nc, v1 + v2, part,
-          [&](int o, int l, Acc& s) {
+  sdot<P>(kv * nc, part,
+          [&](int o) {
             const int c = o % kv, q = o / kv;
-            if (l < v1) P::fma(s, W1s[l + c * ld1], Z1[l + q * v1]);
-            else P::fma(s, W2s[(l - v1) + c * ld2], Z2[(l - v1) + q * v2]);
+            return Terms<E>{W1s + c * ld1, Z1 + q * v1, 1, 1, v1, W2s + c * ld2, Z2 + q * v2, 1, 1, v2};
           },
           [&](int o, const Acc& s) { ws[p.wz + (o % kv) + (int64_t)(j0 + o / kv) * ld] = P::fin(s); });
 }
@@ -377,16 +415,11 @@ __device__ void bterm_node(const Slot& sl, const Node& p, int j0, int nc, typena
   stage_ws(Z2, v2, ws + p.cwz[1] + (int64_t)j0 * ld, ld, v2, nc);
   cp_wait<0>();
   __syncthreads();
-  sdot<P>((u1 + u2) * nc, max(v1, v2), part,
-          [&](int o, int l, Acc& s) {
-            if (o < u1 * nc) {
-              const int i = o % u1, q = o / u1;
-              if (l < v2) P::fma(s, B12[i + l * u1], Z2[l + q * v2]);
-            } else {
-              const int o2 = o - u1 * nc;
-              const int i = o2 % u2, q = o2 / u2;
-              if (l < v1) P::fma(s, B21[i + l * u2], Z1[l + q * v1]);
-            }
+  sdot<P>((u1 + u2) * nc, part,
+          [&](int o) {
+            if (o < u1 * nc) return terms1<E>(B12 + o % u1, u1, Z2 + (o / u1) * v2, 1, v2);
+            const int o2 = o - u1 * nc;
+            return terms1<E>(B21 + o2 % u2, u2, Z1 + (o2 / u2) * v1, 1, v1);
           },
           [&](int o, const Acc& s) {
             if (o < u1 * nc) ws[p.cwf[0] + (o % u1) + (int64_t)(j0 + o / u1) * ld] = P::fin(s);
@@ -469,10 +502,11 @@ __device__ void down_node(const Slot& sl, const Node& p, int j0, int nc, typenam
   stage_ws(G2, u2, ws + f2 + (int64_t)j0 * ld, ld, u2, nc);
   cp_wait<0>();
   __syncthreads();
-  sdot<P>((u1 + u2) * nc, kp, part,
-          [&](int o, int l, Acc& s) {
-            if (o < u1 * nc) P::fma(s, R1[(o % u1) + l * u1], Fp[l + (o / u1) * kp]);
-            else P::fma(s, R2[((o - u1 * nc) % u2) + l * u2], Fp[l + ((o - u1 * nc) / u2) * kp]);
+  sdot<P>((u1 + u2) * nc, part,
+          [&](int o) {
+            if (o < u1 * nc) return terms1<E>(R1 + o % u1, u1, Fp + (o / u1) * kp, 1, kp);
+            const int o2 = o - u1 * nc;
+            return terms1<E>(R2 + o2 % u2, u2, Fp + (o2 / u2) * kp, 1, kp);
           },
           [&](int o, const Acc& s) {
             const bool first = o < u1 * nc;
@@ -893,8 +927,8 @@ __device__ void flat_bterm(const Slot& sl, const FlatLink& lk, const double* zs,
   const double* B = lk.B;
   double* ws = (double*)sl.ws;
   const int64_t ld = sl.ldws, off = lk.swf;
-  sdot<PF64>(ks * nc, kv, part,
-             [&](int o, int l, FA& s) { PF64::fma(s, __ldg(B + (o % ks) + (int64_t)l * ks), zs[l + (o / ks) * kv]); },
+  sdot<PF64>(ks * nc, part,
+             [&](int o) { return terms1<double>(B + o % ks, ks, zs + (o / ks) * kv, 1, kv); },
              [&](int o, const FA& s) { ws[off + (o % ks) + (int64_t)(j0 + o / ks) * ld] = s.s; }, 4);
 }
 
@@ -935,8 +969,8 @@ __device__ void flat_up(const FlatArgs& a, int t, int ch, FA* part, double* sm, 
     const int ky = L.kv, kq = L.kpv, ldw = ky | 1;
     const double* Ws = Wb + buf * wstride;
     double* dst = a.ctb + ((int64_t)((d - 1) * a.nleaves + t) * a.nchunk + ch) * a.kw;
-    sdot<PF64>(kq * nc, ky, part,
-               [&](int o, int l, FA& s) { PF64::fma(s, Ws[l + (o % kq) * ldw], cur[l + (o / kq) * ky]); },
+    sdot<PF64>(kq * nc, part,
+               [&](int o) { return terms1<double>(Ws + (o % kq) * ldw, 1, cur + (o / kq) * ky, 1, ky); },
                [&](int o, const FA& s) {
                  nxt[o] = s.s;
                  dst[o] = s.s;
@@ -1123,8 +1157,8 @@ __device__ void flat_down(const FlatArgs& a, int t, int ch, FA* part, double* sm
     const double* Rs = Rb + buf * km * km;
     const double* G = Gs + d * kk;
     double* out = Fb + buf * kk;
-    sdot<PF64>(kc * nc, kp, part,
-               [&](int o, int l, FA& s) { PF64::fma(s, Rs[(o % kc) + l * kc], f[l + (o / kc) * km]); },
+    sdot<PF64>(kc * nc, part,
+               [&](int o) { return terms1<double>(Rs + o % kc, kc, f + (o / kc) * km, 1, kp); },
                [&](int o, const FA& s) {
                  const int i = o % kc, q = o / kc;
                  out[i + q * km] = s.s + G[i + q * km];
