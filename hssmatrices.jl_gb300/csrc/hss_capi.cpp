@@ -804,15 +804,36 @@ int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable&
       return cuda_fail(e, "tensor-core leaf product launch");
     }
   }
+  // ... and the leaf products Z = V^T X and C = alpha (D X + U F) + beta Y as
+  // streams over all leaves around the persistent launch, which keeps the tree part
+  const bool ext = dx && leaf_ext_fits(L.nleaf, L.mleaf, L.kmax);
+  if (ext) {
+    traced(HSS_TRACE_MV_UP, L.leaves.cnt, st, [&] {
+      e = launch_leaf_ext(false, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, rmax, L.nleaf, L.mleaf, L.kmax, st);
+    });
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "leaf upsweep launch");
+    }
+  }
   traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st, [&] {
     const void* pf = pairs ? (const void*)L.pfdf : (const void*)L.pf64;
     e = launch_pmv(pairs, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, L.ntasks, L.ninner, rmax, L.nleaf, L.kmax,
                    pm.pstate.p,
-                   pm.pq.p, pm.epoch, pf, pf ? L.pf_elems * 8 : 0, L.device, st, dx);
+                   pm.pq.p, pm.epoch, pf, pf ? L.pf_elems * 8 : 0, L.device, st, dx, ext);
   });
   if (e != cudaSuccess) {
     cudaGetLastError();
     return cuda_fail(e, "persistent product launch");
+  }
+  if (ext) {
+    traced(HSS_TRACE_MV_FINAL, L.leaves.cnt, st, [&] {
+      e = launch_leaf_ext(true, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, rmax, L.nleaf, L.mleaf, L.kmax, st);
+    });
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "leaf final launch");
+    }
   }
   return HSS_OK;
 }

@@ -58,7 +58,15 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
                        int64_t ninner, int rmax,
                        int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
                        const void* prefetch, int64_t prefetch_bytes, int device, cudaStream_t st,
-                       bool dx_ready = false);
+                       bool dx_ready = false, bool leaf_ext = false);
+// The other leaf products of the double-float residual, outside the persistent
+// launch (hss_pmv.cu): final_part = false: Z = V^T X of every non-root leaf
+// into the pair workspace (before the launch); true: C = alpha (D X + U F) +
+// beta Y with the column sums of squares (after it).  With dx_ready the
+// persistent launch skips both.
+bool leaf_ext_fits(int nleaf, int mleaf, int kmax);
+cudaError_t launch_leaf_ext(bool final_part, const Task* leaves, int64_t nleaves, const Slot* slots, int rmax, int nleaf,
+                            int mleaf, int kmax, cudaStream_t st);
 // Tensor-core leaf products of the double-float residual (hss_dx_tc.cu): for
 // every non-root leaf task and chunk of 32 columns, D X at ~48-bit accuracy
 // into the slot's pair buffer (sl.tmp), X = the slot's B; leaves up to 128 x 128.

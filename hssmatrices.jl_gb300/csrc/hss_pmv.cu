@@ -81,6 +81,7 @@ struct PmvArgs {
   uint32_t epoch;
   uint32_t idle_limit;   // polls of an idle block before DEV_TIMEOUT
   int32_t dx_ready;      // pairs: the non-root leaves' D B is already in the pair buffer (tensor cores)
+  int32_t leaf_ext;      // pairs: Z = V^T B is in the workspace and the final products follow the launch
 };
 
 // ---- arithmetic policies ----------------------------------------------------
@@ -314,11 +315,29 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
   const int slot = threadIdx.x % op, g = threadIdx.x / op;
   const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
   {
+    // four loads of a lane in flight before their conversions
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int q = w; q < nc; q += PT / 32)
-      for (int l = lane; l < n; l += 32) Xs[l + q * n] = P::xin(__ldg(X + l + (int64_t)q * sl.ldb));
+      for (int l0 = 0; l0 < n; l0 += 128) {
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + lane + 32 * u;
+          v[u] = l < n ? __ldg(X + l + (int64_t)q * sl.ldb) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + lane + 32 * u;
+          if (l < n) Xs[l + q * n] = P::xin(v[u]);
+        }
+      }
   }
-  Acc acc[2] = {P::zero(), P::zero()};   // nout <= 512 = 2 PT
+  // nout <= 512 = 2 PT outputs per thread slot; four accumulator chains each
+  Acc acc4[2][4];
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc4[s][c] = P::zero();
   for (int ps = 0; ps < npass; ++ps) {
     const int l0 = ps * LCH, nl = min(LCH, n - l0);
     const E* Vs = Vb[ps & 1];
@@ -330,10 +349,7 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
       const int o = s * op + slot;
       if (o < nout) {
         const int c = o % kv, q = o / kv;
-        const E* v = Vs + c * (LCH + 1);
-        const E* x = Xs + l0 + q * n;
-#pragma unroll 4
-        for (int l = g; l < nl; l += G) P::fma(acc[s], v[l], x[l]);
+        seg_acc<P>(acc4[s], Vs + c * (LCH + 1), 1, Xs + l0 + q * n, 1, nl, g, G);
       }
     }
     if (ps + 2 < npass) {
@@ -342,6 +358,14 @@ __device__ void leaf_up(const Slot& sl, const Node& nd, int j0, int nc, typename
     }
   }
   if (zsm != nullptr) __syncthreads();   // every thread is done with the V buffers
+  Acc acc[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    P::acc(acc4[s][0], acc4[s][1]);
+    P::acc(acc4[s][2], acc4[s][3]);
+    P::acc(acc4[s][0], acc4[s][2]);
+    acc[s] = acc4[s][0];
+  }
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     const int o = s * op + slot;
@@ -660,13 +684,18 @@ __device__ void bulk_unit(const PmvArgs& a, int u, typename P::Acc* part, typena
 
 // Final task of a non-root leaf chunk (F final, bulk done): C += alpha U F
 // (matmul.jl:47), or for pairs C = alpha (D B + U F) + beta Y, with the column
-// sums of squares.
+// sums of squares.  Thread (row ii, group g) takes the columns of group g
+// whole (no split over K, no cross-thread sums), FQ at a time, and loads
+// its epilogue operands (D B, Y, or C) before the product, so that their
+// latency overlaps the loop over U's columns.
 template <class P>
 __device__ void final_leaf(const Slot& sl, const Node& nd, int j0, int nc, typename P::Acc* part,
                            typename P::E* sm) {
   using E = typename P::E;
   using Acc = typename P::Acc;
   constexpr bool pairs = !std::is_same<E, double>::value;
+  constexpr int FQ = 2;   // columns per pass (registers: the launch allows 64 per thread)
+  (void)part;
   if (nc <= 0) return;
   const int m = nd.gm, ku = nd.ku;
   E* ws = P::ws(sl);
@@ -677,24 +706,76 @@ __device__ void final_leaf(const Slot& sl, const Node& nd, int j0, int nc, typen
   __syncthreads();
   double* C = sl.C + nd.row0 + (int64_t)j0 * sl.ldc;
   double* cn = sl.colnorm2 ? sl.colnorm2 + j0 : nullptr;
-  if (pairs) {
-    const E* T = (const E*)sl.tmp + nd.row0 + (int64_t)j0 * sl.ldt2;
-    const double* Y = sl.Y ? sl.Y + nd.row0 + (int64_t)j0 * sl.ldy : nullptr;
-    const bool yterm = sl.beta != 0.0 && Y != nullptr;
-    rows_cols_n<P>(U, m, ku, m, Fs, ku, nc, part, cn, [&](int i, int q, const Acc& s) {
-      Acc t = s;
-      P::addE(t, __ldcg(T + i + (int64_t)q * sl.ldt2));
-      double v = sl.alpha * P::dbl(t);
-      if (yterm) v += sl.beta * __ldcg(Y + i + (int64_t)q * sl.ldy);
-      C[i + (int64_t)q * sl.ldc] = v;
-      return v;
-    });
-  } else {
-    rows_cols_n<P>(U, m, ku, m, Fs, ku, nc, part, cn, [&](int i, int q, const Acc& s) {
-      const double v = __ldcg(C + i + (int64_t)q * sl.ldc) + sl.alpha * P::dbl(s);
-      C[i + (int64_t)q * sl.ldc] = v;
-      return v;
-    });
+  const E* T = pairs ? (const E*)sl.tmp + nd.row0 + (int64_t)j0 * sl.ldt2 : nullptr;
+  const double* Y = sl.Y ? sl.Y + nd.row0 + (int64_t)j0 * sl.ldy : nullptr;
+  const bool yterm = pairs && sl.beta != 0.0 && Y != nullptr;
+  const int tid = threadIdx.x;
+  for (int r0 = 0; r0 < m; r0 += PT) {
+    const int rows = min(PT, m - r0);
+    int rp = 1;
+    while (rp < rows) rp <<= 1;
+    const int G = PT / rp, ii = tid % rp, g = tid / rp;
+    const int i = r0 + ii;
+    const int cpg = (nc + G - 1) / G, q0 = g * cpg, q1 = min(nc, q0 + cpg);
+    for (int qb = q0; qb < q1; qb += FQ) {
+      const int nq = min(FQ, q1 - qb);
+      const bool act = ii < rows;
+      // epilogue operands first
+      E tv[FQ];
+      double yv[FQ];
+#pragma unroll
+      for (int q = 0; q < FQ; ++q) {
+        tv[q] = E{};
+        yv[q] = 0.0;
+        if (act && q < nq) {
+          if (pairs) {
+            tv[q] = __ldcg(T + i + (int64_t)(qb + q) * sl.ldt2);
+            if (yterm) yv[q] = __ldcg(Y + i + (int64_t)(qb + q) * sl.ldy);
+          } else {
+            yv[q] = __ldcg(C + i + (int64_t)(qb + q) * sl.ldc);
+          }
+        }
+      }
+      Acc acc[FQ];
+#pragma unroll
+      for (int q = 0; q < FQ; ++q) acc[q] = P::zero();
+      if (act) {
+        const E* a = U + i;
+#pragma unroll 8
+        for (int l = 0; l < ku; ++l) {
+          const E d = __ldg(a + (int64_t)l * m);
+#pragma unroll
+          for (int q = 0; q < FQ; ++q)
+            if (q < nq) P::fma(acc[q], d, Fs[l + (qb + q) * ku]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < FQ; ++q) {
+        double v = 0.0;
+        if (act && q < nq) {
+          if (pairs) {
+            Acc t = acc[q];
+            P::addE(t, tv[q]);
+            v = sl.alpha * P::dbl(t);
+            if (yterm) v += sl.beta * yv[q];
+          } else {
+            v = yv[q] + sl.alpha * P::dbl(acc[q]);
+          }
+          C[i + (int64_t)(qb + q) * sl.ldc] = v;
+        }
+        if (cn != nullptr) {
+          // a warp lies within one group when rp >= 32: warp sums, one atomic per column
+          double v2 = v * v;
+          if (rp >= 32) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+            if ((tid & 31) == 0 && q < nq && v2 != 0.0) atomicAdd(cn + qb + q, v2);
+          } else if (q < nq && v2 != 0.0) {
+            atomicAdd(cn + qb + q, v2);
+          }
+        }
+      }
+    }
   }
 }
 
@@ -703,6 +784,7 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
   using E = typename P::E;
   using Acc = typename P::Acc;
   extern __shared__ __align__(16) unsigned char pmv_smem[];
+  constexpr bool pairs_k = !std::is_same<E, double>::value;
   Acc* part = (Acc*)pmv_smem;                    // PART_ELEMS split-K partials
   E* sm = (E*)pmv_smem + PART_ELEMS;             // per-phase staging
   __shared__ int s_cmd, s_x, s_y, s_k;
@@ -782,7 +864,9 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
           node_event(a, slot, sl, node, ch);
         }
       } else if (x.leaf) {
-        final_leaf<P>(sl, x, j0, nc, part, sm);
+        // with the leaf products outside the launch (leaf_ext), the final
+        // products C = alpha (D B + U F) + beta Y follow it (leaf_uf_kernel)
+        if (!(pairs_k && a.leaf_ext)) final_leaf<P>(sl, x, j0, nc, part, sm);
       } else {
         down_node<P>(sl, x, j0, nc, part, sm);
         __syncthreads();
@@ -801,7 +885,8 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
         const Node& nd = tk.nodes[tk.node];
         if (!nd.root) {
           const int j0 = ch * a.cw;
-          leaf_up<P>(sl, nd, j0, min(a.cw, sl.r - j0), part, sm);
+          // leaf_ext: Z = V^T B is already in the workspace (leaf_vtx_kernel)
+          if (!(pairs_k && a.leaf_ext)) leaf_up<P>(sl, nd, j0, min(a.cw, sl.r - j0), part, sm);
           climb_from<P>(a, tk.slot, sl, tk.nodes, tk.node, ch, part, sm);
         }
       } else {
@@ -820,6 +905,146 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
       a.state[ST_BULK] = 0;
       __threadfence();
       a.state[ST_DONE] = 0;
+    }
+  }
+}
+
+// ---- leaf products of the double-float residual outside the persistent launch ----
+//
+// With the leaf blocks D X on the tensor cores (dx_tc_kernel), the other two
+// leaf products of the residual are streamed over all leaves at the width of
+// 32 columns, before and after the tree part: Z = V^T X into the workspace
+// (matmul.jl:34) and C = alpha (D X + U F) + beta Y with the column sums of
+// squares (:46-47).  Each block stages its leaf's generator block and column
+// block once in shared memory; a thread keeps two outputs of one row (V^T X)
+// or four of one row (U F) with their own accumulator chains.
+
+constexpr int XW = 32;   // columns per block of the leaf kernels
+
+__global__ void __launch_bounds__(PT) leaf_vtx_kernel(const Task* __restrict__ leaves, const Slot* __restrict__ slots) {
+  extern __shared__ __align__(16) unsigned char ext_smem[];
+  using P = PDF;
+  using Acc = P::Acc;
+  const Task tk = leaves[blockIdx.x];
+  const Slot& sl = slots[tk.slot];
+  const Node& nd = tk.nodes[tk.node];
+  const int j0 = blockIdx.y * XW;
+  if (nd.root || nd.kv == 0 || j0 >= sl.r) return;
+  const int n = nd.gn, kv = nd.kv, nc = min(XW, sl.r - j0);
+  const int ld = n | 1;             // odd: a warp's rows c (or columns q) fall in distinct bank pairs
+  float2* Vs = (float2*)ext_smem;   // n x kv, ld ld
+  float2* Xs = Vs + ld * kv;        // n x nc, ld ld
+  const float2* V = P::gen(sl, nd.V);
+  for (int e = threadIdx.x; e < n * kv; e += PT) Vs[e % n + (e / n) * ld] = __ldg(V + e);
+  const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
+  for (int e0 = threadIdx.x; e0 < n * nc; e0 += 4 * PT) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * PT;
+      v[u] = e < n * nc ? __ldg(X + e % n + (int64_t)(e / n) * sl.ldb) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * PT;
+      if (e < n * nc) Xs[e % n + (e / n) * ld] = split_bits(v[u]);
+    }
+  }
+  __syncthreads();
+  float2* ws = sl.ws2;
+  // 2 x 2 tiles: rows c, c + hc of Z, columns q, q + hq
+  const int hc = (kv + 1) / 2, hq = (nc + 1) / 2;
+  for (int it = threadIdx.x; it < hc * hq; it += PT) {
+    const int c = it % hc, q = it / hc;
+    const int c2 = c + hc < kv ? c + hc : c, q2 = q + hq < nc ? q + hq : q;
+    const float2* va = Vs + c * ld;
+    const float2* vb = Vs + c2 * ld;
+    const float2* xa = Xs + q * ld;
+    const float2* xb = Xs + q2 * ld;
+    Acc s00 = P::zero(), s01 = P::zero(), s10 = P::zero(), s11 = P::zero();
+#pragma unroll 2
+    for (int l = 0; l < n; ++l) {
+      const float2 a0 = va[l], a1 = vb[l], b0 = xa[l], b1 = xb[l];
+      P::fma(s00, a0, b0);
+      P::fma(s01, a0, b1);
+      P::fma(s10, a1, b0);
+      P::fma(s11, a1, b1);
+    }
+    ws[nd.wz + c + (int64_t)(j0 + q) * sl.ldws] = P::fin(s00);
+    if (q2 != q) ws[nd.wz + c + (int64_t)(j0 + q2) * sl.ldws] = P::fin(s01);
+    if (c2 != c) ws[nd.wz + c2 + (int64_t)(j0 + q) * sl.ldws] = P::fin(s10);
+    if (c2 != c && q2 != q) ws[nd.wz + c2 + (int64_t)(j0 + q2) * sl.ldws] = P::fin(s11);
+  }
+}
+
+__global__ void __launch_bounds__(PT) leaf_uf_kernel(const Task* __restrict__ leaves, const Slot* __restrict__ slots) {
+  extern __shared__ __align__(16) unsigned char ext_smem[];
+  using P = PDF;
+  using Acc = P::Acc;
+  const Task tk = leaves[blockIdx.x];
+  const Slot& sl = slots[tk.slot];
+  const Node& nd = tk.nodes[tk.node];
+  const int j0 = blockIdx.y * XW;
+  if (nd.root || j0 >= sl.r) return;
+  const int m = nd.gm, ku = nd.ku, nc = min(XW, sl.r - j0);
+  float2* Us = (float2*)ext_smem;   // m x ku, ld m
+  float2* Fs = Us + m * ku;         // ku x nc, ld ku
+  if (ku > 0) {
+    const float2* U = P::gen(sl, nd.U);
+    for (int e = threadIdx.x; e < m * ku; e += PT) Us[e] = __ldg(U + e);
+    const float2* F = sl.ws2 + nd.wf + (int64_t)j0 * sl.ldws;
+    for (int e = threadIdx.x; e < ku * nc; e += PT) Fs[e] = __ldcg(F + e % ku + (int64_t)(e / ku) * sl.ldws);
+  }
+  __syncthreads();
+  const float2* T = (const float2*)sl.tmp + nd.row0 + (int64_t)j0 * sl.ldt2;
+  const double* Y = sl.Y ? sl.Y + nd.row0 + (int64_t)j0 * sl.ldy : nullptr;
+  const bool yterm = sl.beta != 0.0 && Y != nullptr;
+  double* C = sl.C + nd.row0 + (int64_t)j0 * sl.ldc;
+  double* cn = sl.colnorm2 ? sl.colnorm2 + j0 : nullptr;
+  const int tid = threadIdx.x, lane = tid & 31;
+  // a warp takes 32 consecutive rows and, per pass, 4 columns (each thread
+  // 2 rows 32 apart x 4 columns: 8 accumulator chains); warps cycle through
+  // (row block, column block) pairs
+  const int nrb = (m + 63) / 64, ncb = (nc + 3) / 4;
+  for (int job = tid >> 5; job < nrb * ncb; job += PT / 32) {
+    const int rb = job % nrb, cb = job / nrb;
+    const int i0 = rb * 64 + lane, i1 = i0 + 32;
+    const int qb = cb * 4, nq = min(4, nc - qb);
+    const bool a0 = i0 < m, a1 = i1 < m;
+    Acc acc0[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
+    Acc acc1[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
+    const float2* f = Fs + qb * ku;
+#pragma unroll 2
+    for (int l = 0; l < ku; ++l) {
+      const float2 u0 = a0 ? Us[i0 + l * m] : make_float2(0.f, 0.f);
+      const float2 u1 = a1 ? Us[i1 + l * m] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float2 fq = q < nq ? f[l + q * ku] : make_float2(0.f, 0.f);
+        P::fma(acc0[q], u0, fq);
+        P::fma(acc1[q], u1, fq);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      double v2 = 0.0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = h ? i1 : i0;
+        if ((h ? a1 : a0) && q < nq) {
+          Acc t = h ? acc1[q] : acc0[q];
+          P::addE(t, __ldcg(T + i + (int64_t)(qb + q) * sl.ldt2));
+          double v = sl.alpha * P::dbl(t);
+          if (yterm) v += sl.beta * __ldcg(Y + i + (int64_t)(qb + q) * sl.ldy);
+          C[i + (int64_t)(qb + q) * sl.ldc] = v;
+          v2 = fma(v, v, v2);
+        }
+      }
+      if (cn != nullptr) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+        if (lane == 0 && q < nq && v2 != 0.0) atomicAdd(cn + qb + q, v2);
+      }
     }
   }
 }
@@ -1285,7 +1510,7 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
                        int64_t ninner, int rmax,
                        int nleaf, int kmax, uint32_t* state, unsigned long long* qent, uint32_t epoch,
                        const void* prefetch,
-                       int64_t prefetch_bytes, int device, cudaStream_t st, bool dx_ready) {
+                       int64_t prefetch_bytes, int device, cudaStream_t st, bool dx_ready, bool leaf_ext) {
   if (nleaves <= 0) return cudaSuccess;
   const size_t smem = pmv_smem_elems(nleaf, kmax, nullptr) * 8;
   PmvArgs a;
@@ -1304,6 +1529,7 @@ cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Sl
   a.pf_bytes = prefetch ? prefetch_bytes : 0;
   a.idle_limit = g_idle_limit;
   a.dx_ready = (pairs && dx_ready) ? 1 : 0;
+  a.leaf_ext = (pairs && leaf_ext) ? 1 : 0;
   void* args[] = {&a};
   const int cap = pairs ? resident_blocks<PDF>(smem, device) : resident_blocks<PF64>(smem, device);
   if (cap <= 0) return cudaErrorLaunchOutOfResources;
@@ -1368,6 +1594,34 @@ cudaError_t launch_pmv_flat(const Task* leaves, int64_t nleaves, const Task* bra
   const unsigned grid = (unsigned)std::min<int64_t>(cap, std::max<int64_t>(1, units));
   void* args[] = {&a};
   return cudaLaunchCooperativeKernel((void*)pmv_flat_kernel, grid, PT, args, smem, st);
+}
+
+size_t leaf_ext_smem(int nleaf, int mleaf, int kmax) {
+  const size_t up = ((size_t)(nleaf | 1) * kmax + (size_t)(nleaf | 1) * XW) * sizeof(float2);
+  const size_t fin = ((size_t)mleaf * kmax + (size_t)kmax * XW) * sizeof(float2);
+  return std::max(up, fin);
+}
+
+bool leaf_ext_fits(int nleaf, int mleaf, int kmax) { return leaf_ext_smem(nleaf, mleaf, kmax) <= 160 * 1024; }
+
+cudaError_t launch_leaf_ext(bool final_part, const Task* leaves, int64_t nleaves, const Slot* slots, int rmax, int nleaf,
+                            int mleaf, int kmax, cudaStream_t st) {
+  if (nleaves <= 0 || rmax <= 0) return cudaSuccess;
+  const size_t smem = leaf_ext_smem(nleaf, mleaf, kmax);
+  auto* k = final_part ? leaf_uf_kernel : leaf_vtx_kernel;
+  static size_t set_up = 0, set_fin = 0;
+  size_t& set = final_part ? set_fin : set_up;
+  if (smem > 48 * 1024 && smem > set) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    set = smem;
+  }
+  const unsigned gy = (unsigned)((rmax + XW - 1) / XW);
+  for (int64_t b = 0; b < nleaves; b += 65535) {
+    const dim3 grid((unsigned)std::min<int64_t>(65535, nleaves - b), gy);
+    k<<<grid, PT, smem, st>>>(leaves + b, slots);
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace hss
