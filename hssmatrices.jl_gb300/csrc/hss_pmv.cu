@@ -921,14 +921,13 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
 
 constexpr int XW = 32;   // columns per block of the leaf kernels
 
-__global__ void __launch_bounds__(PT) leaf_vtx_kernel(const Task* __restrict__ leaves, const Slot* __restrict__ slots) {
+__device__ void leaf_vtx_unit(const Task tk, const Slot* __restrict__ slots, int cb) {
   extern __shared__ __align__(16) unsigned char ext_smem[];
   using P = PDF;
   using Acc = P::Acc;
-  const Task tk = leaves[blockIdx.x];
   const Slot& sl = slots[tk.slot];
   const Node& nd = tk.nodes[tk.node];
-  const int j0 = blockIdx.y * XW;
+  const int j0 = cb * XW;
   if (nd.root || nd.kv == 0 || j0 >= sl.r) return;
   const int n = nd.gn, kv = nd.kv, nc = min(XW, sl.r - j0);
   const int ld = n | 1;             // odd: a warp's rows c (or columns q) fall in distinct bank pairs
@@ -977,14 +976,13 @@ __global__ void __launch_bounds__(PT) leaf_vtx_kernel(const Task* __restrict__ l
   }
 }
 
-__global__ void __launch_bounds__(PT) leaf_uf_kernel(const Task* __restrict__ leaves, const Slot* __restrict__ slots) {
+__device__ void leaf_uf_unit(const Task tk, const Slot* __restrict__ slots, int cb) {
   extern __shared__ __align__(16) unsigned char ext_smem[];
   using P = PDF;
   using Acc = P::Acc;
-  const Task tk = leaves[blockIdx.x];
   const Slot& sl = slots[tk.slot];
   const Node& nd = tk.nodes[tk.node];
-  const int j0 = blockIdx.y * XW;
+  const int j0 = cb * XW;
   if (nd.root || j0 >= sl.r) return;
   const int m = nd.gm, ku = nd.ku, nc = min(XW, sl.r - j0);
   float2* Us = (float2*)ext_smem;   // m x ku, ld m
@@ -1046,6 +1044,19 @@ __global__ void __launch_bounds__(PT) leaf_uf_kernel(const Task* __restrict__ le
         if (lane == 0 && q < nq && v2 != 0.0) atomicAdd(cn + qb + q, v2);
       }
     }
+  }
+}
+
+// Units (leaf, block of XW columns) taken in turn by a grid of resident blocks,
+// so that the last wave is not a partial one.
+template <bool FINAL>
+__global__ void __launch_bounds__(PT, 2) leaf_ext_kernel(const Task* __restrict__ leaves, const Slot* __restrict__ slots,
+                                                      int nunits, int ncb) {
+  for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const Task tk = leaves[u / ncb];
+    if (FINAL) leaf_uf_unit(tk, slots, u % ncb);
+    else leaf_vtx_unit(tk, slots, u % ncb);
+    __syncthreads();   // the shared buffers are reused by the next unit
   }
 }
 
@@ -1608,19 +1619,26 @@ cudaError_t launch_leaf_ext(bool final_part, const Task* leaves, int64_t nleaves
                             int mleaf, int kmax, cudaStream_t st) {
   if (nleaves <= 0 || rmax <= 0) return cudaSuccess;
   const size_t smem = leaf_ext_smem(nleaf, mleaf, kmax);
-  auto* k = final_part ? leaf_uf_kernel : leaf_vtx_kernel;
-  static size_t set_up = 0, set_fin = 0;
-  size_t& set = final_part ? set_fin : set_up;
-  if (smem > 48 * 1024 && smem > set) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  void (*k)(const Task*, const Slot*, int, int) = final_part ? leaf_ext_kernel<true> : leaf_ext_kernel<false>;
+  // resident blocks per SM for this shared-memory size (cached per kernel)
+  static size_t c_smem[2] = {0, 0};
+  static int c_blocks[2] = {0, 0};
+  const int w = final_part ? 1 : 0;
+  if (c_smem[w] != smem || c_blocks[w] <= 0) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
     if (e != cudaSuccess) return e;
-    set = smem;
+    int per_sm = 0, sms = 0, dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, PT, smem)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    c_smem[w] = smem;
+    c_blocks[w] = std::max(1, per_sm * sms);
   }
-  const unsigned gy = (unsigned)((rmax + XW - 1) / XW);
-  for (int64_t b = 0; b < nleaves; b += 65535) {
-    const dim3 grid((unsigned)std::min<int64_t>(65535, nleaves - b), gy);
-    k<<<grid, PT, smem, st>>>(leaves + b, slots);
-  }
+  const int ncb = (rmax + XW - 1) / XW;
+  const int64_t units = nleaves * (int64_t)ncb;
+  if (units > (int64_t)INT32_MAX) return cudaErrorInvalidValue;
+  const unsigned grid = (unsigned)std::min<int64_t>(units, c_blocks[w]);
+  k<<<grid, PT, smem, st>>>(leaves, slots, (int)units, ncb);
   return cudaGetLastError();
 }
 
