@@ -398,6 +398,7 @@ int hss_hssmul(hss_handle hA, hss_handle hB, hss_handle* out, void* stream) {
   std::vector<std::pair<int64_t, int64_t>> ranges;
   for (auto& sg : stages) {
     if (sg.empty()) continue;
+    split_mm_columns(sg);   // wide assembly blocks at the upper levels
     ranges.emplace_back((int64_t)all.size(), (int64_t)sg.size());
     all.insert(all.end(), sg.begin(), sg.end());
   }

@@ -106,10 +106,29 @@ struct Stages {
     else { b.p = X.p ? X.at(0, j0) : nullptr; b.cols = nc; }
     return b;
   }
+  // rows [i0, i0 + nr) of op(X) as a block of X
+  static Blk rows_of(const Blk& X, int tx, int64_t i0, int64_t nr) {
+    Blk b = X;
+    if (tx) { b.p = X.p ? X.at(0, i0) : nullptr; b.cols = nr; }
+    else { b.p = X.p ? X.at(i0, 0) : nullptr; b.rows = nr; }
+    return b;
+  }
+  static constexpr int64_t kRowSlice = 512;
   // C = A1 op B1 (+ A2 op B2): shapes from the blocks, ta / tb transpose
   void gemm(const Blk& C, const Blk& A1, int ta1, const Blk& B1, int tb1, const Blk* A2 = nullptr, int ta2 = 0,
             const Blk* B2 = nullptr, int tb2 = 0) {
     if (C.rows * C.cols == 0) return;
+    if (C.rows > kRowSlice) {
+      for (int64_t i0 = 0; i0 < C.rows; i0 += kRowSlice) {
+        const int64_t nr = std::min(kRowSlice, C.rows - i0);
+        Blk Ci = C; Ci.p = C.at(i0, 0); Ci.rows = nr;
+        const Blk A1i = rows_of(A1, ta1, i0, nr);
+        Blk A2i;
+        if (A2) A2i = rows_of(*A2, ta2, i0, nr);
+        gemm(Ci, A1i, ta1, B1, tb1, A2 ? &A2i : nullptr, ta2, B2, tb2);
+      }
+      return;
+    }
     if (C.cols > kSlice) {
       for (int64_t j0 = 0; j0 < C.cols; j0 += kSlice) {
         const int64_t nc = std::min(kSlice, C.cols - j0);
@@ -152,6 +171,14 @@ struct Stages {
   // a copy-family task (cmode, see MmTask); COPY and AXPY are split in column slices
   void copy_task(const Blk& C, const Blk& A, int ta, int cmode, double a, double beta) {
     if (C.rows * C.cols == 0) return;
+    if ((cmode == MM_COPY || cmode == MM_AXPY) && C.rows > kRowSlice && C.rows * C.cols > kSlice * 64) {
+      for (int64_t i0 = 0; i0 < C.rows; i0 += kRowSlice) {
+        const int64_t nr = std::min(kRowSlice, C.rows - i0);
+        Blk Ci = C; Ci.p = C.at(i0, 0); Ci.rows = nr;
+        copy_task(Ci, rows_of(A, ta, i0, nr), ta, cmode, a, beta);
+      }
+      return;
+    }
     if ((cmode == MM_COPY || cmode == MM_AXPY) && C.cols > kSlice && C.rows * C.cols > kSlice * 64) {
       for (int64_t j0 = 0; j0 < C.cols; j0 += kSlice) {
         const int64_t nc = std::min(kSlice, C.cols - j0);
@@ -190,22 +217,131 @@ struct Stages {
     return e == cudaSuccess ? cudaGetLastError() : e;
   }
   // pivoted QRs of the listed blocks (factored in place); returns their ranks
+  // one launch of pivoted QRs; ranks read back (synchronises st)
+  cudaError_t launch_qr_list(std::vector<PqrTask>& list, std::vector<int32_t>& rk) {
+    rk.assign(list.size(), 0);
+    if (list.empty()) return cudaSuccess;
+    int qm = 1, km = 1;
+    for (const PqrTask& t : list) {
+      qm = std::max(qm, (int)t.q);
+      km = std::max(km, (int)std::min(t.p, t.q));
+    }
+    auto* dr = (int32_t*)ar.raw(list.size() * sizeof(int32_t));
+    auto* d = (PqrTask*)ar.raw(list.size() * sizeof(PqrTask));
+    if (!d || !dr) return ar.err;
+    for (size_t i = 0; i < list.size(); ++i) list[i].rank = dr + i;
+    cudaError_t e = cudaMemcpyAsync(d, list.data(), list.size() * sizeof(PqrTask), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) launch_pqr(d, (int64_t)list.size(), qm, km, st);
+    count_launches(1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rk.data(), dr, list.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+  }
+  // Runs the queued QRs.  A tall block (p >= 1024 rows, p >= 4 q) is factored
+  // as a tall-skinny QR: its row chunks (max(256, 2 q) rows) by unpivoted-rank
+  // QRs in parallel, their R factors stacked and factored with the task's own
+  // tolerances (the column pivoting and the rank decision of the block: the
+  // stacked R's have the block's singular values), then Q = diag(Q_chunk) Q2
+  // by products.  One block-per-task QR of a tall block is the FP64 rate of one
+  // SM; this spreads it over the grid.
   cudaError_t run_qr(std::vector<int32_t>& ranks) {
     ranks.assign(qr.size(), 0);
     if (qr.empty()) return cudaSuccess;
-    auto* dr = (int32_t*)ar.raw(qr.size() * sizeof(int32_t));
-    auto* d = (PqrTask*)ar.raw(qr.size() * sizeof(PqrTask));
-    if (!d || !dr) return ar.err;
-    for (size_t i = 0; i < qr.size(); ++i) qr[i].rank = dr + i;
-    cudaError_t e = cudaMemcpyAsync(d, qr.data(), qr.size() * sizeof(PqrTask), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) launch_pqr(d, (int64_t)qr.size(), qmax, kmax, st);
-    count_launches(1);
-    if (e == cudaSuccess) e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ranks.data(), dr, qr.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    struct Tall { size_t idx; int64_t ch, nch; Blk Rst, Q2, Qc; };
+    std::vector<Tall> tall;
+    std::vector<PqrTask> s1;
+    std::vector<int64_t> s1_owner;   // index into qr, or -1 for a chunk task
+    for (size_t i = 0; i < qr.size(); ++i) {
+      const PqrTask& t = qr[i];
+      if (t.p >= 1024 && t.p >= 4 * (int64_t)t.q) {
+        Tall tl;
+        tl.idx = i;
+        tl.ch = std::max<int64_t>(256, 2 * (int64_t)t.q);
+        tl.nch = (t.p + tl.ch - 1) / tl.ch;
+        tl.Rst = ar.blk(tl.nch * t.q, t.q);
+        tl.Qc = ar.blk(t.p, t.q);
+        tl.Q2 = ar.blk(tl.nch * t.q, t.q);
+        if (!tl.Rst.p || !tl.Qc.p || !tl.Q2.p) return ar.err;
+        zero(tl.Rst);   // rows of chunks of lower rank stay zero
+        zero(tl.Qc);    // and so do the matching columns of their Q
+        tall.push_back(tl);
+      } else {
+        s1.push_back(t);
+        s1_owner.push_back((int64_t)i);
+      }
+    }
+    cudaError_t e = run_mm();
+    if (e != cudaSuccess) return e;
+    for (const Tall& tl : tall) {
+      const PqrTask& t = qr[tl.idx];
+      for (int64_t c = 0; c < tl.nch; ++c) {
+        PqrTask u{};
+        u.G = t.G + c * tl.ch;
+        u.ldg = t.ldg;
+        u.p = (int32_t)std::min<int64_t>(tl.ch, t.p - c * tl.ch);
+        u.q = t.q;
+        u.Q = tl.Qc.p + c * tl.ch;
+        u.ldq = tl.Qc.ld;
+        u.R = tl.Rst.p + c * t.q;
+        u.ldr = tl.Rst.ld;
+        u.atol = 0.0;
+        u.rtol = 0.0;
+        s1.push_back(u);
+        s1_owner.push_back(-1);
+      }
+    }
+    std::vector<int32_t> rk;
+    if ((e = launch_qr_list(s1, rk)) != cudaSuccess) return e;
+    for (size_t j = 0; j < s1.size(); ++j)
+      if (s1_owner[j] >= 0) ranks[(size_t)s1_owner[j]] = rk[j];
+    if (!tall.empty()) {
+      std::vector<PqrTask> s2;
+      for (const Tall& tl : tall) {
+        const PqrTask& t = qr[tl.idx];
+        PqrTask u{};
+        u.G = tl.Rst.p;
+        u.ldg = tl.Rst.ld;
+        u.p = (int32_t)tl.Rst.rows;
+        u.q = t.q;
+        u.Q = tl.Q2.p;
+        u.ldq = tl.Q2.ld;
+        u.R = t.R;
+        u.ldr = t.ldr;
+        u.atol = t.atol;
+        u.rtol = t.rtol;
+        s2.push_back(u);
+      }
+      if ((e = launch_qr_list(s2, rk)) != cudaSuccess) return e;
+      for (size_t j = 0; j < tall.size(); ++j) {
+        const Tall& tl = tall[j];
+        const PqrTask& t = qr[tl.idx];
+        const int32_t r = rk[j];
+        ranks[tl.idx] = r;
+        // Q (p x r) = diag(Q_chunk) Q2[:, 0:r], chunk by chunk
+        for (int64_t c = 0; c < tl.nch; ++c) {
+          const int64_t rows = std::min<int64_t>(tl.ch, t.p - c * tl.ch);
+          Blk Cq;
+          Cq.p = t.Q + c * tl.ch;
+          Cq.ld = t.ldq;
+          Cq.rows = rows;
+          Cq.cols = r;
+          Blk A = tl.Qc;
+          A.p = tl.Qc.p + c * tl.ch;
+          A.rows = rows;
+          A.cols = t.q;
+          Blk Bq = tl.Q2;
+          Bq.p = tl.Q2.p + c * t.q;
+          Bq.rows = t.q;
+          Bq.cols = r;
+          gemm(Cq, A, 0, Bq, 0);
+        }
+      }
+      if ((e = run_mm()) != cudaSuccess) return e;
+    }
     qr.clear();
     qmax = kmax = 1;
-    return e;
+    return cudaSuccess;
   }
   // queue the QR of a copy of G: returns (Q, R) blocks sized for the full rank
   std::pair<Blk, Blk> pqr(const Blk& G, double atol, double rtol) {
@@ -223,6 +359,33 @@ struct Stages {
   }
 };
 
+
+// Splits products and plain copies wider than `slice` columns into column
+// slices (one task each), so that a wide block spreads over many thread blocks.
+inline void split_mm_columns(std::vector<MmTask>& v, int64_t slice = Stages::kSlice) {
+  std::vector<MmTask> out;
+  out.reserve(v.size());
+  for (const MmTask& t : v) {
+    const bool sliceable = t.n > slice && (t.k1 >= 0 || t.cmode == MM_COPY || t.cmode == MM_AXPY);
+    if (!sliceable) {
+      out.push_back(t);
+      continue;
+    }
+    for (int64_t j0 = 0; j0 < t.n; j0 += slice) {
+      MmTask u = t;
+      u.n = (int32_t)std::min<int64_t>(slice, t.n - j0);
+      u.C = t.C + j0 * (int64_t)t.ldc;
+      if (t.k1 >= 0) {
+        if (t.B1) u.B1 = t.tb1 ? t.B1 + j0 : t.B1 + j0 * (int64_t)t.ldb1;
+        if (t.B2) u.B2 = t.tb2 ? t.B2 + j0 : t.B2 + j0 * (int64_t)t.ldb2;
+      } else if (t.A1) {
+        u.A1 = t.ta1 ? t.A1 + j0 : t.A1 + j0 * (int64_t)t.lda1;
+      }
+      out.push_back(u);
+    }
+  }
+  v.swap(out);
+}
 
 // orthonormalize_generators! and (unless ortho_only) recompress! of a
 // single-tree handle into a new handle with the same node numbering.
