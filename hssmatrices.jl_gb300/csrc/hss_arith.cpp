@@ -436,6 +436,7 @@ int recompress_impl(hss_plan_s* h, double atol, double rtol, bool ortho_only, hs
   const std::vector<Node>& N = plan_nodes(h);
   const int64_t nn = (int64_t)N.size();
   Arena ar;
+  ar.on_stream(st);
   Stages S{st, ar, {}, {}};
   struct G { Blk D, U, V, B12, B21, R1, R2, W1, W2, RU, RV; };
   std::vector<G> g(nn);

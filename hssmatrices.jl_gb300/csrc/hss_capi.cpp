@@ -1621,6 +1621,32 @@ cudaError_t dev_alloc(void** p, size_t bytes) {
   return cudaMalloc(p, bytes);
 }
 
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t st) {
+  int64_t k = g_fail_alloc.load();
+  while (k > 0) {
+    if (g_fail_alloc.compare_exchange_weak(k, k - 1)) {
+      if (k == 1) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  // the device's default pool keeps up to 4 GB of freed blocks for reuse
+  // (a setting of this process's pool, not of the device)
+  static bool pool_set[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !pool_set[dev]) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = uint64_t(4) << 30;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pool_set[dev] = true;
+  }
+  return cudaMallocAsync(p, bytes, st);
+}
+
 int plan_create_device(int64_t nnodes, const int64_t* table, int64_t npacked, hss_plan_s** out, double** d_gen) {
   *out = nullptr;
   *d_gen = nullptr;

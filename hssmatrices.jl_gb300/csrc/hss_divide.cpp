@@ -248,6 +248,7 @@ int transpose_impl(const hss_plan_s* h, PlanPtr& out, cudaStream_t st) {
   const std::vector<Gen> a = plan_views(h);
   const std::vector<Node>& N = plan_nodes(h);
   Arena ar;
+  ar.on_stream(st);
   ar.rg = &rg;
   Stages T{st, ar, {}, {}};
   T.rg = &rg;
@@ -359,6 +360,7 @@ int ldiv_impl(hss_plan_s* hA, hss_plan_s* hB, double atol, double rtol, PlanPtr&
       if (NB[t].gm != want) return set_error(HSS_ERR_BAD_DIMS, "division: unexpected block rows");
     }
     Arena ar;
+    ar.on_stream(st);
     ar.rg = &rg;
     Stages S{st, ar, {}, {}};
     S.rg = &rg;
@@ -580,6 +582,7 @@ int ldiv_impl(hss_plan_s* hA, hss_plan_s* hB, double atol, double rtol, PlanPtr&
   if (top < H) {
     // the early exit: V-transforms of Y0 at level `top`, no recompression
     Arena ar;
+    ar.on_stream(st);
     ar.rg = &rg;
     DivList dv;
     dv.rg = &rg;
@@ -636,6 +639,7 @@ int ldiv_impl(hss_plan_s* hA, hss_plan_s* hB, double atol, double rtol, PlanPtr&
     std::vector<Gen> gz;
     if ((rc = make_plan(SZ, Z, gz, &rg))) return rc;
     Arena ar;
+    ar.on_stream(st);
     ar.rg = &rg;
     Stages S{st, ar, {}, {}};
     S.rg = &rg;

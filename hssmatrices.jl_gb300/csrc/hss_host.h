@@ -18,6 +18,8 @@ namespace hss {
 // while a failure is armed (hss_set_option(HSS_OPT_FAIL_ALLOC, k)), the k-th
 // call from then on returns cudaErrorMemoryAllocation without reaching the driver.
 cudaError_t dev_alloc(void** p, size_t bytes);
+// The same from the device's stream-ordered pool on st (freed with cudaFreeAsync).
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t st);
 
 // Grow-only device buffer.
 template <typename T>

@@ -48,9 +48,16 @@ struct Ranges {
   }
 };
 
-// Device memory for the intermediate blocks: chunks of at least 64 MB, freed together.
+// Device memory for the intermediate blocks: chunks of at least 64 MB (16 MB
+// from the stream-ordered pool), freed together.
 struct Arena {
   Ranges* rg = nullptr;   // chunks are registered here when set
+  bool async = false;     // chunks from the pool, ordered on `ast`
+  cudaStream_t ast = nullptr;
+  void on_stream(cudaStream_t s) {
+    async = true;
+    ast = s;
+  }
   std::vector<void*> chunks;
   char* cur = nullptr;
   size_t left = 0;
@@ -58,9 +65,9 @@ struct Arena {
   void* raw(size_t bytes) {
     bytes = (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
     if (bytes > left) {
-      const size_t sz = std::max<size_t>(bytes, size_t(64) << 20);
+      const size_t sz = std::max<size_t>(bytes, size_t(async ? 16 : 64) << 20);
       void* q = nullptr;
-      const cudaError_t e = dev_alloc(&q, sz);
+      const cudaError_t e = async ? dev_alloc_async(&q, sz, ast) : dev_alloc(&q, sz);
       if (e != cudaSuccess) { err = e; return nullptr; }
       chunks.push_back(q);
       if (rg) rg->add(q, sz);
@@ -81,7 +88,10 @@ struct Arena {
     return b;
   }
   ~Arena() {
-    for (void* q : chunks) cudaFree(q);
+    for (void* q : chunks) {
+      if (async) cudaFreeAsync(q, ast);
+      else cudaFree(q);
+    }
   }
 };
 
@@ -217,9 +227,9 @@ struct Stages {
     return e == cudaSuccess ? cudaGetLastError() : e;
   }
   // pivoted QRs of the listed blocks (factored in place); returns their ranks
-  // one launch of pivoted QRs; ranks read back (synchronises st)
-  cudaError_t launch_qr_list(std::vector<PqrTask>& list, std::vector<int32_t>& rk) {
-    rk.assign(list.size(), 0);
+  // one launch of pivoted QRs; with `rk`, the ranks are read back (synchronises st)
+  cudaError_t launch_qr_list(std::vector<PqrTask>& list, std::vector<int32_t>* rk) {
+    if (rk) rk->assign(list.size(), 0);
     if (list.empty()) return cudaSuccess;
     int qm = 1, km = 1;
     for (const PqrTask& t : list) {
@@ -234,37 +244,52 @@ struct Stages {
     if (e == cudaSuccess) launch_pqr(d, (int64_t)list.size(), qm, km, st);
     count_launches(1);
     if (e == cudaSuccess) e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(rk.data(), dr, list.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (rk) {
+      if (e == cudaSuccess) e = cudaMemcpyAsync(rk->data(), dr, list.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    } else if (e == cudaSuccess) {
+      // the host copy of the task list must outlive the asynchronous upload
+      e = cudaStreamSynchronize(st);
+    }
     return e;
   }
+  static bool tall_block(int64_t p, int64_t q) { return p >= 1024 && p >= 4 * q; }
   // Runs the queued QRs.  A tall block (p >= 1024 rows, p >= 4 q) is factored
-  // as a tall-skinny QR: its row chunks (max(256, 2 q) rows) by unpivoted-rank
-  // QRs in parallel, their R factors stacked and factored with the task's own
-  // tolerances (the column pivoting and the rank decision of the block: the
-  // stacked R's have the block's singular values), then Q = diag(Q_chunk) Q2
-  // by products.  One block-per-task QR of a tall block is the FP64 rate of one
-  // SM; this spreads it over the grid.
+  // as a tall-skinny QR: its row chunks (4 q rows, at least 256) by
+  // unpivoted-rank QRs in parallel, their R factors stacked, and the stack
+  // reduced the same way while it is tall; the last stack is factored with the
+  // task's own tolerances (the column pivoting and the rank decision of the
+  // block: the stacked R's keep its singular values), and Q is assembled back
+  // down the levels, Q_l = diag(Q_chunk) Q_{l+1}, by products.  A block-per-task
+  // QR of a tall block runs at one SM's FP64 rate; this spreads it over the grid.
   cudaError_t run_qr(std::vector<int32_t>& ranks) {
     ranks.assign(qr.size(), 0);
     if (qr.empty()) return cudaSuccess;
-    struct Tall { size_t idx; int64_t ch, nch; Blk Rst, Q2, Qc; };
+    struct Lev { Blk G, Qc, Rst; int64_t ch, nch; };   // one reduction level of a tall task
+    struct Tall { size_t idx; std::vector<Lev> lev; Blk Qf; };
     std::vector<Tall> tall;
     std::vector<PqrTask> s1;
-    std::vector<int64_t> s1_owner;   // index into qr, or -1 for a chunk task
+    std::vector<int64_t> s1_owner;
     for (size_t i = 0; i < qr.size(); ++i) {
       const PqrTask& t = qr[i];
-      if (t.p >= 1024 && t.p >= 4 * (int64_t)t.q) {
+      if (tall_block(t.p, t.q)) {
         Tall tl;
         tl.idx = i;
-        tl.ch = std::max<int64_t>(256, 2 * (int64_t)t.q);
-        tl.nch = (t.p + tl.ch - 1) / tl.ch;
-        tl.Rst = ar.blk(tl.nch * t.q, t.q);
-        tl.Qc = ar.blk(t.p, t.q);
-        tl.Q2 = ar.blk(tl.nch * t.q, t.q);
-        if (!tl.Rst.p || !tl.Qc.p || !tl.Q2.p) return ar.err;
-        zero(tl.Rst);   // rows of chunks of lower rank stay zero
-        zero(tl.Qc);    // and so do the matching columns of their Q
+        Blk G;
+        G.p = t.G; G.ld = t.ldg; G.rows = t.p; G.cols = t.q;
+        while (tall_block(G.rows, G.cols)) {
+          Lev L;
+          L.G = G;
+          L.ch = std::max<int64_t>(256, 4 * G.cols);
+          L.nch = (G.rows + L.ch - 1) / L.ch;
+          L.Qc = ar.blk(G.rows, G.cols);
+          L.Rst = ar.blk(L.nch * G.cols, G.cols);
+          if (!L.Qc.p || !L.Rst.p) return ar.err;
+          zero(L.Qc);    // columns of chunks of lower rank stay zero
+          zero(L.Rst);   // and so do the matching rows of their R
+          tl.lev.push_back(L);
+          G = L.Rst;
+        }
         tall.push_back(tl);
       } else {
         s1.push_back(t);
@@ -273,69 +298,97 @@ struct Stages {
     }
     cudaError_t e = run_mm();
     if (e != cudaSuccess) return e;
-    for (const Tall& tl : tall) {
-      const PqrTask& t = qr[tl.idx];
-      for (int64_t c = 0; c < tl.nch; ++c) {
+    // the small tasks, with every tall task's first level
+    std::vector<int32_t> rk;
+    auto chunk_tasks = [&](const Lev& L, std::vector<PqrTask>& out) {
+      for (int64_t c = 0; c < L.nch; ++c) {
         PqrTask u{};
-        u.G = t.G + c * tl.ch;
-        u.ldg = t.ldg;
-        u.p = (int32_t)std::min<int64_t>(tl.ch, t.p - c * tl.ch);
-        u.q = t.q;
-        u.Q = tl.Qc.p + c * tl.ch;
-        u.ldq = tl.Qc.ld;
-        u.R = tl.Rst.p + c * t.q;
-        u.ldr = tl.Rst.ld;
+        u.G = L.G.p + c * L.ch;
+        u.ldg = L.G.ld;
+        u.p = (int32_t)std::min<int64_t>(L.ch, L.G.rows - c * L.ch);
+        u.q = (int32_t)L.G.cols;
+        u.Q = L.Qc.p + c * L.ch;
+        u.ldq = L.Qc.ld;
+        u.R = L.Rst.p + c * L.G.cols;
+        u.ldr = L.Rst.ld;
         u.atol = 0.0;
         u.rtol = 0.0;
-        s1.push_back(u);
-        s1_owner.push_back(-1);
+        out.push_back(u);
       }
+    };
+    for (const Tall& tl : tall) chunk_tasks(tl.lev[0], s1);
+    if ((e = launch_qr_list(s1, s1_owner.empty() ? nullptr : &rk)) != cudaSuccess) return e;
+    for (size_t j = 0; j < s1_owner.size(); ++j) ranks[(size_t)s1_owner[j]] = rk[j];
+    if (tall.empty()) {
+      qr.clear();
+      qmax = kmax = 1;
+      return cudaSuccess;
     }
-    std::vector<int32_t> rk;
-    if ((e = launch_qr_list(s1, rk)) != cudaSuccess) return e;
-    for (size_t j = 0; j < s1.size(); ++j)
-      if (s1_owner[j] >= 0) ranks[(size_t)s1_owner[j]] = rk[j];
-    if (!tall.empty()) {
-      std::vector<PqrTask> s2;
-      for (const Tall& tl : tall) {
-        const PqrTask& t = qr[tl.idx];
-        PqrTask u{};
-        u.G = tl.Rst.p;
-        u.ldg = tl.Rst.ld;
-        u.p = (int32_t)tl.Rst.rows;
-        u.q = t.q;
-        u.Q = tl.Q2.p;
-        u.ldq = tl.Q2.ld;
-        u.R = t.R;
-        u.ldr = t.ldr;
-        u.atol = t.atol;
-        u.rtol = t.rtol;
-        s2.push_back(u);
-      }
-      if ((e = launch_qr_list(s2, rk)) != cudaSuccess) return e;
+    // the further reduction levels, all tall tasks together
+    size_t maxlev = 0;
+    for (const Tall& tl : tall) maxlev = std::max(maxlev, tl.lev.size());
+    for (size_t l = 1; l < maxlev; ++l) {
+      std::vector<PqrTask> sl;
+      for (const Tall& tl : tall)
+        if (l < tl.lev.size()) chunk_tasks(tl.lev[l], sl);
+      if ((e = launch_qr_list(sl, nullptr)) != cudaSuccess) return e;
+    }
+    // the last stacks, with the tasks' tolerances
+    std::vector<PqrTask> s2;
+    for (Tall& tl : tall) {
+      const PqrTask& t = qr[tl.idx];
+      const Blk& last = tl.lev.back().Rst;
+      tl.Qf = ar.blk(last.rows, last.cols);
+      if (!tl.Qf.p) return ar.err;
+      PqrTask u{};
+      u.G = last.p;
+      u.ldg = last.ld;
+      u.p = (int32_t)last.rows;
+      u.q = (int32_t)last.cols;
+      u.Q = tl.Qf.p;
+      u.ldq = tl.Qf.ld;
+      u.R = t.R;
+      u.ldr = t.ldr;
+      u.atol = t.atol;
+      u.rtol = t.rtol;
+      s2.push_back(u);
+    }
+    if ((e = launch_qr_list(s2, &rk)) != cudaSuccess) return e;
+    // Q back down the levels: Q_l = diag(chunk Q of level l) Q_{l+1} (r columns)
+    for (size_t j = 0; j < tall.size(); ++j) ranks[tall[j].idx] = rk[j];
+    for (size_t l = maxlev; l-- > 0;) {
       for (size_t j = 0; j < tall.size(); ++j) {
-        const Tall& tl = tall[j];
+        Tall& tl = tall[j];
+        if (l >= tl.lev.size()) continue;
         const PqrTask& t = qr[tl.idx];
         const int32_t r = rk[j];
-        ranks[tl.idx] = r;
-        // Q (p x r) = diag(Q_chunk) Q2[:, 0:r], chunk by chunk
-        for (int64_t c = 0; c < tl.nch; ++c) {
-          const int64_t rows = std::min<int64_t>(tl.ch, t.p - c * tl.ch);
-          Blk Cq;
-          Cq.p = t.Q + c * tl.ch;
-          Cq.ld = t.ldq;
+        const Lev& L = tl.lev[l];
+        const Blk Qn = tl.Qf;   // Q of the level above (rows = L.nch * q), r columns used
+        Blk Out;
+        if (l == 0) {
+          Out.p = t.Q; Out.ld = t.ldq;
+        } else {
+          Out = ar.blk(L.G.rows, L.G.cols);
+          if (!Out.p) return ar.err;
+        }
+        Out.rows = L.G.rows;
+        Out.cols = r;
+        for (int64_t c = 0; c < L.nch; ++c) {
+          const int64_t rows = std::min<int64_t>(L.ch, L.G.rows - c * L.ch);
+          Blk Cq = Out;
+          Cq.p = Out.p + c * L.ch;
           Cq.rows = rows;
-          Cq.cols = r;
-          Blk A = tl.Qc;
-          A.p = tl.Qc.p + c * tl.ch;
+          Blk A = L.Qc;
+          A.p = L.Qc.p + c * L.ch;
           A.rows = rows;
-          A.cols = t.q;
-          Blk Bq = tl.Q2;
-          Bq.p = tl.Q2.p + c * t.q;
-          Bq.rows = t.q;
+          A.cols = L.G.cols;
+          Blk Bq = Qn;
+          Bq.p = Qn.p + c * L.G.cols;
+          Bq.rows = L.G.cols;
           Bq.cols = r;
           gemm(Cq, A, 0, Bq, 0);
         }
+        tl.Qf = Out;
       }
       if ((e = run_mm()) != cudaSuccess) return e;
     }
