@@ -54,7 +54,7 @@ EXPORTS = [
     "hss_batcher_create", "hss_batcher_destroy", "hss_batcher_factor", "hss_batcher_solve",
     "hss_sample", "hss_sumsq", "hss_rc_create", "hss_rc_destroy", "hss_rc_size", "hss_rc_compress",
     "hss_rc_ranks", "hss_rc_sample", "hss_export_size", "hss_export", "hss_getindex", "hss_full", "hss_hssmul", "hss_recompress", "hss_orthonormalize",
-    "hss_device_bytes", "hss_transpose", "hss_matmul_t", "hss_ldiv", "hss_rdiv",
+    "hss_device_bytes", "hss_transpose", "hss_matmul_t", "hss_ldiv", "hss_rdiv", "hss_ulvfactsolve",
 ]
 
 
@@ -106,6 +106,7 @@ def _declare(lib):
         "hss_factor_destroy": (C.c_int, [P]),
         "hss_ulvsolve": (C.c_int, [P, P, I64, I64, P, I64, D, I32, C.POINTER(SolveStats), P]),
         "hss_ulvsolve_host": (C.c_int, [P, PD, I64, I64, PD, I64, D, I32, C.POINTER(SolveStats)]),
+        "hss_ulvfactsolve": (C.c_int, [P, P, I64, I64, P, I64, D, I32, C.POINTER(SolveStats), P]),
         "hss_ulvsolve_batch": (C.c_int, [P, C.POINTER(P), PI64, PI64, C.POINTER(P), PI64, D, I32,
                                          C.POINTER(SolveStats), P]),
         "hss_ulvfactsolve_host": (C.c_int, [P, I32, PD, I64, I64, PD, I64, D, I32, C.POINTER(SolveStats)]),

@@ -236,7 +236,15 @@ struct hss_factor_s {
   SlotTable fac_slots;
   SolveBufs bufs;
   DBuf<double> hB, hX;                  // staging for the _host solve
+  // the pipelined factorization + first solve (hss_ulvfactsolve): a second
+  // stream for the upward solve and events [fork, join, level 0, level 1, ...]
+  cudaStream_t pipe_st = nullptr;
+  std::vector<cudaEvent_t> pipe_ev;
+  GraphCache pipe_graph;
   ~hss_factor_s() {
+    pipe_graph.reset();
+    for (cudaEvent_t e : pipe_ev) cudaEventDestroy(e);
+    if (pipe_st) cudaStreamDestroy(pipe_st);
     if (d_fac) cudaFree(d_fac);
   }
 };
@@ -917,25 +925,36 @@ int ensure_df(hss_plan_s* P, cudaStream_t st) {
 
 // Returns true when every level ran the on-chip kernel (for FP32 the blocked
 // reduction, whose factors also carry the panel T matrices and L1 block inverses).
+// merge staging of a factor level: converted generators, children's reduced U/V, T12/T21
+inline size_t factor_extra(const Seg& g) {
+  return (size_t)g.c1u * g.c2v + (size_t)g.c2u * g.c1v + (size_t)(g.c1u + g.c2u) * g.kumax +
+         (size_t)(g.c1v + g.c2v) * g.kvmax + (size_t)g.c1mr * g.c1u + (size_t)g.c2mr * g.c2u +
+         (size_t)g.c1nr * g.c1v + (size_t)g.c2nr * g.c2v + (size_t)g.c1mr * g.c2v + (size_t)g.c2mr * g.c1v;
+}
+
+template <typename T>
+bool factor_level_fast(const Seg& g) {
+  return !g_generic_factor && factor_blk_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, factor_extra(g));
+}
+
+// One factor level (h = tree height); true when it ran the on-chip kernel.
+template <typename T>
+bool run_factor_level(const Levels& L, size_t h, const Slot* slots, cudaStream_t st) {
+  const Seg& g = (*L.by_h)[h];
+  const bool fast = factor_level_fast<T>(g);
+  traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, g.cnt, st, [&] {
+    if (fast)
+      launch_ulv_factor_blk<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, g.kvmax, factor_extra(g), st);
+    else
+      launch_ulv_factor<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
+  });
+  return fast;
+}
+
 template <typename T>
 bool run_factor(const Levels& L, const Slot* slots, cudaStream_t st) {
   bool all_fast = true;
-  for (size_t h = 0; h < L.by_h->size(); ++h) {
-    const Seg& g = (*L.by_h)[h];
-    traced(h == 0 ? HSS_TRACE_FACTOR_LEAF : HSS_TRACE_FACTOR_MERGE, g.cnt, st, [&] {
-      // merge staging: converted generators, children's reduced U/V, T12/T21
-      const size_t extra = (size_t)g.c1u * g.c2v + (size_t)g.c2u * g.c1v + (size_t)(g.c1u + g.c2u) * g.kumax +
-                           (size_t)(g.c1v + g.c2v) * g.kvmax + (size_t)g.c1mr * g.c1u + (size_t)g.c2mr * g.c2u +
-                           (size_t)g.c1nr * g.c1v + (size_t)g.c2nr * g.c2v + (size_t)g.c1mr * g.c2v +
-                           (size_t)g.c2mr * g.c1v;
-      if (!g_generic_factor && factor_blk_fits<T>(g.mmax, g.nmax, g.kumax, g.kvmax, extra)) {
-        launch_ulv_factor_blk<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, g.kumax, g.kvmax, extra, st);
-      } else {
-        launch_ulv_factor<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, st);
-        all_fast = false;
-      }
-    });
-  }
+  for (size_t h = 0; h < L.by_h->size(); ++h) all_fast = run_factor_level<T>(L, h, slots, st) && all_fast;
   return all_fast;
 }
 
@@ -963,21 +982,35 @@ inline bool pick_bsolve(bool blocked, const Seg& g, const std::vector<int8_t>* t
 // blocked: the factors come from the blocked FP32 reduction (T = float only);
 // tf: the factor whose tuned choices apply (the plan's own task lists), or null.
 template <typename T>
+void run_solve_up_level(const Levels& L, size_t h, const Slot* slots, int rmax, cudaStream_t st, bool blocked,
+                        const std::vector<int8_t>* tup) {
+  const Seg& g = (*L.by_h)[h];
+  traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
+    if (pick_bsolve(blocked, g, tup, h))
+      launch_bsolve_up(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g), rmax, st);
+    else if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
+      launch_ulv_solve_up_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.sv_stage, rmax, st);
+    else
+      launch_ulv_solve_up<T>(L.d_tasks + g.off, g.cnt, slots, st);
+  });
+}
+
+template <typename T>
+void run_solve_down(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, bool blocked,
+                    const std::vector<int8_t>* tdn);
+
+template <typename T>
 void run_solve(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, bool blocked = false,
                const hss_factor_s* tf = nullptr) {
   const std::vector<int8_t>* tup = tf ? &tf->tune_up : nullptr;
   const std::vector<int8_t>* tdn = tf ? &tf->tune_down : nullptr;
-  for (size_t h = 0; h < L.by_h->size(); ++h) {
-    const Seg& g = (*L.by_h)[h];
-    traced(HSS_TRACE_SOLVE_UP, g.cnt, st, [&] {
-      if (pick_bsolve(blocked, g, tup, h))
-        launch_bsolve_up(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.nmax, seg_kmax(g), seg_kvmax(g), rmax, st);
-      else if (!g_generic_factor && solve_reg_fits(g.mmax, g.nmax))
-        launch_ulv_solve_up_reg<T>(L.d_tasks + g.off, g.cnt, slots, g.mmax, g.sv_stage, rmax, st);
-      else
-        launch_ulv_solve_up<T>(L.d_tasks + g.off, g.cnt, slots, st);
-    });
-  }
+  for (size_t h = 0; h < L.by_h->size(); ++h) run_solve_up_level<T>(L, h, slots, rmax, st, blocked, tup);
+  run_solve_down<T>(L, slots, rmax, st, blocked, tdn);
+}
+
+template <typename T>
+void run_solve_down(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, bool blocked,
+                    const std::vector<int8_t>* tdn) {
   for (size_t d = 0; d < L.by_d->size(); ++d) {
     const Seg& g = (*L.by_d)[d];
     traced(HSS_TRACE_SOLVE_DOWN, g.cnt, st, [&] {
@@ -1284,6 +1317,80 @@ int solve_pass(const std::vector<Item>& items, const Levels& L, const double* sc
   return HSS_OK;
 }
 
+// The factorization of f's plan and the first solve pass of `items` (all on
+// f's plan) in one launch sequence: level h is factored on st, then the
+// upward solve of level h runs on a second stream once that level is done
+// (an event per level), so the upward solve runs one level behind the
+// factorization instead of after it; the downward solve follows both on st.
+// Replayed as one CUDA graph (fork and join through events) where graphs apply.
+template <typename T>
+int factsolve_pass(hss_factor_s* f, const std::vector<Item>& items, const Levels& L, const double* scale,
+                   const int64_t* off, int64_t rtot, SlotTable& table, cudaStream_t st) {
+  hss_plan_s* P = f->plan;
+  int64_t rmax = 0;
+  for (auto& it : items) rmax = std::max(rmax, it.io.r);
+  std::vector<Slot> fsl(P->ntrees);
+  for (Slot& x : fsl) {
+    std::memset(&x, 0, sizeof(Slot));
+    x.fbase = f->d_fac;
+    x.err = P->d_err;
+  }
+  CUDA_TRY(f->fac_slots.upload(fsl, st));
+  std::vector<Slot> s(items.size());
+  for (size_t i = 0; i < items.size(); ++i) {
+    const Item& it = items[i];
+    CUDA_TRY(it.f->sv_ws.ensure((size_t)P->ws_sv * std::max<int64_t>(rmax, 1) * sizeof(T)));
+    Slot& x = s[i];
+    std::memset(&x, 0, sizeof(Slot));
+    x.B = it.io.B; x.ldb = it.io.ldb;
+    x.C = it.io.C; x.ldc = it.io.ldc;
+    x.ws = it.f->sv_ws.p; x.ldws = P->ws_sv;
+    x.fbase = f->d_fac;
+    x.colscale = scale ? scale + off[i] : nullptr;
+    x.colinv = scale ? scale + rtot + off[i] : nullptr;
+    x.r = (int32_t)it.io.r;
+    x.mode = 0;
+    x.err = P->d_err;
+  }
+  CUDA_TRY(table.upload(s, st));
+  bool all_fast = true;
+  for (size_t h = 0; h < L.by_h->size(); ++h) all_fast = factor_level_fast<T>((*L.by_h)[h]) && all_fast;
+  const bool blocked = all_fast && sizeof(T) == sizeof(float);
+  if (!f->pipe_st) CUDA_TRY(cudaStreamCreateWithFlags(&f->pipe_st, cudaStreamNonBlocking));
+  while (f->pipe_ev.size() < 2 + L.by_h->size()) {
+    cudaEvent_t e = nullptr;
+    CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    f->pipe_ev.push_back(e);
+  }
+  uint64_t key = fnv(levels_key(L, f->fac_slots.dev.p, (int64_t)sizeof(T) + (g_generic_factor ? 16 : 0)),
+                     levels_key(L, table.dev.p, rmax * 64 + (blocked ? 1 : 0) + (sizeof(T) == 4 ? 2 : 0)));
+  for (const std::vector<int8_t>* v : {&f->tune_up, &f->tune_down})
+    for (int8_t c : *v) key = fnv(key, (uint64_t)(c + 2));
+  bool unused = false;
+  cudaError_t ev_err = cudaSuccess;
+  auto chk = [&](cudaError_t e) { if (e != cudaSuccess && ev_err == cudaSuccess) ev_err = e; };
+  int rc = graphed(f->pipe_graph, key, st, unused, [&] {
+    cudaStream_t s2 = f->pipe_st;
+    chk(cudaEventRecord(f->pipe_ev[0], st));
+    chk(cudaStreamWaitEvent(s2, f->pipe_ev[0], 0));
+    for (size_t h = 0; h < L.by_h->size(); ++h) {
+      run_factor_level<T>(L, h, f->fac_slots.dev.p, st);
+      chk(cudaEventRecord(f->pipe_ev[2 + h], st));
+      chk(cudaStreamWaitEvent(s2, f->pipe_ev[2 + h], 0));
+      run_solve_up_level<T>(L, h, table.dev.p, (int)rmax, s2, blocked, &f->tune_up);
+    }
+    chk(cudaEventRecord(f->pipe_ev[1], s2));
+    chk(cudaStreamWaitEvent(st, f->pipe_ev[1], 0));
+    run_solve_down<T>(L, table.dev.p, (int)rmax, st, blocked, &f->tune_down);
+    return true;
+  });
+  if (rc) return rc;
+  if (ev_err != cudaSuccess) return cuda_fail(ev_err, "pipelined factorization events");
+  f->blocked = blocked;
+  CUDA_TRY(cudaGetLastError());
+  return HSS_OK;
+}
+
 int read_dev_err(hss_plan_s* P, cudaStream_t st) {
   int32_t e = 0;
   CUDA_TRY(cudaMemcpyAsync(&e, P->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -1306,7 +1413,8 @@ int read_dev_err(hss_plan_s* P, cudaStream_t st) {
 // Solve every item, then refine (FP32 factors, or FP64 with tol > 0) until the
 // largest relative residual over all columns of all items is <= tol.
 int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, double tol, int32_t maxit,
-                hss_solve_stats* stats, cudaStream_t st, const hss_factor_s* tf = nullptr) {
+                hss_solve_stats* stats, cudaStream_t st, const hss_factor_s* tf = nullptr,
+                hss_factor_s* fuse = nullptr) {
   if (items.empty()) return HSS_OK;
   const int prec = items[0].f->prec;
   for (auto& it : items)
@@ -1324,7 +1432,12 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     xoff[i + 1] = xoff[i] + items[i].io.r * P->tree_n[items[i].tree];
   }
   const int64_t rtot = off[ni];
-  if (rtot == 0) { if (stats) stats->converged = 1; return HSS_OK; }
+  if (rtot == 0) {
+    if (stats) stats->converged = 1;
+    if (fuse)
+      return fuse->prec == HSS_PREC_FP32 ? factor_impl<float>(fuse, st) : factor_impl<double>(fuse, st);
+    return HSS_OK;
+  }
   int64_t rmax = 0;
   for (auto& it : items) rmax = std::max(rmax, it.io.r);
   const double* scale = nullptr;
@@ -1348,8 +1461,11 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     }
     CUDA_TRY(cudaMemcpyAsync(B.h_bn2.p, B.bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
-  int rc = fp32 ? solve_pass<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf)
-                : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf);
+  // fuse: the factorization of fuse's plan runs first, pipelined with this pass
+  int rc = fuse ? (fp32 ? factsolve_pass<float>(fuse, items, L, scale, off.data(), rtot, B.sv0, st)
+                        : factsolve_pass<double>(fuse, items, L, scale, off.data(), rtot, B.sv0, st))
+                : (fp32 ? solve_pass<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf)
+                        : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf));
   if (rc) return rc;
   if (!refine) return HSS_OK;
   // refinement: R = b - A x (double-float product for FP32 factors unless
@@ -1445,13 +1561,13 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
 }
 
 int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t maxit,
-               hss_solve_stats* stats, cudaStream_t st) {
+               hss_solve_stats* stats, cudaStream_t st, bool refactor = false) {
   hss_plan_s* P = f->plan;
   int rc = check_cols(P, io, true);
   if (rc) return rc;
   std::vector<Item> items;
   for (int32_t t = 0; t < P->ntrees; ++t) items.push_back(Item{f, t, io[t]});
-  return solve_items(items, plan_levels(P), f->bufs, tol, maxit, stats, st, f);
+  return solve_items(items, plan_levels(P), f->bufs, tol, maxit, stats, st, f, refactor ? f : nullptr);
 }
 
 // Per-launch times (ms) of the traced kind since hss_trace_begin, in launch order.
@@ -2041,6 +2157,14 @@ int hss_ulvsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double*
   return solve_impl(f, {Cols{dB, ldb, r, dX, ldx}}, tol, maxit, stats, (cudaStream_t)stream);
 }
 
+int hss_ulvfactsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double* dX, int64_t ldx, double tol,
+                     int32_t maxit, hss_solve_stats* stats, void* stream) {
+  if (!f) return fail(HSS_ERR_INVALID, "null factor");
+  if (f->plan->ntrees != 1) return fail(HSS_ERR_INVALID, "the fused factorization and solve take a single matrix");
+  CUDA_TRY(cudaSetDevice(f->plan->device));
+  return solve_impl(f, {Cols{dB, ldb, r, dX, ldx}}, tol, maxit, stats, (cudaStream_t)stream, true);
+}
+
 int hss_ulvsolve_batch(hss_factor f, const double* const* dB, const int64_t* ldb, const int64_t* r,
                        double* const* dX, const int64_t* ldx, double tol, int32_t maxit,
                        hss_solve_stats* stats, void* stream) {
@@ -2080,10 +2204,27 @@ int hss_ulvfactsolve_host(hss_handle h, int32_t precision, const double* B, int6
   // the factorization is recomputed on every call; only its storage is reused
   int rc;
   hss_factor& f = h->fused[precision];
-  if (f == nullptr) rc = hss_ulvfactor(h, precision, &f, nullptr);
-  else rc = hss_ulvrefactor(f, nullptr);
-  if (rc) return rc;
-  return hss_ulvsolve_host(f, B, ldb, r, X, ldx, tol, maxit, stats);
+  if (f == nullptr) {
+    rc = hss_ulvfactor(h, precision, &f, nullptr);
+    if (rc) return rc;
+    return hss_ulvsolve_host(f, B, ldb, r, X, ldx, tol, maxit, stats);
+  }
+  // later calls: the factorization pipelined with the first solve pass
+  const int64_t m = h->tree_m[0], n = h->tree_n[0];
+  std::vector<Cols> io{Cols{B, ldb, r, X, ldx}};
+  if ((rc = check_cols(h, io, true))) return rc;
+  cudaStream_t st = 0;
+  if ((rc = copy_in(f->hB, B, m, ldb, r, st))) return rc;
+  CUDA_TRY(f->hX.ensure((size_t)n * std::max<int64_t>(r, 1)));
+  rc = solve_impl(f, {Cols{f->hB.p, m, r, f->hX.p, n}}, tol, maxit, stats, st, true);
+  if (rc && rc != HSS_ERR_NO_CONVERGENCE) return rc;
+  if (r > 0) {
+    int rc2 = copy_out(X, ldx, f->hX.p, n, r, st);
+    if (rc2) return rc2;
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (!rc) rc = read_dev_err(h, st);
+  return rc;
 }
 
 int hss_batcher_create(hss_batcher* out) {

@@ -265,6 +265,15 @@ class UlvFactor:
                                     int(maxit), C.byref(self.stats), _stream(stream)))
         return self.stats
 
+    def factsolve_device(self, dB, ldb, r, dX, ldx, tol=None, maxit=10, stream=None):
+        """Refactor (the generators may have changed) and solve in one call
+        (``hss_ulvfactsolve``): the first solve's upward sweep runs one tree level
+        behind the factorization on a second stream."""
+        tol = self.default_tol() if tol is None else tol
+        check(self.lib.hss_ulvfactsolve(self.handle, _ptr(dB), ldb, r, _ptr(dX), ldx, float(tol),
+                                        int(maxit), C.byref(self.stats), _stream(stream)))
+        return self.stats
+
     def solve_batch_device(self, dBs, ldbs, rs, dXs, ldxs, tol=None, maxit=10, stream=None):
         tol = self.default_tol() if tol is None else tol
         k = self.dev.ntrees

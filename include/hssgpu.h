@@ -149,6 +149,13 @@ typedef struct {
 int hss_ulvsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double* dX,
                  int64_t ldx, double tol, int32_t maxit, hss_solve_stats* stats,
                  void* stream);
+/* Refactor f's plan (its generators may have changed) and solve, in one call:
+ * `hssA \ B` (src/hssmatrix.jl:234) as hss_ulvrefactor + hss_ulvsolve, with the
+ * first solve's upward sweep of level h started as soon as level h is factored
+ * (a second stream, one event per level), so it runs behind the factorization
+ * instead of after it.  Same arguments and results as hss_ulvsolve. */
+int hss_ulvfactsolve(hss_factor f, const double* dB, int64_t ldb, int64_t r, double* dX, int64_t ldx, double tol,
+                     int32_t maxit, hss_solve_stats* stats, void* stream);
 int hss_ulvsolve_host(hss_factor f, const double* B, int64_t ldb, int64_t r, double* X,
                       int64_t ldx, double tol, int32_t maxit, hss_solve_stats* stats);
 

@@ -202,3 +202,53 @@ def test_graph_replay_matches(pkg, lib, orc):
         for t, b, x, x0 in zip(trees, bs, xs, eager):
             assert rel(x, x0) <= 1e-12
             assert rel(x, orc.ulvfactsolve(t, b)) <= 1e-8
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_fused_factor_solve_matches(pkg, lib, prec):
+    """hss_ulvfactsolve (the factorization with the first solve's upward sweep one
+    level behind it on a second stream) gives the solution of hss_ulvrefactor +
+    hss_ulvsolve: eagerly, on the default stream, and captured and replayed as a
+    CUDA graph (HSS_OPT_GRAPHS) on a non-default stream; the host entry point
+    hss_ulvfactsolve_host (fused from its second call) agrees too.  Bit for bit
+    in FP64 (no refinement); in FP32 + refinement to 1e-9 relative, the
+    refinement's own accuracy (the column norms that scale each pass are summed
+    with atomics in any order, so the FP32 passes may round differently)."""
+    torch = pytest.importorskip("torch")
+    n, r = 8192, 8
+    A = pkg.synthetic_hss(n, 128, 32, np.random.default_rng(3))
+    dev = A.device()
+    F = dev.ulvfactor(prec)
+    tol = 1e-10 if prec == "fp32" else 0.0
+    B = torch.randn((r, n), dtype=torch.float64, device="cuda")
+
+    def same(a, b):
+        if prec == "fp64":
+            return bool(torch.equal(a, b))
+        return float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) <= 1e-9
+
+    X1 = torch.empty_like(B)
+    F.refactor()
+    st = F.solve_device(B, n, r, X1, n, tol=tol, maxit=20)
+    it1 = st.iterations
+    torch.cuda.synchronize()
+    X2 = torch.empty_like(B)
+    st = F.factsolve_device(B, n, r, X2, n, tol=tol, maxit=20)
+    torch.cuda.synchronize()
+    assert same(X2, X1) and st.converged
+    stream = torch.cuda.Stream()
+    assert lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 1) == 0
+    try:
+        for _ in range(3):   # eager, captured, replayed
+            X3 = torch.zeros_like(B)
+            torch.cuda.synchronize()
+            st = F.factsolve_device(B, n, r, X3, n, tol=tol, maxit=20, stream=stream)
+            stream.synchronize()
+            assert same(X3, X1) and st.converged
+    finally:
+        lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 0)
+    Bh = B.cpu().numpy().T.copy(order="F")
+    x0 = pkg.ldiv(A, Bh, precision=prec, tol=tol if tol > 0 else None)
+    x1 = pkg.ldiv(A, Bh, precision=prec, tol=tol if tol > 0 else None)   # second call: fused
+    assert same(torch.from_numpy(x1.T.copy()).cuda(), torch.from_numpy(x0.T.copy()).cuda())
+    assert same(torch.from_numpy(x1.T.copy()).cuda(), X1)
