@@ -147,6 +147,18 @@ function Base.adjoint(a::GpuHss)
     adopt(h[])
 end
 
+# refactor (after the generators changed) and solve in one call, the first
+# solve's upward sweep pipelined behind the factorization (device buffers)
+function factsolve!(X::Ptr{Float64}, ldx::Integer, F::GpuUlv, B::Ptr{Float64}, ldb::Integer, r::Integer;
+                    tol=0.0, maxit=10, stream=C_NULL)
+    st = Ref{SolveStats}()
+    check(ccall((:hss_ulvfactsolve, lib), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Int64, Int64, Ptr{Float64}, Int64, Float64, Int32, Ref{SolveStats},
+                 Ptr{Cvoid}),
+                F.ptr, B, ldb, r, X, ldx, tol, maxit, st, stream))
+    st[]
+end
+
 # process-wide switches (HSS_OPT_* of the header)
 set_option(opt::Integer, value::Integer) =
     check(ccall((:hss_set_option, lib), Cint, (Int32, Int64), Int32(opt), Int64(value)))
