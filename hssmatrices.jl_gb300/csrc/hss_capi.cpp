@@ -64,6 +64,24 @@ struct SlotTable {
   DBuf<Slot> dev;
   std::vector<Slot> last;
   GraphCache graph;
+  // a second stream and two events, for launches of a product that may overlap
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaError_t ensure_side() {
+    cudaError_t e = cudaSuccess;
+    if (!side) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !ev_fork) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess && !ev_join) e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
+    return e;
+  }
+  SlotTable() = default;
+  SlotTable(const SlotTable&) = delete;
+  SlotTable& operator=(const SlotTable&) = delete;
+  ~SlotTable() {
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
+  }
   DBuf<uint32_t> pstate;             // launch counters: zero between launches
   DBuf<unsigned long long> pq;       // queue entries, tagged with the epoch of their launch
   uint32_t epoch = 0;                // tag of the last persistent launch on pq
@@ -802,8 +820,27 @@ int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable&
   CUDA_TRY(pm.ensure_pmv(pmv_queue_entries(L.ntasks, L.ninner, pmv_chunks(pairs, rmax)), st));
   ++pm.epoch;
   cudaError_t e = cudaSuccess;
-  // double-float residual: the leaf products D X on the tensor cores first
+  // double-float residual: the leaf products D X on the tensor cores first,
+  // and the leaf products Z = V^T X and C = alpha (D X + U F) + beta Y as
+  // streams over all leaves around the persistent launch, which keeps the tree
+  // part.  D X and Z = V^T X (both read X, write different buffers) run
+  // concurrently on two streams, joined before the persistent launch.
   const bool dx = pairs && dx_slices && dx_tc_fits(L.mleaf, L.nleaf);
+  const bool ext = dx && leaf_ext_fits(L.nleaf, L.mleaf, L.kmax);
+  cudaStream_t sv = st;   // stream of the V^T X launch
+  if (ext) {
+    CUDA_TRY(pm.ensure_side());
+    CUDA_TRY(cudaEventRecord(pm.ev_fork, st));
+    CUDA_TRY(cudaStreamWaitEvent(pm.side, pm.ev_fork, 0));
+    sv = pm.side;
+    traced(HSS_TRACE_MV_UP, L.leaves.cnt, sv, [&] {
+      e = launch_leaf_ext(false, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, rmax, L.nleaf, L.mleaf, L.kmax, sv);
+    });
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "leaf upsweep launch");
+    }
+  }
   if (dx) {
     traced(HSS_TRACE_MV_DX, L.leaves.cnt, st, [&] { e = launch_dx_tc(L.d_tasks + L.leaves.off, L.leaves.cnt,
                                                                      slots, rmax, st); });
@@ -812,17 +849,9 @@ int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable&
       return cuda_fail(e, "tensor-core leaf product launch");
     }
   }
-  // ... and the leaf products Z = V^T X and C = alpha (D X + U F) + beta Y as
-  // streams over all leaves around the persistent launch, which keeps the tree part
-  const bool ext = dx && leaf_ext_fits(L.nleaf, L.mleaf, L.kmax);
   if (ext) {
-    traced(HSS_TRACE_MV_UP, L.leaves.cnt, st, [&] {
-      e = launch_leaf_ext(false, L.d_tasks + L.leaves.off, L.leaves.cnt, slots, rmax, L.nleaf, L.mleaf, L.kmax, st);
-    });
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return cuda_fail(e, "leaf upsweep launch");
-    }
+    CUDA_TRY(cudaEventRecord(pm.ev_join, sv));
+    CUDA_TRY(cudaStreamWaitEvent(st, pm.ev_join, 0));
   }
   traced(HSS_TRACE_MV_LEAF, L.leaves.cnt, st, [&] {
     const void* pf = pairs ? (const void*)L.pfdf : (const void*)L.pf64;
