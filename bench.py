@@ -56,8 +56,8 @@ def parse():
     p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch", "compress", "matvec"])
     p.add_argument("--compress-n", type=int, default=16384)
     p.add_argument("--requests", type=int, default=10000)
-    p.add_argument("--rate", type=float, default=1000.0)
-    p.add_argument("--rates", default="1000,2000,4000,8000", help="offered loads of the serving sweep (requests/s)")
+    p.add_argument("--rate", type=float, default=500.0)
+    p.add_argument("--rates", default="500,1000,2000,4000,8000", help="offered loads of the serving sweep (requests/s)")
     p.add_argument("--pool", type=int, default=32)
     p.add_argument("--budget-gb", type=float, default=120.0)
     p.add_argument("--matrices", type=int, default=256)
