@@ -9,6 +9,7 @@
 #include <array>
 #include <atomic>
 #include <cmath>
+#include <limits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -136,6 +137,10 @@ inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
 // thread's capture counter and added each time the graph is replayed.
 std::atomic<int64_t> g_launches{0};
 thread_local int64_t* t_capture = nullptr;
+// Set while this thread records the refinement loop into a graph: launches
+// whose per-launch host state (the persistent product's queue epoch) would be
+// frozen by the recording reset that state on the device instead.
+thread_local bool t_graph_capture = false;
 inline void add_launches(int64_t n) {
   if (t_capture) *t_capture += n;
   else g_launches += n;
@@ -237,6 +242,14 @@ struct SolveBufs {
   HBuf<double> h_bn2, h_rn2;
   DBuf<float2> xs, tmp;
   SlotTable sv0, sv1, mv;
+  // the refinement loop recorded as one CUDA graph: the first pass, the first
+  // residual and its check, then a while node around (correction, residual,
+  // check); the check kernel sets the node's condition
+  DBuf<double> status;                  // RefineStatus
+  HBuf<double> h_status;
+  GraphCache loop;
+  int64_t loop_body_launches = 0;       // kernel launches of one pass of the while body
+  uint64_t loop_failed = 0;             // key whose recording failed (the host loop runs it)
 };
 
 struct hss_factor_s {
@@ -817,8 +830,11 @@ int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable&
     }
     return HSS_OK;
   }
-  CUDA_TRY(pm.ensure_pmv(pmv_queue_entries(L.ntasks, L.ninner, pmv_chunks(pairs, rmax)), st));
+  const int64_t qents = pmv_queue_entries(L.ntasks, L.ninner, pmv_chunks(pairs, rmax));
+  CUDA_TRY(pm.ensure_pmv(qents, st));
   ++pm.epoch;
+  // a recorded launch replays with this epoch: its queue entries are cleared first
+  if (t_graph_capture) CUDA_TRY(cudaMemsetAsync(pm.pq.p, 0, (size_t)qents * sizeof(unsigned long long), st));
   cudaError_t e = cudaSuccess;
   // double-float residual: the leaf products D X on the tensor cores first,
   // and the leaf products Z = V^T X and C = alpha (D X + U F) + beta Y as
@@ -873,6 +889,22 @@ int run_pmv(const Levels& L, const Slot* slots, int rmax, bool pairs, SlotTable&
     }
   }
   return HSS_OK;
+}
+
+// The launch state run_pmv needs, allocated ahead (nothing is allocated while
+// the launches are recorded into a graph).
+cudaError_t pmv_prepare(const Levels& L, bool pairs, int rmax, SlotTable& pm, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (use_flat(L, pairs, rmax)) {
+    e = pm.ensure_pmv(1, st);
+    if (e == cudaSuccess)
+      e = pm.ensure_flat(pmv_flat_ctb_elems(L.leaves.cnt, L.flat_dep, L.kmax, rmax),
+                         L.leaves.cnt * pmv_flat_chunks(rmax), st);
+  } else {
+    e = pm.ensure_pmv(pmv_queue_entries(L.ntasks, L.ninner, pmv_chunks(pairs, rmax)), st);
+  }
+  if (e == cudaSuccess) e = pm.ensure_side();
+  return e;
 }
 
 int run_matvec(const Levels& L, const Slot* slots, int rmax, cudaStream_t st, SlotTable* pm = nullptr) {
@@ -1301,12 +1333,21 @@ struct Item {
   Cols io;
 };
 
+// A solve pass made ready to launch: its slot table uploaded and the key of
+// its launch sequence.
+struct PassPrep {
+  uint64_t key = 0;
+  int64_t rmax = 0;
+  bool blocked = false;
+};
+
 template <typename T>
-int solve_pass(const std::vector<Item>& items, const Levels& L, const double* scale, const int64_t* off,
+int solve_prep(const std::vector<Item>& items, const Levels& L, const double* scale, const int64_t* off,
                int64_t rtot, int mode, bool residual_input, const int64_t* roff, double* R, SlotTable& table,
-               cudaStream_t st, const hss_factor_s* tf = nullptr) {
+               cudaStream_t st, const hss_factor_s* tf, PassPrep& pp) {
   int64_t rmax = 0;
   for (auto& it : items) rmax = std::max(rmax, it.io.r);
+  pp.rmax = rmax;
   if (rmax == 0) return HSS_OK;
   std::vector<Slot> s(items.size());
   for (size_t i = 0; i < items.size(); ++i) {
@@ -1332,13 +1373,31 @@ int solve_pass(const std::vector<Item>& items, const Levels& L, const double* sc
   CUDA_TRY(table.upload(s, st));
   bool blocked = true;
   for (auto& it : items) blocked = blocked && it.f->blocked;
+  pp.blocked = blocked;
   uint64_t key = levels_key(L, table.dev.p, rmax * 64 + (blocked ? 1 : 0) + (sizeof(T) == 4 ? 2 : 0));
   if (tf)
     for (const std::vector<int8_t>* v : {&tf->tune_up, &tf->tune_down})
       for (int8_t c : *v) key = fnv(key, (uint64_t)(c + 2));
+  pp.key = key;
+  return HSS_OK;
+}
+
+template <typename T>
+void solve_issue(const Levels& L, const SlotTable& table, const PassPrep& pp, cudaStream_t st,
+                 const hss_factor_s* tf) {
+  if (pp.rmax > 0) run_solve<T>(L, table.dev.p, (int)pp.rmax, st, pp.blocked, tf);
+}
+
+template <typename T>
+int solve_pass(const std::vector<Item>& items, const Levels& L, const double* scale, const int64_t* off,
+               int64_t rtot, int mode, bool residual_input, const int64_t* roff, double* R, SlotTable& table,
+               cudaStream_t st, const hss_factor_s* tf = nullptr) {
+  PassPrep pp;
+  int rc = solve_prep<T>(items, L, scale, off, rtot, mode, residual_input, roff, R, table, st, tf, pp);
+  if (rc || pp.rmax == 0) return rc;
   bool unused = false;
-  int rc = graphed(table.graph, key, st, unused, [&] {
-    run_solve<T>(L, table.dev.p, (int)rmax, st, blocked, tf);
+  rc = graphed(table.graph, pp.key, st, unused, [&] {
+    solve_issue<T>(L, table, pp, st, tf);
     return true;
   });
   if (rc) return rc;
@@ -1353,11 +1412,12 @@ int solve_pass(const std::vector<Item>& items, const Levels& L, const double* sc
 // factorization instead of after it; the downward solve follows both on st.
 // Replayed as one CUDA graph (fork and join through events) where graphs apply.
 template <typename T>
-int factsolve_pass(hss_factor_s* f, const std::vector<Item>& items, const Levels& L, const double* scale,
-                   const int64_t* off, int64_t rtot, SlotTable& table, cudaStream_t st) {
+int factsolve_prep(hss_factor_s* f, const std::vector<Item>& items, const Levels& L, const double* scale,
+                   const int64_t* off, int64_t rtot, SlotTable& table, cudaStream_t st, PassPrep& pp) {
   hss_plan_s* P = f->plan;
   int64_t rmax = 0;
   for (auto& it : items) rmax = std::max(rmax, it.io.r);
+  pp.rmax = rmax;
   std::vector<Slot> fsl(P->ntrees);
   for (Slot& x : fsl) {
     std::memset(&x, 0, sizeof(Slot));
@@ -1384,7 +1444,7 @@ int factsolve_pass(hss_factor_s* f, const std::vector<Item>& items, const Levels
   CUDA_TRY(table.upload(s, st));
   bool all_fast = true;
   for (size_t h = 0; h < L.by_h->size(); ++h) all_fast = factor_level_fast<T>((*L.by_h)[h]) && all_fast;
-  const bool blocked = all_fast && sizeof(T) == sizeof(float);
+  pp.blocked = all_fast && sizeof(T) == sizeof(float);
   if (!f->pipe_st) CUDA_TRY(cudaStreamCreateWithFlags(&f->pipe_st, cudaStreamNonBlocking));
   while (f->pipe_ev.size() < 2 + L.by_h->size()) {
     cudaEvent_t e = nullptr;
@@ -1392,30 +1452,50 @@ int factsolve_pass(hss_factor_s* f, const std::vector<Item>& items, const Levels
     f->pipe_ev.push_back(e);
   }
   uint64_t key = fnv(levels_key(L, f->fac_slots.dev.p, (int64_t)sizeof(T) + (g_generic_factor ? 16 : 0)),
-                     levels_key(L, table.dev.p, rmax * 64 + (blocked ? 1 : 0) + (sizeof(T) == 4 ? 2 : 0)));
+                     levels_key(L, table.dev.p, rmax * 64 + (pp.blocked ? 1 : 0) + (sizeof(T) == 4 ? 2 : 0)));
   for (const std::vector<int8_t>* v : {&f->tune_up, &f->tune_down})
     for (int8_t c : *v) key = fnv(key, (uint64_t)(c + 2));
-  bool unused = false;
+  pp.key = key;
+  // the solves that follow (and the correction passes of a refinement) read
+  // this factorization's kind
+  f->blocked = pp.blocked;
+  return HSS_OK;
+}
+
+template <typename T>
+cudaError_t factsolve_issue(hss_factor_s* f, const Levels& L, const SlotTable& table, const PassPrep& pp,
+                            cudaStream_t st) {
   cudaError_t ev_err = cudaSuccess;
   auto chk = [&](cudaError_t e) { if (e != cudaSuccess && ev_err == cudaSuccess) ev_err = e; };
-  int rc = graphed(f->pipe_graph, key, st, unused, [&] {
-    cudaStream_t s2 = f->pipe_st;
-    chk(cudaEventRecord(f->pipe_ev[0], st));
-    chk(cudaStreamWaitEvent(s2, f->pipe_ev[0], 0));
-    for (size_t h = 0; h < L.by_h->size(); ++h) {
-      run_factor_level<T>(L, h, f->fac_slots.dev.p, st);
-      chk(cudaEventRecord(f->pipe_ev[2 + h], st));
-      chk(cudaStreamWaitEvent(s2, f->pipe_ev[2 + h], 0));
-      run_solve_up_level<T>(L, h, table.dev.p, (int)rmax, s2, blocked, &f->tune_up);
-    }
-    chk(cudaEventRecord(f->pipe_ev[1], s2));
-    chk(cudaStreamWaitEvent(st, f->pipe_ev[1], 0));
-    run_solve_down<T>(L, table.dev.p, (int)rmax, st, blocked, &f->tune_down);
+  cudaStream_t s2 = f->pipe_st;
+  chk(cudaEventRecord(f->pipe_ev[0], st));
+  chk(cudaStreamWaitEvent(s2, f->pipe_ev[0], 0));
+  for (size_t h = 0; h < L.by_h->size(); ++h) {
+    run_factor_level<T>(L, h, f->fac_slots.dev.p, st);
+    chk(cudaEventRecord(f->pipe_ev[2 + h], st));
+    chk(cudaStreamWaitEvent(s2, f->pipe_ev[2 + h], 0));
+    run_solve_up_level<T>(L, h, table.dev.p, (int)pp.rmax, s2, pp.blocked, &f->tune_up);
+  }
+  chk(cudaEventRecord(f->pipe_ev[1], s2));
+  chk(cudaStreamWaitEvent(st, f->pipe_ev[1], 0));
+  run_solve_down<T>(L, table.dev.p, (int)pp.rmax, st, pp.blocked, &f->tune_down);
+  return ev_err;
+}
+
+template <typename T>
+int factsolve_pass(hss_factor_s* f, const std::vector<Item>& items, const Levels& L, const double* scale,
+                   const int64_t* off, int64_t rtot, SlotTable& table, cudaStream_t st) {
+  PassPrep pp;
+  int rc = factsolve_prep<T>(f, items, L, scale, off, rtot, table, st, pp);
+  if (rc) return rc;
+  bool unused = false;
+  cudaError_t ev_err = cudaSuccess;
+  rc = graphed(f->pipe_graph, pp.key, st, unused, [&] {
+    ev_err = factsolve_issue<T>(f, L, table, pp, st);
     return true;
   });
   if (rc) return rc;
   if (ev_err != cudaSuccess) return cuda_fail(ev_err, "pipelined factorization events");
-  f->blocked = blocked;
   CUDA_TRY(cudaGetLastError());
   return HSS_OK;
 }
@@ -1439,8 +1519,88 @@ int read_dev_err(hss_plan_s* P, cudaStream_t st) {
   return HSS_OK;
 }
 
+// Records the refinement loop into a graph: `first` issues the launches up
+// to and including the first convergence check, `body` one refinement step
+// ending with a check; both get the while node's condition handle.  Returns
+// false (nothing recorded, the stream out of capture, errors cleared) when the
+// runtime refuses any part of it.
+template <typename F0, typename F1>
+bool record_loop(GraphCache& gc, uint64_t key, int64_t& body_launches, cudaStream_t st, F0&& first, F1&& body) {
+  cudaGraph_t G = nullptr;
+  if (cudaGraphCreate(&G, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaGraphConditionalHandle cond = 0;
+  int64_t n0 = 0, n1 = 0;
+  bool ok = cudaGraphConditionalHandleCreate(&cond, G, 0, cudaGraphCondAssignDefault) == cudaSuccess &&
+            cudaStreamBeginCaptureToGraph(st, G, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                cudaSuccess;
+  std::vector<cudaGraphNode_t> tail;
+  if (ok) {
+    t_capture = &n0;
+    t_graph_capture = true;
+    const int rc = first(cond);
+    t_capture = nullptr;
+    t_graph_capture = false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusActive && deps)
+      tail.assign(deps, deps + nd);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    ok = rc == HSS_OK && e == cudaSuccess && g == G && !tail.empty();
+  }
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};   // the rest zero
+  if (ok) {
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    ok = cudaGraphAddNode(&node, G, tail.data(), nullptr, tail.size(), &cp) == cudaSuccess &&
+         cp.conditional.phGraph_out != nullptr;
+  }
+  if (ok) {
+    cudaGraph_t bg = cp.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(st, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      t_capture = &n1;
+      t_graph_capture = true;
+      const int rc = body(cond);
+      t_capture = nullptr;
+      t_graph_capture = false;
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(st, &g);
+      ok = rc == HSS_OK && e == cudaSuccess;
+    }
+  }
+  cudaGraphExec_t ex = nullptr;
+  if (ok && cudaGraphInstantiate(&ex, G, 0) != cudaSuccess) {
+    ex = nullptr;
+    ok = false;
+  }
+  cudaGraphDestroy(G);
+  cudaGetLastError();
+  if (!ok) return false;
+  gc.reset();
+  gc.exec = ex;
+  gc.key = key;
+  gc.launches = n0;
+  body_launches = n1;
+  return true;
+}
+
+// Largest maxit run by the recorded loop (larger ones run the host loop).
+constexpr int32_t kLoopMaxIt = 64;
+
 // Solve every item, then refine (FP32 factors, or FP64 with tol > 0) until the
 // largest relative residual over all columns of all items is <= tol.
+// With graphs enabled on a non-default stream the whole loop is one replayed
+// graph: the convergence check runs on the device and sets the condition of a
+// while node, and the host reads the loop's status once at the end.
 int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, double tol, int32_t maxit,
                 hss_solve_stats* stats, cudaStream_t st, const hss_factor_s* tf = nullptr,
                 hss_factor_s* fuse = nullptr) {
@@ -1469,14 +1629,24 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
   }
   int64_t rmax = 0;
   for (auto& it : items) rmax = std::max(rmax, it.io.r);
-  const double* scale = nullptr;
-  if (refine) {
-    CUDA_TRY(B.bn2.ensure(rtot));
-    CUDA_TRY(B.rn2.ensure(rtot));
-    CUDA_TRY(B.scale.ensure(2 * rtot));
-    CUDA_TRY(B.R.ensure(std::max<int64_t>(roff[ni], 1)));
-    CUDA_TRY(B.h_bn2.ensure(rtot));
-    CUDA_TRY(B.h_rn2.ensure(rtot));
+  auto first_pass = [&](const double* scale) {
+    return fuse ? (fp32 ? factsolve_pass<float>(fuse, items, L, scale, off.data(), rtot, B.sv0, st)
+                        : factsolve_pass<double>(fuse, items, L, scale, off.data(), rtot, B.sv0, st))
+                : (fp32 ? solve_pass<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0,
+                                            st, tf)
+                        : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0,
+                                             st, tf));
+  };
+  if (!refine) return first_pass(nullptr);
+  CUDA_TRY(B.bn2.ensure(rtot));
+  CUDA_TRY(B.rn2.ensure(rtot));
+  CUDA_TRY(B.scale.ensure(2 * rtot));
+  CUDA_TRY(B.R.ensure(std::max<int64_t>(roff[ni], 1)));
+  CUDA_TRY(B.h_bn2.ensure(rtot));
+  CUDA_TRY(B.h_rn2.ensure(rtot));
+  const double* scale = fp32 ? B.scale.p : nullptr;
+  // ||b_j||^2 of every column (and the FP32 column scaling from it)
+  auto issue_norms = [&]() -> int {
     CUDA_TRY(cudaMemsetAsync(B.bn2.p, 0, rtot * sizeof(double), st));
     for (size_t i = 0; i < ni; ++i) {
       const Item& it = items[i];
@@ -1486,17 +1656,9 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     if (fp32) {
       launch_sqrt_scale(B.bn2.p, B.scale.p, rtot, st);
       add_launches(1);
-      scale = B.scale.p;
     }
-    CUDA_TRY(cudaMemcpyAsync(B.h_bn2.p, B.bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
-  }
-  // fuse: the factorization of fuse's plan runs first, pipelined with this pass
-  int rc = fuse ? (fp32 ? factsolve_pass<float>(fuse, items, L, scale, off.data(), rtot, B.sv0, st)
-                        : factsolve_pass<double>(fuse, items, L, scale, off.data(), rtot, B.sv0, st))
-                : (fp32 ? solve_pass<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf)
-                        : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0, st, tf));
-  if (rc) return rc;
-  if (!refine) return HSS_OK;
+    return HSS_OK;
+  };
   // refinement: R = b - A x (double-float product for FP32 factors unless
   // the FP64 product is forced), x += A_f^{-1} R
   bool dfres = fp32 && !g_residual_fp64;
@@ -1542,8 +1704,8 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
   // the tuned residual product of this factor, else the persistent one where it fits
   SlotTable* pm = (tf && tf->tune_pmv == 0) ? nullptr : &B.mv;
   const bool persistent = use_pmv(L, pm, dfres, (int)rmax);
-  double res = 0.0;
-  for (int32_t iter = 0;; ++iter) {
+  // R = b - A x and ||R_j||^2 into rn2
+  auto issue_residual = [&]() -> int {
     CUDA_TRY(cudaMemsetAsync(B.rn2.p, 0, rtot * sizeof(double), st));
     if (dfres && !persistent)   // the persistent product splits B itself
       for (size_t i = 0; i < ni; ++i) {
@@ -1551,20 +1713,134 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
         launch_df_split_cols(it.io.C, it.io.ldc, it.f->plan->tree_n[it.tree], it.io.r, B.xs.p + xoff[i], st);
         add_launches(1);
       }
+    return dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, pm, dx_slices)
+                 : run_matvec(L, B.mv.dev.p, (int)rmax, st, pm);
+  };
+  const bool loop_on_device = g_graphs && st != nullptr && g_trace.kind < 0 && g_pick_force < 0 &&
+                              maxit >= 0 && maxit <= kLoopMaxIt && ni <= (size_t)INT32_MAX;
+  if (loop_on_device) {
+    // everything the recorded launches read from the host is made ready here
+    PassPrep p0, p1;
+    int rc = fuse ? (fp32 ? factsolve_prep<float>(fuse, items, L, scale, off.data(), rtot, B.sv0, st, p0)
+                          : factsolve_prep<double>(fuse, items, L, scale, off.data(), rtot, B.sv0, st, p0))
+                  : (fp32 ? solve_prep<float>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0,
+                                              st, tf, p0)
+                          : solve_prep<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr,
+                                               B.sv0, st, tf, p0));
+    if (rc) return rc;
+    rc = fp32 ? solve_prep<float>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st,
+                                  tf, p1)
+              : solve_prep<double>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st,
+                                   tf, p1);
+    if (rc) return rc;
     CUDA_TRY(B.mv.upload(ms, st));
-    rc = dfres ? run_matvec_df(L, B.mv.dev.p, (int)rmax, st, pm, dx_slices)
-               : run_matvec(L, B.mv.dev.p, (int)rmax, st, pm);
+    if (persistent) CUDA_TRY(pmv_prepare(L, dfres, (int)rmax, *pm, st));
+    CUDA_TRY(B.status.ensure(4));
+    CUDA_TRY(B.h_status.ensure(4));
+    // every address and choice the recorded launches hold
+    uint64_t key = fnv(fnv(p0.key, p1.key), levels_key(L, B.mv.dev.p, rmax));
+    for (const Item& it : items)
+      for (uint64_t v : {(uint64_t)(uintptr_t)it.f, (uint64_t)it.tree, (uint64_t)(uintptr_t)it.io.B,
+                         (uint64_t)it.io.ldb, (uint64_t)(uintptr_t)it.io.C, (uint64_t)it.io.ldc, (uint64_t)it.io.r})
+        key = fnv(key, v);
+    double tolv = tol;
+    uint64_t tolbits = 0;
+    std::memcpy(&tolbits, &tolv, sizeof(tolbits));
+    for (uint64_t v : {(uint64_t)(uintptr_t)fuse, tolbits, (uint64_t)maxit, (uint64_t)fp32, (uint64_t)dfres,
+                       (uint64_t)persistent, (uint64_t)dx_slices, (uint64_t)(uintptr_t)pm,
+                       (uint64_t)g_generic_factor, (uint64_t)g_flat_product, (uint64_t)pmv_poll_limit(),
+                       (uint64_t)(uintptr_t)B.mv.pq.p, (uint64_t)(uintptr_t)B.mv.pstate.p,
+                       (uint64_t)(uintptr_t)B.mv.ctb.p, (uint64_t)(uintptr_t)B.mv.dcnt.p,
+                       (uint64_t)(uintptr_t)B.bn2.p, (uint64_t)(uintptr_t)B.rn2.p, (uint64_t)(uintptr_t)B.scale.p,
+                       (uint64_t)(uintptr_t)B.R.p, (uint64_t)(uintptr_t)B.xs.p, (uint64_t)(uintptr_t)B.tmp.p,
+                       (uint64_t)(uintptr_t)B.status.p})
+      key = fnv(key, v);
+    GraphCache& gc = B.loop;
+    RefineStatus* dst = (RefineStatus*)B.status.p;
+    auto issue_check = [&](cudaGraphConditionalHandle cond) {
+      launch_refine_check(B.bn2.p, B.rn2.p, rtot, tol, maxit, dst, B.mv.dev.p, (int32_t)ni, cond, st);
+      add_launches(1);
+    };
+    bool have = gc.key == key;
+    if (!have && gc.seen == key && B.loop_failed != key) {
+      have = record_loop(
+          gc, key, B.loop_body_launches, st,
+          [&](cudaGraphConditionalHandle cond) -> int {
+            int e = issue_norms();
+            if (e) return e;
+            CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(RefineStatus), st));
+            if (fuse) {
+              CUDA_TRY(fp32 ? factsolve_issue<float>(fuse, L, B.sv0, p0, st)
+                            : factsolve_issue<double>(fuse, L, B.sv0, p0, st));
+            } else if (fp32) {
+              solve_issue<float>(L, B.sv0, p0, st, tf);
+            } else {
+              solve_issue<double>(L, B.sv0, p0, st, tf);
+            }
+            if ((e = issue_residual())) return e;
+            issue_check(cond);
+            return HSS_OK;
+          },
+          [&](cudaGraphConditionalHandle cond) -> int {
+            launch_sqrt_scale(B.rn2.p, B.scale.p, rtot, st);
+            add_launches(1);
+            if (fp32) solve_issue<float>(L, B.sv1, p1, st, tf);
+            else solve_issue<double>(L, B.sv1, p1, st, tf);
+            const int e = issue_residual();
+            if (e) return e;
+            issue_check(cond);
+            return HSS_OK;
+          });
+      if (!have) {
+        B.loop_failed = key;
+        g_err.clear();
+      }
+    }
+    if (have) {
+      CUDA_TRY(cudaGraphLaunch(gc.exec, st));
+      CUDA_TRY(cudaMemcpyAsync(B.h_status.p, dst, sizeof(RefineStatus), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      RefineStatus rs;
+      std::memcpy(&rs, B.h_status.p, sizeof(rs));
+      add_launches(gc.launches + B.loop_body_launches * (int64_t)rs.iterations);
+      for (auto& it : items) {
+        rc = read_dev_err(it.f->plan, st);
+        if (rc) return rc;
+      }
+      if (stats) {
+        stats->iterations = rs.iterations;
+        stats->residual = rs.residual;
+        stats->converged = rs.converged;
+      }
+      if (rs.converged) return HSS_OK;
+      return fail(HSS_ERR_NO_CONVERGENCE, "iterative refinement did not reach the tolerance (residual " +
+                                              std::to_string(rs.residual) + ")");
+    }
+    gc.seen = key;   // recorded on the next call with this key
+  }
+  // the loop on the host: one read of the residual norms per step
+  int rc = issue_norms();
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(B.h_bn2.p, B.bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if ((rc = first_pass(scale))) return rc;
+  double res = 0.0;
+  for (int32_t iter = 0;; ++iter) {
+    CUDA_TRY(B.mv.upload(ms, st));
+    rc = issue_residual();
     if (rc) return rc;
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(B.h_rn2.p, B.rn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     res = 0.0;
+    bool nan = false;
     for (int64_t j = 0; j < rtot; ++j) {
       const double bn = std::sqrt(B.h_bn2.p[j]);
       const double rn = std::sqrt(B.h_rn2.p[j]);
       const double rel = bn > 0.0 ? rn / bn : rn;
-      if (!(rel <= res)) res = rel;   // NaN propagates
+      if (std::isnan(rel)) nan = true;
+      else if (rel > res) res = rel;
     }
+    if (nan) res = std::numeric_limits<double>::quiet_NaN();
     if (stats) { stats->iterations = iter; stats->residual = res; }
     if (res <= tol) {
       if (stats) stats->converged = 1;
@@ -1574,7 +1850,7 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
       }
       return HSS_OK;
     }
-    if (iter >= maxit || std::isnan(res)) break;
+    if (iter >= maxit || nan) break;
     launch_sqrt_scale(B.rn2.p, B.scale.p, rtot, st);
     add_launches(1);
     rc = fp32 ? solve_pass<float>(items, L, B.scale.p, off.data(), rtot, 1, true, roff.data(), B.R.p, B.sv1, st, tf)

@@ -169,4 +169,14 @@ struct PqrTask {
 // device status codes written into Slot::err
 enum { DEV_OK = 0, DEV_SINGULAR = 1, DEV_BAD = 2, DEV_TIMEOUT = 3 };
 
+// State of the refinement loop run on the device (hss_ulvsolve with a
+// tolerance): written by the convergence check after every residual.
+struct RefineStatus {
+  double residual;      // largest relative residual over all columns (NaN if any is NaN)
+  int32_t iterations;   // refinement steps before this residual
+  int32_t converged;    // residual <= tol
+  int32_t next;         // steps taken so far: the loop continues while next grows
+  int32_t pad;
+};
+
 }  // namespace hss

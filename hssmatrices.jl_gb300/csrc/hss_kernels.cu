@@ -867,6 +867,51 @@ __global__ void sqrt_scale_kernel(const double* __restrict__ n2, double* __restr
   }
 }
 
+// Convergence check of the refinement loop on the device (one block): the
+// largest relative residual over all columns, ||r_j|| / ||b_j|| (||r_j|| where
+// b_j = 0), written to `st`, and the condition of the enclosing while node set
+// to 1 when another step follows: not converged, no NaN, fewer than maxit steps
+// taken and no device error in any slot.  `next` grows by one per continued
+// step, so the loop ends after at most maxit steps.
+__global__ void refine_check_kernel(const double* __restrict__ bn2, const double* __restrict__ rn2, int64_t r,
+                                    double tol, int32_t maxit, RefineStatus* st, const Slot* __restrict__ slots,
+                                    int32_t nslots, cudaGraphConditionalHandle cond) {
+  __shared__ double s_max[NT];
+  __shared__ int s_nan[NT];
+  double m = 0.0;
+  int nan = 0;
+  for (int64_t j = threadIdx.x; j < r; j += blockDim.x) {
+    const double bn = sqrt(bn2[j]), rn = sqrt(rn2[j]);
+    const double rel = bn > 0.0 ? rn / bn : rn;
+    if (isnan(rel)) nan = 1;
+    else m = fmax(m, rel);
+  }
+  s_max[threadIdx.x] = m;
+  s_nan[threadIdx.x] = nan;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      s_max[threadIdx.x] = fmax(s_max[threadIdx.x], s_max[threadIdx.x + w]);
+      s_nan[threadIdx.x] |= s_nan[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    int err = 0;
+    for (int32_t i = 0; i < nslots; ++i)
+      if (slots[i].err && *(const volatile int32_t*)slots[i].err != DEV_OK) err = 1;
+    const double res = s_nan[0] ? __longlong_as_double(0x7ff8000000000000ll) : s_max[0];
+    const int it = st->next;
+    const int conv = (!s_nan[0] && res <= tol) ? 1 : 0;
+    const int more = (!conv && !s_nan[0] && !err && it < maxit) ? 1 : 0;
+    st->residual = res;
+    st->iterations = it;
+    st->converged = conv;
+    st->next = it + more;
+    cudaGraphSetConditional(cond, (unsigned)more);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
@@ -951,6 +996,11 @@ void launch_colnorm2(const double* B, int64_t ldb, int64_t n, int64_t r, double*
 void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st) {
   if (r <= 0) return;
   sqrt_scale_kernel<<<(unsigned)((r + 255) / 256), 256, 0, st>>>(n2, s, r);
+}
+void launch_refine_check(const double* bn2, const double* rn2, int64_t r, double tol, int32_t maxit,
+                         RefineStatus* status, const Slot* slots, int32_t nslots, cudaGraphConditionalHandle cond,
+                         cudaStream_t st) {
+  refine_check_kernel<<<1, NT, 0, st>>>(bn2, rn2, r, tol, maxit, status, slots, nslots, cond);
 }
 
 }  // namespace hss

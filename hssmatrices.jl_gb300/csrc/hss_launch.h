@@ -51,6 +51,7 @@ int pmv_sync_chunks();
 // Polls of an idle or waiting block of the persistent products before it
 // records DEV_TIMEOUT and gives up (0: the default, 2^22); taken by later launches.
 void pmv_set_poll_limit(uint32_t polls);
+uint32_t pmv_poll_limit();
 // ntasks = non-root nodes of all trees, ninner = non-root branches; the slots' nodes/sync must be set and
 // every sync counter even (zeroed at allocation); epoch must differ from every earlier launch on state.
 // [prefetch, prefetch + prefetch_bytes) (nullable) is brought into L2 first.
@@ -158,6 +159,11 @@ void launch_colnorm2(const double* B, int64_t ldb, int64_t n, int64_t r, double*
                      cudaStream_t st);
 // s[j] = sqrt(n2[j]) (1 where n2[j] == 0) and s[r + j] = 1 / s[j]; s holds 2r values.
 void launch_sqrt_scale(const double* n2, double* s, int64_t r, cudaStream_t st);
+// The refinement loop's convergence check (one block; sets `cond`, the condition
+// of the CUDA graph while node that repeats the refinement step).
+void launch_refine_check(const double* bn2, const double* rn2, int64_t r, double tol, int32_t maxit,
+                         RefineStatus* status, const Slot* slots, int32_t nslots, cudaGraphConditionalHandle cond,
+                         cudaStream_t st);
 
 // Fixed scratch of the allocation-free product (hss_noalloc.cu): device
 // addresses of the file-scope arrays on `device`, resolved once per device.

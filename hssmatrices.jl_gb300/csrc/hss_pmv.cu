@@ -1516,6 +1516,7 @@ bool pmv_queue_fits(int64_t nodes, int64_t slots) {
 }
 int pmv_sync_chunks() { return kSyncChunks; }
 void pmv_set_poll_limit(uint32_t polls) { g_idle_limit = polls == 0 ? kIdleLimit : polls; }
+uint32_t pmv_poll_limit() { return g_idle_limit; }
 
 cudaError_t launch_pmv(bool pairs, const Task* leaves, int64_t nleaves, const Slot* slots, int64_t ntasks,
                        int64_t ninner, int rmax,

@@ -167,7 +167,9 @@ def test_autotune_keeps_results(pkg, orc):
 def test_graph_replay_matches(pkg, lib, orc):
     """HSS_OPT_GRAPHS: factorizations and solve passes on a non-default stream are
     captured on their second identical call and replayed afterwards; every call
-    gives the same solution as the eager launches."""
+    gives the same solution as the eager launches.  From the second call the
+    whole refinement loop is one graph whose convergence check runs on the
+    device: the eager launches plus one check kernel per residual."""
     torch = pytest.importorskip("torch")
     HSS_OPT_GRAPHS = 4
     rng = np.random.default_rng(12)
@@ -185,20 +187,21 @@ def test_graph_replay_matches(pkg, lib, orc):
             dX = [torch.zeros_like(b) for b in dB]
         c0 = lib.hss_launch_counter()
         F.refactor(stream=stream)
-        F.solve_batch_device(dB, [b.shape[0] for b in bs], rs, dX, [b.shape[0] for b in bs], tol=1e-10, maxit=20,
-                             stream=stream)
+        st = F.solve_batch_device(dB, [b.shape[0] for b in bs], rs, dX, [b.shape[0] for b in bs], tol=1e-10,
+                                  maxit=20, stream=stream)
         stream.synchronize()
-        return [x.cpu().numpy().T for x in dX], lib.hss_launch_counter() - c0
+        return [x.cpu().numpy().T for x in dX], lib.hss_launch_counter() - c0, st.iterations
 
     run()   # the first solve also prepares the plan's tensor-core slices (once)
-    eager, n_eager = run()
+    eager, n_eager, it_eager = run()
     assert lib.hss_set_option(HSS_OPT_GRAPHS, 1) == 0
     try:
         outs = [run() for _ in range(4)]   # eager (key seen), capture, replay, replay
     finally:
         lib.hss_set_option(HSS_OPT_GRAPHS, 0)
-    for xs, n in outs:
-        assert n == n_eager
+    for i, (xs, n, it) in enumerate(outs):
+        assert it == it_eager
+        assert n == (n_eager if i == 0 else n_eager + it + 1)
         for t, b, x, x0 in zip(trees, bs, xs, eager):
             assert rel(x, x0) <= 1e-12
             assert rel(x, orc.ulvfactsolve(t, b)) <= 1e-8
@@ -252,3 +255,51 @@ def test_fused_factor_solve_matches(pkg, lib, prec):
     x1 = pkg.ldiv(A, Bh, precision=prec, tol=tol if tol > 0 else None)   # second call: fused
     assert same(torch.from_numpy(x1.T.copy()).cuda(), torch.from_numpy(x0.T.copy()).cuda())
     assert same(torch.from_numpy(x1.T.copy()).cuda(), X1)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_device_refinement_loop(pkg, lib, prec):
+    """The refinement loop recorded as one graph (HSS_OPT_GRAPHS, non-default
+    stream): the convergence check on the device ends the loop at the same step
+    as the host loop, with the same residual to rounding, in FP32 (double-float
+    residual) and in FP64 (FP64 residual, tol > 0); with tol = 0 the loop stops
+    after maxit steps, reports no convergence with maxit iterations, and the
+    next call on the same factorization still solves."""
+    torch = pytest.importorskip("torch")
+    n, r = 4096, 4
+    A = pkg.synthetic_hss(n, 128, 24, np.random.default_rng(21))
+    F = A.device().ulvfactor(prec)
+    B = torch.randn((r, n), dtype=torch.float64, device="cuda")
+    tol = 1e-10 if prec == "fp32" else 1e-13
+    stream = torch.cuda.Stream()
+
+    def solve(tol, maxit):
+        X = torch.zeros_like(B)
+        torch.cuda.synchronize()
+        try:
+            st = F.solve_device(B, n, r, X, n, tol=tol, maxit=maxit, stream=stream)
+            ok = True
+        except pkg._lib.NoConvergence:
+            st, ok = F.stats, False
+        stream.synchronize()
+        return X, ok, st.iterations, st.residual, st.converged
+
+    X0, ok0, it0, res0, _ = solve(tol, 20)   # host loop (graphs off)
+    assert ok0 and res0 <= tol
+    Xs, ok, its, res_s, conv_s = solve(0.0, 3)
+    assert not ok and its == 3 and conv_s == 0
+    assert lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 1) == 0
+    try:
+        for _ in range(3):   # host loop (key seen), recorded, replayed
+            X, ok, it, res, conv = solve(tol, 20)
+            assert ok and conv == 1 and it == it0 and res <= tol
+            assert abs(res - res0) <= 0.5 * res0 + 1e-300
+            assert float(torch.linalg.norm(X - X0) / torch.linalg.norm(X0)) <= 1e-9
+        for _ in range(3):   # tol = 0: bounded by maxit on the device
+            X, ok, it, res, conv = solve(0.0, 3)
+            assert not ok and it == 3 and conv == 0 and np.isfinite(res)
+            assert float(torch.linalg.norm(X - X0) / torch.linalg.norm(X0)) <= 1e-9
+        X, ok, it, res, conv = solve(tol, 20)
+        assert ok and it == it0
+    finally:
+        lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 0)
