@@ -262,7 +262,8 @@ def test_device_refinement_loop(pkg, lib, prec):
     """The refinement loop recorded as one graph (HSS_OPT_GRAPHS, non-default
     stream): the convergence check on the device ends the loop at the same step
     as the host loop, with the same residual to rounding, in FP32 (double-float
-    residual) and in FP64 (FP64 residual, tol > 0); with tol = 0 the loop stops
+    residual) and in FP64 (FP64 residual, tol > 0); with an unreachable tolerance
+    (0 in FP32; 1e-300 in FP64, where tol = 0 means no refinement) the loop stops
     after maxit steps, reports no convergence with maxit iterations, and the
     next call on the same factorization still solves."""
     torch = pytest.importorskip("torch")
@@ -271,6 +272,7 @@ def test_device_refinement_loop(pkg, lib, prec):
     F = A.device().ulvfactor(prec)
     B = torch.randn((r, n), dtype=torch.float64, device="cuda")
     tol = 1e-10 if prec == "fp32" else 1e-13
+    never = 0.0 if prec == "fp32" else 1e-300
     stream = torch.cuda.Stream()
 
     def solve(tol, maxit):
@@ -286,7 +288,7 @@ def test_device_refinement_loop(pkg, lib, prec):
 
     X0, ok0, it0, res0, _ = solve(tol, 20)   # host loop (graphs off)
     assert ok0 and res0 <= tol
-    Xs, ok, its, res_s, conv_s = solve(0.0, 3)
+    Xs, ok, its, res_s, conv_s = solve(never, 3)
     assert not ok and its == 3 and conv_s == 0
     assert lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 1) == 0
     try:
@@ -295,8 +297,8 @@ def test_device_refinement_loop(pkg, lib, prec):
             assert ok and conv == 1 and it == it0 and res <= tol
             assert abs(res - res0) <= 0.5 * res0 + 1e-300
             assert float(torch.linalg.norm(X - X0) / torch.linalg.norm(X0)) <= 1e-9
-        for _ in range(3):   # tol = 0: bounded by maxit on the device
-            X, ok, it, res, conv = solve(0.0, 3)
+        for _ in range(3):   # unreachable tolerance: bounded by maxit on the device
+            X, ok, it, res, conv = solve(never, 3)
             assert not ok and it == 3 and conv == 0 and np.isfinite(res)
             assert float(torch.linalg.norm(X - X0) / torch.linalg.norm(X0)) <= 1e-9
         X, ok, it, res, conv = solve(tol, 20)
