@@ -233,6 +233,8 @@ struct hss_plan_s {
   int64_t h_npacked = 0;                // its packed generator length
   hss_plan_s* tplan = nullptr;          // the adjoint's plan (hss_matmul_t), made on first use
   std::string ulv_why;                  // why the ULV reduction cannot factor this plan (empty: it can)
+  cudaStream_t host_st = nullptr;       // stream of the host-buffer solves (made on first use)
+  cudaEvent_t host_ev = nullptr;
   ~hss_plan_s();
 };
 
@@ -281,6 +283,8 @@ struct hss_factor_s {
 };
 
 hss_plan_s::~hss_plan_s() {
+  if (host_ev) cudaEventDestroy(host_ev);
+  if (host_st) cudaStreamDestroy(host_st);
   delete tplan;
   delete fused[0];
   delete fused[1];
@@ -2479,6 +2483,20 @@ int hss_ulvsolve_batch(hss_factor f, const double* const* dB, const int64_t* ldb
   return solve_impl(f, io, tol, maxit, stats, (cudaStream_t)stream);
 }
 
+// The stream of the host-buffer solves: the plan's own non-blocking stream,
+// ordered after the work already queued on the legacy default stream, so that
+// their launch sequences (and refinement loop) replay as graphs like those of
+// the device entry points on a user stream.  The calls return after their
+// results are on the host.
+int host_stream(hss_plan_s* P, cudaStream_t* out) {
+  if (!P->host_st) CUDA_TRY(cudaStreamCreateWithFlags(&P->host_st, cudaStreamNonBlocking));
+  if (!P->host_ev) CUDA_TRY(cudaEventCreateWithFlags(&P->host_ev, cudaEventDisableTiming));
+  CUDA_TRY(cudaEventRecord(P->host_ev, 0));
+  CUDA_TRY(cudaStreamWaitEvent(P->host_st, P->host_ev, 0));
+  *out = P->host_st;
+  return HSS_OK;
+}
+
 int hss_ulvsolve_host(hss_factor f, const double* B, int64_t ldb, int64_t r, double* X, int64_t ldx,
                       double tol, int32_t maxit, hss_solve_stats* stats) {
   if (!f) return fail(HSS_ERR_INVALID, "null factor");
@@ -2490,6 +2508,7 @@ int hss_ulvsolve_host(hss_factor f, const double* B, int64_t ldb, int64_t r, dou
   if (rc) return rc;
   if (r == 0) return HSS_OK;
   cudaStream_t st = 0;
+  if ((rc = host_stream(P, &st))) return rc;
   if ((rc = copy_in(f->hB, B, m, ldb, r, st))) return rc;
   CUDA_TRY(f->hX.ensure((size_t)n * r));
   rc = solve_impl(f, {Cols{f->hB.p, m, r, f->hX.p, n}}, tol, maxit, stats, st);
@@ -2519,6 +2538,7 @@ int hss_ulvfactsolve_host(hss_handle h, int32_t precision, const double* B, int6
   std::vector<Cols> io{Cols{B, ldb, r, X, ldx}};
   if ((rc = check_cols(h, io, true))) return rc;
   cudaStream_t st = 0;
+  if ((rc = host_stream(h, &st))) return rc;
   if ((rc = copy_in(f->hB, B, m, ldb, r, st))) return rc;
   CUDA_TRY(f->hX.ensure((size_t)n * std::max<int64_t>(r, 1)));
   rc = solve_impl(f, {Cols{f->hB.p, m, r, f->hX.p, n}}, tol, maxit, stats, st, true);

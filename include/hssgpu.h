@@ -294,7 +294,11 @@ int64_t hss_launch_counter(void);
  * HSS_OPT_GRAPHS = 1 replays the per-level launch sequences of factorizations
  * and solve passes issued on a non-default stream as CUDA graphs: the second
  * call with unchanged task lists, buffers and sizes is captured, later ones
- * replay the graph (no capture on the legacy default stream).
+ * replay the graph (no capture on the legacy default stream).  A solve with
+ * refinement (maxit <= 64) is then one graph: the convergence check runs on
+ * the device and sets the condition of a while node around the refinement
+ * step, and the host reads the loop's status once.  The "_host" solves run on
+ * the plan's own non-blocking stream, ordered after the legacy default stream.
  * HSS_OPT_SAMPLE_DF = 1 computes hss_sample's products in double-float
  * arithmetic on the FP32 pipe (~2^-47 relative per operation instead of
  * FP64's 2^-53, several times faster on GB300; entries of A and X must lie
