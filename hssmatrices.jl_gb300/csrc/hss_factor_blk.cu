@@ -826,6 +826,177 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
   const int g = tid >> 3, l8 = tid & 7;            // panel column / row g, lane l8 of its group
   const unsigned gm = 0xFFu << (lane & 24);        // the group's 8 lanes
 
+  if constexpr (S == 64) {
+    if (k <= BP && ku <= BP && mk <= BP && m - mk <= BP && kv <= BP) {
+      // Nodes of at most 64 x 64 with one QL and one LQ panel (the merges of
+      // rank-32 children): every reflector is applied, as soon as it is
+      // generated, to everything it acts on, each column (row) held in
+      // registers by a group of 8 lanes, one barrier per reflector.  QL: the
+      // U panel and D's columns (two per group); LQ: the panel rows, D's rows
+      // below them and V's columns (one each per group).  This replaces the
+      // panels' block updates (shared-memory GEMMs after the panel loops); the
+      // panels' T matrices and the L1 block inverses are still formed and
+      // stored for the blocked solve, so the factor storage is the same.
+      auto refl = [&](T(&x)[PE], const T(&vv)[PE], T tau) {
+        T w0 = T(0), w1 = T(0);
+#pragma unroll
+        for (int t = 0; t < PE; t += 2) {
+          w0 = fma_t(vv[t], x[t], w0);
+          w1 = fma_t(vv[t + 1], x[t + 1], w1);
+        }
+        const T w = gsum8(w0 + w1, gm) * tau;
+#pragma unroll
+        for (int t = 0; t < PE; ++t) x[t] = fma_t(-w, vv[t], x[t]);
+      };
+      // ---- QL of U (geqlf!, :39), applied to D (ormql!, :41) ----
+      {
+        T u[PE], dq0[PE], dq1[PE];
+#pragma unroll
+        for (int t = 0; t < PE; ++t) {
+          const int row = l8 + PL * t;
+          u[t] = (g < k && row < m) ? sW[row + g * LDU] : T(0);
+          dq0[t] = (g < n && row < m) ? sD[row + g * LDD] : T(0);
+          dq1[t] = (g + BP < n && row < m) ? sD[row + (g + BP) * LDD] : T(0);
+        }
+        auto gen = [&](int c, int buf) {   // the 8 lanes of column c
+          const int p = mk + c;
+          T sq[4] = {T(0), T(0), T(0), T(0)}, mine = T(0);
+#pragma unroll
+          for (int t = 0; t < PE; ++t) {
+            const int row = l8 + PL * t;
+            if (row < p) sq[t & 3] = fma_t(u[t], u[t], sq[t & 3]);
+            if (row == p) mine = u[t];
+          }
+          const T ss = gsum8((sq[0] + sq[1]) + (sq[2] + sq[3]), gm);
+          const T alpha = __shfl_sync(gm, mine, (lane & 24) | (p & 7));
+          T beta, tau, sc;
+          larfg_t(alpha, ss, beta, tau, sc);
+#pragma unroll
+          for (int t = 0; t < PE; ++t) {
+            const int row = l8 + PL * t;
+            if (row < p && tau != T(0)) u[t] *= sc;
+            if (row == p) u[t] = beta;
+            sv[buf * SVP + row] = row < p ? u[t] : (row == p ? T(1) : T(0));
+          }
+          if (l8 == 0) {
+            stau[buf] = tau;
+            ptau[c] = tau;
+            tq[c] = tau;
+          }
+        };
+        if (g == k - 1) gen(k - 1, 0);
+        __syncthreads();
+        for (int c = k - 1; c >= 0; --c) {
+          const int cur = (k - 1 - c) & 1;
+          const T tau = stau[cur];
+          const T* v = sv + cur * SVP;
+          T vv[PE];
+#pragma unroll
+          for (int t = 0; t < PE; ++t) vv[t] = v[l8 + PL * t];
+          if (g < c && tau != T(0)) refl(u, vv, tau);
+          if (c > 0 && g == c - 1) gen(c - 1, cur ^ 1);   // the next reflector first: it is on the critical path
+          if (tau != T(0)) {
+            if (g < n) refl(dq0, vv, tau);
+            if (g + BP < n) refl(dq1, vv, tau);
+          }
+          __syncthreads();
+        }
+#pragma unroll
+        for (int t = 0; t < PE; ++t) {
+          const int row = l8 + PL * t;
+          if (row < m) {
+            if (g < k) sW[row + g * LDU] = u[t];
+            if (g < n) sD[row + g * LDD] = dq0[t];
+            if (g + BP < n) sD[row + (g + BP) * LDD] = dq1[t];
+          }
+        }
+      }
+      __syncthreads();
+      ql_gram(sW, LDU, 0, k, mk, G);
+      blk_tmat(k, G, ptau, Tm, fb + nd.fTq);
+      for (int e = tid; e < m * ku; e += NT) gU[e] = sW[(e % m) + (e / m) * LDU];
+      __syncthreads();
+      // ---- LQ of D[0:mk, :] (gelqf!, :44), applied to the rows below (:47) and to V (:50) ----
+      {
+        T d[PE], dt[PE], vc[PE];
+#pragma unroll
+        for (int t = 0; t < PE; ++t) {
+          const int col = l8 + PL * t;
+          d[t] = (g < mk && col < n) ? sD[g + col * LDD] : T(0);
+          dt[t] = (mk + g < m && col < n) ? sD[(mk + g) + col * LDD] : T(0);
+          vc[t] = (g < kv && col < n) ? sV[col + g * LDV] : T(0);
+        }
+        auto gen = [&](int i, int buf) {   // the 8 lanes of row i
+          T sq[4] = {T(0), T(0), T(0), T(0)}, mine = T(0);
+#pragma unroll
+          for (int t = 0; t < PE; ++t) {
+            const int col = l8 + PL * t;
+            if (col > i) sq[t & 3] = fma_t(d[t], d[t], sq[t & 3]);
+            if (col == i) mine = d[t];
+          }
+          const T ss = gsum8((sq[0] + sq[1]) + (sq[2] + sq[3]), gm);
+          const T alpha = __shfl_sync(gm, mine, (lane & 24) | (i & 7));
+          T beta, tau, sc;
+          larfg_t(alpha, ss, beta, tau, sc);
+#pragma unroll
+          for (int t = 0; t < PE; ++t) {
+            const int col = l8 + PL * t;
+            if (col > i && tau != T(0)) d[t] *= sc;
+            if (col == i) d[t] = beta;
+            sv[buf * SVP + col] = col < i ? T(0) : (col == i ? T(1) : d[t]);
+          }
+          if (l8 == 0) {
+            stau[buf] = tau;
+            ptau[i] = tau;
+            tl[i] = tau;
+          }
+        };
+        if (g == 0) gen(0, 0);
+        __syncthreads();
+        for (int i = 0; i < mk; ++i) {
+          const int cur = i & 1;
+          const T tau = stau[cur];
+          const T* v = sv + cur * SVP;
+          T vv[PE];
+#pragma unroll
+          for (int t = 0; t < PE; ++t) vv[t] = v[l8 + PL * t];
+          if (g > i && g < mk && tau != T(0)) refl(d, vv, tau);
+          if (i + 1 < mk && g == i + 1) gen(i + 1, cur ^ 1);
+          if (tau != T(0)) {
+            if (mk + g < m) refl(dt, vv, tau);
+            if (g < kv) refl(vc, vv, tau);
+          }
+          __syncthreads();
+        }
+        // write back; the reflectors also reflector-major (zero-padded to YP - 4
+        // columns) for the Gram matrix, and transposed to global memory
+        T* gQt = fb + nd.fQt;
+        T* Yc = sW;   // U is in global memory now
+#pragma unroll
+        for (int t = 0; t < PE; ++t) {
+          const int col = l8 + PL * t;
+          const T y = col < g ? T(0) : (col == g ? T(1) : d[t]);
+          if (col < n) {
+            if (g < mk) {
+              sD[g + col * LDD] = d[t];
+              gQt[col + (int64_t)g * n] = y;
+            }
+            if (mk + g < m) sD[(mk + g) + col * LDD] = dt[t];
+            if (g < kv) sV[col + g * LDV] = vc[t];
+          }
+          if (g < mk && col < YP - 4) Yc[g * YP + col] = col < n ? y : T(0);
+        }
+        __syncthreads();
+        lq_gram(Yc, YP, n, mk, G);
+        blk_tmat(mk, G, ptau, Tm, fb + nd.fTl);
+      }
+      blk_linv(mk, sD, LDD, sW, fb + nd.fLi);
+      for (int e = tid; e < m * n; e += NT) gD[e] = sD[(e % m) + (e / m) * LDD];
+      for (int e = tid; e < n * kv; e += NT) gV[e] = sV[(e % n) + (e / n) * LDV];
+      return;
+    }
+  }
+
   // ---- P1: QL of U, panels of BP columns from the last -------------------------
   for (int c1 = k; c1 > 0; c1 -= BP) {
     const int c0 = max(0, c1 - BP), nb = c1 - c0;
