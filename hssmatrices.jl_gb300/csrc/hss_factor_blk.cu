@@ -826,10 +826,11 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 2 : 1))
   const int g = tid >> 3, l8 = tid & 7;            // panel column / row g, lane l8 of its group
   const unsigned gm = 0xFFu << (lane & 24);        // the group's 8 lanes
 
-  if constexpr (S == 64) {
+  if constexpr (S == 64 && sizeof(T) == sizeof(float)) {
     if (k <= BP && ku <= BP && mk <= BP && m - mk <= BP && kv <= BP) {
-      // Nodes of at most 64 x 64 with one QL and one LQ panel (the merges of
-      // rank-32 children): every reflector is applied, as soon as it is
+      // FP32 nodes of at most 64 x 64 with one QL and one LQ panel (the merges
+      // of rank-32 children; FP64 keeps the block updates, measured faster on
+      // its slower FMA pipe): every reflector is applied, as soon as it is
       // generated, to everything it acts on, each column (row) held in
       // registers by a group of 8 lanes, one barrier per reflector.  QL: the
       // U panel and D's columns (two per group); LQ: the panel rows, D's rows
