@@ -50,7 +50,7 @@ EXPORTS = [
     "hss_ulv_cols", "hss_matmul", "hss_matmul_host", "hss_matmul_batch", "hss_ulvfactor",
     "hss_factor_destroy", "hss_ulvsolve", "hss_ulvsolve_host", "hss_ulvsolve_batch",
     "hss_ulvfactsolve_host", "hss_factor_bytes", "hss_autotune", "hss_autotune_info", "hss_last_error", "hss_version", "hss_ulvrefactor",
-    "hss_trace_begin", "hss_trace_end", "hss_launch_counter", "hss_set_option", "hss_matmul_noalloc",
+    "hss_trace_begin", "hss_trace_end", "hss_trace_times", "hss_launch_counter", "hss_set_option", "hss_matmul_noalloc",
     "hss_batcher_create", "hss_batcher_destroy", "hss_batcher_factor", "hss_batcher_solve",
     "hss_sample", "hss_sumsq", "hss_rc_create", "hss_rc_destroy", "hss_rc_size", "hss_rc_compress",
     "hss_rc_ranks", "hss_rc_sample", "hss_export_size", "hss_export", "hss_getindex", "hss_full", "hss_hssmul", "hss_recompress", "hss_orthonormalize",
@@ -122,6 +122,7 @@ def _declare(lib):
         "hss_ulvrefactor": (C.c_int, [P, P]),
         "hss_trace_begin": (C.c_int, [I32]),
         "hss_trace_end": (C.c_int, [C.POINTER(D), PI64]),
+        "hss_trace_times": (C.c_int, [C.POINTER(D), I64, PI64]),
         "hss_launch_counter": (C.c_int64, []),
         "hss_set_option": (C.c_int, [I32, I64]),
         "hss_batcher_create": (C.c_int, [C.POINTER(P)]),

@@ -2368,6 +2368,21 @@ int hss_trace_end(double* total_ms, int64_t* launches) {
   return HSS_OK;
 }
 
+int hss_trace_times(double* ms, int64_t cap, int64_t* launches) {
+  int64_t n = 0;
+  for (size_t i = 0; i + 1 < g_trace.used; i += 2) {
+    float t = 0.f;
+    CUDA_TRY(cudaEventSynchronize(g_trace.pool[i + 1]));
+    CUDA_TRY(cudaEventElapsedTime(&t, g_trace.pool[i], g_trace.pool[i + 1]));
+    if (ms && n < cap) ms[n] = t;
+    ++n;
+  }
+  g_trace.kind = -1;
+  g_trace.used = 0;
+  if (launches) *launches = n;
+  return HSS_OK;
+}
+
 int64_t hss_launch_counter(void) { return g_launches.load(); }
 
 int hss_set_option(int32_t option, int64_t value) {

@@ -920,6 +920,7 @@ __global__ void __launch_bounds__(PT, 4) pmv_kernel(PmvArgs a) {
 // or four of one row (U F) with their own accumulator chains.
 
 constexpr int XW = 32;   // columns per block of the leaf kernels
+constexpr int LB = 16;   // global loads in flight per thread while a block stages its operands
 
 __device__ void leaf_vtx_unit(const Task tk, const Slot* __restrict__ slots, int cb) {
   extern __shared__ __align__(16) unsigned char ext_smem[];
@@ -933,18 +934,31 @@ __device__ void leaf_vtx_unit(const Task tk, const Slot* __restrict__ slots, int
   const int ld = n | 1;             // odd: a warp's rows c (or columns q) fall in distinct bank pairs
   float2* Vs = (float2*)ext_smem;   // n x kv, ld ld
   float2* Xs = Vs + ld * kv;        // n x nc, ld ld
+  // staging: LB loads in flight per thread before the shared-memory stores
   const float2* V = P::gen(sl, nd.V);
-  for (int e = threadIdx.x; e < n * kv; e += PT) Vs[e % n + (e / n) * ld] = __ldg(V + e);
-  const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
-  for (int e0 = threadIdx.x; e0 < n * nc; e0 += 4 * PT) {
-    double v[4];
+  for (int e0 = threadIdx.x; e0 < n * kv; e0 += LB * PT) {
+    float2 v[LB];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < LB; ++u) {
+      const int e = e0 + u * PT;
+      v[u] = e < n * kv ? __ldg(V + e) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int e = e0 + u * PT;
+      if (e < n * kv) Vs[e % n + (e / n) * ld] = v[u];
+    }
+  }
+  const double* X = sl.B + nd.col0 + (int64_t)j0 * sl.ldb;
+  for (int e0 = threadIdx.x; e0 < n * nc; e0 += LB * PT) {
+    double v[LB];
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
       const int e = e0 + u * PT;
       v[u] = e < n * nc ? __ldg(X + e % n + (int64_t)(e / n) * sl.ldb) : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < LB; ++u) {
       const int e = e0 + u * PT;
       if (e < n * nc) Xs[e % n + (e / n) * ld] = split_bits(v[u]);
     }
@@ -989,9 +1003,33 @@ __device__ void leaf_uf_unit(const Task tk, const Slot* __restrict__ slots, int 
   float2* Fs = Us + m * ku;         // ku x nc, ld ku
   if (ku > 0) {
     const float2* U = P::gen(sl, nd.U);
-    for (int e = threadIdx.x; e < m * ku; e += PT) Us[e] = __ldg(U + e);
+    for (int e0 = threadIdx.x; e0 < m * ku; e0 += LB * PT) {
+      float2 v[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        const int e = e0 + u * PT;
+        v[u] = e < m * ku ? __ldg(U + e) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        const int e = e0 + u * PT;
+        if (e < m * ku) Us[e] = v[u];
+      }
+    }
     const float2* F = sl.ws2 + nd.wf + (int64_t)j0 * sl.ldws;
-    for (int e = threadIdx.x; e < ku * nc; e += PT) Fs[e] = __ldcg(F + e % ku + (int64_t)(e / ku) * sl.ldws);
+    for (int e0 = threadIdx.x; e0 < ku * nc; e0 += LB * PT) {
+      float2 v[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        const int e = e0 + u * PT;
+        v[u] = e < ku * nc ? __ldcg(F + e % ku + (int64_t)(e / ku) * sl.ldws) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        const int e = e0 + u * PT;
+        if (e < ku * nc) Fs[e] = v[u];
+      }
+    }
   }
   __syncthreads();
   const float2* T = (const float2*)sl.tmp + nd.row0 + (int64_t)j0 * sl.ldt2;
@@ -1009,6 +1047,19 @@ __device__ void leaf_uf_unit(const Task tk, const Slot* __restrict__ slots, int 
     const int i0 = rb * 64 + lane, i1 = i0 + 32;
     const int qb = cb * 4, nq = min(4, nc - qb);
     const bool a0 = i0 < m, a1 = i1 < m;
+    // the epilogue's operands (D X pairs, Y) loaded before the accumulation,
+    // so that their latency overlaps it
+    float2 tp[2][4];
+    double yp[2][4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = h ? i1 : i0;
+        const bool ok = (h ? a1 : a0) && q < nq;
+        tp[h][q] = ok ? __ldcg(T + i + (int64_t)(qb + q) * sl.ldt2) : make_float2(0.f, 0.f);
+        yp[h][q] = (ok && yterm) ? __ldcg(Y + i + (int64_t)(qb + q) * sl.ldy) : 0.0;
+      }
     Acc acc0[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
     Acc acc1[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
     const float2* f = Fs + qb * ku;
@@ -1031,9 +1082,9 @@ __device__ void leaf_uf_unit(const Task tk, const Slot* __restrict__ slots, int 
         const int i = h ? i1 : i0;
         if ((h ? a1 : a0) && q < nq) {
           Acc t = h ? acc1[q] : acc0[q];
-          P::addE(t, __ldcg(T + i + (int64_t)(qb + q) * sl.ldt2));
+          P::addE(t, tp[h][q]);
           double v = sl.alpha * P::dbl(t);
-          if (yterm) v += sl.beta * __ldcg(Y + i + (int64_t)(qb + q) * sl.ldy);
+          if (yterm) v += sl.beta * yp[h][q];
           C[i + (int64_t)(qb + q) * sl.ldc] = v;
           v2 = fma(v, v, v2);
         }

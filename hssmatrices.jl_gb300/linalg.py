@@ -302,6 +302,15 @@ def trace_end():
     return ms.value, n.value
 
 
+def trace_times(cap=4096):
+    """Per-launch device milliseconds (launch order) since ``trace_begin``; ends the trace."""
+    lib = _lib.load()
+    buf = np.zeros(cap, dtype=np.float64)
+    n = C.c_int64()
+    check(lib.hss_trace_times(buf.ctypes.data_as(_lib.PD), cap, C.byref(n)))
+    return buf[:min(n.value, cap)].tolist()
+
+
 def launch_counter():
     return _lib.load().hss_launch_counter()
 

@@ -223,6 +223,10 @@ enum {
 };
 int hss_trace_begin(int32_t kind);
 int hss_trace_end(double* total_ms, int64_t* launches);
+/* Like hss_trace_end, and the device time of every traced launch in launch
+ * order (ms[i] for i < cap; *launches is the count, which may exceed cap):
+ * per tree level for the level kinds. */
+int hss_trace_times(double* ms, int64_t cap, int64_t* launches);
 
 /* Entries of a single-tree handle: out(i, j) = A(rows[i], cols[j]) into the
  * nr x nc device matrix dOut (column-major, ld ldo >= nr), 0-based indices in
