@@ -1047,19 +1047,6 @@ __device__ void leaf_uf_unit(const Task tk, const Slot* __restrict__ slots, int 
     const int i0 = rb * 64 + lane, i1 = i0 + 32;
     const int qb = cb * 4, nq = min(4, nc - qb);
     const bool a0 = i0 < m, a1 = i1 < m;
-    // the epilogue's operands (D X pairs, Y) loaded before the accumulation,
-    // so that their latency overlaps it
-    float2 tp[2][4];
-    double yp[2][4];
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i = h ? i1 : i0;
-        const bool ok = (h ? a1 : a0) && q < nq;
-        tp[h][q] = ok ? __ldcg(T + i + (int64_t)(qb + q) * sl.ldt2) : make_float2(0.f, 0.f);
-        yp[h][q] = (ok && yterm) ? __ldcg(Y + i + (int64_t)(qb + q) * sl.ldy) : 0.0;
-      }
     Acc acc0[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
     Acc acc1[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
     const float2* f = Fs + qb * ku;
@@ -1082,9 +1069,9 @@ __device__ void leaf_uf_unit(const Task tk, const Slot* __restrict__ slots, int 
         const int i = h ? i1 : i0;
         if ((h ? a1 : a0) && q < nq) {
           Acc t = h ? acc1[q] : acc0[q];
-          P::addE(t, tp[h][q]);
+          P::addE(t, __ldcg(T + i + (int64_t)(qb + q) * sl.ldt2));
           double v = sl.alpha * P::dbl(t);
-          if (yterm) v += sl.beta * yp[h][q];
+          if (yterm) v += sl.beta * __ldcg(Y + i + (int64_t)(qb + q) * sl.ldy);
           C[i + (int64_t)(qb + q) * sl.ldc] = v;
           v2 = fma(v, v, v2);
         }
