@@ -66,42 +66,18 @@ __device__ void mm(int R, int K, const float* A, int lda, const float* B, float*
   }
 }
 
-constexpr int SLB = 16;   // global loads in flight per thread while a block stages an operand
-
-// Stages elements e < total of a block: get(e) loads element e from global
-// memory, put(e, v) stores it on chip; SLB loads are issued before their stores.
-template <typename Get, typename Put>
-__device__ __forceinline__ void stage(int total, Get&& get, Put&& put) {
-  for (int e0 = threadIdx.x; e0 < total; e0 += SLB * BT) {
-    float v[SLB];
-#pragma unroll
-    for (int u = 0; u < SLB; ++u) {
-      const int e = e0 + u * BT;
-      v[u] = e < total ? get(e) : 0.f;
-    }
-#pragma unroll
-    for (int u = 0; u < SLB; ++u) {
-      const int e = e0 + u * BT;
-      if (e < total) put(e, v[u]);
-    }
-  }
-}
-
-// dst(i + l*ldd) = src(i + l*lds), i < rows, l < cols.
+// dst(i + l*ldd) = src(i + l*lds), i < rows, l < cols (warp per column).
 __device__ void stage_cm(float* dst, int ldd, const float* src, int64_t lds, int rows, int cols) {
-  stage(rows * cols, [&](int e) { return __ldg(src + e % rows + (int64_t)(e / rows) * lds); },
-        [&](int e, float v) { dst[e % rows + (e / rows) * ldd] = v; });
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int l = w; l < cols; l += BT / 32)
+    for (int i = lane; i < rows; i += 32) dst[i + l * ldd] = __ldg(src + i + (int64_t)l * lds);
 }
 
 // dst(l + i*ldd) = src(i + l*lds): the transpose of a column-major block.
 __device__ void stage_tr(float* dst, int ldd, const float* src, int64_t lds, int rows, int cols) {
-  stage(rows * cols, [&](int e) { return __ldg(src + e % rows + (int64_t)(e / rows) * lds); },
-        [&](int e, float v) { dst[e / rows + (e % rows) * ldd] = v; });
-}
-
-// the 32 x 32 panel matrix at g (T or an L1 block inverse)
-__device__ void stage_pb(float* dst, const float* g) {
-  stage(PB * PB, [&](int e) { return __ldg(g + e); }, [&](int e, float v) { dst[e] = v; });
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int l = w; l < cols; l += BT / 32)
+    for (int i = lane; i < rows; i += 32) dst[l + i * ldd] = __ldg(src + i + (int64_t)l * lds);
 }
 
 // Shared-memory layout (floats) of the two kernels, from the level's largest sizes.
@@ -173,15 +149,12 @@ __global__ void __launch_bounds__(BT) bsolve_up(const Task* __restrict__ tasks, 
   // ---- b (and the branch part of u)
   if (nd.leaf) {
     const double* B = sl.B + nd.row0;
-    stage(
-        m * CW,
-        [&](int e) {
-          const int col = j0 + e / m;
-          if (col >= r) return 0.f;
-          const double sc = sl.colinv ? sl.colinv[col] : 1.0;
-          return (float)(B[e % m + (int64_t)col * sl.ldb] * sc);
-        },
-        [&](int e, float v) { sb[(e % m) * BL + e / m] = v; });
+    for (int q = w; q < CW; q += BT / 32) {
+      const int col = j0 + q;
+      const double sc = (col < r && sl.colinv) ? sl.colinv[col] : 1.0;
+      for (int row = lane; row < m; row += 32)
+        sb[row * BL + q] = col < r ? (float)(B[row + (int64_t)col * sl.ldb] * sc) : 0.f;
+    }
     if (mk == 0)
       for (int e = tid; e < kv * BL; e += BT) su[e] = 0.f;
   } else {
@@ -251,19 +224,14 @@ __global__ void __launch_bounds__(BT) bsolve_up(const Task* __restrict__ tasks, 
     for (int c1 = k; c1 > 0; c1 -= PB) {
       const int c0 = max(0, c1 - PB), nb = c1 - c0;
       const int lm = r4(m);
-      stage(
-          m * nb,
-          [&](int e) {
-            const int row = e % m, c = e / m;
-            const int p = mk + c0 + c;
-            return row < p ? U[row + (int64_t)(c0 + c) * m] : (row == p ? 1.f : 0.f);
-          },
-          [&](int e, float y) {
-            const int row = e % m, c = e / m;
-            sA[c + row * KPS] = y;    // Y^T operand
-            sB[row + c * lm] = y;     // Y operand
-          });
-      stage_pb(sT, fb + nd.fTq + (int64_t)((k - c1) / PB) * 1024);
+      for (int e = tid; e < m * nb; e += BT) {
+        const int row = e % m, c = e / m;
+        const int p = mk + c0 + c;
+        const float y = row < p ? U[row + (int64_t)(c0 + c) * m] : (row == p ? 1.f : 0.f);
+        sA[c + row * KPS] = y;    // Y^T operand
+        sB[row + c * lm] = y;     // Y operand
+      }
+      for (int e = tid; e < PB * PB; e += BT) sT[e] = fb[nd.fTq + (int64_t)((k - c1) / PB) * 1024 + e];
       __syncthreads();
       mm<MM_SET>(nb, m, sA, KPS, sb, sX);   // X = Y^T b
       __syncthreads();
@@ -281,7 +249,7 @@ __global__ void __launch_bounds__(BT) bsolve_up(const Task* __restrict__ tasks, 
         mm<MM_SUB>(nb, i0, sA, PB, sb, sb + i0 * BL);
         __syncthreads();
       }
-      stage_pb(sT, fb + nd.fLi + (int64_t)(i0 / PB) * 1024);
+      for (int e = tid; e < PB * PB; e += BT) sT[e] = fb[nd.fLi + (int64_t)(i0 / PB) * 1024 + e];
       __syncthreads();
       mm<MM_SET>(nb, nb, sT, PB, sb + i0 * BL, sX);
       __syncthreads();
@@ -293,9 +261,10 @@ __global__ void __launch_bounds__(BT) bsolve_up(const Task* __restrict__ tasks, 
     {
       const float* V = fb + nd.fV;
       const int lk = r4(kv);
-      const int vn = nd.n;
-      stage(mk * kv, [&](int e) { return __ldg(V + e % mk + (int64_t)(e / mk) * vn); },
-            [&](int e, float v) { sB[e / mk + (e % mk) * lk] = v; });
+      for (int e = tid; e < mk * kv; e += BT) {
+        const int l = e % mk, c = e / mk;
+        sB[c + l * lk] = V[l + (int64_t)c * nd.n];
+      }
     }
     __syncthreads();
     mm<MM_SUB>(mr, mk, sA, r4(mr), sb, sb + mk * BL);
@@ -345,13 +314,11 @@ __global__ void __launch_bounds__(BT) bsolve_down(const Task* __restrict__ tasks
   float* sA = smf + ly.sA;
   float* sB = smf + ly.sB;
   const int ncol = min(CW, r - j0);
-  stage(
-      n * CW,
-      [&](int e) {
-        const int q = e / n;
-        return q < ncol ? ws[nd.wx + e % n + (int64_t)(j0 + q) * ld] : 0.f;
-      },
-      [&](int e, float v) { sb[(e % n) * BL + e / n] = v; });
+  for (int q = w; q < CW; q += BT / 32) {
+    const bool cv = q < ncol;
+    const int64_t co = (int64_t)(j0 + q) * ld;
+    for (int row = lane; row < n; row += 32) sb[row * BL + q] = cv ? ws[nd.wx + row + co] : 0.f;
+  }
   if (mk > 0) {
     const float* Qt = fb + nd.fQt;   // n x mk: reflector i in column i
     const int ln = r4(n);
@@ -360,7 +327,7 @@ __global__ void __launch_bounds__(BT) bsolve_down(const Task* __restrict__ tasks
       __syncthreads();
       stage_tr(sA, KPS, Qt + (int64_t)i0 * n, n, n, nb);   // Y (rows = reflectors)
       stage_cm(sB, ln, Qt + (int64_t)i0 * n, n, n, nb);    // Y^T
-      stage_pb(sT, fb + nd.fTl + (int64_t)p * 1024);
+      for (int e = tid; e < PB * PB; e += BT) sT[e] = fb[nd.fTl + (int64_t)p * 1024 + e];
       __syncthreads();
       mm<MM_SET>(nb, n, sA, KPS, sb, sX);    // X = Y x
       __syncthreads();
