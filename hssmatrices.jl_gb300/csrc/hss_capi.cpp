@@ -269,15 +269,18 @@ struct hss_factor_s {
   SlotTable fac_slots;
   SolveBufs bufs;
   DBuf<double> hB, hX;                  // staging for the _host solve
-  // the pipelined factorization + first solve (hss_ulvfactsolve): a second
-  // stream for the upward solve and events [fork, join, level 0, level 1, ...]
+  // the pipelined factorization + first solve (hss_ulvfactsolve): a stream for
+  // the upward solve, one for the factorization, and events [fork, solve join,
+  // factorization join, level 0, level 1, ...]
   cudaStream_t pipe_st = nullptr;
+  cudaStream_t fac_st = nullptr;        // the factorization's stream there (highest priority)
   std::vector<cudaEvent_t> pipe_ev;
   GraphCache pipe_graph;
   ~hss_factor_s() {
     pipe_graph.reset();
     for (cudaEvent_t e : pipe_ev) cudaEventDestroy(e);
     if (pipe_st) cudaStreamDestroy(pipe_st);
+    if (fac_st) cudaStreamDestroy(fac_st);
     if (d_fac) cudaFree(d_fac);
   }
 };
@@ -1270,7 +1273,7 @@ uint64_t levels_key(const Levels& L, const void* slots, int64_t extra) {
 // with graphs enabled on a non-default stream, as a replayed CUDA graph: the
 // second run with an unchanged key is captured and every later one replays it.
 template <typename F>
-int graphed(GraphCache& gc, uint64_t key, cudaStream_t st, bool& flag, F&& launch) {
+int graphed(GraphCache& gc, uint64_t key, cudaStream_t st, bool& flag, F&& launch, unsigned inst_flags = 0) {
   const bool can = g_graphs && st != nullptr && g_trace.kind < 0 && g_pick_force < 0;
   if (!can || (gc.key != key && gc.seen != key)) {
     if (can) gc.seen = key;
@@ -1287,7 +1290,7 @@ int graphed(GraphCache& gc, uint64_t key, cudaStream_t st, bool& flag, F&& launc
     t_capture = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    const cudaError_t ie = cudaGraphInstantiate(&gc.exec, g, 0);
+    const cudaError_t ie = cudaGraphInstantiate(&gc.exec, g, inst_flags);
     cudaGraphDestroy(g);
     if (ie != cudaSuccess) {
       gc.exec = nullptr;
@@ -1410,11 +1413,12 @@ int solve_pass(const std::vector<Item>& items, const Levels& L, const double* sc
 }
 
 // The factorization of f's plan and the first solve pass of `items` (all on
-// f's plan) in one launch sequence: level h is factored on st, then the
-// upward solve of level h runs on a second stream once that level is done
-// (an event per level), so the upward solve runs one level behind the
-// factorization instead of after it; the downward solve follows both on st.
-// Replayed as one CUDA graph (fork and join through events) where graphs apply.
+// f's plan) in one launch sequence: level h is factored on a stream of the
+// highest priority, then the upward solve of level h runs on a second stream
+// once that level is done (an event per level), so the upward solve runs one
+// level behind the factorization instead of after it; the downward solve
+// follows both on st.  Replayed as one CUDA graph (fork and join through
+// events, node priorities kept) where graphs apply.
 template <typename T>
 int factsolve_prep(hss_factor_s* f, const std::vector<Item>& items, const Levels& L, const double* scale,
                    const int64_t* off, int64_t rtot, SlotTable& table, cudaStream_t st, PassPrep& pp) {
@@ -1450,7 +1454,12 @@ int factsolve_prep(hss_factor_s* f, const std::vector<Item>& items, const Levels
   for (size_t h = 0; h < L.by_h->size(); ++h) all_fast = factor_level_fast<T>((*L.by_h)[h]) && all_fast;
   pp.blocked = all_fast && sizeof(T) == sizeof(float);
   if (!f->pipe_st) CUDA_TRY(cudaStreamCreateWithFlags(&f->pipe_st, cudaStreamNonBlocking));
-  while (f->pipe_ev.size() < 2 + L.by_h->size()) {
+  if (!f->fac_st) {
+    int least = 0, greatest = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CUDA_TRY(cudaStreamCreateWithPriority(&f->fac_st, cudaStreamNonBlocking, greatest));
+  }
+  while (f->pipe_ev.size() < 3 + L.by_h->size()) {
     cudaEvent_t e = nullptr;
     CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     f->pipe_ev.push_back(e);
@@ -1471,16 +1480,21 @@ cudaError_t factsolve_issue(hss_factor_s* f, const Levels& L, const SlotTable& t
                             cudaStream_t st) {
   cudaError_t ev_err = cudaSuccess;
   auto chk = [&](cudaError_t e) { if (e != cudaSuccess && ev_err == cudaSuccess) ev_err = e; };
-  cudaStream_t s2 = f->pipe_st;
+  // the factorization on the highest-priority stream, so that the merges (a
+  // chain of small launches) are scheduled ahead of the upward solve's blocks
+  cudaStream_t s2 = f->pipe_st, sf = f->fac_st;
   chk(cudaEventRecord(f->pipe_ev[0], st));
+  chk(cudaStreamWaitEvent(sf, f->pipe_ev[0], 0));
   chk(cudaStreamWaitEvent(s2, f->pipe_ev[0], 0));
   for (size_t h = 0; h < L.by_h->size(); ++h) {
-    run_factor_level<T>(L, h, f->fac_slots.dev.p, st);
-    chk(cudaEventRecord(f->pipe_ev[2 + h], st));
-    chk(cudaStreamWaitEvent(s2, f->pipe_ev[2 + h], 0));
+    run_factor_level<T>(L, h, f->fac_slots.dev.p, sf);
+    chk(cudaEventRecord(f->pipe_ev[3 + h], sf));
+    chk(cudaStreamWaitEvent(s2, f->pipe_ev[3 + h], 0));
     run_solve_up_level<T>(L, h, table.dev.p, (int)pp.rmax, s2, pp.blocked, &f->tune_up);
   }
+  chk(cudaEventRecord(f->pipe_ev[2], sf));
   chk(cudaEventRecord(f->pipe_ev[1], s2));
+  chk(cudaStreamWaitEvent(st, f->pipe_ev[2], 0));
   chk(cudaStreamWaitEvent(st, f->pipe_ev[1], 0));
   run_solve_down<T>(L, table.dev.p, (int)pp.rmax, st, pp.blocked, &f->tune_down);
   return ev_err;
@@ -1494,10 +1508,13 @@ int factsolve_pass(hss_factor_s* f, const std::vector<Item>& items, const Levels
   if (rc) return rc;
   bool unused = false;
   cudaError_t ev_err = cudaSuccess;
-  rc = graphed(f->pipe_graph, pp.key, st, unused, [&] {
-    ev_err = factsolve_issue<T>(f, L, table, pp, st);
-    return true;
-  });
+  rc = graphed(
+      f->pipe_graph, pp.key, st, unused,
+      [&] {
+        ev_err = factsolve_issue<T>(f, L, table, pp, st);
+        return true;
+      },
+      cudaGraphInstantiateFlagUseNodePriority);
   if (rc) return rc;
   if (ev_err != cudaSuccess) return cuda_fail(ev_err, "pipelined factorization events");
   CUDA_TRY(cudaGetLastError());
@@ -1582,7 +1599,9 @@ bool record_loop(GraphCache& gc, uint64_t key, int64_t& body_launches, cudaStrea
     }
   }
   cudaGraphExec_t ex = nullptr;
-  if (ok && cudaGraphInstantiate(&ex, G, 0) != cudaSuccess) {
+  // kernel nodes keep the priority of the stream they were recorded from (the
+  // factorization's high-priority stream)
+  if (ok && cudaGraphInstantiate(&ex, G, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess) {
     ex = nullptr;
     ok = false;
   }
