@@ -305,3 +305,31 @@ def test_device_refinement_loop(pkg, lib, prec):
         assert ok and it == it0
     finally:
         lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 0)
+
+
+def test_trace_per_level_times(pkg, lib):
+    """hss_trace_times: one device time per traced launch, in launch order, for
+    every level of an upward solve (the tree's 7 levels at n = 8192, leafsize
+    128) and of the factorization's merges; their sum is the summed time
+    hss_trace_end reports for the same launches."""
+    torch = pytest.importorskip("torch")
+    from hssmatrices_gb300 import linalg as L
+    n, r = 8192, 4
+    A = pkg.synthetic_hss(n, 128, 16, np.random.default_rng(8))
+    F = A.device().ulvfactor("fp32")
+    B = torch.randn((r, n), dtype=torch.float64, device="cuda")
+    X = torch.empty_like(B)
+    F.solve_device(B, n, r, X, n, tol=-1.0)   # warm-up
+    torch.cuda.synchronize()
+    L.trace_begin("solve_up")
+    F.solve_device(B, n, r, X, n, tol=-1.0)
+    t = L.trace_times()
+    assert len(t) == 7 and all(v > 0 for v in t)
+    L.trace_begin("factor_merge")
+    F.refactor()
+    t = L.trace_times()
+    L.trace_begin("factor_merge")
+    F.refactor()
+    total, count = L.trace_end()
+    assert len(t) == count == 6 and all(v > 0 for v in t)
+    assert abs(sum(t) - total) <= 0.5 * total
