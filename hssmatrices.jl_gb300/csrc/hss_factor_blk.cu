@@ -15,6 +15,11 @@
 //       to the rows below it, C <- C - (C Y^T) T Y (ormlq!, :47), and to V,
 //       V <- V - Y^T T^T Y V (ormlq!('L', 'N'), :50).
 //
+// FP32 nodes of at most 64 x 64 with a single QL and a single LQ panel (the
+// merges of rank-32 children) skip the block updates instead: each reflector
+// is applied to D (QL) or to D's trailing rows and V (LQ) in the panel loop
+// itself, as it is generated; T and the L1 inverses are still stored.
+//
 // Y is never copied for the QL panels: it is read from the panel's columns of
 // U (entries above the pivot, an implicit 1 at the pivot, zeros below); the LQ
 // panel is copied reflector-major (rows of D are strided in shared memory).
