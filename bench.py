@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--roofline-kernel", default="factor_leaf")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="precision workload: skip the batching and compression headlines")
     p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch", "compress", "matvec"])
     p.add_argument("--compress-n", type=int, default=16384)
     p.add_argument("--requests", type=int, default=10000)
@@ -426,6 +428,18 @@ def run_ours(args, rank, world, local_rank):
     }
     for rr, us in matvec_us.items():
         line[f"matvec_r{rr}_us"] = us
+    # the batching and compression workloads' headlines (their own runs,
+    # --workload batch / compress, add the FP64 and CPU comparisons)
+    if not args.no_extras:
+        del F32, F64, dev
+        gc.collect()
+        torch.cuda.empty_cache()
+        line["batch"] = batch_headline(pkg, args)
+        line["batch_ms"] = line["batch"]["ms_per_step"]
+        gc.collect()
+        torch.cuda.empty_cache()
+        line["compress"] = compress_headline(pkg, args.compress_n)
+        line["compress_ms"] = line["compress"]["ms"]
     print(json.dumps(line), flush=True)
     return 0
 
@@ -533,6 +547,88 @@ def run_serve(args):
     return 0
 
 
+def batch_trees(pkg, count):
+    """The batching workload's matrices (seed 2): n uniform 1024..16384 step 128,
+    leafsize in {64, 128, 256}, k 8..48, and r 1..16 right-hand sides each."""
+    import numpy as np
+    rng = np.random.default_rng(2)
+    trees, rs = [], []
+    for _ in range(count):
+        n = int(rng.integers(1024 // 128, 16384 // 128 + 1)) * 128
+        ls = int(rng.choice([64, 128, 256]))
+        k = int(rng.integers(8, 49))
+        trees.append(pkg.synthetic_hss(n, ls, k, rng))
+        rs.append(int(rng.integers(1, 17)))
+    return trees, rs
+
+
+def batch_headline(pkg, args, steps=5):
+    """The batching workload's headline alone: FP32 ULV factor + solve with
+    refinement of all matrices of the forest per step (graphs, autotuned), the
+    mean of `steps` timed steps, and the largest true residual."""
+    import torch
+    trees, rs = batch_trees(pkg, args.matrices)
+    forest = pkg.DeviceHss.from_trees(trees)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        Bs = [torch.randn((r, t.size()[0]), dtype=torch.float64, device="cuda") for t, r in zip(trees, rs)]
+        Xs = [torch.empty_like(b) for b in Bs]
+    stream.synchronize()
+    ns = [t.size()[0] for t in trees]
+    F = forest.ulvfactor("fp32", stream=stream)
+    F.autotune(max(rs), stream=stream)
+    for _ in range(3):
+        F.refactor(stream=stream)
+        F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=args.tol, maxit=20, stream=stream)
+    stream.synchronize()
+    times = []
+    for _ in range(steps):
+        stream.synchronize()
+        t0 = time.perf_counter()
+        F.refactor(stream=stream)
+        F.solve_batch_device(Bs, ns, rs, Xs, ns, tol=args.tol, maxit=20, stream=stream)
+        stream.synchronize()
+        times.append(time.perf_counter() - t0)
+    with torch.cuda.stream(stream):
+        Rs = [b.clone() for b in Bs]
+        forest.matmul_batch_device(Xs, ns, rs, Rs, ns, alpha=-1.0, beta=1.0, stream=stream)
+        res = max(float((torch.linalg.norm(R, dim=1) / torch.linalg.norm(b, dim=1)).max()) for R, b in zip(Rs, Bs))
+    stream.synchronize()
+    ms = 1000.0 * statistics.mean(times)
+    return {"workload": f"{args.matrices} matrices (the batch workload), FP32 ULV factor + solve to {args.tol:g}",
+            "ms_per_step": ms, "matrix_solves_per_s": 1000.0 * args.matrices / ms, "max_residual": res,
+            "steps": steps}
+
+
+def compress_headline(pkg, n, steps=3):
+    """The compression workload's headline alone: randcompress_adaptive of the
+    Cauchy matrix (n, leafsize 128, kest 10, 1e-9) with FP64 sampling, median
+    of `steps` calls."""
+    import numpy as np
+    import torch
+    from hssmatrices_gb300 import compression as CP
+    Ad = CP.DenseDevice.__new__(CP.DenseDevice)
+    Ad.t, Ad.m, Ad.n, Ad.lda = cauchy_device(n), n, n, n
+    cl = pkg.bisection_cluster(n, 128)
+
+    def compress():
+        return pkg.randcompress_adaptive(Ad, cl, cl, kest=10, atol=1e-9, rtol=1e-9, noversampling=10, stepsize=20,
+                                         rng=np.random.default_rng(1), device=True)
+
+    compress()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        compress()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    del Ad
+    torch.cuda.empty_cache()
+    return {"workload": f"randcompress_adaptive, Cauchy matrix n = {n} (the compress workload)",
+            "ms": 1000.0 * statistics.median(times), "steps": steps}
+
+
 def run_batch(args):
     """Batching: many independent HSS matrices of uneven sizes, leaf sizes and ranks
     in one forest, factored and solved with one launch per tree level; FP64 and
@@ -541,14 +637,7 @@ def run_batch(args):
     import torch
     import __graft_entry__ as g
     pkg = g.load_package()
-    rng = np.random.default_rng(2)
-    trees, rs = [], []
-    for _ in range(args.matrices):
-        n = int(rng.integers(1024 // 128, 16384 // 128 + 1)) * 128
-        ls = int(rng.choice([64, 128, 256]))
-        k = int(rng.integers(8, 49))
-        trees.append(pkg.synthetic_hss(n, ls, k, rng))
-        rs.append(int(rng.integers(1, 17)))
+    trees, rs = batch_trees(pkg, args.matrices)
     forest = pkg.DeviceHss.from_trees(trees)
     stream = torch.cuda.Stream()   # graphs need a non-default stream
     with torch.cuda.stream(stream):
