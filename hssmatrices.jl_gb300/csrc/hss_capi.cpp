@@ -9,6 +9,7 @@
 #include <array>
 #include <atomic>
 #include <cmath>
+#include <functional>
 #include <limits>
 #include <cstring>
 #include <string>
@@ -235,6 +236,8 @@ struct hss_plan_s {
   std::string ulv_why;                  // why the ULV reduction cannot factor this plan (empty: it can)
   cudaStream_t host_st = nullptr;       // stream of the host-buffer solves (made on first use)
   cudaEvent_t host_ev = nullptr;
+  cudaStream_t copy_st = nullptr;       // their right-hand sides' copy, beside the factorization
+  cudaEvent_t copy_ev = nullptr;
   ~hss_plan_s();
 };
 
@@ -271,7 +274,7 @@ struct hss_factor_s {
   DBuf<double> hB, hX;                  // staging for the _host solve
   // the pipelined factorization + first solve (hss_ulvfactsolve): a stream for
   // the upward solve, one for the factorization, and events [fork, solve join,
-  // factorization join, level 0, level 1, ...]
+  // factorization join, prelude done, level 0, level 1, ...]
   cudaStream_t pipe_st = nullptr;
   cudaStream_t fac_st = nullptr;        // the factorization's stream there (highest priority)
   std::vector<cudaEvent_t> pipe_ev;
@@ -288,6 +291,8 @@ struct hss_factor_s {
 hss_plan_s::~hss_plan_s() {
   if (host_ev) cudaEventDestroy(host_ev);
   if (host_st) cudaStreamDestroy(host_st);
+  if (copy_ev) cudaEventDestroy(copy_ev);
+  if (copy_st) cudaStreamDestroy(copy_st);
   delete tplan;
   delete fused[0];
   delete fused[1];
@@ -1459,7 +1464,7 @@ int factsolve_prep(hss_factor_s* f, const std::vector<Item>& items, const Levels
     CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     CUDA_TRY(cudaStreamCreateWithPriority(&f->fac_st, cudaStreamNonBlocking, greatest));
   }
-  while (f->pipe_ev.size() < 3 + L.by_h->size()) {
+  while (f->pipe_ev.size() < 4 + L.by_h->size()) {
     cudaEvent_t e = nullptr;
     CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     f->pipe_ev.push_back(e);
@@ -1477,19 +1482,27 @@ int factsolve_prep(hss_factor_s* f, const std::vector<Item>& items, const Levels
 
 template <typename T>
 cudaError_t factsolve_issue(hss_factor_s* f, const Levels& L, const SlotTable& table, const PassPrep& pp,
-                            cudaStream_t st) {
+                            cudaStream_t st, const std::function<int()>* pre = nullptr) {
   cudaError_t ev_err = cudaSuccess;
   auto chk = [&](cudaError_t e) { if (e != cudaSuccess && ev_err == cudaSuccess) ev_err = e; };
   // the factorization on the highest-priority stream, so that the merges (a
-  // chain of small launches) are scheduled ahead of the upward solve's blocks
+  // chain of small launches) are scheduled ahead of the upward solve's blocks;
+  // `pre` (launches on st that the solve needs and the factorization does not,
+  // such as waiting for the right-hand sides' copy) runs beside it
   cudaStream_t s2 = f->pipe_st, sf = f->fac_st;
   chk(cudaEventRecord(f->pipe_ev[0], st));
   chk(cudaStreamWaitEvent(sf, f->pipe_ev[0], 0));
-  chk(cudaStreamWaitEvent(s2, f->pipe_ev[0], 0));
+  if (pre) {
+    if ((*pre)() != HSS_OK && ev_err == cudaSuccess) ev_err = cudaErrorLaunchFailure;
+    chk(cudaEventRecord(f->pipe_ev[3], st));
+    chk(cudaStreamWaitEvent(s2, f->pipe_ev[3], 0));
+  } else {
+    chk(cudaStreamWaitEvent(s2, f->pipe_ev[0], 0));
+  }
   for (size_t h = 0; h < L.by_h->size(); ++h) {
     run_factor_level<T>(L, h, f->fac_slots.dev.p, sf);
-    chk(cudaEventRecord(f->pipe_ev[3 + h], sf));
-    chk(cudaStreamWaitEvent(s2, f->pipe_ev[3 + h], 0));
+    chk(cudaEventRecord(f->pipe_ev[4 + h], sf));
+    chk(cudaStreamWaitEvent(s2, f->pipe_ev[4 + h], 0));
     run_solve_up_level<T>(L, h, table.dev.p, (int)pp.rmax, s2, pp.blocked, &f->tune_up);
   }
   chk(cudaEventRecord(f->pipe_ev[2], sf));
@@ -1624,9 +1637,11 @@ constexpr int32_t kLoopMaxIt = 64;
 // With graphs enabled on a non-default stream the whole loop is one replayed
 // graph: the convergence check runs on the device and sets the condition of a
 // while node, and the host reads the loop's status once at the end.
+// ready: an event the launches that read the right-hand sides wait for (their
+// copy on another stream), or null.
 int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, double tol, int32_t maxit,
                 hss_solve_stats* stats, cudaStream_t st, const hss_factor_s* tf = nullptr,
-                hss_factor_s* fuse = nullptr) {
+                hss_factor_s* fuse = nullptr, cudaEvent_t ready = nullptr) {
   if (items.empty()) return HSS_OK;
   const int prec = items[0].f->prec;
   for (auto& it : items)
@@ -1660,7 +1675,10 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
                         : solve_pass<double>(items, L, scale, off.data(), rtot, 0, false, nullptr, nullptr, B.sv0,
                                              st, tf));
   };
-  if (!refine) return first_pass(nullptr);
+  if (!refine) {
+    if (ready) CUDA_TRY(cudaStreamWaitEvent(st, ready, 0));
+    return first_pass(nullptr);
+  }
   CUDA_TRY(B.bn2.ensure(rtot));
   CUDA_TRY(B.rn2.ensure(rtot));
   CUDA_TRY(B.scale.ensure(2 * rtot));
@@ -1769,7 +1787,8 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     double tolv = tol;
     uint64_t tolbits = 0;
     std::memcpy(&tolbits, &tolv, sizeof(tolbits));
-    for (uint64_t v : {(uint64_t)(uintptr_t)fuse, tolbits, (uint64_t)maxit, (uint64_t)fp32, (uint64_t)dfres,
+    for (uint64_t v : {(uint64_t)(uintptr_t)fuse, (uint64_t)(uintptr_t)ready, tolbits, (uint64_t)maxit,
+                       (uint64_t)fp32, (uint64_t)dfres,
                        (uint64_t)persistent, (uint64_t)dx_slices, (uint64_t)(uintptr_t)pm,
                        (uint64_t)g_generic_factor, (uint64_t)g_flat_product, (uint64_t)pmv_poll_limit(),
                        (uint64_t)(uintptr_t)B.mv.pq.p, (uint64_t)(uintptr_t)B.mv.pstate.p,
@@ -1789,16 +1808,23 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
       have = record_loop(
           gc, key, B.loop_body_launches, st,
           [&](cudaGraphConditionalHandle cond) -> int {
-            int e = issue_norms();
-            if (e) return e;
-            CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(RefineStatus), st));
+            // the right-hand sides' copy (an external event of the graph), their
+            // norms and the status reset: beside the factorization when fused
+            const std::function<int()> pre = [&]() -> int {
+              if (ready) CUDA_TRY(cudaStreamWaitEvent(st, ready, cudaEventWaitExternal));
+              const int e = issue_norms();
+              if (e) return e;
+              CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(RefineStatus), st));
+              return HSS_OK;
+            };
+            int e = HSS_OK;
             if (fuse) {
-              CUDA_TRY(fp32 ? factsolve_issue<float>(fuse, L, B.sv0, p0, st)
-                            : factsolve_issue<double>(fuse, L, B.sv0, p0, st));
-            } else if (fp32) {
-              solve_issue<float>(L, B.sv0, p0, st, tf);
+              CUDA_TRY(fp32 ? factsolve_issue<float>(fuse, L, B.sv0, p0, st, &pre)
+                            : factsolve_issue<double>(fuse, L, B.sv0, p0, st, &pre));
             } else {
-              solve_issue<double>(L, B.sv0, p0, st, tf);
+              if ((e = pre())) return e;
+              if (fp32) solve_issue<float>(L, B.sv0, p0, st, tf);
+              else solve_issue<double>(L, B.sv0, p0, st, tf);
             }
             if ((e = issue_residual())) return e;
             issue_check(cond);
@@ -1842,6 +1868,7 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
     gc.seen = key;   // recorded on the next call with this key
   }
   // the loop on the host: one read of the residual norms per step
+  if (ready) CUDA_TRY(cudaStreamWaitEvent(st, ready, 0));
   int rc = issue_norms();
   if (rc) return rc;
   CUDA_TRY(cudaMemcpyAsync(B.h_bn2.p, B.bn2.p, rtot * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1889,13 +1916,13 @@ int solve_items(const std::vector<Item>& items, const Levels& L, SolveBufs& B, d
 }
 
 int solve_impl(hss_factor_s* f, const std::vector<Cols>& io, double tol, int32_t maxit,
-               hss_solve_stats* stats, cudaStream_t st, bool refactor = false) {
+               hss_solve_stats* stats, cudaStream_t st, bool refactor = false, cudaEvent_t ready = nullptr) {
   hss_plan_s* P = f->plan;
   int rc = check_cols(P, io, true);
   if (rc) return rc;
   std::vector<Item> items;
   for (int32_t t = 0; t < P->ntrees; ++t) items.push_back(Item{f, t, io[t]});
-  return solve_items(items, plan_levels(P), f->bufs, tol, maxit, stats, st, f, refactor ? f : nullptr);
+  return solve_items(items, plan_levels(P), f->bufs, tol, maxit, stats, st, f, refactor ? f : nullptr, ready);
 }
 
 // Per-launch times (ms) of the traced kind since hss_trace_begin, in launch order.
@@ -2573,9 +2600,15 @@ int hss_ulvfactsolve_host(hss_handle h, int32_t precision, const double* B, int6
   if ((rc = check_cols(h, io, true))) return rc;
   cudaStream_t st = 0;
   if ((rc = host_stream(h, &st))) return rc;
-  if ((rc = copy_in(f->hB, B, m, ldb, r, st))) return rc;
+  // the right-hand sides are copied on a second stream while the
+  // factorization (which does not read them) starts
+  if (!h->copy_st) CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_st, cudaStreamNonBlocking));
+  if (!h->copy_ev) CUDA_TRY(cudaEventCreateWithFlags(&h->copy_ev, cudaEventDisableTiming));
+  CUDA_TRY(cudaStreamWaitEvent(h->copy_st, h->host_ev, 0));   // after the legacy default stream's work
+  if ((rc = copy_in(f->hB, B, m, ldb, r, h->copy_st))) return rc;
+  CUDA_TRY(cudaEventRecord(h->copy_ev, h->copy_st));
   CUDA_TRY(f->hX.ensure((size_t)n * std::max<int64_t>(r, 1)));
-  rc = solve_impl(f, {Cols{f->hB.p, m, r, f->hX.p, n}}, tol, maxit, stats, st, true);
+  rc = solve_impl(f, {Cols{f->hB.p, m, r, f->hX.p, n}}, tol, maxit, stats, st, true, h->copy_ev);
   if (rc && rc != HSS_ERR_NO_CONVERGENCE) return rc;
   if (r > 0) {
     int rc2 = copy_out(X, ldx, f->hX.p, n, r, st);

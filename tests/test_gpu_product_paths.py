@@ -333,3 +333,26 @@ def test_trace_per_level_times(pkg, lib):
     total, count = L.trace_end()
     assert len(t) == count == 6 and all(v > 0 for v in t)
     assert abs(sum(t) - total) <= 0.5 * total
+
+
+def test_host_solve_graph_replay_new_rhs(pkg, lib):
+    """hss_ulvfactsolve_host with graph replay on: the right-hand sides are
+    copied on a second stream while the factorization starts (an external event
+    the recorded graph waits on), so every call with new right-hand sides (host
+    loop, recorded, replayed) must solve for those, to the refinement's
+    tolerance, and agree with the call made without graphs."""
+    n, r = 8192, 4
+    A = pkg.synthetic_hss(n, 128, 32, np.random.default_rng(13))
+    rng = np.random.default_rng(14)
+    Bs = [np.asfortranarray(rng.standard_normal((n, r))) for _ in range(5)]
+    x_plain = [pkg.ldiv(A, b, precision="fp32", tol=1e-10) for b in Bs[:2]]
+    assert lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 1) == 0
+    try:
+        xs = [pkg.ldiv(A, b, precision="fp32", tol=1e-10) for b in Bs]
+    finally:
+        lib.hss_set_option(pkg._lib.HSS_OPT_GRAPHS, 0)
+    for b, x in zip(Bs, xs):
+        res = np.linalg.norm(b - pkg.matmul(A, x), axis=0) / np.linalg.norm(b, axis=0)
+        assert res.max() <= 1e-10, res
+    for x0, x1 in zip(x_plain, xs):
+        assert np.linalg.norm(x1 - x0) / np.linalg.norm(x0) <= 1e-9
