@@ -55,7 +55,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="precision workload: skip the batching and compression headlines")
-    p.add_argument("--workload", default="precision", choices=["precision", "serve", "batch", "compress", "matvec"])
+    p.add_argument("--workload", default="precision",
+                   choices=["precision", "serve", "batch", "compress", "matvec", "steps"])
     p.add_argument("--compress-n", type=int, default=16384)
     p.add_argument("--requests", type=int, default=10000)
     p.add_argument("--rate", type=float, default=500.0)
@@ -1003,6 +1004,32 @@ def run_matvec_workload(args):
     return 0
 
 
+def run_steps(args):
+    """Profiling aid: the precision workload's steps (FP32 factor + solve with
+    refinement), --warmup + --steps of them, launched one by one (no graph
+    replay, no autotuning, nothing timed), so that a profiler run on a few steps
+    captures each kernel of a step as its own launch."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    n, r = args.n, args.rhs
+    A = pkg.synthetic_hss(n, args.leafsize, args.rank, np.random.default_rng(args.seed))
+    dev = A.device()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dB = torch.from_numpy(np.ascontiguousarray(np.random.default_rng(1).standard_normal((n, r)).T)).cuda()
+    dX = torch.zeros_like(dB)
+    F = dev.ulvfactor("fp32", stream=stream)
+    st = None
+    for _ in range(args.warmup + args.steps):
+        st = F.factsolve_device(dB, n, r, dX, n, tol=args.tol, maxit=20, stream=stream)
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": "steps", "steps": args.warmup + args.steps, "iterations": st.iterations,
+                      "residual": st.residual}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1018,6 +1045,8 @@ def main():
         return run_compress(args) if rank == 0 else 0
     if args.workload == "matvec":
         return run_matvec_workload(args) if rank == 0 else 0
+    if args.workload == "steps":
+        return run_steps(args) if rank == 0 else 0
     if world > 1:
         import torch
         import torch.distributed as td
