@@ -1086,9 +1086,11 @@ __device__ void leaf_uf_unit(const Task tk, const Slot* __restrict__ slots, int 
 }
 
 // Units (leaf, block of XW columns) taken in turn by a grid of resident blocks,
-// so that the last wave is not a partial one.
+// so that the last wave is not a partial one.  The final products fit four
+// blocks per SM (64 registers, 40 KB of shared memory at k = 32), so 512
+// leaves take one round instead of two.
 template <bool FINAL>
-__global__ void __launch_bounds__(PT, 2) leaf_ext_kernel(const Task* __restrict__ leaves, const Slot* __restrict__ slots,
+__global__ void __launch_bounds__(PT, (FINAL ? 4 : 2)) leaf_ext_kernel(const Task* __restrict__ leaves, const Slot* __restrict__ slots,
                                                       int nunits, int ncb) {
   for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
     const Task tk = leaves[u / ncb];
