@@ -100,6 +100,23 @@ def cpu_solve_sample(args, calls):
     return times
 
 
+def max_over_ranks(value, device):
+    """The largest of `value` over the ranks of the default process group: a
+    one-element all-reduce on `device` ("cuda" under NCCL, "cpu" under gloo).
+    Every rank times its own replica; the job's time is the slowest rank's."""
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, steps_per_rank, seconds):
+    """Whole-job throughput of `world` independent replicas that each ran
+    `steps_per_rank` steps in at most `seconds` (the max over ranks)."""
+    return world * steps_per_rank / seconds
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -304,11 +321,9 @@ def run_ours(args, rank, world, local_rank):
         kms, _kn = L.trace_end()
         breakdown[kind] = kms / 3
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, "cuda")
     ms = total_ms / args.steps
-    value = world * 1000.0 / ms
+    value = job_rate(world, args.steps, total_ms / 1000.0)
     Xh = dX.cpu().numpy().T
     res32 = float(np.max(np.linalg.norm(Bh - pkg.matmul(A, Xh), axis=0) / np.linalg.norm(Bh, axis=0)))
     # plain FP64 form on the same GPU
@@ -360,10 +375,8 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     e2e_total = sum(e2e_t)
     if dist:
-        t = torch.tensor([e2e_total], device="cuda")
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * args.steps / e2e_total
+        e2e_total = max_over_ranks(e2e_total, "cuda")
+    e2e_value = job_rate(world, args.steps, e2e_total)
     # the HSS x dense product (FP64 hss_matmul, persistent kernel) on the same
     # tree: r = 1 and r = rhs columns, L2 flushed before each call
     matvec_us = {}
