@@ -159,8 +159,19 @@ function factsolve!(X::Ptr{Float64}, ldx::Integer, F::GpuUlv, B::Ptr{Float64}, l
     st[]
 end
 
-# process-wide switches (HSS_OPT_* of the header)
+# process-wide switches (HSS_OPT_* of the header); HSS_OPT_GRAPHS = 4 also runs
+# a refined solve's loop on the device (one graph, one status read per solve)
 set_option(opt::Integer, value::Integer) =
     check(ccall((:hss_set_option, lib), Cint, (Int32, Int64), Int32(opt), Int64(value)))
+
+# per-launch device times (ms, launch order) of one kernel kind (HSS_TRACE_* of
+# the header) over the calls made between trace_begin and trace_times
+trace_begin(kind::Integer) = check(ccall((:hss_trace_begin, lib), Cint, (Int32,), Int32(kind)))
+function trace_times(cap::Integer=4096)
+    ms = zeros(Float64, cap)
+    n = Ref{Int64}(0)
+    check(ccall((:hss_trace_times, lib), Cint, (Ptr{Float64}, Int64, Ref{Int64}), ms, cap, n))
+    ms[1:min(n[], cap)]
+end
 
 end # module
